@@ -1,0 +1,101 @@
+"""Build the sm_103a C-ABI library ``libcato_gpu.so`` in-tree (``fvleg_2d_gb300/_lib/``).
+
+The stage kernel family is instantiated once per (precision, flux) pair from ``stage_inst.cu``
+so the 16 translation units compile in parallel; the FP64 units and the helper kernels are built
+with ``--fmad=false`` (each reference operation rounds on its own), the mixed-precision units with
+FMA contraction enabled.  No CMake, no torch: nvcc and a C++ host compiler only.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import hashlib
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+OUT_DIR = os.path.join(HERE, "_lib")
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_NAME = "libcato_gpu.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+N_FLUX = 8
+
+
+def nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libcato_gpu.so")
+
+
+def _sources_digest(extra: list[str]) -> str:
+    h = hashlib.sha256()
+    for d in (CSRC, INCLUDE):
+        for name in sorted(os.listdir(d)):
+            if name.endswith((".cu", ".cuh", ".h", ".hpp", ".cpp")):
+                with open(os.path.join(d, name), "rb") as f:
+                    h.update(name.encode())
+                    h.update(f.read())
+    h.update(" ".join(extra).encode())
+    return h.hexdigest()
+
+
+def _units() -> list[tuple[str, list[str]]]:
+    common = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+              "-I", INCLUDE]
+    units = []
+    for real, fmad in (("double", "false"), ("float", "true")):
+        for flux in range(N_FLUX):
+            obj = os.path.join(BUILD_DIR, f"stage_{real}_{flux}.o")
+            cmd = [nvcc(), *ARCH, *common, f"--fmad={fmad}", f"-DCATO_REAL={real}",
+                   f"-DCATO_FLUX={flux}", "-c", os.path.join(CSRC, "stage_inst.cu"), "-o", obj]
+            units.append((obj, cmd))
+    for src in ("cato_capi.cu", "cato_batch.cu"):
+        path = os.path.join(CSRC, src)
+        if not os.path.exists(path):
+            continue
+        obj = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
+        units.append((obj, [nvcc(), *ARCH, *common, "--fmad=false", "-c", path, "-o", obj]))
+    return units
+
+
+def lib_path() -> str:
+    return os.path.join(OUT_DIR, LIB_NAME)
+
+
+def build(verbose: bool = False, jobs: int | None = None) -> str:
+    """Compile (if sources changed) and return the path of libcato_gpu.so."""
+    os.makedirs(OUT_DIR, exist_ok=True)
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    units = _units()
+    digest = _sources_digest([u[1][-1] for u in units] + [" ".join(units[0][1])])
+    stamp = os.path.join(BUILD_DIR, "stamp")
+    out = lib_path()
+    if os.path.exists(out) and os.path.exists(stamp):
+        with open(stamp) as f:
+            if f.read().strip() == digest:
+                return out
+    jobs = jobs or max(1, min(len(units), os.cpu_count() or 4))
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        if verbose and r.stderr:
+            sys.stderr.write(r.stderr)
+
+    with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
+        list(ex.map(run, [u[1] for u in units]))
+    tmp = out + ".tmp"
+    run([nvcc(), *ARCH, "-shared", "-o", tmp, *[u[0] for u in units], "-lcudart"])
+    os.replace(tmp, out)
+    with open(stamp, "w") as f:
+        f.write(digest)
+    return out
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

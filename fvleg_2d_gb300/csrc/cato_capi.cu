@@ -1,0 +1,708 @@
+// cato_capi.cu -- the C-ABI of include/cato_gpu.h: handles, device state, step sequencing.
+//
+// Device layout of one instance (all interior-only, row-major with i fastest = the reference's
+// Fortran (i, j) order, row pitch rounded up to 32 elements so every row starts 256-B aligned):
+//   FP64 path : U^n (4 x f64) + two stage buffers S0, S1 (4 x f64 each).  The last stage writes
+//               U^{n+1} over U^n in place (U^n is only read point-wise there).
+//   mixed path: U^n double-buffered (2 x 4 x f64) + stage increments delta (2 x 4 x f32):
+//               U^k = U^n + delta_k, delta_{k+1} = b delta_k + c L(U^k), U^{n+1} = U^n + delta.
+// The primitives of an upload are kept (in a buffer not needed before the first step) because
+// the first stage after an upload uses them as is, like the reference after initialize.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/cato_gpu.h"
+#include "cato_kernels.cuh"
+#include "cato_launch.cuh"
+
+using namespace cato;
+
+namespace {
+
+struct Plan {
+  int threads = 128;       // CTA width incl. halo
+  int rows_per_cta = 64;   // rows marched per CTA
+};
+
+struct Stage {
+  int kind;     // StageArgs::kind
+  double a, b;  // combine coefficients (kind 1 / mixed b)
+  double coef;  // c = coef * dt
+};
+
+}  // namespace
+
+struct cato_handle {
+  cato_config cfg{};
+  int ni = 0, nj = 0, ng = 2, pitch = 0;
+  size_t field_elems = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  // device buffers
+  double* U[2][4] = {};    // FP64: U[0] = U^n ; mixed: U[cur], U[1-cur]
+  double* S[2][4] = {};    // FP64 stage buffers
+  float* D[2][4] = {};     // mixed stage increments
+  double* prim_raw[4] = {};  // primitives of the last upload (alias of a free buffer)
+  double* scratch[8] = {};   // solve / download / interpolation scratch (lazy)
+  double* halo[4] = {};      // halo-padded scratch (lazy)
+  size_t halo_elems = 0;
+  StepCtl* ctl = nullptr;    // device
+  StepCtl* ctl_host = nullptr;  // pinned mirror
+  int cur = 0;               // mixed: which U holds U^n
+  bool uploaded = false;
+  bool raw_pending = false;  // next stage 1 uses prim_raw
+  Plan plan;
+  FluxConsts<double> K64{};
+  FluxConsts<float> K32{};
+  Geom G{};
+  std::vector<Stage> stages;
+  std::string err;
+};
+
+static thread_local std::string g_null_err;
+
+static int fail(cato_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+static int cuda_fail(cato_handle* h, cudaError_t e, const char* where) {
+  return fail(h, CATO_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                        \
+  do {                                                  \
+    cudaError_t _e = (call);                            \
+    if (_e != cudaSuccess) return cuda_fail(h, _e, #call); \
+  } while (0)
+
+static int recon_of(int limiter) {
+  return limiter == CATO_LIM_MLP3 ? 3 : (limiter == CATO_LIM_MLP5 ? 5 : 0);
+}
+
+// rk(m,n) stage weights, mod_fluid.f90:926-945
+static const double* rk_alpha(int rk, int* ns) {
+  static const double a13[] = {0.1481, 0.4, 1.0}, a14[] = {0.0833, 0.2069, 0.4265, 1.0},
+                      a15[] = {0.0533, 0.1263, 0.2375, 0.4414, 1.0},
+                      a23[] = {0.1918, 0.4929, 1.0}, a24[] = {0.1084, 0.2602, 0.5052, 1.0},
+                      a25[] = {0.0695, 0.1602, 0.2898, 0.5060, 1.0};
+  switch (rk) {
+    case CATO_RK_1_3: *ns = 3; return a13;
+    case CATO_RK_1_4: *ns = 4; return a14;
+    case CATO_RK_1_5: *ns = 5; return a15;
+    case CATO_RK_2_3: *ns = 3; return a23;
+    case CATO_RK_2_4: *ns = 4; return a24;
+    default: *ns = 5; return a25;
+  }
+}
+
+// The stage sequence of each integrator (mod_fluid.f90:739-1160).
+static std::vector<Stage> build_stages(int rk) {
+  std::vector<Stage> s;
+  if (rk == CATO_RK_SSP2) {
+    s.push_back({0, 1.0, 0.0, 1.0});            // U1 = U + L(U)*dt
+    s.push_back({1, 0.5, 0.5, 0.5});            // U2 = U*0.5 + U1*0.5 + L(U1)*(0.5*dt)
+  } else if (rk == CATO_RK_SSP3) {
+    s.push_back({0, 1.0, 0.0, 1.0});
+    s.push_back({1, 3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0});
+    s.push_back({1, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0});
+  } else {
+    int ns;
+    const double* al = rk_alpha(rk, &ns);
+    for (int m = 0; m < ns; ++m) s.push_back({0, 1.0, 0.0, al[m]});  // U0 + L(Uprev)*(dt*alpha)
+  }
+  return s;
+}
+
+static void fill_consts(cato_handle* h) {
+  const cato_config& c = h->cfg;
+  const double g = c.gamma;
+  FluxConsts<double> K{};
+  K.gamma = g;
+  K.g_over_gm1 = g / (g - 1.0);
+  K.gm1 = g - 1.0;
+  K.two_gm1_over_gp1 = 2.0 * ((g - 1.0) / (g + 1.0));
+  K.gamma_factor = ((2.0 * (g - 1.0)) / (g + 1.0));
+  K.hllc_gf = (g + 1.0) / (2.0 * g);
+  K.harten_delta = c.harten_delta;
+  K.ausm_beta = c.ausm_beta;
+  K.ausm_kp = c.ausm_kp;
+  K.ausm_ku = c.ausm_ku;
+  K.ausm_sigma = c.ausm_sigma;
+  K.low_mach_fix = c.apply_low_mach_fix ? 1 : 0;
+  K.harten = c.roe_entropy_fix == CATO_ROE_HARTEN ? 1 : 0;
+  h->K64 = K;
+  FluxConsts<float> F{};
+  F.gamma = (float)K.gamma;
+  F.g_over_gm1 = (float)K.g_over_gm1;
+  F.gm1 = (float)K.gm1;
+  F.two_gm1_over_gp1 = (float)K.two_gm1_over_gp1;
+  F.gamma_factor = (float)K.gamma_factor;
+  F.hllc_gf = (float)K.hllc_gf;
+  F.harten_delta = (float)K.harten_delta;
+  F.ausm_beta = (float)K.ausm_beta;
+  F.ausm_kp = (float)K.ausm_kp;
+  F.ausm_ku = (float)K.ausm_ku;
+  F.ausm_sigma = (float)K.ausm_sigma;
+  F.low_mach_fix = K.low_mach_fix;
+  F.harten = K.harten;
+  h->K32 = F;
+  // quad_cell_t metrics of a dx x dy axis-aligned cell (quad_cell.f90:69-229): volume dx*dy,
+  // edge lengths dx, dy, dx, dy (all set to the largest when they differ by < 2 eps),
+  // min_dx = dx, min_dy = dy.
+  Geom G{};
+  G.vol = (c.dx - 0.0) * (c.dy - 0.0) - (0.0 - 0.0) * (0.0 - 0.0);
+  double l[4] = {c.dx, c.dy, c.dx, c.dy};
+  double mx = l[0], mn = l[0];
+  for (int k = 1; k < 4; ++k) { mx = l[k] > mx ? l[k] : mx; mn = l[k] < mn ? l[k] : mn; }
+  if (mx - mn < 2.0 * 2.220446049250313080847263336181640625e-16) l[0] = l[1] = l[2] = l[3] = mx;
+  G.l1 = l[0]; G.l2 = l[1]; G.l3 = l[2]; G.l4 = l[3];
+  G.dx = c.dx;
+  G.dy = c.dy;
+  h->G = G;
+}
+
+static void default_plan(cato_handle* h) {
+  // Wide strips for large grids; narrow strips and short marches for small grids so that the
+  // launch fills the 152 SMs.
+  const long long cells = (long long)h->ni * h->nj;
+  Plan p;
+  if (cells < 200000) { p.threads = 64; p.rows_per_cta = 8; }
+  else if (cells < 4000000) { p.threads = 128; p.rows_per_cta = 32; }
+  else { p.threads = 128; p.rows_per_cta = 64; }
+  if (p.threads - 2 * h->ng > h->ni + 2 * h->ng) p.threads = 64;
+  h->plan = p;
+}
+
+static StageArgs base_args(cato_handle* h) {
+  StageArgs A;
+  std::memset(&A, 0, sizeof(A));
+  A.ni = h->ni;
+  A.nj = h->nj;
+  A.pitch = h->pitch;
+  for (int s = 0; s < 4; ++s) A.bc[s] = h->cfg.bc[s];
+  A.limiter = h->cfg.limiter;
+  A.rows_per_cta = h->plan.rows_per_cta;
+  A.dt = &h->ctl->dt;
+  A.active = &h->ctl->active;
+  A.dt_min = &h->ctl->dt_min;
+  A.status = &h->ctl->status;
+  A.gamma = h->cfg.gamma;
+  A.cfl = h->cfg.cfl;
+  A.G = h->G;
+  return A;
+}
+
+static cudaError_t launch(cato_handle* h, const StageArgs& A) {
+  const int T = h->plan.threads;
+  const int W = T - 2 * h->ng;
+  dim3 grid((h->ni + W - 1) / W, (h->nj + A.rows_per_cta - 1) / A.rows_per_cta);
+  const int recon = recon_of(h->cfg.limiter);
+  if (h->cfg.precision == CATO_FP64)
+    return launch_stage<double>(h->cfg.flux, recon, grid, T, h->stream, A, h->K64);
+  return launch_stage<float>(h->cfg.flux, recon, grid, T, h->stream, A, h->K32);
+}
+
+// Enqueue one full time step (step control + every stage) on the handle's stream.
+static int enqueue_step(cato_handle* h) {
+  step_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctl);
+  CK(cudaGetLastError());
+  const int ns = (int)h->stages.size();
+  const bool fp64 = h->cfg.precision == CATO_FP64;
+  for (int k = 0; k < ns; ++k) {
+    const Stage& st = h->stages[k];
+    StageArgs A = base_args(h);
+    A.kind = st.kind;
+    A.a = st.a;
+    A.b = st.b;
+    A.coef = st.coef;
+    A.last = (k == ns - 1);
+    const bool raw = (k == 0) && h->raw_pending;
+    if (fp64) {
+      double** Un = h->U[0];
+      // stencil operand: U^n for the first stage, else the previous stage's output
+      double** prev = (k == 0) ? Un : h->S[(k - 1) & 1];
+      double** out = A.last ? Un : h->S[k & 1];
+      for (int v = 0; v < 4; ++v) {
+        A.Uk[v] = prev[v];
+        A.Ua[v] = Un[v];
+        A.Uo[v] = out[v];
+        A.Pin[v] = raw ? h->prim_raw[v] : nullptr;
+      }
+    } else {
+      double** Un = h->U[h->cur];
+      double** Unext = h->U[1 - h->cur];
+      for (int v = 0; v < 4; ++v) {
+        A.Uk[v] = Un[v];
+        A.Ua[v] = Un[v];
+        A.Uo[v] = A.last ? Unext[v] : nullptr;
+        A.Pin[v] = raw ? h->prim_raw[v] : nullptr;
+        A.dk[v] = (k == 0) ? nullptr : h->D[(k - 1) & 1][v];
+        A.dout[v] = A.last ? nullptr : h->D[k & 1][v];
+      }
+      if (st.kind == 0) A.b = 0.0;  // rk(m,n): U_curr = U_0 + c L(U_prev)
+    }
+    CK(launch(h, A));
+  }
+  if (!fp64) h->cur = 1 - h->cur;
+  h->raw_pending = false;
+  return CATO_OK;
+}
+
+static int pull_ctl(cato_handle* h) {
+  CK(cudaMemcpyAsync(h->ctl_host, h->ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return CATO_OK;
+}
+
+static int status_code(int bits) {
+  if (bits & ST_NEG_DENSITY) return CATO_NEG_DENSITY;
+  if (bits & ST_NEG_PRESSURE) return CATO_NEG_PRESSURE;
+  if (bits & ST_NAN) return CATO_NANS_FOUND;
+  return CATO_OK;
+}
+
+static double host_decode(unsigned long long b) {
+  if (b == ~0ULL) return INFINITY;
+  double d;
+  std::memcpy(&d, &b, sizeof d);
+  return d;
+}
+
+static int ensure_scratch(cato_handle* h) {
+  if (h->scratch[0]) return CATO_OK;
+  for (int k = 0; k < 8; ++k) CK(cudaMalloc(&h->scratch[k], h->field_elems * sizeof(double)));
+  return CATO_OK;
+}
+
+static int ensure_halo(cato_handle* h) {
+  if (h->halo[0]) return CATO_OK;
+  h->halo_elems = (size_t)(h->ni + 2 * h->ng) * (h->nj + 2 * h->ng);
+  for (int k = 0; k < 4; ++k) CK(cudaMalloc(&h->halo[k], h->halo_elems * sizeof(double)));
+  return CATO_OK;
+}
+
+// host halo-padded (ld) <-> device interior (pitch)
+static int h2d_interior(cato_handle* h, double* dst, const double* src, int64_t ld) {
+  const double* first = src + (size_t)h->ng * ld + h->ng;
+  CK(cudaMemcpy2DAsync(dst, (size_t)h->pitch * sizeof(double), first, (size_t)ld * sizeof(double),
+                       (size_t)h->ni * sizeof(double), (size_t)h->nj, cudaMemcpyHostToDevice,
+                       h->stream));
+  return CATO_OK;
+}
+
+static int d2h_interior(cato_handle* h, double* dst, const double* src, int64_t ld) {
+  double* first = dst + (size_t)h->ng * ld + h->ng;
+  CK(cudaMemcpy2DAsync(first, (size_t)ld * sizeof(double), src, (size_t)h->pitch * sizeof(double),
+                       (size_t)h->ni * sizeof(double), (size_t)h->nj, cudaMemcpyDeviceToHost,
+                       h->stream));
+  return CATO_OK;
+}
+
+static void zero_host_field(cato_handle* h, double* a, int64_t ld) {
+  const size_t rows = (size_t)h->nj + 2 * h->ng;
+  for (size_t j = 0; j < rows; ++j) std::memset(a + j * ld, 0, sizeof(double) * (h->ni + 2 * h->ng));
+}
+
+static int grid_for(long long n) {
+  long long b = (n + 255) / 256;
+  if (b > 152LL * 32) b = 152LL * 32;
+  return (int)(b < 1 ? 1 : b);
+}
+
+extern "C" {
+
+const char* cato_gpu_version(void) { return "cato-gb300 0.1 (sm_103a)"; }
+
+int cato_config_default(cato_config* c, int32_t ni, int32_t nj) {
+  if (!c) return CATO_ERR_ARG;
+  std::memset(c, 0, sizeof(*c));
+  // mod_input.f90:34-148 defaults
+  c->ni = ni;
+  c->nj = nj;
+  c->n_ghost = 2;
+  c->flux = CATO_FLUX_AUSMPW_PLUS;
+  c->limiter = CATO_LIM_MINMOD;
+  c->rk = CATO_RK_SSP2;
+  for (int s = 0; s < 4; ++s) c->bc[s] = CATO_BC_PERIODIC;
+  c->apply_low_mach_fix = 1;
+  c->precision = CATO_FP64;
+  c->roe_entropy_fix = CATO_ROE_REFERENCE;
+  c->gamma = 5.0 / 3.0;
+  c->cfl = 0.1;
+  c->dx = 1.0;
+  c->dy = 1.0;
+  c->harten_delta = 0.1;
+  c->ausm_beta = 1.0 / 8.0;
+  c->ausm_kp = 0.25;
+  c->ausm_ku = 0.75;
+  c->ausm_sigma = 1.0;
+  return CATO_OK;
+}
+
+int cato_config_check(const cato_config* c) {
+  if (!c) return CATO_ERR_ARG;
+  if (c->ni < 1 || c->nj < 1) return CATO_ERR_CONFIG;
+  if (c->flux < CATO_FLUX_AUSMPW_PLUS || c->flux > CATO_FLUX_HLLC) return CATO_ERR_CONFIG;
+  if (c->limiter < CATO_LIM_MINMOD || c->limiter > CATO_LIM_MLP5) return CATO_ERR_CONFIG;
+  if (c->rk < CATO_RK_SSP2 || c->rk > CATO_RK_2_5) return CATO_ERR_CONFIG;
+  const int need = (c->limiter == CATO_LIM_MLP5) ? 3 : 2;  // mod_input.f90:320-338
+  if (c->n_ghost != need) return CATO_ERR_CONFIG;
+  if (c->ni < c->n_ghost || c->nj < c->n_ghost) return CATO_ERR_CONFIG;
+  for (int s = 0; s < 4; ++s)
+    if (c->bc[s] < CATO_BC_ZERO_GRADIENT || c->bc[s] > CATO_BC_PERIODIC) return CATO_ERR_CONFIG;
+  // periodic must be paired on an axis: an unpaired periodic side leaves ghost corners unset
+  if ((c->bc[CATO_PLUS_X] == CATO_BC_PERIODIC) != (c->bc[CATO_MINUS_X] == CATO_BC_PERIODIC))
+    return CATO_ERR_CONFIG;
+  if ((c->bc[CATO_PLUS_Y] == CATO_BC_PERIODIC) != (c->bc[CATO_MINUS_Y] == CATO_BC_PERIODIC))
+    return CATO_ERR_CONFIG;
+  if (!(c->gamma > 1.0) || !(c->cfl > 0.0) || !(c->dx > 0.0) || !(c->dy > 0.0))
+    return CATO_ERR_CONFIG;
+  if (c->precision != CATO_FP64 && c->precision != CATO_MIXED) return CATO_ERR_CONFIG;
+  if (c->roe_entropy_fix != CATO_ROE_REFERENCE && c->roe_entropy_fix != CATO_ROE_HARTEN)
+    return CATO_ERR_CONFIG;
+  if ((long long)c->ni > (1LL << 30) || (long long)c->nj > (1LL << 30)) return CATO_ERR_CONFIG;
+  return CATO_OK;
+}
+
+int cato_gpu_create(const cato_config* cfg, cato_handle** out) {
+  if (!cfg || !out) return CATO_ERR_ARG;
+  *out = nullptr;
+  int rc = cato_config_check(cfg);
+  if (rc != CATO_OK) return rc;
+  cato_handle* h = new cato_handle();
+  h->cfg = *cfg;
+  h->ni = cfg->ni;
+  h->nj = cfg->nj;
+  h->ng = cfg->n_ghost;
+  h->pitch = (cfg->ni + 31) / 32 * 32;
+  h->field_elems = (size_t)h->pitch * h->nj;
+  h->stages = build_stages(cfg->rk);
+  fill_consts(h);
+  default_plan(h);
+  auto cleanup = [&](int code) {
+    cato_gpu_destroy(h);
+    return code;
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete h; return CATO_ERR_CUDA; }
+  h->own_stream = true;
+  const size_t fb = h->field_elems * sizeof(double);
+  const bool fp64 = cfg->precision == CATO_FP64;
+  auto dalloc = [&](void** p, size_t bytes) -> bool {
+    cudaError_t ee = cudaMalloc(p, bytes);
+    if (ee != cudaSuccess) { (void)cudaGetLastError(); return false; }
+    return true;
+  };
+  for (int v = 0; v < 4; ++v) {
+    if (!dalloc((void**)&h->U[0][v], fb)) return cleanup(CATO_ERR_OOM);
+    if (fp64) {
+      if (!dalloc((void**)&h->S[0][v], fb)) return cleanup(CATO_ERR_OOM);
+      if (!dalloc((void**)&h->S[1][v], fb)) return cleanup(CATO_ERR_OOM);
+      h->prim_raw[v] = h->S[1][v];  // S1 is first written by stage 2, after stage 1 read these
+    } else {
+      if (!dalloc((void**)&h->U[1][v], fb)) return cleanup(CATO_ERR_OOM);
+      if (!dalloc((void**)&h->D[0][v], h->field_elems * sizeof(float))) return cleanup(CATO_ERR_OOM);
+      if (!dalloc((void**)&h->D[1][v], h->field_elems * sizeof(float))) return cleanup(CATO_ERR_OOM);
+      h->prim_raw[v] = h->U[1][v];  // U[1] is first written by the last stage of step 1
+    }
+  }
+  if (!dalloc((void**)&h->ctl, sizeof(StepCtl))) return cleanup(CATO_ERR_OOM);
+  if (cudaMallocHost((void**)&h->ctl_host, sizeof(StepCtl)) != cudaSuccess) return cleanup(CATO_ERR_OOM);
+  std::memset(h->ctl_host, 0, sizeof(StepCtl));
+  h->ctl_host->dt_min = ~0ULL;
+  h->ctl_host->t_end = INFINITY;
+  h->ctl_host->max_iter = (1LL << 62);
+  if (cudaMemcpy(h->ctl, h->ctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice) != cudaSuccess)
+    return cleanup(CATO_ERR_CUDA);
+  // prepare the kernel's shared-memory attribute outside any stream capture
+  StageArgs A = base_args(h);
+  cudaError_t ee = fp64 ? launch_stage<double>(cfg->flux, recon_of(cfg->limiter), dim3(0, 0), 64,
+                                               h->stream, A, h->K64)
+                        : launch_stage<float>(cfg->flux, recon_of(cfg->limiter), dim3(0, 0), 64,
+                                              h->stream, A, h->K32);
+  if (ee != cudaSuccess) return cleanup(CATO_ERR_CUDA);
+  *out = h;
+  return CATO_OK;
+}
+
+int cato_gpu_destroy(cato_handle* h) {
+  if (!h) return CATO_ERR_ARG;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (int s = 0; s < 2; ++s)
+    for (int v = 0; v < 4; ++v) {
+      cudaFree(h->U[s][v]);
+      cudaFree(h->S[s][v]);
+      cudaFree(h->D[s][v]);
+    }
+  for (int k = 0; k < 8; ++k) cudaFree(h->scratch[k]);
+  for (int k = 0; k < 4; ++k) cudaFree(h->halo[k]);
+  cudaFree(h->ctl);
+  if (h->ctl_host) cudaFreeHost(h->ctl_host);
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return CATO_OK;
+}
+
+const char* cato_gpu_last_error(const cato_handle* h) {
+  return h ? h->err.c_str() : g_null_err.c_str();
+}
+
+int cato_gpu_upload_primitive(cato_handle* h, const double* rho, const double* u, const double* v,
+                              const double* p, int64_t ld) {
+  if (!h) return CATO_ERR_ARG;
+  if (!rho || !u || !v || !p) return fail(h, CATO_ERR_ARG, "null field pointer");
+  if (ld < h->ni + 2 * h->ng) return fail(h, CATO_ERR_ARG, "leading dimension too small");
+  const double* src[4] = {rho, u, v, p};
+  for (int k = 0; k < 4; ++k) {
+    int rc = h2d_interior(h, h->prim_raw[k], src[k], ld);
+    if (rc) return rc;
+  }
+  StepCtl c{};
+  c.dt_min = ~0ULL;
+  c.t_end = INFINITY;
+  c.max_iter = (1LL << 62);
+  *h->ctl_host = c;
+  CK(cudaMemcpyAsync(h->ctl, h->ctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice, h->stream));
+  h->cur = 0;
+  double** Un = h->U[0];
+  upload_init_kernel<<<grid_for((long long)h->ni * h->nj), 256, 0, h->stream>>>(
+      h->ni, h->nj, h->pitch, h->cfg.gamma, h->cfg.cfl, h->G.dx, h->G.dy, h->prim_raw[0],
+      h->prim_raw[1], h->prim_raw[2], h->prim_raw[3], Un[0], Un[1], Un[2], Un[3], h->ctl);
+  CK(cudaGetLastError());
+  int rc = pull_ctl(h);
+  if (rc) return rc;
+  h->uploaded = true;
+  h->raw_pending = true;
+  return status_code(h->ctl_host->status);
+}
+
+int cato_gpu_get_timestep(cato_handle* h, double* dt) {
+  if (!h || !dt) return CATO_ERR_ARG;
+  if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  int rc = pull_ctl(h);
+  if (rc) return rc;
+  *dt = host_decode(h->ctl_host->dt_min);
+  return CATO_OK;
+}
+
+int cato_gpu_integrate(cato_handle* h, double dt, double* dt_used, int32_t* error_code) {
+  if (!h) return CATO_ERR_ARG;
+  if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  // one step regardless of t_end; fixed dt when dt > 0
+  int rc = pull_ctl(h);
+  if (rc) return rc;
+  StepCtl c = *h->ctl_host;
+  c.t_end = INFINITY;
+  c.max_iter = c.iter + 1;
+  c.fixed_dt = dt > 0.0 ? dt : 0.0;
+  *h->ctl_host = c;
+  CK(cudaMemcpyAsync(h->ctl, h->ctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice, h->stream));
+  if (c.status == 0) {
+    rc = enqueue_step(h);
+    if (rc) return rc;
+  }
+  rc = pull_ctl(h);
+  if (rc) return rc;
+  if (dt_used) *dt_used = h->ctl_host->dt;
+  if (error_code) *error_code = status_code(h->ctl_host->status);
+  return CATO_OK;
+}
+
+int cato_gpu_run(cato_handle* h, int64_t max_steps, double t_end, int64_t* steps_done,
+                 double* time, int32_t* error_code) {
+  if (!h) return CATO_ERR_ARG;
+  if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  int rc = pull_ctl(h);
+  if (rc) return rc;
+  StepCtl c = *h->ctl_host;
+  const long long it0 = c.iter;
+  c.t_end = t_end;
+  c.max_iter = max_steps >= 0 ? it0 + max_steps : (1LL << 62);
+  c.fixed_dt = 0.0;
+  *h->ctl_host = c;
+  CK(cudaMemcpyAsync(h->ctl, h->ctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice, h->stream));
+  const long long total = max_steps >= 0 ? max_steps : (1LL << 62);
+  long long issued = 0;
+  const long long chunk = 32;
+  while (issued < total) {
+    const long long n = (total - issued) < chunk ? (total - issued) : chunk;
+    const int parity0 = h->cur;
+    for (long long k = 0; k < n; ++k) {
+      rc = enqueue_step(h);
+      if (rc) return rc;
+    }
+    issued += n;
+    rc = pull_ctl(h);
+    if (rc) return rc;
+    if (h->cfg.precision == CATO_MIXED) {
+      // steps past the stop condition were no-ops: U^n sits in the buffer of the last active one
+      const long long active = h->ctl_host->iter - (it0 + (issued - n));
+      h->cur = (int)((parity0 + active) & 1);
+    }
+    if (!h->ctl_host->active || h->ctl_host->status) break;
+  }
+  if (steps_done) *steps_done = h->ctl_host->iter - it0;
+  if (time) *time = h->ctl_host->time;
+  if (error_code) *error_code = status_code(h->ctl_host->status);
+  return CATO_OK;
+}
+
+int cato_gpu_set_time(cato_handle* h, double time, int64_t iteration) {
+  if (!h) return CATO_ERR_ARG;
+  int rc = pull_ctl(h);
+  if (rc) return rc;
+  h->ctl_host->time = time;
+  h->ctl_host->iter = iteration;
+  CK(cudaMemcpyAsync(h->ctl, h->ctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return CATO_OK;
+}
+
+int cato_gpu_get_time(cato_handle* h, double* time, int64_t* iteration, double* last_dt) {
+  if (!h) return CATO_ERR_ARG;
+  int rc = pull_ctl(h);
+  if (rc) return rc;
+  if (time) *time = h->ctl_host->time;
+  if (iteration) *iteration = h->ctl_host->iter;
+  if (last_dt) *last_dt = h->ctl_host->dt;
+  return CATO_OK;
+}
+
+int cato_gpu_download(cato_handle* h, double* rho, double* rho_u, double* rho_v, double* rho_E,
+                      double* u, double* v, double* p, double* cs, int64_t ld) {
+  if (!h) return CATO_ERR_ARG;
+  if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  if (ld < h->ni + 2 * h->ng) return fail(h, CATO_ERR_ARG, "leading dimension too small");
+  double** Un = h->U[h->cfg.precision == CATO_FP64 ? 0 : h->cur];
+  double* cons_out[4] = {rho, rho_u, rho_v, rho_E};
+  double* der_out[4] = {u, v, p, cs};
+  int rc;
+  for (int k = 0; k < 4; ++k)
+    if (cons_out[k]) {
+      zero_host_field(h, cons_out[k], ld);
+      if ((rc = d2h_interior(h, cons_out[k], Un[k], ld))) return rc;
+    }
+  if (u || v || p || cs) {
+    if ((rc = ensure_scratch(h))) return rc;
+    const int raw = h->raw_pending ? 1 : 0;
+    double* const* src = raw ? h->prim_raw : Un;
+    derive_kernel<<<grid_for((long long)h->ni * h->nj), 256, 0, h->stream>>>(
+        h->ni, h->nj, h->pitch, h->cfg.gamma, raw, src[0], src[1], src[2], src[3], h->scratch[0],
+        h->scratch[1], h->scratch[2], h->scratch[3]);
+    CK(cudaGetLastError());
+    for (int k = 0; k < 4; ++k)
+      if (der_out[k]) {
+        zero_host_field(h, der_out[k], ld);
+        if ((rc = d2h_interior(h, der_out[k], h->scratch[k], ld))) return rc;
+      }
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  return CATO_OK;
+}
+
+int cato_gpu_solve(cato_handle* h, double* rho, double* u, double* v, double* p,
+                   double* d_rho_dt, double* d_rho_u_dt, double* d_rho_v_dt, double* d_rho_E_dt,
+                   int64_t ld) {
+  if (!h) return CATO_ERR_ARG;
+  if (!rho || !u || !v || !p || !d_rho_dt || !d_rho_u_dt || !d_rho_v_dt || !d_rho_E_dt)
+    return fail(h, CATO_ERR_ARG, "null field pointer");
+  if (ld < h->ni + 2 * h->ng) return fail(h, CATO_ERR_ARG, "leading dimension too small");
+  if (h->cfg.precision != CATO_FP64)
+    return fail(h, CATO_ERR_CONFIG, "solve is the FP64 reference boundary");
+  int rc;
+  if ((rc = ensure_scratch(h))) return rc;
+  if ((rc = ensure_halo(h))) return rc;
+  double* prim[4] = {rho, u, v, p};
+  for (int k = 0; k < 4; ++k)
+    if ((rc = h2d_interior(h, h->scratch[k], prim[k], ld))) return rc;
+  // residual: one stage in kind 2 reading the given primitives
+  StepCtl* ctl = h->ctl;  // dt unused by kind 2; keep the handle's dt_min untouched
+  (void)ctl;
+  StageArgs A = base_args(h);
+  A.kind = 2;
+  A.last = 0;
+  A.active = nullptr;
+  A.coef = 0.0;
+  for (int k = 0; k < 4; ++k) {
+    A.Pin[k] = h->scratch[k];
+    A.Uk[k] = h->scratch[k];
+    A.Ua[k] = nullptr;
+    A.Uo[k] = h->scratch[4 + k];
+  }
+  CK(launch(h, A));
+  // write the BC-filled ghosts back into the caller's primitive arrays (intent(inout))
+  const int4 bc = make_int4(h->cfg.bc[0], h->cfg.bc[1], h->cfg.bc[2], h->cfg.bc[3]);
+  const long long hld = h->ni + 2 * h->ng;
+  fill_ghosts_kernel<<<grid_for((long long)h->halo_elems), 256, 0, h->stream>>>(
+      h->ni, h->nj, h->pitch, h->ng, bc, h->scratch[0], h->scratch[1], h->scratch[2],
+      h->scratch[3], h->halo[0], h->halo[1], h->halo[2], h->halo[3], hld);
+  CK(cudaGetLastError());
+  for (int k = 0; k < 4; ++k)
+    CK(cudaMemcpy2DAsync(prim[k], (size_t)ld * sizeof(double), h->halo[k], (size_t)hld * sizeof(double),
+                         (size_t)hld * sizeof(double), (size_t)(h->nj + 2 * h->ng),
+                         cudaMemcpyDeviceToHost, h->stream));
+  double* dout[4] = {d_rho_dt, d_rho_u_dt, d_rho_v_dt, d_rho_E_dt};
+  for (int k = 0; k < 4; ++k) {
+    zero_host_field(h, dout[k], ld);
+    if ((rc = d2h_interior(h, dout[k], h->scratch[4 + k], ld))) return rc;
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  return CATO_OK;
+}
+
+int cato_gpu_interpolate_edges(cato_handle* h, const double* q, int64_t ld, double* i_edges,
+                               double* j_edges) {
+  if (!h) return CATO_ERR_ARG;
+  if (!q || !i_edges || !j_edges) return fail(h, CATO_ERR_ARG, "null pointer");
+  if (ld < h->ni + 2 * h->ng) return fail(h, CATO_ERR_ARG, "leading dimension too small");
+  int rc;
+  if ((rc = ensure_halo(h))) return rc;
+  const long long hld = h->ni + 2 * h->ng;
+  CK(cudaMemcpy2DAsync(h->halo[0], (size_t)hld * sizeof(double), q, (size_t)ld * sizeof(double),
+                       (size_t)hld * sizeof(double), (size_t)(h->nj + 2 * h->ng),
+                       cudaMemcpyHostToDevice, h->stream));
+  const size_t nie = 2 * (size_t)(h->ni + 2) * (h->nj + 1), nje = 2 * (size_t)(h->ni + 1) * (h->nj + 2);
+  double *die = nullptr, *dje = nullptr;
+  CK(cudaMallocAsync(&die, nie * sizeof(double), h->stream));
+  CK(cudaMallocAsync(&dje, nje * sizeof(double), h->stream));
+  CK(cudaMemsetAsync(die, 0, nie * sizeof(double), h->stream));
+  CK(cudaMemsetAsync(dje, 0, nje * sizeof(double), h->stream));
+  const long long ne = (long long)(h->ni + 1) * (h->nj + 1);
+  const int recon = recon_of(h->cfg.limiter);
+  if (recon == 0)
+    interp_edges_kernel<2, 0><<<grid_for(ne), 256, 0, h->stream>>>(h->ni, h->nj, h->cfg.limiter,
+                                                                   h->halo[0], hld, die, dje);
+  else if (recon == 3)
+    interp_edges_kernel<2, 3><<<grid_for(ne), 256, 0, h->stream>>>(h->ni, h->nj, h->cfg.limiter,
+                                                                   h->halo[0], hld, die, dje);
+  else
+    interp_edges_kernel<3, 5><<<grid_for(ne), 256, 0, h->stream>>>(h->ni, h->nj, h->cfg.limiter,
+                                                                   h->halo[0], hld, die, dje);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(i_edges, die, nie * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(j_edges, dje, nje * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaFreeAsync(die, h->stream));
+  CK(cudaFreeAsync(dje, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return CATO_OK;
+}
+
+int cato_gpu_status(cato_handle* h, int32_t* status_bits) {
+  if (!h || !status_bits) return CATO_ERR_ARG;
+  int rc = pull_ctl(h);
+  if (rc) return rc;
+  *status_bits = h->ctl_host->status;
+  return CATO_OK;
+}
+
+int cato_gpu_synchronize(cato_handle* h) {
+  if (!h) return CATO_ERR_ARG;
+  CK(cudaStreamSynchronize(h->stream));
+  return CATO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,174 @@
+// cato_kernels.cuh -- small kernels around the stage kernel: upload (primitive -> conserved with
+// the initial CFL dt), per-step control, derived-quantity download, ghost fill and the
+// stand-alone edge reconstruction.  Built with --fmad=false (FP64 reference arithmetic).
+#pragma once
+
+#include "cato_stage.cuh"
+
+namespace cato {
+
+// Device-resident step control: lets a chunk of steps run (and be captured in a CUDA graph)
+// without host round trips.  `active` gates every kernel of a step.
+struct StepCtl {
+  double dt;          // dt of the current step
+  double time;        // simulation time after the last active step
+  double t_end;       // stop once time >= t_end (main.f90:138)
+  double fixed_dt;    // > 0: use this dt instead of the CFL dt (use_constant_delta_t)
+  long long iter;     // iteration counter
+  long long max_iter; // stop once iter >= max_iter
+  unsigned long long dt_min;  // CFL dt of the current state (bits; ~0 = none)
+  int active;
+  int status;         // ST_* bits of the current state
+};
+
+__device__ __forceinline__ double decode_dt(unsigned long long b) {
+  return b == ~0ULL ? INFINITY : __longlong_as_double((long long)b);
+}
+
+// one thread: decide whether this step runs and with which dt (master_puppeteer.f90:155-200)
+__global__ void step_begin_kernel(StepCtl* c) {
+  int act = (c->status == 0) && (c->time < c->t_end) && (c->iter < c->max_iter);
+  c->active = act;
+  if (!act) return;
+  double dt = c->fixed_dt > 0.0 ? c->fixed_dt : decode_dt(c->dt_min);
+  c->dt = dt;
+  c->time = c->time + dt;
+  c->iter = c->iter + 1;
+  c->dt_min = ~0ULL;
+}
+
+// initialize_from_hdf5 + eos%primitive_to_conserved (equation_of_state.f90:316-324 through the
+// field operators) and the CFL dt of the raw primitives (mod_fluid.f90:249, 518-562).
+__global__ void upload_init_kernel(int ni, int nj, int pitch, double gamma, double cfl, double dx,
+                                   double dy, const double* __restrict__ r_,
+                                   const double* __restrict__ u_, const double* __restrict__ v_,
+                                   const double* __restrict__ p_, double* rho, double* rhou,
+                                   double* rhov, double* rhoE, StepCtl* ctl) {
+  const double EPS = Num<double>::eps, TINY = Num<double>::tiny;
+  const double g1 = gamma - 1.0, one_over_g1 = 1.0 / g1;
+  double dmin = INFINITY;
+  int st = 0;
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < (long long)ni * nj;
+       n += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(n % ni), j = (int)(n / ni);
+    const size_t idx = (size_t)j * pitch + i;
+    const double r = r_[idx], u = u_[idx], v = v_[idx], p = p_[idx];
+    rho[idx] = r;
+    rhou[idx] = u * r;
+    rhov[idx] = v * r;
+    double s = u * u + v * v;
+    if (abs_lt(s, EPS)) s = 0.0;
+    double E = p * one_over_g1 + (r * 0.5) * s;
+    if (abs_lt(E, EPS)) E = 0.0;
+    rhoE[idx] = E;
+    const double pr = abs_lt(p, TINY) ? 0.0 : p / r;
+    const double cs = sqrt(gamma * pr);
+    const double d = cfl / (((fabs(u) + cs) / dx) + ((fabs(v) + cs) / dy));
+    if (d < dmin) dmin = d;
+    if (isnan(r) || isnan(u) || isnan(v) || isnan(p)) st |= ST_NAN;
+    // initialize_from_hdf5 refuses ~0 density or pressure (mod_fluid.f90:352-360)
+    if (r < TINY) st |= ST_NEG_DENSITY;
+    if (p < TINY) st |= ST_NEG_PRESSURE;
+  }
+  unsigned long long bits = (dmin > 0.0) ? (unsigned long long)__double_as_longlong(dmin) : ~0ULL;
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long ob = __shfl_xor_sync(0xffffffffu, bits, o);
+    bits = ob < bits ? ob : bits;
+    st |= __shfl_xor_sync(0xffffffffu, st, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (bits != ~0ULL) atomicMin(&ctl->dt_min, bits);
+    if (st) atomicOr(&ctl->status, st);
+  }
+}
+
+// fluid_t's derived quantities for download: u, v, p, cs of the conserved state (FP64,
+// calculate_derived_quantities), or of the raw primitives before the first step.
+__global__ void derive_kernel(int ni, int nj, int pitch, double gamma, int raw,
+                              const double* __restrict__ a0, const double* __restrict__ a1,
+                              const double* __restrict__ a2, const double* __restrict__ a3,
+                              double* u, double* v, double* p, double* cs) {
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < (long long)ni * nj;
+       n += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(n % ni), j = (int)(n / ni);
+    const size_t idx = (size_t)j * pitch + i;
+    if (raw) {
+      const double r = a0[idx], pp = a3[idx];
+      u[idx] = a1[idx];
+      v[idx] = a2[idx];
+      p[idx] = pp;
+      const double pr = abs_lt(pp, Num<double>::tiny) ? 0.0 : pp / r;
+      cs[idx] = sqrt(gamma * pr);
+    } else {
+      double uu, vv, pp, cc;
+      prim_from_cons(gamma, gamma - 1.0, a0[idx], a1[idx], a2[idx], a3[idx], uu, vv, pp, cc);
+      u[idx] = uu;
+      v[idx] = vv;
+      p[idx] = pp;
+      cs[idx] = cc;
+    }
+  }
+}
+
+// Halo-padded primitive fields with every ghost cell filled by the boundary conditions, as after
+// flux_solver_t%apply_primitive_bc (flux_solver.f90:138-185).
+__global__ void fill_ghosts_kernel(int ni, int nj, int pitch, int ng, int4 bc,
+                                   const double* __restrict__ r_, const double* __restrict__ u_,
+                                   const double* __restrict__ v_, const double* __restrict__ p_,
+                                   double* ro, double* uo, double* vo, double* po, long long ld) {
+  const int W = ni + 2 * ng, H = nj + 2 * ng;
+  const int bcs[4] = {bc.x, bc.y, bc.z, bc.w};
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < (long long)W * H;
+       n += (long long)gridDim.x * blockDim.x) {
+    const int ii = (int)(n % W), jj = (int)(n / W);
+    bool fx, fy;
+    const int sx = map_index(ii - ng, ni, bcs[SIDE_MX], bcs[SIDE_PX], fx);
+    const int sy = map_index(jj - ng, nj, bcs[SIDE_MY], bcs[SIDE_PY], fy);
+    const size_t s = (size_t)sy * pitch + sx;
+    const size_t o = (size_t)jj * ld + ii;
+    ro[o] = r_[s];
+    uo[o] = fx ? -u_[s] : u_[s];
+    vo[o] = fy ? -v_[s] : v_[s];
+    po[o] = p_[s];
+  }
+}
+
+// muscl_interpolation_t%interpolate_edge_values on a halo-filled field q (ld = ni + 2 ng):
+// i_edges(1:2, -1:ni, 0:nj) and j_edges(1:2, 0:ni, -1:nj), both computed for i, j = 0..ni, 0..nj.
+template <int NG, int RECON>
+__global__ void interp_edges_kernel(int ni, int nj, int lim, const double* __restrict__ q,
+                                    long long ld, double* ie, double* je) {
+  auto Q = [&](int i, int j) -> double {  // reference (i, j), 1-based interior
+    return q[(size_t)(j + NG - 1) * ld + (i + NG - 1)];
+  };
+  const long long n_e = (long long)(ni + 1) * (nj + 1);
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < n_e;
+       n += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(n % (ni + 1)), j = (int)(n / (ni + 1));
+    double L, R;
+    // i-direction edge (i+1/2, j)
+    if (RECON == 0) {
+      recon_tvd2<double>(lim, Q(i - 1, j), Q(i, j), Q(i + 1, j), Q(i + 2, j), L, R);
+    } else {
+      recon_mlp<double, RECON>(RECON == 5 ? Q(i - 2, j) : 0.0, Q(i - 1, j), Q(i, j), Q(i + 1, j),
+                               Q(i + 2, j), RECON == 5 ? Q(i + 3, j) : 0.0, Q(i, j + 1),
+                               Q(i, j - 1), Q(i + 1, j + 1), Q(i + 1, j - 1), L, R);
+    }
+    const size_t oi = 2 * ((size_t)(i + 1) + (size_t)j * (ni + 2));
+    ie[oi] = L;
+    ie[oi + 1] = R;
+    // j-direction edge (i, j+1/2)
+    if (RECON == 0) {
+      recon_tvd2<double>(lim, Q(i, j - 1), Q(i, j), Q(i, j + 1), Q(i, j + 2), L, R);
+    } else {
+      recon_mlp<double, RECON>(RECON == 5 ? Q(i, j - 2) : 0.0, Q(i, j - 1), Q(i, j), Q(i, j + 1),
+                               Q(i, j + 2), RECON == 5 ? Q(i, j + 3) : 0.0, Q(i + 1, j),
+                               Q(i - 1, j), Q(i + 1, j + 1), Q(i - 1, j + 1), L, R);
+    }
+    const size_t oj = 2 * ((size_t)i + (size_t)(j + 1) * (ni + 1));
+    je[oj] = L;
+    je[oj + 1] = R;
+  }
+}
+
+}  // namespace cato

@@ -1,0 +1,386 @@
+// cato_stage.cuh -- the fused RK stage kernel: ghost-cell boundary conditions, primitive
+// recovery, MUSCL/MLP reconstruction, edge fluxes, flux divergence and the RK stage combine in
+// one pass over HBM, with the CFL dt min-reduction and the state checks fused into the last stage.
+//
+// Work decomposition ("marching strip"): a CTA of T threads owns a strip of W = T - 2*NG output
+// columns and marches over rows_per_cta rows.  Thread t always handles column x0 - NG + t, so a
+// row of primitives (T cells incl. the x-halo) is produced by one coalesced row load.  Shared
+// memory keeps a ring of the last 2*NG primitive rows, the i-edge fluxes of the current row and
+// the j-edge fluxes below/above it; each row costs two __syncthreads.  Every primitive is
+// computed once per stage (x-halo overhead 2*NG/T, y-halo 2*NG/rows_per_cta).
+//
+// Ghost cells are never stored: a ghost row/column index maps to its source interior cell
+// (zero-gradient copy, symmetry mirror with the normal velocity negated, periodic wrap).  This
+// reproduces the reference's sequential application (flux_solver.f90:138-185, zero_gradient
+// full-length rows incl. corners, periodic corners only when all four sides are periodic)
+// because for every valid side combination the final ghost value is that composition.
+#pragma once
+
+#include "cato_physics.cuh"
+
+namespace cato {
+
+struct StageArgs {
+  int ni, nj, pitch;       // interior cells, row pitch (elements) of the state arrays
+  int bc[4];               // by side: +x, +y, -x, -y
+  int limiter;             // TVD2 limiter id (runtime)
+  int rows_per_cta;
+  int kind;                // 0: out = U_a + L*c ; 1: out = (U_a*a + U_k*b) + L*c  (each '+'
+                           // flushed) ; 2: out = L (flux_solver_t%solve output, FP64 path)
+  int last;                // last stage of the step: emit the CFL dt and the state checks
+  double a, b, coef;       // c = coef * dt (the reference's (0.5_rk*dt), ((1/4)*dt), dt*alpha ...)
+  // FP64 path
+  const double* Uk[4];     // conserved state of this stage (stencil operand)
+  const double* Ua[4];     // U_a (pointwise operand; the step's U^n)
+  double* Uo[4];           // output conserved state
+  const double* Pin[4];    // when non-null: primitives to use as-is for this stage (after upload)
+  // mixed path: U^k = U_a + delta_k
+  const float* dk[4];      // delta_k (null for the first stage)
+  float* dout[4];          // delta_{k+1} (null on the last stage)
+  // device scalars
+  const double* dt;
+  const int* active;
+  unsigned long long* dt_min;  // bits of the smallest positive dt candidate (atomicMin)
+  int* status;
+  // physics
+  double gamma, cfl;
+  Geom G;
+};
+
+// Source interior index of (possibly ghost) index g in [-ng, n+ng) along an axis with
+// boundary types lo/hi; flip = the normal velocity component is negated (symmetry).
+__device__ __forceinline__ int map_index(int g, int n, int bc_lo, int bc_hi, bool& flip) {
+  flip = false;
+  if (g < 0) {
+    if (bc_lo == BC_PERIODIC) return max(n + g, 0);
+    if (bc_lo == BC_SYMMETRY) { flip = true; return min(-g - 1, n - 1); }
+    return 0;
+  }
+  if (g >= n) {
+    if (bc_hi == BC_PERIODIC) return min(g - n, n - 1);
+    if (bc_hi == BC_SYMMETRY) { flip = true; return max(2 * n - 1 - g, 0); }
+    return n - 1;
+  }
+  return g;
+}
+
+template <typename R> struct Cons4 { double q[4]; };
+
+// shared-memory accessor: ring[slot][var][col]
+template <typename R>
+__device__ __forceinline__ R& RQ(R* ring, int T, int slot, int var, int col) {
+  return ring[(slot * 4 + var) * T + col];
+}
+
+template <int RING> __device__ __forceinline__ int slot_of(int row) {
+  return (row + 4 * RING) % RING;  // rows are >= -NG
+}
+
+// ---------------------------------------------------------------------------------------------
+// one edge: reconstruct the four primitives from the ring and evaluate the flux
+// ---------------------------------------------------------------------------------------------
+template <typename R, int NG, int FLUX, int RECON, int DIR>
+__device__ __forceinline__ void edge_flux(const R* __restrict__ ring, int T, int lim, int row,
+                                          int col, const FluxConsts<R>& K, R F[4]) {
+  constexpr int RING = 2 * NG;
+  // stencil sample at normal offset n and tangential offset t from the edge's left cell
+  auto Q = [&](int var, int n, int t) -> R {
+    const int c = DIR == 0 ? col + n : col + t;
+    const int r = DIR == 0 ? row + t : row + n;
+    return ring[(slot_of<RING>(r) * 4 + var) * T + c];
+  };
+  R Lv[4], Rv[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (RECON == 0) {
+      recon_tvd2<R>(lim, Q(k, -1, 0), Q(k, 0, 0), Q(k, 1, 0), Q(k, 2, 0), Lv[k], Rv[k]);
+    } else {
+      R qm2 = RECON == 5 ? Q(k, -2, 0) : R(0), qp3 = RECON == 5 ? Q(k, 3, 0) : R(0);
+      recon_mlp<R, RECON>(qm2, Q(k, -1, 0), Q(k, 0, 0), Q(k, 1, 0), Q(k, 2, 0), qp3, Q(k, 0, 1),
+                          Q(k, 0, -1), Q(k, 1, 1), Q(k, 1, -1), Lv[k], Rv[k]);
+    }
+  }
+  Prim<R> A = {Lv[0], Lv[1], Lv[2], Lv[3]}, B = {Rv[0], Rv[1], Rv[2], Rv[3]};
+  // cell pressures in reference (i, j) terms: P(di, dj) = p(i+di, j+dj), (i, j) = left cell
+  auto P = [&](int di, int dj) -> R { return DIR == 0 ? Q(3, di, dj) : Q(3, dj, di); };
+  if (FLUX == FLUX_AUSMPW) {
+    R pc[4];
+    if (DIR == 0) { pc[0] = P(0, -1); pc[1] = P(1, -1); pc[2] = P(0, 1); pc[3] = P(1, 1); }
+    else { pc[0] = P(1, 0); pc[1] = P(1, 1); pc[2] = P(-1, 0); pc[3] = P(-1, 1); }
+    flux_ausmpw<R, DIR>(K, A, B, pc, F);
+  } else if (FLUX == FLUX_SLAU || FLUX == FLUX_SLAU2 || FLUX == FLUX_SD_SLAU ||
+             FLUX == FLUX_SD_SLAU2) {
+    R pa[6], pb[6];
+    if (FLUX == FLUX_SD_SLAU || FLUX == FLUX_SD_SLAU2) {
+      if (DIR == 0) {  // slau_solver.fypp:410-417
+        pa[0] = P(0, 1);  pb[0] = P(0, 0);
+        pa[1] = P(-1, 0); pb[1] = P(0, 0);
+        pa[2] = P(0, -1); pb[2] = P(0, 0);
+        pa[3] = P(1, -1); pb[3] = P(1, 0);
+        pa[4] = P(2, 0);  pb[4] = P(1, 0);
+        pa[5] = P(1, 1);  pb[5] = P(1, 0);
+      } else {         // slau_solver.fypp:421-428
+        pa[0] = P(-1, 0); pb[0] = P(0, 0);
+        pa[1] = P(0, -1); pb[1] = P(0, 0);
+        pa[2] = P(1, 0);  pb[2] = P(0, 0);
+        pa[3] = P(1, 1);  pb[3] = P(0, 1);
+        pa[4] = P(0, 2);  pb[4] = P(0, 1);
+        pa[5] = P(-1, 1); pb[5] = P(0, 1);
+      }
+    }
+    flux_slau<R, DIR, FLUX>(K, A, B, pa, pb, F);
+  } else if (FLUX == FLUX_ROE) {
+    R fa[5], fb[5];
+    if (DIR == 0) {  // roe_solver.fypp:496-500
+      fa[0] = P(0, 0); fb[0] = P(1, 0);
+      fa[1] = P(0, 0); fb[1] = P(0, 1);
+      fa[2] = P(0, 0); fb[2] = P(0, -1);
+      fa[3] = P(0, 1); fb[3] = P(1, 1);
+      fa[4] = P(0, -1); fb[4] = P(1, -1);
+    } else {         // roe_solver.fypp:502-506
+      fa[0] = P(0, 0); fb[0] = P(0, 1);
+      fa[1] = P(0, 0); fb[1] = P(-1, 0);
+      fa[2] = P(0, 0); fb[2] = P(1, 0);
+      fa[3] = P(0, 1); fb[3] = P(-1, 1);
+      fa[4] = P(0, 1); fb[4] = P(1, 1);
+    }
+    flux_roe<R, DIR>(K, A, B, fa, fb, F);
+  } else if (FLUX == FLUX_AUSM_UP) {
+    flux_ausm_up<R, DIR>(K, A, B, F);
+  } else {
+    flux_hllc<R, DIR>(K, A, B, F);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// primitive row load
+// ---------------------------------------------------------------------------------------------
+struct RowSrc {
+  double c[4];  // conserved (or raw primitives) as loaded
+  float d[4];   // mixed path delta_k
+  bool flipy;
+};
+
+template <typename R>
+__device__ __forceinline__ void load_src(const StageArgs& A, int sx, int row, RowSrc& s) {
+  bool fy;
+  const int sy = map_index(row, A.nj, A.bc[SIDE_MY], A.bc[SIDE_PY], fy);
+  s.flipy = fy;
+  const size_t idx = (size_t)sy * A.pitch + sx;
+  if (A.Pin[0]) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) s.c[k] = __ldg(A.Pin[k] + idx);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) s.c[k] = __ldg(A.Uk[k] + idx);
+  }
+  if (sizeof(R) == 4) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) s.d[k] = A.dk[0] ? __ldg(A.dk[k] + idx) : 0.0f;
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void src_to_prim(const StageArgs& A, const RowSrc& s, bool flipx,
+                                            R g, R g1, R out[4]) {
+  R r, u, v, p;
+  if (sizeof(R) == 8) {
+    if (A.Pin[0]) {
+      r = (R)s.c[0]; u = (R)s.c[1]; v = (R)s.c[2]; p = (R)s.c[3];
+    } else {
+      R cs;
+      r = (R)s.c[0];
+      prim_from_cons(g, g1, r, (R)s.c[1], (R)s.c[2], (R)s.c[3], u, v, p, cs);
+    }
+  } else {
+    float c0 = d2f_int(s.c[0]), c1 = d2f_int(s.c[1]), c2 = d2f_int(s.c[2]), c3 = d2f_int(s.c[3]);
+    if (A.Pin[0]) {
+      r = c0; u = c1; v = c2; p = c3;
+    } else {
+      R cs;
+      r = c0 + s.d[0];
+      prim_from_cons(g, g1, r, (R)(c1 + s.d[1]), (R)(c2 + s.d[2]), (R)(c3 + s.d[3]), u, v, p,
+                     cs);
+    }
+  }
+  out[0] = r;
+  out[1] = flipx ? -u : u;
+  out[2] = s.flipy ? -v : v;
+  out[3] = p;
+}
+
+// ---------------------------------------------------------------------------------------------
+// the kernel
+// ---------------------------------------------------------------------------------------------
+template <typename R, int NG, int FLUX, int RECON>
+__global__ void __launch_bounds__(256) stage_kernel(const StageArgs A, const FluxConsts<R> K) {
+  if (A.active && *A.active == 0) return;
+  constexpr int RING = 2 * NG;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int T = blockDim.x, W = T - 2 * NG, t = threadIdx.x;
+  const int x0 = blockIdx.x * W;
+  const int gx = x0 - NG + t;
+  const int y0 = blockIdx.y * A.rows_per_cta;
+  const int y1 = min(y0 + A.rows_per_cta, A.nj);
+  R* ring = reinterpret_cast<R*>(smem_raw);  // [RING][4][T]
+  R* sfi = ring + RING * 4 * T;              // [4][T]   i-edge between cols t and t+1
+  R* sfj = sfi + 4 * T;                      // [2][4][T] j-edge between rows j and j+1 at slot j&1
+
+  const R g = R(A.gamma), g1 = R(A.gamma - 1.0);
+  bool flipx;
+  const int sx = map_index(min(gx, A.ni + NG - 1), A.ni, A.bc[SIDE_MX], A.bc[SIDE_PX], flipx);
+  const bool in_i_edge = (t >= NG - 1) && (t <= NG + W - 1) && (gx <= A.ni - 1);
+  const bool in_cell = (t >= NG) && (t <= NG + W - 1) && (gx < A.ni);
+  const double dt = *A.dt;
+  const double cc = A.coef * dt;
+
+  // prologue: rows y0-NG .. y0+NG-1
+  for (int r = y0 - NG; r < y0 + NG; ++r) {
+    RowSrc s;
+    load_src<R>(A, sx, r, s);
+    R q[4];
+    src_to_prim<R>(A, s, flipx, g, g1, q);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) RQ(ring, T, slot_of<RING>(r), k, t) = q[k];
+  }
+  __syncthreads();
+  if (in_cell && y0 < y1) {
+    R F[4];
+    edge_flux<R, NG, FLUX, RECON, 1>(ring, T, A.limiter, y0 - 1, t, K, F);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) sfj[(((y0 - 1) & 1) * 4 + k) * T + t] = F[k];
+  }
+  __syncthreads();
+
+  RowSrc pre;
+  if (y0 < y1) load_src<R>(A, sx, y0 + NG, pre);
+
+  double dt_loc = INFINITY;
+  int st_loc = 0;
+
+  for (int j = y0; j < y1; ++j) {
+    // operands of this row's cell update, issued early
+    const size_t cidx = (size_t)j * A.pitch + (size_t)min(max(gx, 0), A.ni - 1);
+    double ua[4], uk[4];
+    float dk[4];
+    if (in_cell) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        ua[k] = A.Ua[k] ? A.Ua[k][cidx] : 0.0;  // may alias Uo: plain load, read before write
+        uk[k] = (sizeof(R) == 8 && A.kind == 1) ? __ldg(A.Uk[k] + cidx) : 0.0;
+        dk[k] = (sizeof(R) == 4 && A.dk[0]) ? __ldg(A.dk[k] + cidx) : 0.0f;
+      }
+    }
+    RowSrc nxt;
+    if (j + 1 < y1) load_src<R>(A, sx, j + 1 + NG, nxt);
+    {
+      R q[4];
+      src_to_prim<R>(A, pre, flipx, g, g1, q);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) RQ(ring, T, slot_of<RING>(j + NG), k, t) = q[k];
+    }
+    pre = nxt;
+    __syncthreads();
+    if (in_i_edge) {
+      R F[4];
+      edge_flux<R, NG, FLUX, RECON, 0>(ring, T, A.limiter, j, t, K, F);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) sfi[k * T + t] = F[k];
+    }
+    if (in_cell) {
+      R F[4];
+      edge_flux<R, NG, FLUX, RECON, 1>(ring, T, A.limiter, j, t, K, F);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) sfj[((j & 1) * 4 + k) * T + t] = F[k];
+    }
+    __syncthreads();
+    if (in_cell) {
+      double un[4];
+      if (sizeof(R) == 8) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          double Fi = (double)sfi[k * T + t], Fim = (double)sfi[k * T + t - 1];
+          double Fj = (double)sfj[((j & 1) * 4 + k) * T + t];
+          double Fjm = (double)sfj[(((j - 1) & 1) * 4 + k) * T + t];
+          double L = divergence_fp64(Fi, Fim, Fj, Fjm, A.G);
+          double r;
+          if (A.kind == 2) {
+            r = L;
+          } else if (A.kind == 0) {
+            r = ua[k] + L * cc;
+            if (abs_lt(r, Num<double>::eps)) r = 0.0;
+          } else {
+            double s = ua[k] * A.a + uk[k] * A.b;
+            if (abs_lt(s, Num<double>::eps)) s = 0.0;
+            r = s + L * cc;
+            if (abs_lt(r, Num<double>::eps)) r = 0.0;
+          }
+          un[k] = r;
+          A.Uo[k][cidx] = r;
+        }
+      } else {
+        const float ccf = (float)cc, bf = (float)A.b;
+        const float idx_f = (float)(1.0 / A.G.dx), idy_f = (float)(1.0 / A.G.dy);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          float Fi = (float)sfi[k * T + t], Fim = (float)sfi[k * T + t - 1];
+          float Fj = (float)sfj[((j & 1) * 4 + k) * T + t];
+          float Fjm = (float)sfj[(((j - 1) & 1) * 4 + k) * T + t];
+          float L = -((Fi - Fim) * idx_f + (Fj - Fjm) * idy_f);
+          float dn = (A.dk[0] ? bf * dk[k] : 0.0f) + L * ccf;
+          if (A.last) {
+            un[k] = ua[k] + f2d_int(dn);
+            A.Uo[k][cidx] = un[k];
+          } else {
+            A.dout[k][cidx] = dn;
+          }
+        }
+      }
+      if (A.last) {
+        // CFL dt of the new state (get_timestep, mod_fluid.f90:554-558) and the sanity checks
+        if (sizeof(R) == 8) {
+          double u, v, p, cs;
+          prim_from_cons(A.gamma, A.gamma - 1.0, un[0], un[1], un[2], un[3], u, v, p, cs);
+          double d = A.cfl / (((fabs(u) + cs) / A.G.dx) + ((fabs(v) + cs) / A.G.dy));
+          if (d < dt_loc) dt_loc = d;
+          if (isnan(un[0]) || isnan(u) || isnan(v) || isnan(p)) st_loc |= ST_NAN;
+          if (un[0] < 0.0) st_loc |= ST_NEG_DENSITY;
+          if (p < 0.0) st_loc |= ST_NEG_PRESSURE;
+        } else {
+          float r = d2f_int(un[0]), u, v, p, cs;
+          prim_from_cons((float)A.gamma, (float)(A.gamma - 1.0), r, d2f_int(un[1]),
+                         d2f_int(un[2]), d2f_int(un[3]), u, v, p, cs);
+          float d = (float)A.cfl /
+                    ((fabsf(u) + cs) * (float)(1.0 / A.G.dx) + (fabsf(v) + cs) * (float)(1.0 / A.G.dy));
+          double dd = f2d_int(d);
+          if (dd < dt_loc) dt_loc = dd;
+          if (isnan(r) || isnan(u) || isnan(v) || isnan(p)) st_loc |= ST_NAN;
+          if (r < 0.0f) st_loc |= ST_NEG_DENSITY;
+          if (p < 0.0f) st_loc |= ST_NEG_PRESSURE;
+        }
+      }
+    }
+  }
+
+  if (A.last) {
+    // block min of dt (bits of positive doubles order as unsigned integers) and status OR
+    unsigned long long bits =
+        (dt_loc > 0.0) ? (unsigned long long)__double_as_longlong(dt_loc) : ~0ULL;
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long ob = __shfl_xor_sync(0xffffffffu, bits, o);
+      bits = ob < bits ? ob : bits;
+      st_loc |= __shfl_xor_sync(0xffffffffu, st_loc, o);
+    }
+    if ((t & 31) == 0) {
+      if (bits != ~0ULL) atomicMin(A.dt_min, bits);
+      if (st_loc) atomicOr(A.status, st_loc);
+    }
+  }
+}
+
+// dynamic shared memory of one CTA
+template <typename R> inline size_t stage_smem_bytes(int T, int ng) {
+  return sizeof(R) * (size_t)T * (2 * ng * 4 + 4 + 8);
+}
+
+}  // namespace cato

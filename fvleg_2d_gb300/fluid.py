@@ -1,0 +1,167 @@
+"""Host-side mirror of the reference's interfaces for the time-step hot path.
+
+* :class:`Fluid`          -- ``fluid_t`` (``src/lib/fluid/mod_fluid.f90:68-141``): ``integrate``,
+  ``get_timestep``, ``set_time``, ``t`` (time derivative) and the conserved/derived fields.
+* :class:`FluxSolver`     -- ``flux_solver_t%solve`` (``src/lib/flux_solvers/flux_solver.f90:66-87``).
+* :class:`MusclInterpolator` -- ``muscl_interpolation_t%interpolate_edge_values``
+  (``src/lib/spatial_reconstruction/muscl_interpolation.f90:37-43``).
+
+All arithmetic runs on the GPU through ``libcato_gpu.so``; these classes only move arrays across
+the C-ABI.  Where the reference stops the program (``error stop``), these raise
+:class:`CatoError` carrying the reference's error code.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .config import STATUS_NAMES, SchemeConfig
+
+
+class CatoError(RuntimeError):
+    def __init__(self, code: int, message: str = ""):
+        self.code = code
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {message}".rstrip(": "))
+
+
+def _check(rc: int, h=None, what: str = ""):
+    if rc != 0:
+        msg = ""
+        if h is not None:
+            m = _lib.load().cato_gpu_last_error(h)
+            msg = m.decode() if m else ""
+        raise CatoError(rc, f"{what} {msg}".strip())
+
+
+def _field(cfg: SchemeConfig) -> np.ndarray:
+    return np.zeros(cfg.halo_shape, dtype=np.float64, order="F")
+
+
+def _as_field(cfg: SchemeConfig, a) -> np.ndarray:
+    a = np.asfortranarray(a, dtype=np.float64)
+    if a.shape != cfg.halo_shape:
+        raise ValueError(f"field shape {a.shape} != halo-padded shape {cfg.halo_shape}")
+    return a
+
+
+class _Handle:
+    def __init__(self, cfg: SchemeConfig):
+        self.cfg = cfg
+        self.L = _lib.load()
+        self._c = cfg.to_c()
+        h = ctypes.c_void_p()
+        _check(self.L.cato_gpu_create(ctypes.byref(self._c), ctypes.byref(h)), None,
+               "cato_gpu_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cato_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def ld(self) -> int:
+        return self.cfg.halo_shape[0]
+
+
+class Fluid(_Handle):
+    """fluid_t on the GPU.  ``Fluid(cfg).initialize(rho, u, v, p)`` replaces
+    fluid_t%initialize + initialize_from_hdf5 (mod_fluid.f90:159-381)."""
+
+    def initialize(self, rho, u, v, p) -> "Fluid":
+        arrs = [_as_field(self.cfg, a) for a in (rho, u, v, p)]
+        _check(self.L.cato_gpu_upload_primitive(self.h, *(_lib.ptr(a) for a in arrs), self.ld),
+               self.h, "initialize")
+        return self
+
+    def get_timestep(self) -> float:
+        dt = ctypes.c_double()
+        _check(self.L.cato_gpu_get_timestep(self.h, ctypes.byref(dt)), self.h, "get_timestep")
+        return dt.value
+
+    def integrate(self, dt: float | None = None) -> tuple[float, int]:
+        """One time step; dt=None uses the CFL dt (master_puppeteer.f90:166-170).
+        Returns (dt taken, error_code)."""
+        used = ctypes.c_double()
+        ec = ctypes.c_int32()
+        _check(self.L.cato_gpu_integrate(self.h, float(dt) if dt else 0.0, ctypes.byref(used),
+                                         ctypes.byref(ec)), self.h, "integrate")
+        return used.value, ec.value
+
+    def run(self, t_end: float, max_iterations: int = -1) -> int:
+        """The main.f90:138-198 time loop (CFL dt each step, no last-step trim) on the device.
+        Returns the number of steps; raises CatoError on a fluid error code."""
+        steps = ctypes.c_int64()
+        t = ctypes.c_double()
+        ec = ctypes.c_int32()
+        _check(self.L.cato_gpu_run(self.h, int(max_iterations), float(t_end), ctypes.byref(steps),
+                                   ctypes.byref(t), ctypes.byref(ec)), self.h, "run")
+        if ec.value:
+            raise CatoError(ec.value, f"after {steps.value} steps at t={t.value}")
+        return steps.value
+
+    def set_time(self, time: float, iteration: int) -> None:
+        _check(self.L.cato_gpu_set_time(self.h, float(time), int(iteration)), self.h, "set_time")
+
+    @property
+    def time(self) -> float:
+        t = ctypes.c_double()
+        _check(self.L.cato_gpu_get_time(self.h, ctypes.byref(t), None, None), self.h)
+        return t.value
+
+    @property
+    def iteration(self) -> int:
+        it = ctypes.c_int64()
+        _check(self.L.cato_gpu_get_time(self.h, None, ctypes.byref(it), None), self.h)
+        return it.value
+
+    def state(self, names=("rho", "rho_u", "rho_v", "rho_E", "u", "v", "p", "cs")) -> dict:
+        """Download conserved and derived fields (halo-padded, ghosts zero)."""
+        all_names = ("rho", "rho_u", "rho_v", "rho_E", "u", "v", "p", "cs")
+        out = {k: (_field(self.cfg) if k in names else None) for k in all_names}
+        _check(self.L.cato_gpu_download(self.h, *(_lib.ptr(out[k]) for k in all_names), self.ld),
+               self.h, "download")
+        return {k: v for k, v in out.items() if v is not None}
+
+    def t(self):
+        """Time derivative of the current state (fluid_t%t, mod_fluid.f90:460-516)."""
+        s = self.state(("rho", "u", "v", "p"))
+        return FluxSolver(self.cfg).solve(s["rho"], s["u"], s["v"], s["p"])
+
+
+class FluxSolver(_Handle):
+    """flux_solver_t%solve for the configured flux / limiter / boundary conditions."""
+
+    def solve(self, rho, u, v, p, dt: float = 0.0):
+        """Returns (d_rho_dt, d_rho_u_dt, d_rho_v_dt, d_rho_E_dt), halo-padded with zero ghosts.
+        The boundary conditions are written into the ghosts of rho/u/v/p when they are
+        Fortran-ordered float64 arrays of the halo-padded shape (intent(inout))."""
+        prims = [_as_field(self.cfg, a) for a in (rho, u, v, p)]
+        outs = [_field(self.cfg) for _ in range(4)]
+        _check(self.L.cato_gpu_solve(self.h, *(_lib.ptr(a) for a in prims),
+                                     *(_lib.ptr(a) for a in outs), self.ld), self.h, "solve")
+        for src, dst in zip(prims, (rho, u, v, p)):
+            if src is not dst and isinstance(dst, np.ndarray) and dst.shape == src.shape:
+                dst[...] = src
+        return tuple(outs)
+
+
+class MusclInterpolator(_Handle):
+    """interpolate_edge_values(q) -> (i_edges(2, -1:ni, 0:nj), j_edges(2, 0:ni, -1:nj))."""
+
+    def interpolate_edge_values(self, q):
+        q = _as_field(self.cfg, q)
+        ni, nj = self.cfg.ni, self.cfg.nj
+        ie = np.zeros((2, ni + 2, nj + 1), order="F")
+        je = np.zeros((2, ni + 1, nj + 2), order="F")
+        _check(self.L.cato_gpu_interpolate_edges(self.h, _lib.ptr(q), self.ld, _lib.ptr(ie),
+                                                 _lib.ptr(je)), self.h, "interpolate_edge_values")
+        return ie, je

@@ -1,0 +1,187 @@
+/*
+ * cato_gpu.h -- C-ABI of the GB300 (sm_103a) implementation of CATO's time-step hot path.
+ *
+ * One handle is one 2-D structured grid instance whose state lives in device memory (HBM)
+ * between calls.  Host arrays crossing this boundary use the reference's field_2d_t layout:
+ * real64, Fortran column-major (i fastest), halo-padded with bounds
+ * (1-n_ghost : ni+n_ghost, 1-n_ghost : nj+n_ghost)   [src/lib/field/field_2d.f90:58-64].
+ * A pointer argument points at element (1-n_ghost, 1-n_ghost); `ld` is the leading dimension
+ * (>= ni + 2*n_ghost).  Only interior cells are read on upload.
+ *
+ * Every entry point returns CATO_OK (0) or a negative-free error code and never aborts; the
+ * reference instead stops the program (`error stop`, src/lib/error.f90:33-35).  A handle is
+ * used by one host thread at a time; different handles are independent (no global state: the
+ * reference's singleton EOS, src/lib/equation_of_state.f90:70, becomes per-handle gamma).
+ */
+#ifndef CATO_GPU_H
+#define CATO_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Return / error codes.  1..3 are the reference's fluid error codes (src/lib/error.f90:6-9). */
+enum cato_status {
+  CATO_OK = 0,
+  CATO_NEG_DENSITY = 1,
+  CATO_NEG_PRESSURE = 2,
+  CATO_NANS_FOUND = 3,
+  CATO_ERR_CONFIG = 10,   /* invalid configuration (unknown flux/limiter, bad ghost count, ...) */
+  CATO_ERR_OOM = 11,      /* device allocation failed */
+  CATO_ERR_CUDA = 12,     /* CUDA runtime error (message via cato_gpu_last_error) */
+  CATO_ERR_ARG = 13,      /* bad argument (null pointer, too-small leading dimension, ...) */
+  CATO_ERR_TIMEOUT = 14,  /* a bounded device-side wait gave up */
+  CATO_ERR_STATE = 15     /* call out of order (e.g. integrate before upload) */
+};
+
+/* Flux solvers.  Names as accepted by the reference deck key [scheme] flux_solver
+ * (src/lib/fluid/mod_fluid.f90:223-238); AUSM+-up and HLLC have no runnable reference. */
+enum cato_flux {
+  CATO_FLUX_AUSMPW_PLUS = 0,  /* 'AUSMPW+'   ausmpw_plus_solver.fypp:214-463 */
+  CATO_FLUX_SLAU = 1,         /* 'SLAU'      slau_solver.fypp:253-494 */
+  CATO_FLUX_SLAU2 = 2,        /* 'SLAU2' */
+  CATO_FLUX_SD_SLAU = 3,      /* 'SD-SLAU' */
+  CATO_FLUX_SD_SLAU2 = 4,     /* 'SD-SLAU2' */
+  CATO_FLUX_ROE = 5,          /* 'Roe'       roe_solver.fypp:229-515 */
+  CATO_FLUX_AUSM_PLUS_UP = 6, /* 'AUSM+-up'  ausm_plus_solver.f90:394-643 (driver restated) */
+  CATO_FLUX_HLLC = 7          /* 'HLLC'      Toro HLLC, PVRS wave speeds (reference is a stub) */
+};
+
+/* Edge reconstruction (src/lib/spatial_reconstruction/muscl_factory.f90:54-94). */
+enum cato_limiter {
+  CATO_LIM_MINMOD = 0,   /* muscl_tvd2.fypp:195-197 */
+  CATO_LIM_SUPERBEE = 1, /* muscl_tvd2.fypp:197-199 */
+  CATO_LIM_VAN_LEER = 2, /* muscl_tvd2.fypp:199-200 */
+  CATO_LIM_MLP3 = 3,     /* muscl_mlp.fypp, ORDER=3 */
+  CATO_LIM_MLP5 = 4      /* muscl_mlp.fypp, ORDER=5, needs n_ghost = 3 */
+};
+
+/* Time integration ([time] integration_strategy, mod_fluid.f90:424-446). */
+enum cato_rk {
+  CATO_RK_SSP2 = 0,  /* 'ssp_rk2'             mod_fluid.f90:1081-1160 */
+  CATO_RK_SSP3 = 1,  /* 'ssp_rk3'|'ssp_rk33'  mod_fluid.f90:739-854 */
+  CATO_RK_1_3 = 2,   /* 'rk(1,3)'  low-storage family, mod_fluid.f90:889-1007 */
+  CATO_RK_1_4 = 3,
+  CATO_RK_1_5 = 4,
+  CATO_RK_2_3 = 5,
+  CATO_RK_2_4 = 6,
+  CATO_RK_2_5 = 7
+};
+
+/* Boundary conditions (src/lib/boundary_conditions/bc_factory.f90:39-66). */
+enum cato_bc {
+  CATO_BC_ZERO_GRADIENT = 0, /* priority 1, zero_gradient_bc.f90:54-121 */
+  CATO_BC_SYMMETRY = 1,      /* priority 1, symmetry_bc.f90:56-133 */
+  CATO_BC_PERIODIC = 2       /* priority 2, periodic_bc.fypp:78-283 */
+};
+
+/* Sides in the reference's application order within one priority (flux_solver.f90:165-183). */
+enum cato_side { CATO_PLUS_X = 0, CATO_PLUS_Y = 1, CATO_MINUS_X = 2, CATO_MINUS_Y = 3 };
+
+enum cato_precision {
+  CATO_FP64 = 0,   /* the drop-in path: IEEE FP64 throughout, reference operation order */
+  CATO_MIXED = 1   /* FP32 reconstruction + flux arithmetic, FP64 conserved state and RK update */
+};
+
+enum cato_roe_fix {
+  CATO_ROE_REFERENCE = 0, /* as built: no entropy fix (roe_solver.fypp:460-465 commented) */
+  CATO_ROE_HARTEN = 1     /* Harten fix of roe_solver.fypp:529-536 with delta = harten_delta * c~ */
+};
+
+typedef struct cato_config {
+  int32_t ni, nj;             /* interior cells in i (x) and j (y) */
+  int32_t n_ghost;            /* ghost layers: 2, or 3 for MLP5 (mod_input.f90:320-338) */
+  int32_t flux;               /* enum cato_flux */
+  int32_t limiter;            /* enum cato_limiter */
+  int32_t rk;                 /* enum cato_rk */
+  int32_t bc[4];              /* enum cato_bc, indexed by enum cato_side */
+  int32_t apply_low_mach_fix; /* AUSMPW+ low-Mach fix; reference default true (mod_input.f90:134) */
+  int32_t precision;          /* enum cato_precision */
+  int32_t roe_entropy_fix;    /* enum cato_roe_fix */
+  int32_t reserved0;
+  double gamma;               /* [physics] polytropic_index */
+  double cfl;                 /* [time] cfl */
+  double dx, dy;              /* uniform Cartesian cell size (geometry of quad_cell.f90:69-229) */
+  double harten_delta;        /* Harten delta coefficient (CATO_ROE_HARTEN only) */
+  double ausm_beta;           /* [ausm] beta, default 1/8 */
+  double ausm_kp;             /* [ausm] pressure_diffusion_coeff, default 0.25 */
+  double ausm_ku;             /* K_u, default 0.75 (not read from the deck by the reference) */
+  double ausm_sigma;          /* [ausm] sonic_point_sigma, default 1 */
+} cato_config;
+
+typedef struct cato_handle cato_handle;
+
+/* Library version string. */
+const char* cato_gpu_version(void);
+
+/* Fill `cfg` with the reference's deck defaults (mod_input.f90:34-148) for an ni x nj grid. */
+int cato_config_default(cato_config* cfg, int32_t ni, int32_t nj);
+
+/* Validate a configuration without touching the GPU; returns CATO_OK or CATO_ERR_CONFIG. */
+int cato_config_check(const cato_config* cfg);
+
+/* Create / destroy a grid instance.  Replaces fluid_t%initialize + flux_solver_t%initialize
+ * (mod_fluid.f90:159-254, flux_solver.f90:89-95).  Allocates the device state. */
+int cato_gpu_create(const cato_config* cfg, cato_handle** out);
+int cato_gpu_destroy(cato_handle* h);
+
+/* Last error message of this handle (empty string if none). */
+const char* cato_gpu_last_error(const cato_handle* h);
+
+/* Upload primitive initial conditions (rho, u, v, p; interior of halo-padded arrays).
+ * Replaces fluid_t%initialize_from_hdf5 + eos%primitive_to_conserved (mod_fluid.f90:339-363):
+ * the conserved state is derived on the device; the first stage uses these primitives as is. */
+int cato_gpu_upload_primitive(cato_handle* h, const double* rho, const double* u,
+                              const double* v, const double* p, int64_t ld);
+
+/* CFL time step of the current state.  Replaces fluid_t%get_timestep (mod_fluid.f90:518-562). */
+int cato_gpu_get_timestep(cato_handle* h, double* dt);
+
+/* Advance one time step.  Replaces fluid_t%integrate (mod_fluid.f90:411-450) as called by
+ * master_puppeteer_t%integrate (master_puppeteer.f90:155-200): with dt <= 0 the CFL dt of the
+ * current state is used (computed on the device), otherwise the given dt.  On return *dt_used
+ * (may be NULL) holds the dt taken and *error_code (may be NULL) the fluid error code. */
+int cato_gpu_integrate(cato_handle* h, double dt, double* dt_used, int32_t* error_code);
+
+/* Run the time loop of src/main.f90:138-198 on the device without per-step host round trips:
+ * CFL dt every step, stop once time >= t_end or after max_steps steps (no last-step trim).
+ * Steps run in CUDA-graph chunks; the stop test is evaluated on the device. */
+int cato_gpu_run(cato_handle* h, int64_t max_steps, double t_end, int64_t* steps_done,
+                 double* time, int32_t* error_code);
+
+/* Time bookkeeping (fluid_t%set_time, mod_fluid.f90:400-409). */
+int cato_gpu_set_time(cato_handle* h, double time, int64_t iteration);
+int cato_gpu_get_time(cato_handle* h, double* time, int64_t* iteration, double* last_dt);
+
+/* Download state into halo-padded host arrays (interior written, ghosts set to 0).  Any pointer
+ * may be NULL.  u, v, p, cs are fluid_t's derived quantities (mod_fluid.f90:564-591). */
+int cato_gpu_download(cato_handle* h, double* rho, double* rho_u, double* rho_v, double* rho_E,
+                      double* u, double* v, double* p, double* cs, int64_t ld);
+
+/* flux_solver_t%solve (flux_solver.f90:66-87) on caller-given primitive fields: applies the BCs
+ * to the ghosts of rho/u/v/p (written back, as the reference's intent(inout)), reconstructs,
+ * computes edge fluxes and the flux divergence into d_*_dt (halo-padded, ghosts zeroed as in
+ * flux_solver.f90:433-457).  Uses the handle's scheme; does not change the handle's state. */
+int cato_gpu_solve(cato_handle* h, double* rho, double* u, double* v, double* p,
+                   double* d_rho_dt, double* d_rho_u_dt, double* d_rho_v_dt, double* d_rho_E_dt,
+                   int64_t ld);
+
+/* muscl_interpolation_t%interpolate_edge_values (muscl_interpolation.f90:37-43) for one field
+ * q whose ghosts are already filled.  Output layouts are the reference's:
+ * i_edges(1:2, -1:ni, 0:nj) and j_edges(1:2, 0:ni, -1:nj), Fortran order, (1)=L (2)=R. */
+int cato_gpu_interpolate_edges(cato_handle* h, const double* q, int64_t ld,
+                               double* i_edges, double* j_edges);
+
+/* Current device status word (bit 0: negative density, bit 1: negative pressure, bit 2: NaN). */
+int cato_gpu_status(cato_handle* h, int32_t* status_bits);
+
+/* Synchronise the handle's stream. */
+int cato_gpu_synchronize(cato_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CATO_GPU_H */

@@ -1,0 +1,1144 @@
+/*
+ * cato_oracle.c -- TEST INFRASTRUCTURE ONLY: the parity oracle.
+ *
+ * A plain-C CPU restatement of the reference (smillerc/fvleg_2d, "CATO", Fortran 2018) FP64
+ * time-step arithmetic for the hot path: primitive recovery, ghost-cell boundary conditions,
+ * MUSCL TVD2 / MLP edge reconstruction, the AUSMPW+, SLAU family and Roe edge fluxes, the flux
+ * divergence, the SSP-RK / rk(m,n) stage updates and the CFL time step.  Every function cites
+ * the reference file:line it follows (paths relative to the reference repository root).
+ * Operation order follows Fortran's left-to-right evaluation of each source expression, the
+ * field operators' interior-only semantics and their epsilon flushes; build with
+ * -ffp-contract=off so that no multiply-add is fused.
+ *
+ * AUSM+-up (driver), HLLC, the van Leer limiter and the Harten entropy fix have no runnable
+ * reference code (see cato_gpu.h); their restatements here are marked "unpinned".
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this library; the
+ * product (fvleg_2d_gb300/) never loads it.
+ */
+#include "cato_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* epsilon(1.0_rk), tiny(1.0_rk) */
+#define EPS DBL_EPSILON
+#define TINY DBL_MIN
+
+static inline double dmax(double a, double b) { return (a < b) ? b : a; }
+static inline double dmin(double a, double b) { return (b < a) ? b : a; }
+/* Fortran SIGN(1.0, x): +1 for x >= +0, -1 for negative (incl. -0 in gfortran). */
+static inline double fsign1(double x) { return signbit(x) ? -1.0 : 1.0; }
+
+int oracle_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
+
+int oracle_get_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* indexing of halo-padded (1-ng:ni+ng, 1-ng:nj+ng) arrays                                     */
+/* ------------------------------------------------------------------------------------------ */
+typedef struct {
+  int ni, nj, ng, ld;
+} dims_t;
+
+static inline dims_t mkdims(const cato_config* c) {
+  dims_t d = {c->ni, c->nj, c->n_ghost, c->ni + 2 * c->n_ghost};
+  return d;
+}
+#define AT(a, i, j) (a)[((i) + d.ng - 1) + (size_t)((j) + d.ng - 1) * d.ld]
+/* i-edge arrays (1:2, -1:ni, 0:nj) and j-edge arrays (1:2, 0:ni, -1:nj) */
+#define IE(a, lr, i, j) (a)[(lr) + 2 * (((i) + 1) + (size_t)(j) * (d.ni + 2))]
+#define JE(a, lr, i, j) (a)[(lr) + 2 * ((i) + (size_t)((j) + 1) * (d.ni + 1))]
+/* edge flux arrays iflux(4, 0:ni, 1:nj) and jflux(4, 1:ni, 0:nj) */
+#define IF(a, k, i, j) (a)[(k) + 4 * ((i) + (size_t)((j) - 1) * (d.ni + 1))]
+#define JF(a, k, i, j) (a)[(k) + 4 * (((i) - 1) + (size_t)(j) * d.ni)]
+
+static size_t nfield(dims_t d) { return (size_t)d.ld * (size_t)(d.nj + 2 * d.ng); }
+
+/* ------------------------------------------------------------------------------------------ */
+/* geometry: quad_cell_t (src/lib/geometry/quad_cell.f90:69-229) */
+/* ------------------------------------------------------------------------------------------ */
+void oracle_quad_metrics(const double xin[4], const double yin[4], double* volume,
+                         double el[4], double nv[8], double* min_dx, double* min_dy) {
+  double x[4], y[4];
+  memcpy(x, xin, sizeof x);
+  memcpy(y, yin, sizeof y);
+  /* round-off snapping, quad_cell.f90:78-92 */
+  if (fabs(y[1] - y[0]) < EPS) y[1] = y[0];
+  if (fabs(y[3] - y[2]) < EPS) y[3] = y[2];
+  if (fabs(x[2] - x[1]) < EPS) x[2] = x[1];
+  if (fabs(x[3] - x[0]) < EPS) x[3] = x[0];
+  /* calculate_volume, quad_cell.f90:176-191 */
+  *volume = (x[1] - x[0]) * (y[3] - y[0]) - (x[3] - x[0]) * (y[1] - y[0]);
+  /* calculate_edge_stats, quad_cell.f90:101-126 */
+  el[0] = sqrt((x[1] - x[0]) * (x[1] - x[0]) + (y[1] - y[0]) * (y[1] - y[0]));
+  el[1] = sqrt((x[2] - x[1]) * (x[2] - x[1]) + (y[2] - y[1]) * (y[2] - y[1]));
+  el[2] = sqrt((x[3] - x[2]) * (x[3] - x[2]) + (y[3] - y[2]) * (y[3] - y[2]));
+  el[3] = sqrt((x[0] - x[3]) * (x[0] - x[3]) + (y[0] - y[3]) * (y[0] - y[3]));
+  double mx = dmax(dmax(dmax(el[0], el[1]), el[2]), el[3]);
+  double mn = dmin(dmin(dmin(el[0], el[1]), el[2]), el[3]);
+  if (mx - mn < 2.0 * EPS) el[0] = el[1] = el[2] = el[3] = mx;
+  double midx[4], midy[4];
+  midx[0] = (x[1] + x[0]) / 2.0; midy[0] = (y[1] + y[0]) / 2.0;
+  midx[1] = (x[2] + x[1]) / 2.0; midy[1] = (y[2] + y[1]) / 2.0;
+  midx[2] = (x[3] + x[2]) / 2.0; midy[2] = (y[3] + y[2]) / 2.0;
+  midx[3] = (x[0] + x[3]) / 2.0; midy[3] = (y[0] + y[3]) / 2.0;
+  *min_dx = dmin(fabs(x[1] - x[0]), fabs(x[2] - x[3]));
+  *min_dy = dmin(fabs(y[3] - y[0]), fabs(y[2] - y[1]));
+  /* calculate_edge_norm_vectors, quad_cell.f90:193-229 with vector.f90:68-96 */
+  static const int head[4] = {1, 2, 3, 0};
+  for (int e = 0; e < 4; ++e) {
+    double ddx = x[head[e]] - midx[e];
+    double ddy = y[head[e]] - midy[e];
+    double vx = (midx[e] + ddy) - midx[e];
+    double vy = (midy[e] - ddx) - midy[e];
+    double len = sqrt(vx * vx + vy * vy);
+    nv[2 * e] = vx / len;
+    nv[2 * e + 1] = vy / len;
+  }
+}
+
+/* Uniform Cartesian geometry shared by every cell: the quad_cell_t metrics of a dx x dy cell. */
+typedef struct {
+  double vol, l[4], dx, dy;
+} geom_t;
+
+static geom_t uniform_geom(const cato_config* c) {
+  double x[4] = {0.0, c->dx, c->dx, 0.0}, y[4] = {0.0, 0.0, c->dy, c->dy};
+  geom_t g;
+  double nv[8];
+  oracle_quad_metrics(x, y, &g.vol, g.l, nv, &g.dx, &g.dy);
+  return g;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* limiters as inlined in muscl_tvd2.fypp:195-213                                              */
+/* ------------------------------------------------------------------------------------------ */
+double oracle_limiter(int32_t lim, double r) {
+  switch (lim) {
+    case CATO_LIM_MINMOD: return dmax(0.0, dmin(r, 1.0));
+    case CATO_LIM_SUPERBEE: return dmax(dmax(0.0, dmin(2.0 * r, 1.0)), dmin(r, 2.0));
+    case CATO_LIM_VAN_LEER: return (r + fabs(r)) / (1.0 + fabs(r)); /* unpinned: unreachable */
+    default: return 0.0;
+  }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* boundary conditions                                                                         */
+/* ------------------------------------------------------------------------------------------ */
+/* zero_gradient_bc.f90:64-119 (full-length rows/columns), symmetry_bc.f90:75-131,
+ * periodic_bc.fypp:138-278 on a single image (x: rows jlo:jhi; y: columns ilo:ihi; corners
+ * only when all four sides are periodic, periodic_bc.fypp:68-74). */
+static void apply_one_bc(dims_t d, int type, int side, int do_corners, double* f[4]) {
+  const int ng = d.ng, ni = d.ni, nj = d.nj;
+  for (int g = 1; g <= ng; ++g) {
+    if (type == CATO_BC_ZERO_GRADIENT) {
+      for (int k = 0; k < 4; ++k) {
+        double* a = f[k];
+        if (side == CATO_PLUS_X)
+          for (int j = 1 - ng; j <= nj + ng; ++j) AT(a, ni + g, j) = AT(a, ni, j);
+        if (side == CATO_MINUS_X)
+          for (int j = 1 - ng; j <= nj + ng; ++j) AT(a, 1 - g, j) = AT(a, 1, j);
+        if (side == CATO_PLUS_Y)
+          for (int i = 1 - ng; i <= ni + ng; ++i) AT(a, i, nj + g) = AT(a, i, nj);
+        if (side == CATO_MINUS_Y)
+          for (int i = 1 - ng; i <= ni + ng; ++i) AT(a, i, 1 - g) = AT(a, i, 1);
+      }
+    } else if (type == CATO_BC_SYMMETRY) {
+      for (int k = 0; k < 4; ++k) {
+        double* a = f[k];
+        /* normal velocity negated: u (k=1) on +-x, v (k=2) on +-y */
+        int neg_x = (k == 1), neg_y = (k == 2);
+        if (side == CATO_PLUS_X)
+          for (int j = 1 - ng; j <= nj + ng; ++j)
+            AT(a, ni + g, j) = neg_x ? -AT(a, ni - (g - 1), j) : AT(a, ni - (g - 1), j);
+        if (side == CATO_MINUS_X)
+          for (int j = 1 - ng; j <= nj + ng; ++j)
+            AT(a, 1 - g, j) = neg_x ? -AT(a, 1 + (g - 1), j) : AT(a, 1 + (g - 1), j);
+        if (side == CATO_PLUS_Y)
+          for (int i = 1 - ng; i <= ni + ng; ++i)
+            AT(a, i, nj + g) = neg_y ? -AT(a, i, nj - (g - 1)) : AT(a, i, nj - (g - 1));
+        if (side == CATO_MINUS_Y)
+          for (int i = 1 - ng; i <= ni + ng; ++i)
+            AT(a, i, 1 - g) = neg_y ? -AT(a, i, 1 + (g - 1)) : AT(a, i, 1 + (g - 1));
+      }
+    }
+  }
+  if (type == CATO_BC_PERIODIC) {
+    for (int k = 0; k < 4; ++k) {
+      double* a = f[k];
+      if (side == CATO_PLUS_X || side == CATO_MINUS_X) {
+        /* ihi+1:ihi_halo <- ilo:ilo+ng-1 ; ilo_halo:ilo-1 <- ihi-ng+1:ihi */
+        for (int j = 1; j <= nj; ++j)
+          for (int g = 1; g <= ng; ++g) {
+            AT(a, ni + g, j) = AT(a, g, j);
+            AT(a, 1 - g, j) = AT(a, ni + 1 - g, j);
+          }
+      } else {
+        for (int i = 1; i <= ni; ++i)
+          for (int g = 1; g <= ng; ++g) {
+            AT(a, i, nj + g) = AT(a, i, g);
+            AT(a, i, 1 - g) = AT(a, i, nj + 1 - g);
+          }
+      }
+      if (do_corners) {
+        for (int gi = 1; gi <= ng; ++gi)
+          for (int gj = 1; gj <= ng; ++gj) {
+            AT(a, 1 - gi, 1 - gj) = AT(a, ni + 1 - gi, nj + 1 - gj);
+            AT(a, ni + gi, 1 - gj) = AT(a, gi, nj + 1 - gj);
+            AT(a, 1 - gi, nj + gj) = AT(a, ni + 1 - gi, gj);
+            AT(a, ni + gi, nj + gj) = AT(a, gi, gj);
+          }
+      }
+    }
+  }
+}
+
+static int bc_priority(int type) { return type == CATO_BC_PERIODIC ? 2 : 1; }
+
+/* flux_solver_t%apply_primitive_bc, flux_solver.f90:138-185: priority high -> low and, within
+ * one priority, +x, +y, -x, -y. */
+int oracle_apply_bc(const cato_config* c, double* rho, double* u, double* v, double* p) {
+  dims_t d = mkdims(c);
+  double* f[4] = {rho, u, v, p};
+  int all_periodic = 1;
+  for (int s = 0; s < 4; ++s) all_periodic &= (c->bc[s] == CATO_BC_PERIODIC);
+  int maxp = 0;
+  for (int s = 0; s < 4; ++s) maxp = bc_priority(c->bc[s]) > maxp ? bc_priority(c->bc[s]) : maxp;
+  for (int prio = maxp; prio >= 0; --prio)
+    for (int s = 0; s < 4; ++s)
+      if (bc_priority(c->bc[s]) == prio) apply_one_bc(d, c->bc[s], s, all_periodic, f);
+  return 0;
+}
+
+/* One boundary_condition_t%apply on one side (used to replay the reference's own BC unit tests,
+ * tests/unit/test_bc/mod_test_bc.f90, which apply single sides). */
+int oracle_apply_bc_side(const cato_config* c, int side, int type, int do_corners, double* rho,
+                         double* u, double* v, double* p) {
+  dims_t d = mkdims(c);
+  double* f[4] = {rho, u, v, p};
+  apply_one_bc(d, type, side, do_corners, f);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* reconstruction                                                                              */
+/* ------------------------------------------------------------------------------------------ */
+/* cell value along the edge-normal direction: offset n along the normal, t along the tangent */
+#define QN(n, t) (dir == 0 ? AT(q, i + (n), j + (t)) : AT(q, i + (t), j + (n)))
+
+/* muscl_tvd2.fypp:172-223 for one edge (i,j) in direction dir (0 = i, 1 = j). */
+static void tvd2_edge(dims_t d, int lim, const double* q, int dir, int i, int j, double* L,
+                      double* R) {
+  double dm = QN(0, 0) - QN(-1, 0);
+  double d0 = QN(1, 0) - QN(0, 0);
+  double dp = QN(2, 0) - QN(1, 0);
+  if (fabs(dm) < EPS) dm = 0.0;
+  if (fabs(d0) < EPS) d0 = 0.0;
+  if (fabs(dp) < EPS) dp = 0.0;
+  double rL = d0 / (dm + 1e-16);
+  double rR = d0 / (dp + 1e-16);
+  double phi = oracle_limiter(lim, rL);
+  *L = QN(0, 0) + 0.5 * phi * dm;
+  phi = oracle_limiter(lim, rR);
+  *R = QN(1, 0) - 0.5 * phi * dp;
+}
+
+/* muscl_mlp.fypp:190-281 (Kim & Kim 2005 MLP) for one edge; order 3 or 5. */
+static void mlp_edge(dims_t d, int order, const double* q, int dir, int i, int j, double* L,
+                     double* R) {
+  const double S = 1e-30; /* SMALL_NUM, muscl_mlp.fypp:122 */
+  double dm = QN(0, 0) - QN(-1, 0);
+  double d0 = QN(1, 0) - QN(0, 0);
+  double dp = QN(2, 0) - QN(1, 0);
+  if (fabs(dm) < EPS) dm = 0.0;
+  if (fabs(d0) < EPS) d0 = 0.0;
+  if (fabs(dp) < EPS) dp = 0.0;
+  double dm3 = 0.0, dp5 = 0.0;
+  if (order == 5) {
+    dm3 = QN(-1, 0) - QN(-2, 0);
+    dp5 = QN(3, 0) - QN(2, 0);
+    if (fabs(dm3) < EPS) dm3 = 0.0;
+    if (fabs(dp5) < EPS) dp5 = 0.0;
+  }
+  double rR_p1 = d0 / (dp + S);
+  double rL = d0 / (dm + S);
+  double bL, bR;
+  if (order == 5) {
+    double rL_m1 = dm / (dm3 + S);
+    double rL_p1 = dp / (d0 + S);
+    double rR_p2 = dp / (dp5 + S);
+    double rR = dm / (d0 + S);
+    bL = ((((-2.0 / (rL_m1 + S)) + 11.0) + 24.0 * rL) - 3.0 * rL * rL_p1) / 30.0;
+    bR = ((((-2.0 / (rR_p2 + S)) + 11.0) + 24.0 * rR_p1) - 3.0 * rR_p1 * rR) / 30.0;
+  } else {
+    bL = (1.0 + 2.0 * rL) / 3.0;
+    bR = (1.0 + 2.0 * rR_p1) / 3.0;
+  }
+  /* tan(theta) with the transverse neighbours, muscl_mlp.fypp:241-249 */
+  double tt = fabs(QN(0, 1) - QN(0, -1)) / (fabs(QN(1, 0) - QN(-1, 0)) + S);
+  double tt1 = fabs(QN(1, 1) - QN(1, -1)) / (fabs(QN(2, 0) - QN(0, 0)) + S);
+  double aLt = (2.0 * dmax(1.0, rL) * (1.0 + dmax(0.0, tt1 / (rR_p1 + S)))) / (1.0 + tt);
+  double aRt = (2.0 * dmax(1.0, rR_p1) * (1.0 + dmax(0.0, tt / (rL + S)))) / (1.0 + tt1);
+  double aL = dmax(1.0, dmin(2.0, aLt));
+  double aR = dmax(1.0, dmin(2.0, aRt));
+  *L = QN(0, 0) + 0.5 * dmax(0.0, dmin(dmin(aL * rL, aL), bL)) * dm;
+  *R = QN(1, 0) - 0.5 * dmax(0.0, dmin(dmin(aR * rR_p1, aR), bR)) * dp;
+}
+#undef QN
+
+static void edge_recon(dims_t d, int lim, const double* q, int dir, int i, int j, double* L,
+                       double* R) {
+  if (lim == CATO_LIM_MLP3) mlp_edge(d, 3, q, dir, i, j, L, R);
+  else if (lim == CATO_LIM_MLP5) mlp_edge(d, 5, q, dir, i, j, L, R);
+  else tvd2_edge(d, lim, q, dir, i, j, L, R);
+}
+
+/* muscl_interpolation_t%interpolate_edge_values (muscl_tvd2.fypp:126-227, muscl_mlp.fypp:
+ * 117-284): i-edges (L/R, -1:ni, 0:nj) computed for i = 0..ni, j = 0..nj (the i = -1 slot stays
+ * 0); j-edges (L/R, 0:ni, -1:nj) for i = 0..ni, j = 0..nj. */
+int oracle_interpolate_edges(const cato_config* c, const double* q, double* ie, double* je) {
+  dims_t d = mkdims(c);
+  memset(ie, 0, sizeof(double) * 2 * (size_t)(d.ni + 2) * (d.nj + 1));
+  memset(je, 0, sizeof(double) * 2 * (size_t)(d.ni + 1) * (d.nj + 2));
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j <= d.nj; ++j)
+    for (int i = 0; i <= d.ni; ++i) {
+      edge_recon(d, c->limiter, q, 0, i, j, &IE(ie, 0, i, j), &IE(ie, 1, i, j));
+      edge_recon(d, c->limiter, q, 1, i, j, &JE(je, 0, i, j), &JE(je, 1, i, j));
+    }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* edge fluxes                                                                                 */
+/* ------------------------------------------------------------------------------------------ */
+typedef struct {
+  double r, u, v, p;
+} prim_t;
+
+/* AUSMPW+ split functions, ausmpw_plus_solver.fypp:486-530 (alpha = 1/8, :61) */
+static double ausmpw_p_plus(double M) {
+  const double alpha = 1.0 / 8.0;
+  if (fabs(M) > 1.0) return 0.5 * (1.0 + fsign1(M));
+  return 0.25 * ((M + 1.0) * (M + 1.0)) * (2.0 - M) + alpha * M * ((M * M - 1.0) * (M * M - 1.0));
+}
+static double ausmpw_p_minus(double M) {
+  const double alpha = 1.0 / 8.0;
+  if (fabs(M) > 1.0) return 0.5 * (1.0 - fsign1(M));
+  return 0.25 * ((M - 1.0) * (M - 1.0)) * (2.0 + M) - alpha * M * ((M * M - 1.0) * (M * M - 1.0));
+}
+static double ausmpw_m_plus(double M) {
+  if (fabs(M) > 1.0) return 0.5 * (M + fabs(M));
+  return 0.25 * ((M + 1.0) * (M + 1.0));
+}
+static double ausmpw_m_minus(double M) {
+  if (fabs(M) > 1.0) return 0.5 * (M - fabs(M));
+  return -(0.25 * ((M - 1.0) * (M - 1.0)));
+}
+
+/* AUSMPW+ edge flux, ausmpw_plus_solver.fypp:336-459 with get_f (:532-556) and get_w
+ * (:558-568).  pc = cell pressures p1_L, p1_R, p2_L, p2_R. */
+static void flux_ausmpw(const cato_config* c, int dir, double nx, double ny, prim_t Lq, prim_t Rq,
+                        const double pc[4], double F[4]) {
+  const double g = c->gamma;
+  double rho_L = Lq.r, u_LHS = Lq.u, v_LHS = Lq.v, p_L = Lq.p;
+  double rho_R = Rq.r, u_RHS = Rq.u, v_RHS = Rq.v, p_R = Rq.p;
+  double U_L, U_R, V_L, V_R;
+  if (dir == 0) { U_L = u_LHS; U_R = u_RHS; V_L = v_LHS; V_R = v_RHS; }
+  else { U_L = v_LHS; U_R = v_RHS; V_L = u_LHS; V_R = u_RHS; }
+  double cs_L = sqrt(g * p_L / rho_L);
+  double cs_R = sqrt(g * p_R / rho_R);
+  double M_LHS = sqrt(u_LHS * u_LHS + v_LHS * v_LHS) / cs_L;
+  double M_RHS = sqrt(u_RHS * u_RHS + v_RHS * v_RHS) / cs_R;
+  if (c->apply_low_mach_fix && (fabs(M_LHS) < 0.1 || fabs(M_RHS) < 0.1)) { /* LOW_MACH */
+    double f_M = dmin(1.0, dmax(M_LHS, M_RHS));
+    double uLf = 0.5 * (u_LHS + u_RHS) + f_M * 0.5 * (u_LHS - u_RHS);
+    double uRf = 0.5 * (u_LHS + u_RHS) - f_M * 0.5 * (u_LHS - u_RHS);
+    double vLf = 0.5 * (v_LHS + v_RHS) + f_M * 0.5 * (v_LHS - v_RHS);
+    double vRf = 0.5 * (v_LHS + v_RHS) - f_M * 0.5 * (v_LHS - v_RHS);
+    u_LHS = uLf; u_RHS = uRf; v_LHS = vLf; v_RHS = vRf;
+  }
+  double H_L = (g / (g - 1.0)) * (p_L / rho_L) + 0.5 * (u_LHS * u_LHS + v_LHS * v_LHS);
+  double H_R = (g / (g - 1.0)) * (p_R / rho_R) + 0.5 * (u_RHS * u_RHS + v_RHS * v_RHS);
+  double H_normal = dmin(H_L - 0.5 * (V_L * V_L), H_R - 0.5 * (V_R * V_R));
+  double c_s = sqrt(2.0 * ((g - 1.0) / (g + 1.0)) * H_normal);
+  double c_half;
+  if (0.5 * (U_L + U_R) < 0.0) c_half = (c_s * c_s) / dmax(fabs(U_R), c_s);
+  else c_half = (c_s * c_s) / dmax(fabs(U_L), c_s);
+  double M_L = U_L / c_half;
+  double M_R = U_R / c_half;
+  double M_L_plus = ausmpw_m_plus(M_L);
+  double M_R_minus = ausmpw_m_minus(M_R);
+  double P_R_minus = ausmpw_p_minus(M_R);
+  double P_L_plus = ausmpw_p_plus(M_L);
+  double p_s = p_L * P_L_plus + p_R * P_R_minus;
+  double mt = dmin(p_L / p_R, p_R / p_L);
+  double w = 1.0 - mt * mt * mt;
+  double f_L, f_R;
+  if (fabs(p_s) < TINY) {
+    f_L = 0.0;
+    f_R = 0.0;
+  } else {
+    double t = dmin(1.0, dmin(dmin(dmin(pc[0], pc[1]), pc[2]), pc[3]) / dmin(p_L, p_R));
+    double min_term = t * t;
+    f_L = ((p_L / p_s) - 1.0) * min_term;
+    f_R = ((p_R / p_s) - 1.0) * min_term;
+  }
+  double Mb_L, Mb_R;
+  if (M_L_plus + M_R_minus < 0.0) {
+    Mb_L = M_L_plus * w * (1.0 + f_L);
+    Mb_R = M_R_minus + M_L_plus * ((1.0 - w) * (1.0 + f_L) - f_R);
+  } else {
+    Mb_L = M_L_plus + M_R_minus * ((1.0 - w) * (1.0 + f_R) - f_L);
+    Mb_R = M_R_minus * w * (1.0 + f_R);
+  }
+  double mL = Mb_L * c_half * rho_L;
+  double mR = Mb_R * c_half * rho_R;
+  F[0] = mL + mR;
+  F[1] = (mL * u_LHS) + (mR * u_RHS) + ((P_L_plus * nx * p_L) + (P_R_minus * nx * p_R));
+  F[2] = (mL * v_LHS) + (mR * v_RHS) + ((P_L_plus * ny * p_L) + (P_R_minus * ny * p_R));
+  F[3] = (mL * H_L) + (mR * H_R);
+}
+
+/* SLAU family, slau_solver.fypp:332-490.  pc (SD variants) = delta_p1..6 cell pairs:
+ * pc[0..5] = first cell of each pair, pc[6..11] = second cell. */
+static void flux_slau(const cato_config* c, double nx, double ny, prim_t Lq, prim_t Rq,
+                      const double pc[12], double F[4]) {
+  const double g = c->gamma;
+  const double THRESHOLD = 5e-3, C_SD1 = 0.01;
+  const int variant = c->flux;
+  double rho_L = Lq.r, u_L = Lq.u, v_L = Lq.v, p_L = Lq.p;
+  double rho_R = Rq.r, u_R = Rq.u, v_R = Rq.v, p_R = Rq.p;
+  double Vp = u_L * nx + v_L * ny;
+  double Vm = u_R * nx + v_R * ny;
+  double c_plus = sqrt(g * p_L / rho_L);
+  double c_minus = sqrt(g * p_R / rho_R);
+  double c_bar = 0.5 * (c_plus + c_minus);
+  double V_n_bar = (rho_L * fabs(Vp) + rho_R * fabs(Vm)) / (rho_L + rho_R);
+  double M_hat = dmin(1.0, sqrt(0.5 * (u_L * u_L + v_L * v_L + u_R * u_R + v_R * v_R)) / c_bar);
+  double Chi = (1.0 - M_hat) * (1.0 - M_hat);
+  double M_bar = V_n_bar / c_bar;
+  double p_bar = 0.5 * (p_L + p_R);
+  double rho_bar = 0.5 * (rho_L + rho_R);
+  double M_plus = Vp / c_bar;
+  double M_minus = Vm / c_bar;
+  double B_plus, B_minus;
+  if (fabs(M_plus) < 1.0) B_plus = 0.25 * (2.0 - M_plus) * ((M_plus + 1.0) * (M_plus + 1.0));
+  else B_plus = 0.5 * (1.0 + fsign1(M_plus));
+  if (fabs(M_minus) < 1.0) B_minus = 0.25 * (2.0 + M_minus) * ((M_minus - 1.0) * (M_minus - 1.0));
+  else B_minus = 0.5 * (1.0 + fsign1(-M_minus));
+  double delta_p = p_R - p_L;
+  if (fabs(delta_p) < EPS || fabs(delta_p) < THRESHOLD * p_bar) delta_p = 0.0;
+  double delta_rho = rho_R - rho_L;
+  if (fabs(delta_rho) < EPS) delta_rho = 0.0;
+  double delta_B = B_plus - B_minus;
+  if (fabs(delta_B) < EPS) delta_B = 0.0;
+  double pLmR = p_L - p_R;
+  if (fabs(pLmR) < EPS) pLmR = 0.0;
+  double theta = 0.0;
+  if (variant == CATO_FLUX_SD_SLAU || variant == CATO_FLUX_SD_SLAU2) {
+    double dpk[6];
+    for (int k = 0; k < 6; ++k) {
+      dpk[k] = fabs(pc[k] - pc[6 + k]);
+      if (dpk[k] < EPS || dpk[k] < THRESHOLD * p_bar) dpk[k] = 0.0;
+    }
+    double m6 = dmax(dmax(dmax(dmax(dmax(dpk[0], dpk[1]), dpk[2]), dpk[3]), dpk[4]), dpk[5]);
+    double dp_max = dmax(fabs(delta_p), m6);
+    double ratio = ((C_SD1 * fabs(delta_p) / p_bar) + C_SD1) / ((dp_max / p_bar) + C_SD1);
+    theta = dmin(1.0, ratio * ratio) * dmax(0.0, 1.0 - fabs(M_bar));
+  }
+  double p_tilde;
+  if (variant == CATO_FLUX_SLAU || variant == CATO_FLUX_SD_SLAU)
+    p_tilde = (p_bar + 0.5 * delta_B * pLmR) + (1.0 - Chi) * (B_plus + B_minus - 1.0) * p_bar;
+  else
+    p_tilde = p_bar + (0.5 * delta_B * pLmR) +
+              sqrt(0.5 * (u_L * u_L + v_L * v_L + u_R * u_R + v_R * v_R)) *
+                  (B_plus + B_minus - 1.0) * rho_bar * c_bar;
+  double gg = -(dmax(dmin(M_plus, 0.0), -1.0) * dmin(dmax(M_minus, 0.0), 1.0));
+  double mf;
+  if (variant == CATO_FLUX_SLAU || variant == CATO_FLUX_SLAU2)
+    mf = 0.5 * ((rho_L * Vp) + (rho_R * Vm) - fabs(V_n_bar) * delta_rho) * (1.0 - gg) -
+         ((Chi / (2.0 * c_bar)) * delta_p);
+  else
+    mf = 0.5 * ((rho_L * Vp) + (rho_R * Vm) - fabs(V_n_bar) * delta_rho) * (1.0 - gg) -
+         ((theta / (2.0 * c_bar)) * delta_p);
+  double mL = 0.5 * (mf + fabs(mf));
+  double mR = 0.5 * (mf - fabs(mf));
+  double H_L = (g / (g - 1.0)) * (p_L / rho_L) + 0.5 * (u_L * u_L + v_L * v_L);
+  double H_R = (g / (g - 1.0)) * (p_R / rho_R) + 0.5 * (u_R * u_R + v_R * v_R);
+  F[0] = mL + mR;
+  F[1] = (mL * u_L) + (mR * u_R) + p_tilde * nx;
+  F[2] = (mL * v_L) + (mR * v_R) + p_tilde * ny;
+  F[3] = (mL * H_L) + (mR * H_R);
+}
+
+/* f_h pressure sensor, roe_solver.fypp:519-527 */
+static double roe_f_h(double pL, double pR) {
+  double ratio = fabs(pR - pL) / (dmin(pR, pL) + 1e-16);
+  return (ratio < 1.0) ? 0.0 : 1.0;
+}
+/* entropy_correction, roe_solver.fypp:529-536 (used only with the Harten flag; unpinned) */
+static double roe_entropy_correction(double z, double dd) {
+  if (z > dd) return z;
+  return 0.5 * (z * z + dd * dd) / dd;
+}
+
+/* Roe, roe_solver.fypp:420-512.  pc = the five f_h pressure pairs (first cells pc[0..4],
+ * second cells pc[5..9]). */
+static void flux_roe(const cato_config* c, double nx, double ny, prim_t Lq, prim_t Rq,
+                     const double pc[10], double F[4]) {
+  const double g = c->gamma;
+  double rl = fabs(Lq.r), ul = Lq.u, vl = Lq.v, pl = fabs(Lq.p);
+  double hl = (g / (g - 1.0)) * (pl / rl) + 0.5 * (ul * ul + vl * vl);
+  double rr = fabs(Rq.r), ur = Rq.u, vr = Rq.v, pr = fabs(Rq.p);
+  double hr = (g / (g - 1.0)) * (pr / rr) + 0.5 * (ur * ur + vr * vr);
+  double rav = sqrt(rl * rr);
+  double gam1 = g - 1.0;
+  double dd = rav / rl;
+  double dd1 = 1.0 / (1.0 + dd);
+  double uav = (ul + dd * ur) * dd1;
+  double vav = (vl + dd * vr) * dd1;
+  double hav = (hl + dd * hr) * dd1;
+  double q2a = 0.5 * (uav * uav + vav * vav);
+  double c2a = gam1 * (hav - q2a);
+  double cav = sqrt(c2a);
+  double uv = uav * nx + vav * ny;
+  double du = (ur - ul) * nx + (vr - vl) * ny;
+  double du_trans = -((ur - ul) * ny) + (vr - vl) * nx;
+  double cs_R = sqrt(g * pr / rr);
+  double cs_L = sqrt(g * pl / rl);
+  double h1 = fabs(dmin(uv - cav, (ul * nx + vl * ny) - cs_L));
+  double h2 = fabs(uv);
+  double h4 = fabs(dmax(uv + cav, (ur * nx + vr * ny) + cs_R));
+  double eabs1 = h1, eabs2 = h2, eabs4 = h4;
+  if (c->roe_entropy_fix == CATO_ROE_HARTEN) {
+    double delta = c->harten_delta * cav;
+    eabs1 = roe_entropy_correction(h1, delta);
+    eabs2 = roe_entropy_correction(h2, delta);
+    eabs4 = roe_entropy_correction(h4, delta);
+  }
+  h1 = rav * cav * du;
+  h2 = eabs1 * (pr - pl - h1) / (2.0 * c2a);
+  double h3 = eabs2 * (rr - rl - (pr - pl) / c2a);
+  h4 = eabs2 * rav;
+  double h5 = eabs4 * (pr - pl + h1) / (2.0 * c2a);
+  double psi = fabs(cs_R - cs_L) / dmax(cs_R, cs_L);
+  double FR[4] = {rr * uv, rr * ur * uv + nx * pr, rr * vr * uv + ny * pr, rr * hr * uv};
+  double FL[4] = {rl * uv, rl * ul * uv + nx * pl, rl * vl * uv + ny * pl, rl * hl * uv};
+  double rmt[4];
+  rmt[0] = (h2 + h3 + h5);
+  rmt[1] = (h2 * (uav - cav * nx) + h3 * uav + h4 * (ur - ul - du * nx) + h5 * (uav + cav * nx));
+  rmt[2] = (h2 * (vav - cav * ny) + h3 * vav + h4 * (vr - vl - du * ny) + h5 * (vav + cav * ny));
+  rmt[3] = (h2 * (hav - cav * uv) + h3 * q2a + h4 * (uav * (ur - ul) + vav * (vr - vl) - uv * du) +
+            h5 * (hav + cav * uv));
+  for (int k = 0; k < 4; ++k) F[k] = 0.5 * (FR[k] + FL[k] - rmt[k]);
+  double fmax = 0.0;
+  for (int k = 0; k < 5; ++k) fmax = dmax(fmax, roe_f_h(pc[k], pc[5 + k]));
+  /* maxval(f_p) over {0,1}: the 5 values are non-negative so starting at 0 is exact */
+  F[1] = F[1] - 0.5 * fmax * rav * cav * (-(du_trans * ny) + psi * du * nx);
+  F[2] = F[2] - 0.5 * fmax * rav * cav * (du_trans * nx + psi * du * ny);
+}
+
+/* AUSM+-up split polynomials, ausm_plus_solver.f90:394-485 */
+static double m1p(double M) { return 0.5 * (M + fabs(M)); }
+static double m1m(double M) { return 0.5 * (M - fabs(M)); }
+static double m2p(double M) { return 0.25 * ((M + 1.0) * (M + 1.0)); }
+static double m2m(double M) { return -(0.25 * ((M - 1.0) * (M - 1.0))); }
+static double m4p(double M, double beta) {
+  if (fabs(M) >= 1.0) return m1p(M);
+  return m2p(M) * (1.0 - 16.0 * beta * m2m(M));
+}
+static double m4m(double M, double beta) {
+  if (fabs(M) >= 1.0) return m1m(M);
+  return m2m(M) * (1.0 + 16.0 * beta * m2p(M));
+}
+static double p5p(double M, double alpha) {
+  if (fabs(M) >= 1.0) return m1p(M) / M;
+  return m2p(M) * ((2.0 - M) - 16.0 * alpha * M * m2m(M));
+}
+static double p5m(double M, double alpha) {
+  if (fabs(M) >= 1.0) return m1m(M) / M;
+  return m2m(M) * ((-2.0 - M) + 16.0 * alpha * M * m2p(M));
+}
+
+/* AUSM+-up (basic): interface_state, ausm_plus_solver.f90:499-643, and the upwinding of the
+ * commented driver :313-325.  Unpinned: the reference driver is commented out. */
+static void flux_ausm_up(const cato_config* c, double nx, double ny, prim_t Lq, prim_t Rq,
+                         double F[4]) {
+  const double g = c->gamma;
+  const double alpha = 3.0 / 16.0; /* pressure_split_alpha, :51 */
+  double gamma_factor = ((2.0 * (g - 1.0)) / (g + 1.0));
+  double vel_L = Lq.u * nx + Lq.v * ny;
+  double vel_R = Rq.u * nx + Rq.v * ny;
+  double H_L = (Lq.p / Lq.r) * (g / (g - 1.0)) + 0.5 * (Lq.u * Lq.u + Lq.v * Lq.v);
+  double H_R = (Rq.p / Rq.r) * (g / (g - 1.0)) + 0.5 * (Rq.u * Rq.u + Rq.v * Rq.v);
+  double a_crit_L = sqrt(gamma_factor * fabs(H_L));
+  double a_crit_R = sqrt(gamma_factor * fabs(H_R));
+  double a_circ_L = (a_crit_L * a_crit_L) / dmax(a_crit_L, vel_L);
+  double a_circ_R = (a_crit_R * a_crit_R) / dmax(a_crit_R, -vel_R);
+  double a_half = dmin(a_circ_L, a_circ_R);
+  double M_L = vel_L / a_half;
+  double M_R = vel_R / a_half;
+  double M_bar_sq = 0.5 * (M_L + M_R); /* as written at :585 */
+  double M_plus = m4p(M_L, c->ausm_beta);
+  double M_minus = m4m(M_R, c->ausm_beta);
+  double rho_half = 0.5 * (Rq.r + Lq.r);
+  double M_p;
+  if (fabs(Rq.p - Lq.p) < EPS) M_p = 0.0;
+  else
+    M_p = -(c->ausm_kp * dmax(1.0 - c->ausm_sigma * M_bar_sq, 0.0) *
+            ((Rq.p - Lq.p) / (rho_half * (a_half * a_half))));
+  double M_sum = M_plus + M_minus;
+  if (fabs(M_sum) < 1e-13) M_sum = 0.0;
+  double M_half = M_sum + M_p;
+  if (fabs(M_half) < 1e-13) M_half = 0.0;
+  double P_plus = p5p(M_L, alpha);
+  double P_minus = p5m(M_R, alpha);
+  double p_u;
+  if (fabs(vel_R - vel_L) < EPS) p_u = 0.0;
+  else p_u = -(c->ausm_ku * P_plus * P_minus * (Lq.r + Rq.r) * a_half * (vel_R - vel_L));
+  double p_half = P_plus * Lq.p + P_minus * Rq.p + p_u;
+  if (M_half > 0.0) {
+    double mf = M_half * a_half * Lq.r;
+    F[0] = mf;
+    F[1] = mf * Lq.u + (nx * p_half);
+    F[2] = mf * Lq.v + (ny * p_half);
+    F[3] = mf * H_L;
+  } else {
+    double mf = M_half * a_half * Rq.r;
+    F[0] = mf;
+    F[1] = mf * Rq.u + (nx * p_half);
+    F[2] = mf * Rq.v + (ny * p_half);
+    F[3] = mf * H_R;
+  }
+}
+
+/* HLLC (Toro, "Riemann Solvers and Numerical Methods for Fluid Dynamics", 3rd ed., 2009,
+ * Sec. 10.4-10.6): PVRS pressure estimate and pressure-based wave speeds, as set up by the
+ * unfinished reference stub hllc_solver.fypp:345-353.  Unpinned. */
+static void flux_hllc(const cato_config* c, int dir, prim_t Lq, prim_t Rq, double F[4]) {
+  const double g = c->gamma;
+  double qnL = dir == 0 ? Lq.u : Lq.v, qtL = dir == 0 ? Lq.v : Lq.u;
+  double qnR = dir == 0 ? Rq.u : Rq.v, qtR = dir == 0 ? Rq.v : Rq.u;
+  double cL = sqrt(g * Lq.p / Lq.r), cR = sqrt(g * Rq.p / Rq.r);
+  double rho_bar = 0.5 * (Lq.r + Rq.r), c_bar = 0.5 * (cL + cR);
+  double p_pvrs = 0.5 * (Lq.p + Rq.p) - 0.5 * (qnR - qnL) * rho_bar * c_bar;
+  double p_star = dmax(0.0, p_pvrs);
+  double gf = (g + 1.0) / (2.0 * g);
+  double qL = (p_star <= Lq.p) ? 1.0 : sqrt(1.0 + gf * (p_star / Lq.p - 1.0));
+  double qR = (p_star <= Rq.p) ? 1.0 : sqrt(1.0 + gf * (p_star / Rq.p - 1.0));
+  double SL = qnL - cL * qL, SR = qnR + cR * qR;
+  double EL = Lq.p / (g - 1.0) + 0.5 * Lq.r * (Lq.u * Lq.u + Lq.v * Lq.v);
+  double ER = Rq.p / (g - 1.0) + 0.5 * Rq.r * (Rq.u * Rq.u + Rq.v * Rq.v);
+  double S_star = (Rq.p - Lq.p + Lq.r * qnL * (SL - qnL) - Rq.r * qnR * (SR - qnR)) /
+                  (Lq.r * (SL - qnL) - Rq.r * (SR - qnR));
+  /* flux components in (normal, tangential) frame: mass, normal mom, tangential mom, energy */
+  double FLn[4] = {Lq.r * qnL, Lq.r * qnL * qnL + Lq.p, Lq.r * qnL * qtL, qnL * (EL + Lq.p)};
+  double FRn[4] = {Rq.r * qnR, Rq.r * qnR * qnR + Rq.p, Rq.r * qnR * qtR, qnR * (ER + Rq.p)};
+  double Fn[4];
+  if (SL >= 0.0) {
+    memcpy(Fn, FLn, sizeof Fn);
+  } else if (S_star >= 0.0) {
+    double f = Lq.r * (SL - qnL) / (SL - S_star);
+    double Us[4] = {f, f * S_star, f * qtL,
+                    f * (EL / Lq.r + (S_star - qnL) * (S_star + Lq.p / (Lq.r * (SL - qnL))))};
+    double Uk[4] = {Lq.r, Lq.r * qnL, Lq.r * qtL, EL};
+    for (int k = 0; k < 4; ++k) Fn[k] = FLn[k] + SL * (Us[k] - Uk[k]);
+  } else if (SR > 0.0) {
+    double f = Rq.r * (SR - qnR) / (SR - S_star);
+    double Us[4] = {f, f * S_star, f * qtR,
+                    f * (ER / Rq.r + (S_star - qnR) * (S_star + Rq.p / (Rq.r * (SR - qnR))))};
+    double Uk[4] = {Rq.r, Rq.r * qnR, Rq.r * qtR, ER};
+    for (int k = 0; k < 4; ++k) Fn[k] = FRn[k] + SR * (Us[k] - Uk[k]);
+  } else {
+    memcpy(Fn, FRn, sizeof Fn);
+  }
+  F[0] = Fn[0];
+  F[1] = dir == 0 ? Fn[1] : Fn[2];
+  F[2] = dir == 0 ? Fn[2] : Fn[1];
+  F[3] = Fn[3];
+}
+
+/* One edge flux from the reconstructed states; the cell pressures p (BC-filled) feed the
+ * shock sensors.  Edge (i,j) sits between cells (i,j) and (i+1,j) [dir 0] or (i,j+1) [dir 1]. */
+#define PN(n, t) (dir == 0 ? AT(p, i + (n), j + (t)) : AT(p, i + (t), j + (n)))
+static void edge_flux(dims_t d, const cato_config* c, int dir, const double* p, int i, int j,
+                      prim_t Lq, prim_t Rq, double F[4]) {
+  /* Cartesian edge normals: exactly (1,0) for i-edges and (0,1) for j-edges
+   * (quad_cell.f90:193-229 evaluated on axis-aligned cells) */
+  double nx = dir == 0 ? 1.0 : 0.0, ny = dir == 0 ? 0.0 : 1.0;
+  switch (c->flux) {
+    case CATO_FLUX_AUSMPW_PLUS: {
+      /* get_f arguments, ausmpw_plus_solver.fypp:430-442 */
+      double pc[4];
+      if (dir == 0) {
+        pc[0] = AT(p, i, j - 1); pc[1] = AT(p, i + 1, j - 1);
+        pc[2] = AT(p, i, j + 1); pc[3] = AT(p, i + 1, j + 1);
+      } else {
+        pc[0] = AT(p, i + 1, j); pc[1] = AT(p, i + 1, j + 1);
+        pc[2] = AT(p, i - 1, j); pc[3] = AT(p, i - 1, j + 1);
+      }
+      flux_ausmpw(c, dir, nx, ny, Lq, Rq, pc, F);
+      break;
+    }
+    case CATO_FLUX_SLAU:
+    case CATO_FLUX_SLAU2:
+    case CATO_FLUX_SD_SLAU:
+    case CATO_FLUX_SD_SLAU2: {
+      /* delta_p1..6 cell pairs, slau_solver.fypp:410-430 */
+      double pc[12] = {0};
+      if (c->flux == CATO_FLUX_SD_SLAU || c->flux == CATO_FLUX_SD_SLAU2) {
+        if (dir == 0) {
+          pc[0] = AT(p, i, j + 1);     pc[6] = AT(p, i, j);
+          pc[1] = AT(p, i - 1, j);     pc[7] = AT(p, i, j);
+          pc[2] = AT(p, i, j - 1);     pc[8] = AT(p, i, j);
+          pc[3] = AT(p, i + 1, j - 1); pc[9] = AT(p, i + 1, j);
+          pc[4] = AT(p, i + 2, j);     pc[10] = AT(p, i + 1, j);
+          pc[5] = AT(p, i + 1, j + 1); pc[11] = AT(p, i + 1, j);
+        } else {
+          pc[0] = AT(p, i - 1, j);     pc[6] = AT(p, i, j);
+          pc[1] = AT(p, i, j - 1);     pc[7] = AT(p, i, j);
+          pc[2] = AT(p, i + 1, j);     pc[8] = AT(p, i, j);
+          pc[3] = AT(p, i + 1, j + 1); pc[9] = AT(p, i, j + 1);
+          pc[4] = AT(p, i, j + 2);     pc[10] = AT(p, i, j + 1);
+          pc[5] = AT(p, i - 1, j + 1); pc[11] = AT(p, i, j + 1);
+        }
+      }
+      flux_slau(c, nx, ny, Lq, Rq, pc, F);
+      break;
+    }
+    case CATO_FLUX_ROE: {
+      /* f_p pairs, roe_solver.fypp:495-508 */
+      double pc[10];
+      if (dir == 0) {
+        pc[0] = AT(p, i, j);     pc[5] = AT(p, i + 1, j);
+        pc[1] = AT(p, i, j);     pc[6] = AT(p, i, j + 1);
+        pc[2] = AT(p, i, j);     pc[7] = AT(p, i, j - 1);
+        pc[3] = AT(p, i, j + 1); pc[8] = AT(p, i + 1, j + 1);
+        pc[4] = AT(p, i, j - 1); pc[9] = AT(p, i + 1, j - 1);
+      } else {
+        pc[0] = AT(p, i, j);     pc[5] = AT(p, i, j + 1);
+        pc[1] = AT(p, i, j);     pc[6] = AT(p, i - 1, j);
+        pc[2] = AT(p, i, j);     pc[7] = AT(p, i + 1, j);
+        pc[3] = AT(p, i, j + 1); pc[8] = AT(p, i - 1, j + 1);
+        pc[4] = AT(p, i, j + 1); pc[9] = AT(p, i + 1, j + 1);
+      }
+      flux_roe(c, nx, ny, Lq, Rq, pc, F);
+      break;
+    }
+    case CATO_FLUX_AUSM_PLUS_UP: flux_ausm_up(c, nx, ny, Lq, Rq, F); break;
+    case CATO_FLUX_HLLC: flux_hllc(c, dir, Lq, Rq, F); break;
+    default: F[0] = F[1] = F[2] = F[3] = NAN;
+  }
+}
+#undef PN
+
+/* flux_split_edges, flux_solver.f90:252-425 for one cell and one conserved variable k. */
+static double divergence(double Fi, double Fim, double Fj, double Fjm, const geom_t* g) {
+  const double REL_TOL = 1e-14;
+  const double near0 = 5.0 * TINY; /* near_zero, flux_solver.f90:461-474 */
+  double mi = dmax(dmax(fabs(Fi), fabs(Fim)), 1.0);
+  double mj = dmax(dmax(fabs(Fj), fabs(Fjm)), 1.0);
+  double a = ((Fi / mi * g->l[1]) + (-(Fim / mi * g->l[3]))) * mi;
+  double b = ((Fj / mj * g->l[2]) + (-(Fjm / mj * g->l[0]))) * mj;
+  if (fabs(a) < mi * REL_TOL) a = 0.0;
+  if (fabs(b) < mj * REL_TOL) b = 0.0;
+  double s = a + b;
+  if (fabs(s) < near0) s = 0.0;
+  return (-s) / g->vol;
+}
+
+/* flux_solver_t%solve for the edge-split solvers (e.g. slau_solver.fypp:123-249): BCs on the
+ * primitives, reconstruction, edge fluxes, flux divergence.  d_* are halo-padded, ghosts 0. */
+int oracle_solve(const cato_config* c, double* rho, double* u, double* v, double* p,
+                 double* drho, double* drhou, double* drhov, double* drhoE) {
+  dims_t d = mkdims(c);
+  geom_t geo = uniform_geom(c);
+  oracle_apply_bc(c, rho, u, v, p);
+  double* iflux = (double*)malloc(sizeof(double) * 4 * (size_t)(d.ni + 1) * d.nj);
+  double* jflux = (double*)malloc(sizeof(double) * 4 * (size_t)d.ni * (d.nj + 1));
+  if (!iflux || !jflux) { free(iflux); free(jflux); return CATO_ERR_OOM; }
+  const double* q[4] = {rho, u, v, p};
+  /* i-direction edges (0:ni, 1:nj) */
+#pragma omp parallel for schedule(static)
+  for (int j = 1; j <= d.nj; ++j)
+    for (int i = 0; i <= d.ni; ++i) {
+      double L[4], R[4];
+      for (int k = 0; k < 4; ++k) edge_recon(d, c->limiter, q[k], 0, i, j, &L[k], &R[k]);
+      prim_t Lq = {L[0], L[1], L[2], L[3]}, Rq = {R[0], R[1], R[2], R[3]};
+      edge_flux(d, c, 0, p, i, j, Lq, Rq, &IF(iflux, 0, i, j));
+    }
+  /* j-direction edges (1:ni, 0:nj) */
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j <= d.nj; ++j)
+    for (int i = 1; i <= d.ni; ++i) {
+      double L[4], R[4];
+      for (int k = 0; k < 4; ++k) edge_recon(d, c->limiter, q[k], 1, i, j, &L[k], &R[k]);
+      prim_t Lq = {L[0], L[1], L[2], L[3]}, Rq = {R[0], R[1], R[2], R[3]};
+      edge_flux(d, c, 1, p, i, j, Lq, Rq, &JF(jflux, 0, i, j));
+    }
+  double* out[4] = {drho, drhou, drhov, drhoE};
+  size_t n = nfield(d);
+  for (int k = 0; k < 4; ++k) memset(out[k], 0, n * sizeof(double));
+#pragma omp parallel for schedule(static)
+  for (int j = 1; j <= d.nj; ++j)
+    for (int i = 1; i <= d.ni; ++i)
+      for (int k = 0; k < 4; ++k)
+        AT(out[k], i, j) = divergence(IF(iflux, k, i, j), IF(iflux, k, i - 1, j),
+                                      JF(jflux, k, i, j), JF(jflux, k, i, j - 1), &geo);
+  free(iflux);
+  free(jflux);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* fluid_t                                                                                     */
+/* ------------------------------------------------------------------------------------------ */
+struct oracle_fluid {
+  cato_config c;
+  dims_t d;
+  geom_t geo;
+  /* conserved (U) and derived (u, v, p, cs) of the current state */
+  double *rho, *rhou, *rhov, *rhoE, *u, *v, *p, *cs;
+  /* scratch: stage states, primitive copies for the solver, residuals */
+  double* st[3][4];  /* stage conserved U_1, U_2 / U_prev, U_curr */
+  double* sp[4];     /* primitives handed to the solver (BCs write their ghosts) */
+  double* L[4];
+  double time, dt;
+  int64_t iteration;
+};
+
+static double* falloc(dims_t d) { return (double*)calloc(nfield(d), sizeof(double)); }
+
+oracle_fluid* oracle_create(const cato_config* c) {
+  if (oracle_config_check(c) != CATO_OK) return NULL;
+  oracle_fluid* f = (oracle_fluid*)calloc(1, sizeof(*f));
+  f->c = *c;
+  f->d = mkdims(c);
+  f->geo = uniform_geom(c);
+  double** all[] = {&f->rho, &f->rhou, &f->rhov, &f->rhoE, &f->u, &f->v, &f->p, &f->cs};
+  for (size_t k = 0; k < sizeof all / sizeof all[0]; ++k) *all[k] = falloc(f->d);
+  for (int s = 0; s < 3; ++s)
+    for (int k = 0; k < 4; ++k) f->st[s][k] = falloc(f->d);
+  for (int k = 0; k < 4; ++k) { f->sp[k] = falloc(f->d); f->L[k] = falloc(f->d); }
+  return f;
+}
+
+void oracle_destroy(oracle_fluid* f) {
+  if (!f) return;
+  double* all[] = {f->rho, f->rhou, f->rhov, f->rhoE, f->u, f->v, f->p, f->cs};
+  for (size_t k = 0; k < sizeof all / sizeof all[0]; ++k) free(all[k]);
+  for (int s = 0; s < 3; ++s)
+    for (int k = 0; k < 4; ++k) free(f->st[s][k]);
+  for (int k = 0; k < 4; ++k) { free(f->sp[k]); free(f->L[k]); }
+  free(f);
+}
+
+/* conserved -> primitive + sound speed + Mach filter, per interior cell:
+ * eos%conserved_to_primitive (equation_of_state.f90:297-314) through the field operators
+ * (field_2d_cpu_operators.f90:84-420: +/- flush |x|<eps, field/field returns 0 if |lhs|<tiny),
+ * eos%sound_speed (:269-278), and calculate_derived_quantities (mod_fluid.f90:564-591). */
+static void derive_cell(double g, double r, double ru, double rv, double rE, double* u_out,
+                        double* v_out, double* p_out, double* cs_out) {
+  double g1 = g - 1.0;
+  double u = (fabs(ru) < TINY) ? 0.0 : ru / r;
+  double v = (fabs(rv) < TINY) ? 0.0 : rv / r;
+  double e = (fabs(rE) < TINY) ? 0.0 : rE / r;
+  double s = u * u + v * v;
+  if (fabs(s) < EPS) s = 0.0;
+  double h = s * 0.5;
+  double dd = e - h;
+  if (fabs(dd) < EPS) dd = 0.0;
+  double p = (r * g1) * dd;
+  double pr = (fabs(p) < TINY) ? 0.0 : p / r;
+  double cs = sqrt(pr * g);
+  double mu = (fabs(u) < TINY) ? 0.0 : u / cs;
+  double mv = (fabs(v) < TINY) ? 0.0 : v / cs;
+  if (fabs(mv) < 1e-13) v = 0.0;
+  if (fabs(mu) < 1e-13) u = 0.0;
+  *u_out = u;
+  *v_out = v;
+  *p_out = p;
+  *cs_out = cs;
+}
+
+static void derive_all(oracle_fluid* f, double* const U[4], double* u, double* v, double* p,
+                       double* cs) {
+  dims_t d = f->d;
+#pragma omp parallel for schedule(static)
+  for (int j = 1; j <= d.nj; ++j)
+    for (int i = 1; i <= d.ni; ++i)
+      derive_cell(f->c.gamma, AT(U[0], i, j), AT(U[1], i, j), AT(U[2], i, j), AT(U[3], i, j),
+                  &AT(u, i, j), &AT(v, i, j), &AT(p, i, j), &AT(cs, i, j));
+}
+
+/* initialize_from_hdf5 + primitive_to_conserved (equation_of_state.f90:316-324 via the field
+ * operators) + the initial sound speed (mod_fluid.f90:249; no Mach filter at start). */
+int oracle_set_primitive(oracle_fluid* f, const double* rho, const double* u, const double* v,
+                         const double* p) {
+  dims_t d = f->d;
+  double g1 = f->c.gamma - 1.0;
+  double one_over_g1 = 1.0 / g1; /* field / real = field * (1/real), field_2d.f90:750-771 */
+  for (int j = 1; j <= d.nj; ++j)
+    for (int i = 1; i <= d.ni; ++i) {
+      double r = AT(rho, i, j), uu = AT(u, i, j), vv = AT(v, i, j), pp = AT(p, i, j);
+      AT(f->rho, i, j) = r;
+      AT(f->u, i, j) = uu;
+      AT(f->v, i, j) = vv;
+      AT(f->p, i, j) = pp;
+      AT(f->rhou, i, j) = uu * r;
+      AT(f->rhov, i, j) = vv * r;
+      double s = uu * uu + vv * vv;
+      if (fabs(s) < EPS) s = 0.0;
+      double E = pp * one_over_g1 + (r * 0.5) * s;
+      if (fabs(E) < EPS) E = 0.0;
+      AT(f->rhoE, i, j) = E;
+      double pr = (fabs(pp) < TINY) ? 0.0 : pp / r;
+      AT(f->cs, i, j) = sqrt(f->c.gamma * pr);
+    }
+  f->time = 0.0;
+  f->iteration = 0;
+  return 0;
+}
+
+int oracle_set_conserved(oracle_fluid* f, const double* rho, const double* rho_u,
+                         const double* rho_v, const double* rho_E) {
+  dims_t d = f->d;
+  for (int j = 1; j <= d.nj; ++j)
+    for (int i = 1; i <= d.ni; ++i) {
+      AT(f->rho, i, j) = AT(rho, i, j);
+      AT(f->rhou, i, j) = AT(rho_u, i, j);
+      AT(f->rhov, i, j) = AT(rho_v, i, j);
+      AT(f->rhoE, i, j) = AT(rho_E, i, j);
+    }
+  double* U[4] = {f->rho, f->rhou, f->rhov, f->rhoE};
+  derive_all(f, U, f->u, f->v, f->p, f->cs);
+  return 0;
+}
+
+/* get_timestep, mod_fluid.f90:518-562 (dx, dy = quad min_dx/min_dy, quad_cell.f90:119-123) */
+double oracle_get_timestep(oracle_fluid* f) {
+  dims_t d = f->d;
+  double m = INFINITY;
+  const double cfl = f->c.cfl, dx = f->geo.dx, dy = f->geo.dy;
+#pragma omp parallel for reduction(min : m) schedule(static)
+  for (int j = 1; j <= d.nj; ++j)
+    for (int i = 1; i <= d.ni; ++i) {
+      double cs = AT(f->cs, i, j);
+      double t = cfl / (((fabs(AT(f->u, i, j)) + cs) / dx) + ((fabs(AT(f->v, i, j)) + cs) / dy));
+      if (t < m) m = t;
+    }
+  return m;
+}
+
+/* L(U) for a state whose primitives are (pr, pu, pv, pp): time_derivative, mod_fluid.f90:460-516 */
+static int residual(oracle_fluid* f, const double* pr, const double* pu, const double* pv,
+                    const double* pp) {
+  size_t n = nfield(f->d) * sizeof(double);
+  memcpy(f->sp[0], pr, n);
+  memcpy(f->sp[1], pu, n);
+  memcpy(f->sp[2], pv, n);
+  memcpy(f->sp[3], pp, n);
+  return oracle_solve(&f->c, f->sp[0], f->sp[1], f->sp[2], f->sp[3], f->L[0], f->L[1], f->L[2],
+                      f->L[3]);
+}
+
+/* out = A + L*c with the field '+' flush (fluid operators mod_fluid.f90:609-669) */
+static void stage_a(oracle_fluid* f, double* const out[4], double* const A[4], double cc) {
+  dims_t d = f->d;
+  for (int k = 0; k < 4; ++k)
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= d.nj; ++j)
+      for (int i = 1; i <= d.ni; ++i) {
+        double r = AT(A[k], i, j) + AT(f->L[k], i, j) * cc;
+        if (fabs(r) < EPS) r = 0.0;
+        AT(out[k], i, j) = r;
+      }
+}
+
+/* out = (A*a + B*b) + L*c, each '+' flushed */
+static void stage_b(oracle_fluid* f, double* const out[4], double* const A[4], double a,
+                    double* const B[4], double b, double cc) {
+  dims_t d = f->d;
+  for (int k = 0; k < 4; ++k)
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= d.nj; ++j)
+      for (int i = 1; i <= d.ni; ++i) {
+        double s = AT(A[k], i, j) * a + AT(B[k], i, j) * b;
+        if (fabs(s) < EPS) s = 0.0;
+        double r = s + AT(f->L[k], i, j) * cc;
+        if (fabs(r) < EPS) r = 0.0;
+        AT(out[k], i, j) = r;
+      }
+}
+
+/* stage primitives (u, v, p, cs reused from the scratch solver arrays' neighbours) */
+typedef struct {
+  double *u, *v, *p, *cs;
+} prims_t;
+
+/* fluid_t%integrate (mod_fluid.f90:411-450) for ssp_rk2 (:1081-1160), ssp_rk3 (:739-854) and
+ * rk(m,n) (:889-1007); sanity check of the new state (:726-737) returns the reference codes. */
+int oracle_integrate(oracle_fluid* f, double dt, int32_t* error_code) {
+  dims_t d = f->d;
+  f->dt = dt;
+  f->iteration += 1;
+  double* U[4] = {f->rho, f->rhou, f->rhov, f->rhoE};
+  double *su[4], *sv[4], *spp[4], *scs[4];
+  /* per-stage derived quantities (u, v, p, cs), allocated on demand */
+  for (int s = 0; s < 4; ++s) { su[s] = falloc(d); sv[s] = falloc(d); spp[s] = falloc(d); scs[s] = falloc(d); }
+  int rc = 0;
+  if (f->c.rk == CATO_RK_SSP2) {
+    double* U1[4] = {f->st[0][0], f->st[0][1], f->st[0][2], f->st[0][3]};
+    double* U2[4] = {f->st[1][0], f->st[1][1], f->st[1][2], f->st[1][3]};
+    rc |= residual(f, f->rho, f->u, f->v, f->p);
+    stage_a(f, U1, U, dt);
+    derive_all(f, U1, su[0], sv[0], spp[0], scs[0]);
+    rc |= residual(f, U1[0], su[0], sv[0], spp[0]);
+    stage_b(f, U2, U, 0.5, U1, 0.5, 0.5 * dt);
+    for (int k = 0; k < 4; ++k) memcpy(U[k], U2[k], nfield(d) * sizeof(double));
+  } else if (f->c.rk == CATO_RK_SSP3) {
+    double* U1[4] = {f->st[0][0], f->st[0][1], f->st[0][2], f->st[0][3]};
+    double* U2[4] = {f->st[1][0], f->st[1][1], f->st[1][2], f->st[1][3]};
+    double* U3[4] = {f->st[2][0], f->st[2][1], f->st[2][2], f->st[2][3]};
+    rc |= residual(f, f->rho, f->u, f->v, f->p);
+    stage_a(f, U1, U, dt);
+    derive_all(f, U1, su[0], sv[0], spp[0], scs[0]);
+    rc |= residual(f, U1[0], su[0], sv[0], spp[0]);
+    stage_b(f, U2, U, 3.0 / 4.0, U1, 1.0 / 4.0, (1.0 / 4.0) * dt);
+    derive_all(f, U2, su[1], sv[1], spp[1], scs[1]);
+    rc |= residual(f, U2[0], su[1], sv[1], spp[1]);
+    stage_b(f, U3, U, 1.0 / 3.0, U2, 2.0 / 3.0, (2.0 / 3.0) * dt);
+    for (int k = 0; k < 4; ++k) memcpy(U[k], U3[k], nfield(d) * sizeof(double));
+  } else {
+    /* rk(m,n), mod_fluid.f90:926-966 */
+    static const double a13[] = {0.1481, 0.4, 1.0}, a14[] = {0.0833, 0.2069, 0.4265, 1.0},
+                        a15[] = {0.0533, 0.1263, 0.2375, 0.4414, 1.0}, a23[] = {0.1918, 0.4929, 1.0},
+                        a24[] = {0.1084, 0.2602, 0.5052, 1.0},
+                        a25[] = {0.0695, 0.1602, 0.2898, 0.5060, 1.0};
+    const double* alpha;
+    int ns;
+    switch (f->c.rk) {
+      case CATO_RK_1_3: alpha = a13; ns = 3; break;
+      case CATO_RK_1_4: alpha = a14; ns = 4; break;
+      case CATO_RK_1_5: alpha = a15; ns = 5; break;
+      case CATO_RK_2_3: alpha = a23; ns = 3; break;
+      case CATO_RK_2_4: alpha = a24; ns = 4; break;
+      default: alpha = a25; ns = 5; break;
+    }
+    double* U0[4] = {f->st[0][0], f->st[0][1], f->st[0][2], f->st[0][3]};
+    double* Uc[4] = {f->st[1][0], f->st[1][1], f->st[1][2], f->st[1][3]};
+    for (int k = 0; k < 4; ++k) memcpy(U0[k], U[k], nfield(d) * sizeof(double));
+    /* U_prev starts as a copy of U (its primitives are U's) */
+    for (int m = 0; m < ns; ++m) {
+      if (m == 0) rc |= residual(f, f->rho, f->u, f->v, f->p);
+      else rc |= residual(f, Uc[0], su[0], sv[0], spp[0]);
+      stage_a(f, Uc, U0, dt * alpha[m]);
+      derive_all(f, Uc, su[0], sv[0], spp[0], scs[0]);
+    }
+    for (int k = 0; k < 4; ++k) memcpy(U[k], Uc[k], nfield(d) * sizeof(double));
+  }
+  f->time = f->time + dt;
+  derive_all(f, U, f->u, f->v, f->p, f->cs);
+  int32_t ec = 0;
+  for (int j = 1; j <= d.nj && !ec; ++j)
+    for (int i = 1; i <= d.ni; ++i) {
+      double r = AT(f->rho, i, j), pp = AT(f->p, i, j);
+      if (isnan(r) || isnan(AT(f->u, i, j)) || isnan(AT(f->v, i, j)) || isnan(pp)) { ec = CATO_NANS_FOUND; break; }
+      if (r < 0.0) { ec = CATO_NEG_DENSITY; break; }
+      if (pp < 0.0) { ec = CATO_NEG_PRESSURE; break; }
+    }
+  if (error_code) *error_code = ec;
+  for (int s = 0; s < 4; ++s) { free(su[s]); free(sv[s]); free(spp[s]); free(scs[s]); }
+  return rc;
+}
+
+int oracle_get_state(oracle_fluid* f, double* rho, double* rho_u, double* rho_v, double* rho_E,
+                     double* u, double* v, double* p, double* cs) {
+  size_t n = nfield(f->d) * sizeof(double);
+  dims_t d = f->d;
+  double* src[8] = {f->rho, f->rhou, f->rhov, f->rhoE, f->u, f->v, f->p, f->cs};
+  double* dst[8] = {rho, rho_u, rho_v, rho_E, u, v, p, cs};
+  for (int k = 0; k < 8; ++k) {
+    if (!dst[k]) continue;
+    memset(dst[k], 0, n);
+    for (int j = 1; j <= d.nj; ++j)
+      for (int i = 1; i <= d.ni; ++i) AT(dst[k], i, j) = AT(src[k], i, j);
+  }
+  return 0;
+}
+
+double oracle_time(oracle_fluid* f) { return f->time; }
+int64_t oracle_iteration(oracle_fluid* f) { return f->iteration; }
+
+/* ------------------------------------------------------------------------------------------ */
+/* configuration                                                                                */
+/* ------------------------------------------------------------------------------------------ */
+int oracle_config_default(cato_config* c, int32_t ni, int32_t nj) {
+  if (!c) return CATO_ERR_ARG;
+  memset(c, 0, sizeof(*c));
+  c->ni = ni;
+  c->nj = nj;
+  c->n_ghost = 2;
+  c->flux = CATO_FLUX_AUSMPW_PLUS;
+  c->limiter = CATO_LIM_MINMOD;
+  c->rk = CATO_RK_SSP2;
+  for (int s = 0; s < 4; ++s) c->bc[s] = CATO_BC_PERIODIC;
+  c->apply_low_mach_fix = 1;
+  c->precision = CATO_FP64;
+  c->roe_entropy_fix = CATO_ROE_REFERENCE;
+  c->gamma = 5.0 / 3.0;
+  c->cfl = 0.1;
+  c->dx = 1.0;
+  c->dy = 1.0;
+  c->harten_delta = 0.1;
+  c->ausm_beta = 1.0 / 8.0;
+  c->ausm_kp = 0.25;
+  c->ausm_ku = 0.75;
+  c->ausm_sigma = 1.0;
+  return CATO_OK;
+}
+
+int oracle_config_check(const cato_config* c) {
+  if (!c) return CATO_ERR_ARG;
+  if (c->ni < 1 || c->nj < 1) return CATO_ERR_CONFIG;
+  if (c->flux < CATO_FLUX_AUSMPW_PLUS || c->flux > CATO_FLUX_HLLC) return CATO_ERR_CONFIG;
+  if (c->limiter < CATO_LIM_MINMOD || c->limiter > CATO_LIM_MLP5) return CATO_ERR_CONFIG;
+  if (c->rk < CATO_RK_SSP2 || c->rk > CATO_RK_2_5) return CATO_ERR_CONFIG;
+  int need = (c->limiter == CATO_LIM_MLP5) ? 3 : 2; /* mod_input.f90:320-338 */
+  if (c->n_ghost != need) return CATO_ERR_CONFIG;
+  if (c->ni < c->n_ghost || c->nj < c->n_ghost) return CATO_ERR_CONFIG;
+  for (int s = 0; s < 4; ++s)
+    if (c->bc[s] < CATO_BC_ZERO_GRADIENT || c->bc[s] > CATO_BC_PERIODIC) return CATO_ERR_CONFIG;
+  /* periodic must be paired on an axis (an unpaired side leaves ghost cells unset) */
+  if ((c->bc[CATO_PLUS_X] == CATO_BC_PERIODIC) != (c->bc[CATO_MINUS_X] == CATO_BC_PERIODIC))
+    return CATO_ERR_CONFIG;
+  if ((c->bc[CATO_PLUS_Y] == CATO_BC_PERIODIC) != (c->bc[CATO_MINUS_Y] == CATO_BC_PERIODIC))
+    return CATO_ERR_CONFIG;
+  if (!(c->gamma > 1.0) || !(c->cfl > 0.0) || !(c->dx > 0.0) || !(c->dy > 0.0))
+    return CATO_ERR_CONFIG;
+  if (c->precision != CATO_FP64 && c->precision != CATO_MIXED) return CATO_ERR_CONFIG;
+  if (c->roe_entropy_fix != CATO_ROE_REFERENCE && c->roe_entropy_fix != CATO_ROE_HARTEN)
+    return CATO_ERR_CONFIG;
+  return CATO_OK;
+}

@@ -1,0 +1,199 @@
+"""TEST INFRASTRUCTURE ONLY: Python binding of the C parity oracle (``oracle/cato_oracle.c``).
+
+The oracle restates the reference's FP64 arithmetic on the CPU.  Only ``tests/``,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg import this module; the product
+package ``fvleg_2d_gb300`` never does.
+
+Fields are numpy float64 arrays of shape ``(ni + 2*ng, nj + 2*ng)`` in Fortran order, i.e. the
+reference's ``field_2d_t%data`` with bounds ``(1-ng:ni+ng, 1-ng:nj+ng)``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from fvleg_2d_gb300.config import CatoConfig, SchemeConfig
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libcato_oracle.so")
+_lib = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def build() -> str:
+    """Compile the oracle (make in oracle/); returns the library path."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        cfgp = ctypes.POINTER(CatoConfig)
+        L.oracle_set_threads.restype = ctypes.c_int
+        L.oracle_set_threads.argtypes = [ctypes.c_int]
+        L.oracle_get_threads.restype = ctypes.c_int
+        L.oracle_config_check.argtypes = [cfgp]
+        L.oracle_limiter.restype = ctypes.c_double
+        L.oracle_limiter.argtypes = [ctypes.c_int32, ctypes.c_double]
+        L.oracle_quad_metrics.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.oracle_apply_bc.argtypes = [cfgp, _dp, _dp, _dp, _dp]
+        L.oracle_apply_bc_side.argtypes = [cfgp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           _dp, _dp, _dp, _dp]
+        L.oracle_interpolate_edges.argtypes = [cfgp, _dp, _dp, _dp]
+        L.oracle_solve.argtypes = [cfgp] + [_dp] * 8
+        L.oracle_create.restype = ctypes.c_void_p
+        L.oracle_create.argtypes = [cfgp]
+        L.oracle_destroy.argtypes = [ctypes.c_void_p]
+        L.oracle_set_primitive.argtypes = [ctypes.c_void_p] + [_dp] * 4
+        L.oracle_set_conserved.argtypes = [ctypes.c_void_p] + [_dp] * 4
+        L.oracle_get_timestep.restype = ctypes.c_double
+        L.oracle_get_timestep.argtypes = [ctypes.c_void_p]
+        L.oracle_integrate.argtypes = [ctypes.c_void_p, ctypes.c_double,
+                                       ctypes.POINTER(ctypes.c_int32)]
+        L.oracle_get_state.argtypes = [ctypes.c_void_p] + [_dp] * 8
+        L.oracle_time.restype = ctypes.c_double
+        L.oracle_time.argtypes = [ctypes.c_void_p]
+        L.oracle_iteration.restype = ctypes.c_int64
+        L.oracle_iteration.argtypes = [ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.f_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def set_threads(n: int) -> int:
+    return lib().oracle_set_threads(int(n))
+
+
+def limiter(name_or_id, r: float) -> float:
+    from fvleg_2d_gb300.config import LIMITER_IDS
+
+    lid = LIMITER_IDS[name_or_id] if isinstance(name_or_id, str) else int(name_or_id)
+    return lib().oracle_limiter(lid, float(r))
+
+
+def quad_metrics(x, y):
+    """quad_cell_t metrics of a cell with nodes (x[k], y[k]), k = 1..4 counter-clockwise."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    vol = np.zeros(1)
+    el = np.zeros(4)
+    nv = np.zeros(8)
+    mdx = np.zeros(1)
+    mdy = np.zeros(1)
+    lib().oracle_quad_metrics(*(a.ctypes.data_as(_dp) for a in (x, y, vol, el, nv, mdx, mdy)))
+    return {"volume": vol[0], "edge_lengths": el, "edge_norm_vectors": nv.reshape(4, 2),
+            "min_dx": mdx[0], "min_dy": mdy[0]}
+
+
+def _cfg(cfg):
+    return ctypes.byref(cfg.to_c() if isinstance(cfg, SchemeConfig) else cfg)
+
+
+def empty_field(cfg: SchemeConfig) -> np.ndarray:
+    return np.zeros(cfg.halo_shape, dtype=np.float64, order="F")
+
+
+def apply_bc(cfg: SchemeConfig, rho, u, v, p) -> None:
+    """In place, like flux_solver_t%apply_primitive_bc."""
+    lib().oracle_apply_bc(_cfg(cfg), _ptr(rho), _ptr(u), _ptr(v), _ptr(p))
+
+
+def apply_bc_side(cfg: SchemeConfig, side: str, bc_type: str, do_corners: bool, rho, u, v, p):
+    """One boundary condition on one side ('+x', '+y', '-x', '-y'), in place."""
+    from fvleg_2d_gb300.config import BC_IDS, SIDES
+
+    lib().oracle_apply_bc_side(_cfg(cfg), SIDES.index(side), BC_IDS[bc_type], int(do_corners),
+                               _ptr(rho), _ptr(u), _ptr(v), _ptr(p))
+
+
+def interpolate_edges(cfg: SchemeConfig, q):
+    """Returns (i_edges(2, -1:ni, 0:nj), j_edges(2, 0:ni, -1:nj)) as Fortran-order arrays."""
+    ni, nj = cfg.ni, cfg.nj
+    ie = np.zeros((2, ni + 2, nj + 1), order="F")
+    je = np.zeros((2, ni + 1, nj + 2), order="F")
+    lib().oracle_interpolate_edges(_cfg(cfg), _ptr(q), _ptr(ie), _ptr(je))
+    return ie, je
+
+
+def solve(cfg: SchemeConfig, rho, u, v, p):
+    """flux_solver_t%solve: BCs written into the ghosts of rho/u/v/p; returns d/dt of U."""
+    out = [empty_field(cfg) for _ in range(4)]
+    rc = lib().oracle_solve(_cfg(cfg), _ptr(rho), _ptr(u), _ptr(v), _ptr(p),
+                            *(_ptr(a) for a in out))
+    if rc != 0:
+        raise RuntimeError(f"oracle_solve failed: {rc}")
+    return out
+
+
+class OracleFluid:
+    """fluid_t restated on the CPU."""
+
+    def __init__(self, cfg: SchemeConfig):
+        self.cfg = cfg
+        self._c = cfg.to_c()
+        self._h = lib().oracle_create(ctypes.byref(self._c))
+        if not self._h:
+            raise ValueError("invalid configuration")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().oracle_destroy(h)
+            self._h = None
+
+    def set_primitive(self, rho, u, v, p) -> None:
+        arrs = [np.asfortranarray(a, dtype=np.float64) for a in (rho, u, v, p)]
+        lib().oracle_set_primitive(self._h, *(_ptr(a) for a in arrs))
+
+    def set_conserved(self, rho, rho_u, rho_v, rho_E) -> None:
+        arrs = [np.asfortranarray(a, dtype=np.float64) for a in (rho, rho_u, rho_v, rho_E)]
+        lib().oracle_set_conserved(self._h, *(_ptr(a) for a in arrs))
+
+    def get_timestep(self) -> float:
+        return lib().oracle_get_timestep(self._h)
+
+    def integrate(self, dt: float | None = None) -> int:
+        if dt is None or dt <= 0:
+            dt = self.get_timestep()
+        ec = ctypes.c_int32(0)
+        rc = lib().oracle_integrate(self._h, float(dt), ctypes.byref(ec))
+        if rc != 0:
+            raise RuntimeError(f"oracle_integrate failed: {rc}")
+        self.last_dt = dt
+        return ec.value
+
+    def state(self) -> dict:
+        names = ("rho", "rho_u", "rho_v", "rho_E", "u", "v", "p", "cs")
+        out = {k: empty_field(self.cfg) for k in names}
+        lib().oracle_get_state(self._h, *(_ptr(out[k]) for k in names))
+        return out
+
+    @property
+    def time(self) -> float:
+        return lib().oracle_time(self._h)
+
+    @property
+    def iteration(self) -> int:
+        return lib().oracle_iteration(self._h)
+
+    def run(self, t_end: float, max_steps: int = 10**9) -> int:
+        """The main.f90 time loop (CFL dt each step, no last-step trim); returns steps taken."""
+        n = 0
+        while self.time < t_end and n < max_steps:
+            ec = self.integrate()
+            n += 1
+            if ec != 0:
+                raise RuntimeError(f"fluid error code {ec} at step {n}")
+        return n

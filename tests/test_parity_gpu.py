@@ -1,0 +1,122 @@
+"""GPU parity: the sm_103a kernels against the C oracle, through the C-ABI.
+
+FP64 path: bit-identical to the oracle (the oracle restates the reference's FP64 operation
+order; both sides round every operation on its own), checked with exact equality.
+Mixed path: FP32 reconstruction/flux with FP64 state accumulation; tolerance stated per test.
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+from conftest import interior, random_prims
+from fvleg_2d_gb300 import ic
+from fvleg_2d_gb300.config import SchemeConfig
+from fvleg_2d_gb300.fluid import Fluid, FluxSolver, MusclInterpolator
+
+pytestmark = pytest.mark.gpu
+
+FLUXES = ["AUSMPW+", "SLAU", "SLAU2", "SD-SLAU", "SD-SLAU2", "Roe", "AUSM+-up", "HLLC"]
+LIMITERS = ["minmod", "superbee", "van_leer", "MLP3", "MLP5"]
+BCS = {
+    "zg": {"+x": "zero_gradient", "-x": "zero_gradient", "+y": "zero_gradient", "-y": "zero_gradient"},
+    "zg_sym": {"+x": "zero_gradient", "-x": "zero_gradient", "+y": "symmetry", "-y": "symmetry"},
+    "per_sym": {"+x": "periodic", "-x": "periodic", "+y": "symmetry", "-y": "symmetry"},
+    "per": {"+x": "periodic", "-x": "periodic", "+y": "periodic", "-y": "periodic"},
+    "sym_per": {"+x": "symmetry", "-x": "symmetry", "+y": "periodic", "-y": "periodic"},
+}
+
+
+def _cfg(flux, limiter, bc, ni=131, nj=23, **kw):
+    return SchemeConfig(ni=ni, nj=nj, dx=1.0 / ni, dy=0.7 / nj, flux_solver=flux, limiter=limiter,
+                        bc=BCS[bc], gamma=1.4, cfl=0.4, **kw)
+
+
+@pytest.mark.parametrize("flux,limiter", list(itertools.product(FLUXES, LIMITERS)))
+def test_solve_bitexact(oracle, cato_lib, flux, limiter):
+    """flux_solver_t%solve: residuals and BC-filled ghosts identical to the oracle."""
+    bc = ["zg", "zg_sym", "per_sym", "per", "sym_per"][(FLUXES.index(flux) + LIMITERS.index(limiter)) % 5]
+    cfg = _cfg(flux, limiter, bc)
+    rng = np.random.default_rng(FLUXES.index(flux) * 10 + LIMITERS.index(limiter))
+    prims = random_prims(cfg, rng)
+    ref_in = [a.copy(order="F") for a in prims]
+    gpu_in = [a.copy(order="F") for a in prims]
+    ref = oracle.solve(cfg, *ref_in)
+    got = FluxSolver(cfg).solve(*gpu_in)
+    for k in range(4):
+        np.testing.assert_array_equal(got[k], ref[k], err_msg=f"d/dt var {k}")
+        np.testing.assert_array_equal(gpu_in[k], ref_in[k], err_msg=f"BC ghosts var {k}")
+
+
+@pytest.mark.parametrize("limiter", LIMITERS)
+def test_interpolate_edges_bitexact(oracle, cato_lib, limiter):
+    cfg = _cfg("AUSMPW+", limiter, "per_sym", ni=45, nj=19)
+    rng = np.random.default_rng(7)
+    q = random_prims(cfg, rng)[0]
+    tmp = [q.copy(order="F") for _ in range(4)]
+    oracle.apply_bc(cfg, *tmp)
+    q = tmp[0]
+    ie_ref, je_ref = oracle.interpolate_edges(cfg, q)
+    ie, je = MusclInterpolator(cfg).interpolate_edge_values(q)
+    np.testing.assert_array_equal(ie, ie_ref)
+    np.testing.assert_array_equal(je, je_ref)
+
+
+def _run_pair(oracle, cfg, prims, n_steps):
+    ref = oracle.OracleFluid(cfg)
+    ref.set_primitive(*prims)
+    gpu = Fluid(cfg).initialize(*prims)
+    assert gpu.get_timestep() == ref.get_timestep()
+    for n in range(n_steps):
+        dt_ref = ref.get_timestep()
+        ec_ref = ref.integrate(dt_ref)
+        dt_gpu, ec_gpu = gpu.integrate()
+        assert dt_gpu == dt_ref, f"step {n}: dt {dt_gpu!r} != {dt_ref!r}"
+        assert ec_gpu == ec_ref
+    return ref, gpu
+
+
+@pytest.mark.parametrize("rk", ["ssp_rk2", "ssp_rk3", "rk(1,3)", "rk(2,4)"])
+@pytest.mark.parametrize("flux", FLUXES)
+def test_steps_bitexact(oracle, cato_lib, rk, flux):
+    """fluid_t%integrate over several CFL steps: state identical to the oracle."""
+    limiter = {"SLAU": "MLP5", "SD-SLAU": "MLP3", "Roe": "superbee", "HLLC": "van_leer"}.get(flux, "minmod")
+    bc = ["zg", "zg_sym", "per_sym", "per", "sym_per"][(FLUXES.index(flux) + len(rk)) % 5]
+    cfg = _cfg(flux, limiter, bc, ni=70, nj=41, integration_strategy=rk)
+    prims = random_prims(cfg, np.random.default_rng(3))
+    ref, gpu = _run_pair(oracle, cfg, prims, 6)
+    a, b = ref.state(), gpu.state()
+    for k in ("rho", "rho_u", "rho_v", "rho_E", "u", "v", "p", "cs"):
+        np.testing.assert_array_equal(b[k], a[k], err_msg=k)
+    assert gpu.iteration == ref.iteration == 6
+    assert gpu.time == ref.time
+
+
+def test_sod_full_run_bitexact(oracle, cato_lib):
+    """Sod 400x40, AUSMPW+/minmod/SSP-RK2, CFL 0.5 to t=0.2 (reference semantics: CFL dt each
+    step, no last-step trim): identical step count, time and state."""
+    cfg, prims = ic.sod()
+    ref = oracle.OracleFluid(cfg)
+    ref.set_primitive(*prims)
+    n_ref = ref.run(0.2)
+    gpu = Fluid(cfg).initialize(*prims)
+    n_gpu = gpu.run(0.2)
+    assert n_gpu == n_ref
+    assert gpu.time == ref.time
+    a, b = ref.state(), gpu.state()
+    for k in ("rho", "rho_u", "rho_v", "rho_E"):
+        np.testing.assert_array_equal(b[k], a[k], err_msg=k)
+
+
+def test_mixed_sod_density_error(oracle, cato_lib):
+    """Mixed path (FP32 flux, FP64 state): relative L1 density error vs FP64 <= 1e-6 on Sod."""
+    cfg, prims = ic.sod()
+    fp = Fluid(cfg).initialize(*prims)
+    fp.run(0.2)
+    cfg_m, _ = ic.sod(precision="mixed")
+    mx = Fluid(cfg_m).initialize(*prims)
+    mx.run(0.2)
+    r64 = interior(cfg, fp.state(("rho",))["rho"])
+    r32 = interior(cfg_m, mx.state(("rho",))["rho"])
+    l1 = np.abs(r32 - r64).sum() / np.abs(r64).sum()
+    assert l1 <= 1e-6, l1
