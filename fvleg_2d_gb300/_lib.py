@@ -64,6 +64,15 @@ def load(build_if_missing: bool = False):
         "cato_gpu_interpolate_edges": (ctypes.c_int, [H, _dp, i64, _dp, _dp]),
         "cato_gpu_status": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int32)]),
         "cato_gpu_synchronize": (ctypes.c_int, [H]),
+        "cato_gpu_set_stream": (ctypes.c_int, [H, ctypes.c_void_p]),
+        "cato_gpu_profile_step": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_float), ctypes.c_int32,
+                                                 ctypes.POINTER(ctypes.c_int32)]),
+        "cato_gpu_launches_per_step": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int32)]),
+        "cato_gpu_run_timed": (ctypes.c_int, [H, i64, ctypes.POINTER(ctypes.c_float),
+                                              ctypes.POINTER(ctypes.c_float), ctypes.c_int32]),
+        "cato_gpu_select_device": (ctypes.c_int, [ctypes.c_int32]),
+        "cato_host_alloc": (ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]),
+        "cato_host_free": (ctypes.c_int, [ctypes.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -71,6 +80,33 @@ def load(build_if_missing: bool = False):
         fn.argtypes = args
     _lib = L
     return _lib
+
+
+class PinnedArray:
+    """A Fortran-ordered float64 numpy view of page-locked host memory (cato_host_alloc)."""
+
+    def __init__(self, shape):
+        import numpy as np
+
+        n = int(np.prod(shape)) * 8
+        self._p = ctypes.c_void_p()
+        rc = load().cato_host_alloc(n, ctypes.byref(self._p))
+        if rc != 0:
+            raise CatoLibraryError(f"cato_host_alloc({n}) failed: {rc}")
+        buf = (ctypes.c_double * (n // 8)).from_address(self._p.value)
+        self.array = np.frombuffer(buf, dtype=np.float64).reshape(shape, order="F")
+
+    def free(self):
+        if self._p:
+            self.array = None
+            load().cato_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def ptr(a) -> "ctypes._Pointer":

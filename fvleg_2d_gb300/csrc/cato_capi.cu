@@ -60,6 +60,8 @@ struct cato_handle {
   Geom G{};
   std::vector<Stage> stages;
   std::string err;
+  cudaStream_t own_stream_saved = nullptr;
+  cudaEvent_t* event_hook = nullptr;  // profile_step: event k+1 recorded after kernel k
 };
 
 static thread_local std::string g_null_err;
@@ -210,6 +212,7 @@ static cudaError_t launch(cato_handle* h, const StageArgs& A) {
 static int enqueue_step(cato_handle* h) {
   step_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctl);
   CK(cudaGetLastError());
+  if (h->event_hook) CK(cudaEventRecord(h->event_hook[1], h->stream));
   const int ns = (int)h->stages.size();
   const bool fp64 = h->cfg.precision == CATO_FP64;
   for (int k = 0; k < ns; ++k) {
@@ -246,6 +249,7 @@ static int enqueue_step(cato_handle* h) {
       if (st.kind == 0) A.b = 0.0;  // rk(m,n): U_curr = U_0 + c L(U_prev)
     }
     CK(launch(h, A));
+    if (h->event_hook) CK(cudaEventRecord(h->event_hook[k + 2], h->stream));
   }
   if (!fp64) h->cur = 1 - h->cur;
   h->raw_pending = false;
@@ -442,6 +446,7 @@ int cato_gpu_destroy(cato_handle* h) {
   for (int k = 0; k < 4; ++k) cudaFree(h->halo[k]);
   cudaFree(h->ctl);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
+  if (h->own_stream_saved) h->stream = h->own_stream_saved;
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return CATO_OK;
@@ -703,6 +708,109 @@ int cato_gpu_synchronize(cato_handle* h) {
   if (!h) return CATO_ERR_ARG;
   CK(cudaStreamSynchronize(h->stream));
   return CATO_OK;
+}
+
+int cato_gpu_set_stream(cato_handle* h, void* stream) {
+  if (!h) return CATO_ERR_ARG;
+  CK(cudaStreamSynchronize(h->stream));
+  if (stream) {
+    if (!h->own_stream_saved) h->own_stream_saved = h->stream;
+    h->stream = (cudaStream_t)stream;
+  } else if (h->own_stream_saved) {
+    h->stream = h->own_stream_saved;
+  }
+  return CATO_OK;
+}
+
+int cato_gpu_run_timed(cato_handle* h, int64_t n_steps, float* total_ms, float* kernel_ms,
+                       int32_t capacity) {
+  if (!h || !total_ms || n_steps < 0) return CATO_ERR_ARG;
+  if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  const int nk = 1 + (int)h->stages.size();
+  if (kernel_ms && capacity < nk) return fail(h, CATO_ERR_ARG, "capacity too small");
+  int rc = pull_ctl(h);
+  if (rc) return rc;
+  StepCtl c = *h->ctl_host;
+  const long long it0 = c.iter;
+  c.t_end = INFINITY;
+  c.max_iter = it0 + n_steps;
+  c.fixed_dt = 0.0;
+  *h->ctl_host = c;
+  CK(cudaMemcpyAsync(h->ctl, h->ctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice, h->stream));
+  // events: [start] + one after every kernel of every step
+  std::vector<cudaEvent_t> ev(kernel_ms ? (size_t)n_steps * nk + 1 : 2);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  CK(cudaEventRecord(ev[0], h->stream));
+  const int parity0 = h->cur;
+  for (long long s = 0; s < n_steps; ++s) {
+    if (kernel_ms) h->event_hook = ev.data() + s * nk;
+    rc = enqueue_step(h);
+    h->event_hook = nullptr;
+    if (rc) return rc;
+  }
+  if (!kernel_ms) CK(cudaEventRecord(ev[1], h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaEventElapsedTime(total_ms, ev[0], ev.back()));
+  if (kernel_ms) {
+    for (int k = 0; k < nk; ++k) kernel_ms[k] = 0.0f;
+    for (long long s = 0; s < n_steps; ++s)
+      for (int k = 0; k < nk; ++k) {
+        float ms;
+        CK(cudaEventElapsedTime(&ms, ev[s * nk + k], ev[s * nk + k + 1]));
+        kernel_ms[k] += ms;
+      }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  rc = pull_ctl(h);
+  if (rc) return rc;
+  if (h->cfg.precision == CATO_MIXED)
+    h->cur = (int)((parity0 + (h->ctl_host->iter - it0)) & 1);
+  return status_code(h->ctl_host->status);
+}
+
+int cato_gpu_select_device(int32_t device) {
+  return cudaSetDevice(device) == cudaSuccess ? CATO_OK : CATO_ERR_CUDA;
+}
+
+int cato_host_alloc(uint64_t bytes, void** out) {
+  if (!out) return CATO_ERR_ARG;
+  *out = nullptr;
+  return cudaHostAlloc(out, bytes, cudaHostAllocPortable) == cudaSuccess ? CATO_OK : CATO_ERR_OOM;
+}
+
+int cato_host_free(void* p) { return cudaFreeHost(p) == cudaSuccess ? CATO_OK : CATO_ERR_CUDA; }
+
+int cato_gpu_launches_per_step(const cato_handle* h, int32_t* n) {
+  if (!h || !n) return CATO_ERR_ARG;
+  *n = 1 + (int32_t)h->stages.size();
+  return CATO_OK;
+}
+
+int cato_gpu_profile_step(cato_handle* h, float* kernel_ms, int32_t capacity, int32_t* n_kernels) {
+  if (!h || !kernel_ms) return CATO_ERR_ARG;
+  if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  const int nk = 1 + (int)h->stages.size();
+  if (capacity < nk) return fail(h, CATO_ERR_ARG, "capacity too small");
+  int rc = pull_ctl(h);
+  if (rc) return rc;
+  StepCtl c = *h->ctl_host;
+  c.t_end = INFINITY;
+  c.max_iter = c.iter + 1;
+  c.fixed_dt = 0.0;
+  *h->ctl_host = c;
+  CK(cudaMemcpyAsync(h->ctl, h->ctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice, h->stream));
+  std::vector<cudaEvent_t> ev(nk + 1);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  h->event_hook = ev.data();
+  CK(cudaEventRecord(ev[0], h->stream));
+  rc = enqueue_step(h);
+  h->event_hook = nullptr;
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  for (int k = 0; k < nk; ++k) CK(cudaEventElapsedTime(&kernel_ms[k], ev[k], ev[k + 1]));
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (n_kernels) *n_kernels = nk;
+  return pull_ctl(h);
 }
 
 }  // extern "C"

@@ -108,6 +108,31 @@ class Fluid(_Handle):
             raise CatoError(ec.value, f"after {steps.value} steps at t={t.value}")
         return steps.value
 
+    def run_timed(self, n_steps: int, per_kernel: bool = False):
+        """Exactly n_steps CFL steps on the device, timed with CUDA events on the handle's
+        stream.  Returns (total_ms, per-kernel-slot ms or None)."""
+        total = ctypes.c_float()
+        n = ctypes.c_int32()
+        _check(self.L.cato_gpu_launches_per_step(self.h, ctypes.byref(n)), self.h)
+        ks = (ctypes.c_float * n.value)() if per_kernel else None
+        rc = self.L.cato_gpu_run_timed(self.h, int(n_steps), ctypes.byref(total), ks,
+                                       n.value if per_kernel else 0)
+        _check(rc, self.h, "run_timed")
+        return total.value, (list(ks) if per_kernel else None)
+
+    def launches_per_step(self) -> int:
+        n = ctypes.c_int32()
+        _check(self.L.cato_gpu_launches_per_step(self.h, ctypes.byref(n)), self.h)
+        return n.value
+
+    def profile_step(self) -> list:
+        """One CFL step with per-kernel CUDA-event times (ms): [step control, stage 1, ...]."""
+        n = self.launches_per_step()
+        ks = (ctypes.c_float * n)()
+        got = ctypes.c_int32()
+        _check(self.L.cato_gpu_profile_step(self.h, ks, n, ctypes.byref(got)), self.h, "profile")
+        return list(ks)[: got.value]
+
     def set_time(self, time: float, iteration: int) -> None:
         _check(self.L.cato_gpu_set_time(self.h, float(time), int(iteration)), self.h, "set_time")
 

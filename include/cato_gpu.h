@@ -180,6 +180,31 @@ int cato_gpu_status(cato_handle* h, int32_t* status_bits);
 /* Synchronise the handle's stream. */
 int cato_gpu_synchronize(cato_handle* h);
 
+/* Run all of this handle's work on `stream` (a cudaStream_t; NULL restores the handle's own
+ * stream).  Lets a caller order the solver with its own work or time it with its own events. */
+int cato_gpu_set_stream(cato_handle* h, void* stream);
+
+/* One time step (CFL dt) with a CUDA event between kernels: kernel_ms[k] receives the device
+ * time of kernel k (k = 0: step control, then one entry per RK stage).  The per-stage analogue
+ * of the reference's timing.csv (src/lib/mod_timing.f90:35-128). */
+int cato_gpu_profile_step(cato_handle* h, float* kernel_ms, int32_t capacity, int32_t* n_kernels);
+
+/* Kernel launches per time step of this handle (step control + RK stages). */
+int cato_gpu_launches_per_step(const cato_handle* h, int32_t* n);
+
+/* Exactly n_steps CFL steps with no host round trip, timed with CUDA events on the handle's
+ * stream: *total_ms = device time of all of them; kernel_ms (may be NULL, `capacity` entries)
+ * accumulates per kernel slot (0: step control, k: RK stage k) over the steps. */
+int cato_gpu_run_timed(cato_handle* h, int64_t n_steps, float* total_ms, float* kernel_ms,
+                       int32_t capacity);
+
+/* Select the CUDA device used by handles created afterwards on this host thread. */
+int cato_gpu_select_device(int32_t device);
+
+/* Page-locked host memory for fast uploads/downloads (cudaHostAlloc / cudaFreeHost). */
+int cato_host_alloc(uint64_t bytes, void** out);
+int cato_host_free(void* p);
+
 #ifdef __cplusplus
 }
 #endif
