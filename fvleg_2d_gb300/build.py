@@ -53,7 +53,7 @@ def _units() -> list[tuple[str, list[str]]]:
             cmd = [nvcc(), *ARCH, *common, f"--fmad={fmad}", f"-DCATO_REAL={real}",
                    f"-DCATO_FLUX={flux}", "-c", os.path.join(CSRC, "stage_inst.cu"), "-o", obj]
             units.append((obj, cmd))
-    for src in ("cato_capi.cu", "cato_batch.cu"):
+    for src in ("cato_capi.cu", "cato_batch.cu", "cato_noalloc.cu"):
         path = os.path.join(CSRC, src)
         if not os.path.exists(path):
             continue

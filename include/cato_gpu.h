@@ -33,7 +33,8 @@ enum cato_status {
   CATO_ERR_CUDA = 12,     /* CUDA runtime error (message via cato_gpu_last_error) */
   CATO_ERR_ARG = 13,      /* bad argument (null pointer, too-small leading dimension, ...) */
   CATO_ERR_TIMEOUT = 14,  /* a bounded device-side wait gave up */
-  CATO_ERR_STATE = 15     /* call out of order (e.g. integrate before upload) */
+  CATO_ERR_STATE = 15,    /* call out of order (e.g. integrate before upload) */
+  CATO_ERR_CAPACITY = 16  /* the request exceeds a fixed-size device buffer (no-alloc entry) */
 };
 
 /* Flux solvers.  Names as accepted by the reference deck key [scheme] flux_solver
@@ -200,6 +201,21 @@ int cato_gpu_run_timed(cato_handle* h, int64_t n_steps, float* total_ms, float* 
 
 /* Select the CUDA device used by handles created afterwards on this host thread. */
 int cato_gpu_select_device(int32_t device);
+
+/* cato_gpu_solve for callers that cannot allocate device memory: no handle, no cudaMalloc or
+ * cudaFree.  It has no counterpart in the reference; it serves callers whose device memory is
+ * owned by another allocator (a framework pool, a fixed HBM budget) and callers in
+ * latency-critical loops where an allocation could synchronize the device.  Same arguments and
+ * results as cato_gpu_solve (host arrays, BC ghosts written back), FP64 schemes only.  All device
+ * memory is one fixed 32 MiB array per GPU: grids needing more than
+ * 8*pitch*nj + 4*(ni+2ng)*(nj+2ng) + 32 doubles (pitch = ni rounded up to 32; 512 x 512 fits)
+ * are refused with CATO_ERR_CAPACITY.  The first call on a device sets up the array's address
+ * (cudaGetSymbolAddress) and should come before any stream capture.  Calls share the array and
+ * would race if they overlapped on the GPU, so each call locks its device, runs on the legacy
+ * default stream and synchronizes before returning. */
+int cato_gpu_solve_noalloc(const cato_config* cfg, double* rho, double* u, double* v, double* p,
+                           double* d_rho_dt, double* d_rho_u_dt, double* d_rho_v_dt,
+                           double* d_rho_E_dt, int64_t ld);
 
 /* Page-locked host memory for fast uploads/downloads (cudaHostAlloc / cudaFreeHost). */
 int cato_host_alloc(uint64_t bytes, void** out);
