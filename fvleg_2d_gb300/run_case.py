@@ -1,0 +1,53 @@
+"""Run a named workload for a number of steps on the GPU (the analogue of ``cato.x input.ini``
+for the synthetic workloads), e.g. to profile one kernel on a small case:
+
+    python -m fvleg_2d_gb300.run_case quadrant --n 2048 --precision mixed --steps 2
+
+Workloads: ``sod`` (400x40 Sod tube), ``quadrant`` (four-quadrant Riemann problem, HLLC / van
+Leer / SSP-RK3), ``kh`` (Kelvin-Helmholtz, Roe / superbee / SSP-RK3), ``circles`` (random circles,
+SLAU / MLP5 / SSP-RK2, seeded).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+
+import numpy as np
+
+from . import ic
+from .fluid import Fluid
+
+
+def make(name: str, n: int, precision: str, seed: int = 0):
+    if name == "sod":
+        return ic.sod(precision=precision)
+    if name == "quadrant":
+        return ic.riemann_quadrant(n, precision=precision)
+    if name == "kh":
+        return ic.kelvin_helmholtz(n, precision=precision)
+    if name == "circles":
+        return ic.random_circles(n, n, np.random.default_rng(seed), precision=precision)
+    raise ValueError(f"unknown workload {name!r}")
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("workload", choices=["sod", "quadrant", "kh", "circles"])
+    ap.add_argument("--n", type=int, default=1024)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--seed", type=int, default=0)
+    a = ap.parse_args(argv)
+    cfg, prims = make(a.workload, a.n, a.precision, a.seed)
+    f = Fluid(cfg).initialize(*prims)
+    ms, kern = f.run_timed(a.steps, per_kernel=True)
+    cells = cfg.ni * cfg.nj
+    print(json.dumps({"workload": a.workload, "ni": cfg.ni, "nj": cfg.nj,
+                      "precision": a.precision, "steps": a.steps, "ms": ms,
+                      "kernel_ms": kern, "cell_updates_per_s": cells * a.steps / (ms / 1e3)}))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
