@@ -47,10 +47,11 @@ def _units() -> list[tuple[str, list[str]]]:
     common = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", INCLUDE]
     units = []
-    for real, fmad in (("double", "false"), ("float", "true")):
+    for real, flags in (("double", ["--fmad=false"]),
+                        ("float", ["--fmad=true", "-prec-sqrt=false", "-ftz=true"])):
         for flux in range(N_FLUX):
             obj = os.path.join(BUILD_DIR, f"stage_{real}_{flux}.o")
-            cmd = [nvcc(), *ARCH, *common, f"--fmad={fmad}", f"-DCATO_REAL={real}",
+            cmd = [nvcc(), *ARCH, *common, *flags, f"-DCATO_REAL={real}",
                    f"-DCATO_FLUX={flux}", "-c", os.path.join(CSRC, "stage_inst.cu"), "-o", obj]
             units.append((obj, cmd))
     for src in ("cato_capi.cu", "cato_batch.cu", "cato_noalloc.cu"):

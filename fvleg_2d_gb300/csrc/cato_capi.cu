@@ -4,8 +4,9 @@
 // Fortran (i, j) order, row pitch rounded up to 32 elements so every row starts 256-B aligned):
 //   FP64 path : U^n (4 x f64) + two stage buffers S0, S1 (4 x f64 each).  The last stage writes
 //               U^{n+1} over U^n in place (U^n is only read point-wise there).
-//   mixed path: U^n double-buffered (2 x 4 x f64) + stage increments delta (2 x 4 x f32):
-//               U^k = U^n + delta_k, delta_{k+1} = b delta_k + c L(U^k), U^{n+1} = U^n + delta.
+//   mixed path: U^n double-buffered (2 x 4 x f64) with FP32 copies (2 x float4 per cell) and
+//               stage increments delta (2 x float4 per cell): U^k = U^n + delta_k,
+//               delta_{k+1} = b delta_k + c L(U^k), U^{n+1} = U^n + delta in FP64.
 // The primitives of an upload are kept (in a buffer not needed before the first step) because
 // the first stage after an upload uses them as is, like the reference after initialize.
 #include <cstdio>
@@ -44,7 +45,8 @@ struct cato_handle {
   // device buffers
   double* U[2][4] = {};    // FP64: U[0] = U^n ; mixed: U[cur], U[1-cur]
   double* S[2][4] = {};    // FP64 stage buffers
-  float* D[2][4] = {};     // mixed stage increments
+  float4* D[2] = {};       // mixed stage increments (rho, rho u, rho v, rho E per cell)
+  float4* Uf[2] = {};      // mixed: FP32 copies of U[0], U[1]
   double* prim_raw[4] = {};  // primitives of the last upload (alias of a free buffer)
   double* scratch[8] = {};   // solve / download / interpolation scratch (lazy)
   double* halo[4] = {};      // halo-padded scratch (lazy)
@@ -239,13 +241,15 @@ static int enqueue_step(cato_handle* h) {
       double** Un = h->U[h->cur];
       double** Unext = h->U[1 - h->cur];
       for (int v = 0; v < 4; ++v) {
-        A.Uk[v] = Un[v];
+        A.Uk[v] = nullptr;
         A.Ua[v] = Un[v];
         A.Uo[v] = A.last ? Unext[v] : nullptr;
         A.Pin[v] = raw ? h->prim_raw[v] : nullptr;
-        A.dk[v] = (k == 0) ? nullptr : h->D[(k - 1) & 1][v];
-        A.dout[v] = A.last ? nullptr : h->D[k & 1][v];
       }
+      A.uf = h->Uf[h->cur];
+      A.dk = (k == 0) ? nullptr : h->D[(k - 1) & 1];
+      A.dout = A.last ? nullptr : h->D[k & 1];
+      A.ufo = A.last ? h->Uf[1 - h->cur] : nullptr;
       if (st.kind == 0) A.b = 0.0;  // rk(m,n): U_curr = U_0 + c L(U_prev)
     }
     CK(launch(h, A));
@@ -409,9 +413,13 @@ int cato_gpu_create(const cato_config* cfg, cato_handle** out) {
       h->prim_raw[v] = h->S[1][v];  // S1 is first written by stage 2, after stage 1 read these
     } else {
       if (!dalloc((void**)&h->U[1][v], fb)) return cleanup(CATO_ERR_OOM);
-      if (!dalloc((void**)&h->D[0][v], h->field_elems * sizeof(float))) return cleanup(CATO_ERR_OOM);
-      if (!dalloc((void**)&h->D[1][v], h->field_elems * sizeof(float))) return cleanup(CATO_ERR_OOM);
       h->prim_raw[v] = h->U[1][v];  // U[1] is first written by the last stage of step 1
+    }
+  }
+  if (!fp64) {
+    for (int s2 = 0; s2 < 2; ++s2) {
+      if (!dalloc((void**)&h->D[s2], h->field_elems * sizeof(float4))) return cleanup(CATO_ERR_OOM);
+      if (!dalloc((void**)&h->Uf[s2], h->field_elems * sizeof(float4))) return cleanup(CATO_ERR_OOM);
     }
   }
   if (!dalloc((void**)&h->ctl, sizeof(StepCtl))) return cleanup(CATO_ERR_OOM);
@@ -436,12 +444,14 @@ int cato_gpu_create(const cato_config* cfg, cato_handle** out) {
 int cato_gpu_destroy(cato_handle* h) {
   if (!h) return CATO_ERR_ARG;
   if (h->stream) cudaStreamSynchronize(h->stream);
-  for (int s = 0; s < 2; ++s)
+  for (int s = 0; s < 2; ++s) {
     for (int v = 0; v < 4; ++v) {
       cudaFree(h->U[s][v]);
       cudaFree(h->S[s][v]);
-      cudaFree(h->D[s][v]);
     }
+    cudaFree(h->D[s]);
+    cudaFree(h->Uf[s]);
+  }
   for (int k = 0; k < 8; ++k) cudaFree(h->scratch[k]);
   for (int k = 0; k < 4; ++k) cudaFree(h->halo[k]);
   cudaFree(h->ctl);
@@ -478,6 +488,11 @@ int cato_gpu_upload_primitive(cato_handle* h, const double* rho, const double* u
       h->ni, h->nj, h->pitch, h->cfg.gamma, h->cfg.cfl, h->G.dx, h->G.dy, h->prim_raw[0],
       h->prim_raw[1], h->prim_raw[2], h->prim_raw[3], Un[0], Un[1], Un[2], Un[3], h->ctl);
   CK(cudaGetLastError());
+  if (h->cfg.precision == CATO_MIXED) {
+    pack_f32_kernel<<<grid_for((long long)h->ni * h->nj), 256, 0, h->stream>>>(
+        h->ni, h->nj, h->pitch, Un[0], Un[1], Un[2], Un[3], h->Uf[0]);
+    CK(cudaGetLastError());
+  }
   int rc = pull_ctl(h);
   if (rc) return rc;
   h->uploaded = true;
@@ -766,6 +781,23 @@ int cato_gpu_run_timed(cato_handle* h, int64_t n_steps, float* total_ms, float* 
   if (h->cfg.precision == CATO_MIXED)
     h->cur = (int)((parity0 + (h->ctl_host->iter - it0)) & 1);
   return status_code(h->ctl_host->status);
+}
+
+int cato_gpu_set_plan(cato_handle* h, int32_t threads, int32_t rows_per_cta) {
+  if (!h) return CATO_ERR_ARG;
+  if (threads < 64 || threads > 256 || threads % 32 != 0 || rows_per_cta < 1 ||
+      threads - 2 * h->ng < 1)
+    return fail(h, CATO_ERR_ARG, "invalid plan");
+  h->plan.threads = threads;
+  h->plan.rows_per_cta = rows_per_cta;
+  return CATO_OK;
+}
+
+int cato_gpu_get_plan(const cato_handle* h, int32_t* threads, int32_t* rows_per_cta) {
+  if (!h) return CATO_ERR_ARG;
+  if (threads) *threads = h->plan.threads;
+  if (rows_per_cta) *rows_per_cta = h->plan.rows_per_cta;
+  return CATO_OK;
 }
 
 int cato_gpu_select_device(int32_t device) {

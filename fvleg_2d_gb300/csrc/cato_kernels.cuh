@@ -82,6 +82,18 @@ __global__ void upload_init_kernel(int ni, int nj, int pitch, double gamma, doub
   }
 }
 
+// FP32 copy (one float4 per cell) of an FP64 conserved state, for the mixed path.
+__global__ void pack_f32_kernel(int ni, int nj, int pitch, const double* __restrict__ a0,
+                                const double* __restrict__ a1, const double* __restrict__ a2,
+                                const double* __restrict__ a3, float4* out) {
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < (long long)ni * nj;
+       n += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(n % ni), j = (int)(n / ni);
+    const size_t idx = (size_t)j * pitch + i;
+    out[idx] = make_float4(d2f_int(a0[idx]), d2f_int(a1[idx]), d2f_int(a2[idx]), d2f_int(a3[idx]));
+  }
+}
+
 // fluid_t's derived quantities for download: u, v, p, cs of the conserved state (FP64,
 // calculate_derived_quantities), or of the raw primitives before the first step.
 __global__ void derive_kernel(int ni, int nj, int pitch, double gamma, int raw,

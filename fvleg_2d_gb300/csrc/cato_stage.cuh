@@ -21,7 +21,7 @@
 namespace cato {
 
 struct StageArgs {
-  int ni, nj, pitch;       // interior cells, row pitch (elements) of the state arrays
+  int ni, nj, pitch;       // interior cells, row pitch (cells) of the state arrays
   int bc[4];               // by side: +x, +y, -x, -y
   int limiter;             // TVD2 limiter id (runtime)
   int rows_per_cta;
@@ -29,14 +29,16 @@ struct StageArgs {
                            // flushed) ; 2: out = L (flux_solver_t%solve output, FP64 path)
   int last;                // last stage of the step: emit the CFL dt and the state checks
   double a, b, coef;       // c = coef * dt (the reference's (0.5_rk*dt), ((1/4)*dt), dt*alpha ...)
-  // FP64 path
+  // FP64 path (structure of arrays, one array per conserved variable)
   const double* Uk[4];     // conserved state of this stage (stencil operand)
-  const double* Ua[4];     // U_a (pointwise operand; the step's U^n)
-  double* Uo[4];           // output conserved state
+  const double* Ua[4];     // U_a (point-wise operand; the step's U^n); mixed: U^n (last stage)
+  double* Uo[4];           // output conserved state; mixed: U^{n+1} (last stage)
   const double* Pin[4];    // when non-null: primitives to use as-is for this stage (after upload)
-  // mixed path: U^k = U_a + delta_k
-  const float* dk[4];      // delta_k (null for the first stage)
-  float* dout[4];          // delta_{k+1} (null on the last stage)
+  // mixed path (one float4 (rho, rho u, rho v, rho E) per cell): U^k = U^n + delta_k
+  const float4* uf;        // FP32 copy of U^n (stencil operand)
+  const float4* dk;        // delta_k (null for the first stage)
+  float4* dout;            // delta_{k+1} (not on the last stage)
+  float4* ufo;             // FP32 copy of U^{n+1} (last stage)
   // device scalars
   const double* dt;
   const int* active;
@@ -64,30 +66,27 @@ __device__ __forceinline__ int map_index(int g, int n, int bc_lo, int bc_hi, boo
   return g;
 }
 
-template <typename R> struct Cons4 { double q[4]; };
-
-// shared-memory accessor: ring[slot][var][col]
-template <typename R>
-__device__ __forceinline__ R& RQ(R* ring, int T, int slot, int var, int col) {
-  return ring[(slot * 4 + var) * T + col];
-}
-
 template <int RING> __device__ __forceinline__ int slot_of(int row) {
   return (row + 4 * RING) % RING;  // rows are >= -NG
+}
+
+// Row bases of the shared-memory ring for rows center-2 .. center+3 (each row: [var][col]).
+template <typename R, int RING>
+__device__ __forceinline__ void ring_rows(R* ring, int T, int center, const R* rp[6]) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) rp[k] = ring + slot_of<RING>(center + k - 2) * 4 * T;
 }
 
 // ---------------------------------------------------------------------------------------------
 // one edge: reconstruct the four primitives from the ring and evaluate the flux
 // ---------------------------------------------------------------------------------------------
 template <typename R, int NG, int FLUX, int RECON, int DIR>
-__device__ __forceinline__ void edge_flux(const R* __restrict__ ring, int T, int lim, int row,
-                                          int col, const FluxConsts<R>& K, R F[4]) {
-  constexpr int RING = 2 * NG;
-  // stencil sample at normal offset n and tangential offset t from the edge's left cell
+__device__ __forceinline__ void edge_flux(const R* const rp[6], int T, int lim, int col,
+                                          const FluxConsts<R>& K, R F[4]) {
+  // stencil sample at normal offset n and tangential offset t from the edge's left cell;
+  // rp[k] is the ring row (edge row) + k - 2
   auto Q = [&](int var, int n, int t) -> R {
-    const int c = DIR == 0 ? col + n : col + t;
-    const int r = DIR == 0 ? row + t : row + n;
-    return ring[(slot_of<RING>(r) * 4 + var) * T + c];
+    return DIR == 0 ? rp[t + 2][var * T + col + n] : rp[n + 2][var * T + col + t];
   };
   R Lv[4], Rv[4];
 #pragma unroll
@@ -155,58 +154,67 @@ __device__ __forceinline__ void edge_flux(const R* __restrict__ ring, int T, int
 // ---------------------------------------------------------------------------------------------
 // primitive row load
 // ---------------------------------------------------------------------------------------------
-struct RowSrc {
+template <typename R> struct RowSrc;
+template <> struct RowSrc<double> {
   double c[4];  // conserved (or raw primitives) as loaded
-  float d[4];   // mixed path delta_k
+  bool flipy;
+};
+template <> struct RowSrc<float> {
+  float4 c;     // FP32 copy of U^n (or the raw primitives)
+  float4 d;     // delta_k
   bool flipy;
 };
 
 template <typename R>
-__device__ __forceinline__ void load_src(const StageArgs& A, int sx, int row, RowSrc& s) {
+__device__ __forceinline__ void load_src(const StageArgs& A, int sx, int row, RowSrc<R>& s) {
   bool fy;
   const int sy = map_index(row, A.nj, A.bc[SIDE_MY], A.bc[SIDE_PY], fy);
   s.flipy = fy;
   const size_t idx = (size_t)sy * A.pitch + sx;
-  if (A.Pin[0]) {
+  if constexpr (sizeof(R) == 8) {
+    const double* const* src = A.Pin[0] ? A.Pin : A.Uk;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) s.c[k] = __ldg(A.Pin[k] + idx);
+    for (int k = 0; k < 4; ++k) s.c[k] = __ldg(src[k] + idx);
   } else {
-#pragma unroll
-    for (int k = 0; k < 4; ++k) s.c[k] = __ldg(A.Uk[k] + idx);
-  }
-  if (sizeof(R) == 4) {
-#pragma unroll
-    for (int k = 0; k < 4; ++k) s.d[k] = A.dk[0] ? __ldg(A.dk[k] + idx) : 0.0f;
+    if (A.Pin[0]) {
+      s.c = make_float4(d2f_int(__ldg(A.Pin[0] + idx)), d2f_int(__ldg(A.Pin[1] + idx)),
+                        d2f_int(__ldg(A.Pin[2] + idx)), d2f_int(__ldg(A.Pin[3] + idx)));
+    } else {
+      s.c = __ldg(A.uf + idx);
+    }
+    s.d = A.dk ? __ldg(A.dk + idx) : make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
 
 template <typename R>
-__device__ __forceinline__ void src_to_prim(const StageArgs& A, const RowSrc& s, bool flipx,
+__device__ __forceinline__ void src_to_prim(const StageArgs& A, const RowSrc<R>& s, bool flipx,
                                             R g, R g1, R out[4]) {
   R r, u, v, p;
-  if (sizeof(R) == 8) {
+  if constexpr (sizeof(R) == 8) {
     if (A.Pin[0]) {
-      r = (R)s.c[0]; u = (R)s.c[1]; v = (R)s.c[2]; p = (R)s.c[3];
+      r = s.c[0]; u = s.c[1]; v = s.c[2]; p = s.c[3];
     } else {
       R cs;
-      r = (R)s.c[0];
-      prim_from_cons(g, g1, r, (R)s.c[1], (R)s.c[2], (R)s.c[3], u, v, p, cs);
+      r = s.c[0];
+      prim_from_cons(g, g1, r, s.c[1], s.c[2], s.c[3], u, v, p, cs);
     }
   } else {
-    float c0 = d2f_int(s.c[0]), c1 = d2f_int(s.c[1]), c2 = d2f_int(s.c[2]), c3 = d2f_int(s.c[3]);
     if (A.Pin[0]) {
-      r = c0; u = c1; v = c2; p = c3;
+      r = s.c.x; u = s.c.y; v = s.c.z; p = s.c.w;
     } else {
       R cs;
-      r = c0 + s.d[0];
-      prim_from_cons(g, g1, r, (R)(c1 + s.d[1]), (R)(c2 + s.d[2]), (R)(c3 + s.d[3]), u, v, p,
-                     cs);
+      r = s.c.x + s.d.x;
+      prim_from_cons(g, g1, r, s.c.y + s.d.y, s.c.z + s.d.z, s.c.w + s.d.w, u, v, p, cs);
     }
   }
   out[0] = r;
   out[1] = flipx ? -u : u;
   out[2] = s.flipy ? -v : v;
   out[3] = p;
+}
+
+__device__ __forceinline__ float f4get(const float4& v, int k) {
+  return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -233,26 +241,29 @@ __global__ void __launch_bounds__(256) stage_kernel(const StageArgs A, const Flu
   const bool in_cell = (t >= NG) && (t <= NG + W - 1) && (gx < A.ni);
   const double dt = *A.dt;
   const double cc = A.coef * dt;
+  const R* rp[6];
 
   // prologue: rows y0-NG .. y0+NG-1
   for (int r = y0 - NG; r < y0 + NG; ++r) {
-    RowSrc s;
+    RowSrc<R> s;
     load_src<R>(A, sx, r, s);
     R q[4];
     src_to_prim<R>(A, s, flipx, g, g1, q);
+    R* row = ring + slot_of<RING>(r) * 4 * T;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) RQ(ring, T, slot_of<RING>(r), k, t) = q[k];
+    for (int k = 0; k < 4; ++k) row[k * T + t] = q[k];
   }
   __syncthreads();
   if (in_cell && y0 < y1) {
     R F[4];
-    edge_flux<R, NG, FLUX, RECON, 1>(ring, T, A.limiter, y0 - 1, t, K, F);
+    ring_rows<R, RING>(ring, T, y0 - 1, rp);
+    edge_flux<R, NG, FLUX, RECON, 1>(rp, T, A.limiter, t, K, F);
 #pragma unroll
     for (int k = 0; k < 4; ++k) sfj[(((y0 - 1) & 1) * 4 + k) * T + t] = F[k];
   }
   __syncthreads();
 
-  RowSrc pre;
+  RowSrc<R> pre;
   if (y0 < y1) load_src<R>(A, sx, y0 + NG, pre);
 
   double dt_loc = INFINITY;
@@ -262,46 +273,55 @@ __global__ void __launch_bounds__(256) stage_kernel(const StageArgs A, const Flu
     // operands of this row's cell update, issued early
     const size_t cidx = (size_t)j * A.pitch + (size_t)min(max(gx, 0), A.ni - 1);
     double ua[4], uk[4];
-    float dk[4];
+    float4 dkc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (in_cell) {
+      if constexpr (sizeof(R) == 8) {
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        ua[k] = A.Ua[k] ? A.Ua[k][cidx] : 0.0;  // may alias Uo: plain load, read before write
-        uk[k] = (sizeof(R) == 8 && A.kind == 1) ? __ldg(A.Uk[k] + cidx) : 0.0;
-        dk[k] = (sizeof(R) == 4 && A.dk[0]) ? __ldg(A.dk[k] + cidx) : 0.0f;
+        for (int k = 0; k < 4; ++k) {
+          ua[k] = A.Ua[k] ? A.Ua[k][cidx] : 0.0;  // may alias Uo: plain load, read before write
+          uk[k] = (A.kind == 1) ? __ldg(A.Uk[k] + cidx) : 0.0;
+        }
+      } else {
+        if (A.dk) dkc = __ldg(A.dk + cidx);
+        if (A.last) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) ua[k] = __ldg(A.Ua[k] + cidx);
+        }
       }
     }
-    RowSrc nxt;
+    RowSrc<R> nxt;
     if (j + 1 < y1) load_src<R>(A, sx, j + 1 + NG, nxt);
     {
       R q[4];
       src_to_prim<R>(A, pre, flipx, g, g1, q);
+      R* row = ring + slot_of<RING>(j + NG) * 4 * T;
 #pragma unroll
-      for (int k = 0; k < 4; ++k) RQ(ring, T, slot_of<RING>(j + NG), k, t) = q[k];
+      for (int k = 0; k < 4; ++k) row[k * T + t] = q[k];
     }
     pre = nxt;
     __syncthreads();
+    ring_rows<R, RING>(ring, T, j, rp);
     if (in_i_edge) {
       R F[4];
-      edge_flux<R, NG, FLUX, RECON, 0>(ring, T, A.limiter, j, t, K, F);
+      edge_flux<R, NG, FLUX, RECON, 0>(rp, T, A.limiter, t, K, F);
 #pragma unroll
       for (int k = 0; k < 4; ++k) sfi[k * T + t] = F[k];
     }
     if (in_cell) {
       R F[4];
-      edge_flux<R, NG, FLUX, RECON, 1>(ring, T, A.limiter, j, t, K, F);
+      edge_flux<R, NG, FLUX, RECON, 1>(rp, T, A.limiter, t, K, F);
 #pragma unroll
       for (int k = 0; k < 4; ++k) sfj[((j & 1) * 4 + k) * T + t] = F[k];
     }
     __syncthreads();
     if (in_cell) {
       double un[4];
-      if (sizeof(R) == 8) {
+      if constexpr (sizeof(R) == 8) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          double Fi = (double)sfi[k * T + t], Fim = (double)sfi[k * T + t - 1];
-          double Fj = (double)sfj[((j & 1) * 4 + k) * T + t];
-          double Fjm = (double)sfj[(((j - 1) & 1) * 4 + k) * T + t];
+          double Fi = sfi[k * T + t], Fim = sfi[k * T + t - 1];
+          double Fj = sfj[((j & 1) * 4 + k) * T + t];
+          double Fjm = sfj[(((j - 1) & 1) * 4 + k) * T + t];
           double L = divergence_fp64(Fi, Fim, Fj, Fjm, A.G);
           double r;
           if (A.kind == 2) {
@@ -321,24 +341,28 @@ __global__ void __launch_bounds__(256) stage_kernel(const StageArgs A, const Flu
       } else {
         const float ccf = (float)cc, bf = (float)A.b;
         const float idx_f = (float)(1.0 / A.G.dx), idy_f = (float)(1.0 / A.G.dy);
+        float dn[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          float Fi = (float)sfi[k * T + t], Fim = (float)sfi[k * T + t - 1];
-          float Fj = (float)sfj[((j & 1) * 4 + k) * T + t];
-          float Fjm = (float)sfj[(((j - 1) & 1) * 4 + k) * T + t];
+          float Fi = sfi[k * T + t], Fim = sfi[k * T + t - 1];
+          float Fj = sfj[((j & 1) * 4 + k) * T + t];
+          float Fjm = sfj[(((j - 1) & 1) * 4 + k) * T + t];
           float L = -((Fi - Fim) * idx_f + (Fj - Fjm) * idy_f);
-          float dn = (A.dk[0] ? bf * dk[k] : 0.0f) + L * ccf;
-          if (A.last) {
-            un[k] = ua[k] + f2d_int(dn);
+          dn[k] = bf * f4get(dkc, k) + L * ccf;
+        }
+        if (A.last) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            un[k] = ua[k] + f2d_int(dn[k]);
             A.Uo[k][cidx] = un[k];
-          } else {
-            A.dout[k][cidx] = dn;
           }
+        } else {
+          A.dout[cidx] = make_float4(dn[0], dn[1], dn[2], dn[3]);
         }
       }
       if (A.last) {
         // CFL dt of the new state (get_timestep, mod_fluid.f90:554-558) and the sanity checks
-        if (sizeof(R) == 8) {
+        if constexpr (sizeof(R) == 8) {
           double u, v, p, cs;
           prim_from_cons(A.gamma, A.gamma - 1.0, un[0], un[1], un[2], un[3], u, v, p, cs);
           double d = A.cfl / (((fabs(u) + cs) / A.G.dx) + ((fabs(v) + cs) / A.G.dy));
@@ -347,15 +371,18 @@ __global__ void __launch_bounds__(256) stage_kernel(const StageArgs A, const Flu
           if (un[0] < 0.0) st_loc |= ST_NEG_DENSITY;
           if (p < 0.0) st_loc |= ST_NEG_PRESSURE;
         } else {
-          float r = d2f_int(un[0]), u, v, p, cs;
-          prim_from_cons((float)A.gamma, (float)(A.gamma - 1.0), r, d2f_int(un[1]),
-                         d2f_int(un[2]), d2f_int(un[3]), u, v, p, cs);
-          float d = (float)A.cfl /
-                    ((fabsf(u) + cs) * (float)(1.0 / A.G.dx) + (fabsf(v) + cs) * (float)(1.0 / A.G.dy));
+          const float4 uf = make_float4(d2f_int(un[0]), d2f_int(un[1]), d2f_int(un[2]),
+                                        d2f_int(un[3]));
+          A.ufo[cidx] = uf;
+          float u, v, p, cs;
+          prim_from_cons((float)A.gamma, (float)(A.gamma - 1.0), uf.x, uf.y, uf.z, uf.w, u, v,
+                         p, cs);
+          float d = (float)A.cfl / ((fabsf(u) + cs) * (float)(1.0 / A.G.dx) +
+                                    (fabsf(v) + cs) * (float)(1.0 / A.G.dy));
           double dd = f2d_int(d);
-          if (dd < dt_loc) dt_loc = dd;
-          if (isnan(r) || isnan(u) || isnan(v) || isnan(p)) st_loc |= ST_NAN;
-          if (r < 0.0f) st_loc |= ST_NEG_DENSITY;
+          if (__double_as_longlong(dd) < __double_as_longlong(dt_loc) && d > 0.0f) dt_loc = dd;
+          if (isnan(uf.x) || isnan(u) || isnan(v) || isnan(p)) st_loc |= ST_NAN;
+          if (uf.x < 0.0f) st_loc |= ST_NEG_DENSITY;
           if (p < 0.0f) st_loc |= ST_NEG_PRESSURE;
         }
       }

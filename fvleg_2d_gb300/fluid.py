@@ -120,6 +120,14 @@ class Fluid(_Handle):
         _check(rc, self.h, "run_timed")
         return total.value, (list(ks) if per_kernel else None)
 
+    def set_plan(self, threads: int, rows_per_cta: int) -> None:
+        _check(self.L.cato_gpu_set_plan(self.h, int(threads), int(rows_per_cta)), self.h, "plan")
+
+    def get_plan(self) -> tuple[int, int]:
+        t, r = ctypes.c_int32(), ctypes.c_int32()
+        _check(self.L.cato_gpu_get_plan(self.h, ctypes.byref(t), ctypes.byref(r)), self.h)
+        return t.value, r.value
+
     def launches_per_step(self) -> int:
         n = ctypes.c_int32()
         _check(self.L.cato_gpu_launches_per_step(self.h, ctypes.byref(n)), self.h)

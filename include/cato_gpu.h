@@ -199,6 +199,11 @@ int cato_gpu_launches_per_step(const cato_handle* h, int32_t* n);
 int cato_gpu_run_timed(cato_handle* h, int64_t n_steps, float* total_ms, float* kernel_ms,
                        int32_t capacity);
 
+/* Work decomposition of the stage kernel (the autotuner's knobs): CTA width `threads` (a
+ * multiple of 32 in [64, 256], including 2*n_ghost halo columns) and rows marched per CTA. */
+int cato_gpu_set_plan(cato_handle* h, int32_t threads, int32_t rows_per_cta);
+int cato_gpu_get_plan(const cato_handle* h, int32_t* threads, int32_t* rows_per_cta);
+
 /* Select the CUDA device used by handles created afterwards on this host thread. */
 int cato_gpu_select_device(int32_t device);
 
