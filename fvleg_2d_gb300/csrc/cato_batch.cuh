@@ -1,0 +1,121 @@
+// cato_batch.cuh -- many independent grid instances of uneven sizes advanced together: one
+// persistent launch per RK stage (and per flux/reconstruction group) walks a work list of
+// (instance, tile) items through a device-side queue, so 256 grids cost the launches of one.
+// Every instance keeps its own dt, time, iteration and stop condition in a device descriptor,
+// so a chunk of steps needs no host round trip and can be captured in a CUDA graph.
+#pragma once
+
+#include "cato_ctl.cuh"
+#include "cato_stage.cuh"
+
+namespace cato {
+
+struct InstDesc {
+  StepCtl ctl;             // per-instance step control (dt, time, iteration, stop, status)
+  int ni, nj, pitch, ng;
+  int bc[4];
+  int limiter, rows_per_cta, flux, recon;
+  int cur;                 // mixed: which U buffer holds U^n
+  int raw_pending;         // the first stage uses the uploaded primitives as is
+  int prec;                // 0 FP64, 1 mixed
+  int in_use;
+  double gamma, cfl;
+  Geom G;
+  FluxConsts<double> K64;
+  FluxConsts<float> K32;
+  double* U[2][4];
+  double* S[2][4];
+  float4* D[2];
+  float4* Uf[2];
+  double* prim_raw[4];
+};
+
+struct BatchStageArgs {
+  InstDesc* descs;
+  const int4* items;       // (instance, tile x, tile y, rows per tile)
+  int n_items;
+  int* counter;            // work-queue head, zeroed by batch_step_begin
+  int stage, kind, last;
+  double a, b, coef;
+};
+
+// Build one instance's StageArgs for this stage: the device-side twin of the single-instance
+// host sequencing (cato_capi.cu enqueue_step).
+template <typename R>
+__device__ __forceinline__ void batch_stage_args(InstDesc* d, const BatchStageArgs& B,
+                                                 StageArgs& A) {
+  A.ni = d->ni;
+  A.nj = d->nj;
+  A.pitch = d->pitch;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) A.bc[k] = d->bc[k];
+  A.limiter = d->limiter;
+  A.rows_per_cta = d->rows_per_cta;
+  A.kind = B.kind;
+  A.last = B.last;
+  A.a = B.a;
+  A.b = B.b;
+  A.coef = B.coef;
+  A.dt = &d->ctl.dt;
+  A.active = nullptr;
+  A.dt_min = &d->ctl.dt_min;
+  A.status = &d->ctl.status;
+  A.gamma = d->gamma;
+  A.cfl = d->cfl;
+  A.G = d->G;
+  const bool raw = (B.stage == 0) && d->raw_pending;
+  if constexpr (sizeof(R) == 8) {
+    double* const* prev = (B.stage == 0) ? d->U[0] : d->S[(B.stage - 1) & 1];
+    double* const* out = B.last ? d->U[0] : d->S[B.stage & 1];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      A.Uk[v] = prev[v];
+      A.Ua[v] = d->U[0][v];
+      A.Uo[v] = out[v];
+      A.Pin[v] = raw ? d->prim_raw[v] : nullptr;
+    }
+    A.uf = nullptr;
+    A.dk = nullptr;
+    A.dout = nullptr;
+    A.ufo = nullptr;
+  } else {
+    const int cur = d->cur;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      A.Uk[v] = nullptr;
+      A.Ua[v] = d->U[cur][v];
+      A.Uo[v] = B.last ? d->U[1 - cur][v] : nullptr;
+      A.Pin[v] = raw ? d->prim_raw[v] : nullptr;
+    }
+    A.uf = d->Uf[cur];
+    A.dk = (B.stage == 0) ? nullptr : d->D[(B.stage - 1) & 1];
+    A.dout = B.last ? nullptr : d->D[B.stage & 1];
+    A.ufo = B.last ? d->Uf[1 - cur] : nullptr;
+    if (B.kind == 0) A.b = 0.0;
+  }
+}
+
+template <typename R, int NG, int FLUX, int RECON>
+__global__ void __launch_bounds__(256) batch_stage_kernel(const BatchStageArgs B) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  for (;;) {
+    __syncthreads();  // the previous tile is done with shared memory and s_item
+    if (threadIdx.x == 0) s_item = atomicAdd(B.counter, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= B.n_items) break;
+    const int4 w = B.items[it];
+    InstDesc* d = B.descs + w.x;
+    if (!d->ctl.active) continue;
+    StageArgs A;
+    batch_stage_args<R>(d, B, A);
+    A.rows_per_cta = w.w;
+    if constexpr (sizeof(R) == 8)
+      stage_tile<R, NG, FLUX, RECON>(A, d->K64, w.y, w.z, smem_raw);
+    else
+      stage_tile<R, NG, FLUX, RECON>(A, d->K32, w.y, w.z, smem_raw);
+  }
+}
+
+}  // namespace cato

@@ -3,30 +3,13 @@
 // stand-alone edge reconstruction.  Built with --fmad=false (FP64 reference arithmetic).
 #pragma once
 
+#include "cato_ctl.cuh"
 #include "cato_stage.cuh"
 
 namespace cato {
 
-// Device-resident step control: lets a chunk of steps run (and be captured in a CUDA graph)
-// without host round trips.  `active` gates every kernel of a step.
-struct StepCtl {
-  double dt;          // dt of the current step
-  double time;        // simulation time after the last active step
-  double t_end;       // stop once time >= t_end (main.f90:138)
-  double fixed_dt;    // > 0: use this dt instead of the CFL dt (use_constant_delta_t)
-  long long iter;     // iteration counter
-  long long max_iter; // stop once iter >= max_iter
-  unsigned long long dt_min;  // CFL dt of the current state (bits; ~0 = none)
-  int active;
-  int status;         // ST_* bits of the current state
-};
-
-__device__ __forceinline__ double decode_dt(unsigned long long b) {
-  return b == ~0ULL ? INFINITY : __longlong_as_double((long long)b);
-}
-
 // one thread: decide whether this step runs and with which dt (master_puppeteer.f90:155-200)
-__global__ void step_begin_kernel(StepCtl* c) {
+static __global__ void step_begin_kernel(StepCtl* c) {
   int act = (c->status == 0) && (c->time < c->t_end) && (c->iter < c->max_iter);
   c->active = act;
   if (!act) return;
@@ -39,7 +22,7 @@ __global__ void step_begin_kernel(StepCtl* c) {
 
 // initialize_from_hdf5 + eos%primitive_to_conserved (equation_of_state.f90:316-324 through the
 // field operators) and the CFL dt of the raw primitives (mod_fluid.f90:249, 518-562).
-__global__ void upload_init_kernel(int ni, int nj, int pitch, double gamma, double cfl, double dx,
+static __global__ void upload_init_kernel(int ni, int nj, int pitch, double gamma, double cfl, double dx,
                                    double dy, const double* __restrict__ r_,
                                    const double* __restrict__ u_, const double* __restrict__ v_,
                                    const double* __restrict__ p_, double* rho, double* rhou,
@@ -83,7 +66,7 @@ __global__ void upload_init_kernel(int ni, int nj, int pitch, double gamma, doub
 }
 
 // FP32 copy (one float4 per cell) of an FP64 conserved state, for the mixed path.
-__global__ void pack_f32_kernel(int ni, int nj, int pitch, const double* __restrict__ a0,
+static __global__ void pack_f32_kernel(int ni, int nj, int pitch, const double* __restrict__ a0,
                                 const double* __restrict__ a1, const double* __restrict__ a2,
                                 const double* __restrict__ a3, float4* out) {
   for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < (long long)ni * nj;
@@ -96,7 +79,7 @@ __global__ void pack_f32_kernel(int ni, int nj, int pitch, const double* __restr
 
 // fluid_t's derived quantities for download: u, v, p, cs of the conserved state (FP64,
 // calculate_derived_quantities), or of the raw primitives before the first step.
-__global__ void derive_kernel(int ni, int nj, int pitch, double gamma, int raw,
+static __global__ void derive_kernel(int ni, int nj, int pitch, double gamma, int raw,
                               const double* __restrict__ a0, const double* __restrict__ a1,
                               const double* __restrict__ a2, const double* __restrict__ a3,
                               double* u, double* v, double* p, double* cs) {
@@ -124,7 +107,7 @@ __global__ void derive_kernel(int ni, int nj, int pitch, double gamma, int raw,
 
 // Halo-padded primitive fields with every ghost cell filled by the boundary conditions, as after
 // flux_solver_t%apply_primitive_bc (flux_solver.f90:138-185).
-__global__ void fill_ghosts_kernel(int ni, int nj, int pitch, int ng, int4 bc,
+static __global__ void fill_ghosts_kernel(int ni, int nj, int pitch, int ng, int4 bc,
                                    const double* __restrict__ r_, const double* __restrict__ u_,
                                    const double* __restrict__ v_, const double* __restrict__ p_,
                                    double* ro, double* uo, double* vo, double* po, long long ld) {
@@ -148,7 +131,7 @@ __global__ void fill_ghosts_kernel(int ni, int nj, int pitch, int ng, int4 bc,
 // muscl_interpolation_t%interpolate_edge_values on a halo-filled field q (ld = ni + 2 ng):
 // i_edges(1:2, -1:ni, 0:nj) and j_edges(1:2, 0:ni, -1:nj), both computed for i, j = 0..ni, 0..nj.
 template <int NG, int RECON>
-__global__ void interp_edges_kernel(int ni, int nj, int lim, const double* __restrict__ q,
+static __global__ void interp_edges_kernel(int ni, int nj, int lim, const double* __restrict__ q,
                                     long long ld, double* ie, double* je) {
   auto Q = [&](int i, int j) -> double {  // reference (i, j), 1-based interior
     return q[(size_t)(j + NG - 1) * ld + (i + NG - 1)];

@@ -5,6 +5,7 @@
 
 #include <atomic>
 
+#include "cato_batch.cuh"
 #include "cato_stage.cuh"
 
 namespace cato {
@@ -42,9 +43,50 @@ cudaError_t launch_stage_flux(int recon, dim3 grid, int threads, cudaStream_t st
   }
 }
 
+// Persistent batch launch: as many CTAs as can be resident, each looping over work items.
+template <typename R, int NG, int FLUX, int RECON>
+cudaError_t launch_batch_one(int threads, cudaStream_t stream, const BatchStageArgs& B) {
+  static std::atomic<bool> attr_done{false};
+  static std::atomic<int> sms{0};
+  const size_t smem = stage_smem_bytes<R>(threads, NG);
+  if (!attr_done.load(std::memory_order_acquire)) {
+    cudaError_t e = cudaFuncSetAttribute(batch_stage_kernel<R, NG, FLUX, RECON>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)stage_smem_bytes<R>(256, 3));
+    if (e != cudaSuccess) return e;
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    sms.store(n > 0 ? n : 1);
+    attr_done.store(true, std::memory_order_release);
+  }
+  if (B.n_items <= 0) return cudaSuccess;
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, batch_stage_kernel<R, NG, FLUX, RECON>, threads, smem);
+  if (e != cudaSuccess) return e;
+  long long grid = (long long)(per_sm > 0 ? per_sm : 1) * sms.load();
+  if (grid > B.n_items) grid = B.n_items;
+  batch_stage_kernel<R, NG, FLUX, RECON><<<(unsigned)grid, threads, smem, stream>>>(B);
+  return cudaGetLastError();
+}
+
+template <typename R, int FLUX>
+cudaError_t launch_batch_flux(int recon, int threads, cudaStream_t stream,
+                              const BatchStageArgs& B) {
+  switch (recon) {
+    case 0: return launch_batch_one<R, 2, FLUX, 0>(threads, stream, B);
+    case 3: return launch_batch_one<R, 2, FLUX, 3>(threads, stream, B);
+    case 5: return launch_batch_one<R, 3, FLUX, 5>(threads, stream, B);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 #define CATO_DECLARE_STAGE(R, F)                                                             \
   extern template cudaError_t launch_stage_flux<R, F>(int, dim3, int, cudaStream_t,         \
-                                                      const StageArgs&, const FluxConsts<R>&);
+                                                      const StageArgs&, const FluxConsts<R>&); \
+  extern template cudaError_t launch_batch_flux<R, F>(int, int, cudaStream_t,               \
+                                                      const BatchStageArgs&);
 CATO_DECLARE_STAGE(double, 0) CATO_DECLARE_STAGE(double, 1) CATO_DECLARE_STAGE(double, 2)
 CATO_DECLARE_STAGE(double, 3) CATO_DECLARE_STAGE(double, 4) CATO_DECLARE_STAGE(double, 5)
 CATO_DECLARE_STAGE(double, 6) CATO_DECLARE_STAGE(double, 7)
@@ -65,6 +107,22 @@ inline cudaError_t launch_stage(int flux, int recon, dim3 grid, int threads, cud
     case 5: return launch_stage_flux<R, 5>(recon, grid, threads, s, A, K);
     case 6: return launch_stage_flux<R, 6>(recon, grid, threads, s, A, K);
     case 7: return launch_stage_flux<R, 7>(recon, grid, threads, s, A, K);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename R>
+inline cudaError_t launch_batch(int flux, int recon, int threads, cudaStream_t s,
+                                const BatchStageArgs& B) {
+  switch (flux) {
+    case 0: return launch_batch_flux<R, 0>(recon, threads, s, B);
+    case 1: return launch_batch_flux<R, 1>(recon, threads, s, B);
+    case 2: return launch_batch_flux<R, 2>(recon, threads, s, B);
+    case 3: return launch_batch_flux<R, 3>(recon, threads, s, B);
+    case 4: return launch_batch_flux<R, 4>(recon, threads, s, B);
+    case 5: return launch_batch_flux<R, 5>(recon, threads, s, B);
+    case 6: return launch_batch_flux<R, 6>(recon, threads, s, B);
+    case 7: return launch_batch_flux<R, 7>(recon, threads, s, B);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -41,8 +41,12 @@ template <> struct Num<float> {
   static __device__ __forceinline__ float sqrt(float a) { return ::sqrtf(a); }
 };
 
+// FP64: the reference's MAX/MIN as compare-and-select (identical signed-zero behaviour to the
+// CPU restatement).  FP32 (mixed path): single-instruction min/max.
 template <typename R> __device__ __forceinline__ R rmax(R a, R b) { return (a < b) ? b : a; }
 template <typename R> __device__ __forceinline__ R rmin(R a, R b) { return (b < a) ? b : a; }
+template <> __device__ __forceinline__ float rmax<float>(float a, float b) { return fmaxf(a, b); }
+template <> __device__ __forceinline__ float rmin<float>(float a, float b) { return fminf(a, b); }
 template <typename R> __device__ __forceinline__ R rabs(R a) { return fabs(a); }
 // Fortran SIGN(1.0, x)
 template <typename R> __device__ __forceinline__ R fsign1(R x) { return signbit(x) ? R(-1) : R(1); }
@@ -53,9 +57,7 @@ __device__ __forceinline__ bool abs_lt(double x, double c) {
   unsigned long long bx = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
   return bx < (unsigned long long)__double_as_longlong(c);
 }
-__device__ __forceinline__ bool abs_lt(float x, float c) {
-  return (__float_as_uint(x) & 0x7fffffffu) < __float_as_uint(c);
-}
+__device__ __forceinline__ bool abs_lt(float x, float c) { return fabsf(x) < c; }
 
 // ---------------------------------------------------------------------------------------------
 // FP64 <-> FP32 conversion on the integer pipe (GB300's F2F shares the narrow FP64 pipe).

@@ -220,15 +220,15 @@ __device__ __forceinline__ float f4get(const float4& v, int k) {
 // ---------------------------------------------------------------------------------------------
 // the kernel
 // ---------------------------------------------------------------------------------------------
+// One tile: columns [bx*W, bx*W + W) x rows [by*rows_per_cta, ...) of one instance.
 template <typename R, int NG, int FLUX, int RECON>
-__global__ void __launch_bounds__(256) stage_kernel(const StageArgs A, const FluxConsts<R> K) {
-  if (A.active && *A.active == 0) return;
+__device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<R>& K, int bx,
+                                           int by, unsigned char* smem_raw) {
   constexpr int RING = 2 * NG;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int T = blockDim.x, W = T - 2 * NG, t = threadIdx.x;
-  const int x0 = blockIdx.x * W;
+  const int x0 = bx * W;
   const int gx = x0 - NG + t;
-  const int y0 = blockIdx.y * A.rows_per_cta;
+  const int y0 = by * A.rows_per_cta;
   const int y1 = min(y0 + A.rows_per_cta, A.nj);
   R* ring = reinterpret_cast<R*>(smem_raw);  // [RING][4][T]
   R* sfi = ring + RING * 4 * T;              // [4][T]   i-edge between cols t and t+1
@@ -403,6 +403,13 @@ __global__ void __launch_bounds__(256) stage_kernel(const StageArgs A, const Flu
       if (st_loc) atomicOr(A.status, st_loc);
     }
   }
+}
+
+template <typename R, int NG, int FLUX, int RECON>
+__global__ void __launch_bounds__(256) stage_kernel(const StageArgs A, const FluxConsts<R> K) {
+  if (A.active && *A.active == 0) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  stage_tile<R, NG, FLUX, RECON>(A, K, blockIdx.x, blockIdx.y, smem_raw);
 }
 
 // dynamic shared memory of one CTA

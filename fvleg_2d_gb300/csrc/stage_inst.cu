@@ -14,4 +14,6 @@ namespace cato {
 template cudaError_t launch_stage_flux<CATO_REAL, CATO_FLUX>(int, dim3, int, cudaStream_t,
                                                              const StageArgs&,
                                                              const FluxConsts<CATO_REAL>&);
+template cudaError_t launch_batch_flux<CATO_REAL, CATO_FLUX>(int, int, cudaStream_t,
+                                                             const BatchStageArgs&);
 }  // namespace cato

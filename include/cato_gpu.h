@@ -222,6 +222,46 @@ int cato_gpu_solve_noalloc(const cato_config* cfg, double* rho, double* u, doubl
                            double* d_rho_dt, double* d_rho_u_dt, double* d_rho_v_dt,
                            double* d_rho_E_dt, int64_t ld);
 
+/* ---- Batched engine: many independent instances of uneven sizes advanced together ---------
+ * No counterpart in the reference (CATO runs one grid per process).  Each instance keeps its
+ * own CFL dt, time, iteration count and stop condition; one step of the batch is one persistent
+ * launch per RK stage and per (flux, reconstruction) group, whose CTAs pull (instance, tile)
+ * work items from a device queue.  Chunks of steps are captured in a CUDA graph.  An instance's
+ * results do not depend on the other instances in the batch. */
+typedef struct cato_batch cato_batch;
+
+/* A batch of at most `capacity` instances, all with `precision` and integrator `rk`. */
+int cato_batch_create(int32_t capacity, int32_t precision, int32_t rk, cato_batch** out);
+int cato_batch_destroy(cato_batch* b);
+
+/* Device bytes one instance of `cfg` occupies (state, stage buffers), for admission control. */
+int cato_batch_instance_bytes(const cato_config* cfg, uint64_t* bytes);
+
+/* Add an instance from primitive initial conditions (as cato_gpu_upload_primitive); it runs
+ * until time >= t_end or max_steps steps (max_steps < 0: no limit).  *slot identifies it. */
+int cato_batch_add(cato_batch* b, const cato_config* cfg, const double* rho, const double* u,
+                   const double* v, const double* p, int64_t ld, double t_end, int64_t max_steps,
+                   int32_t* slot);
+int cato_batch_remove(cato_batch* b, int32_t slot);
+
+/* Tile plan shared by all instances (CTA width incl. halo, rows per tile). */
+int cato_batch_set_plan(cato_batch* b, int32_t threads, int32_t rows_per_cta);
+
+/* Advance every running instance n_steps steps (instances that reach their stop condition idle);
+ * with use_graph, whole chunks replay a captured CUDA graph.  *device_ms = event time. */
+int cato_batch_step(cato_batch* b, int32_t n_steps, int32_t use_graph, float* device_ms);
+
+/* One instance's progress; *running = 0 once it reached t_end / max_steps or failed. */
+int cato_batch_query(cato_batch* b, int32_t slot, int64_t* iteration, double* time, double* dt,
+                     int32_t* running, int32_t* error_code);
+
+/* Number of running instances; running_flags (capacity entries, may be NULL) per slot. */
+int cato_batch_running(cato_batch* b, int32_t* n_running, int32_t* running_flags);
+
+/* Conserved state of one instance into halo-padded host arrays (any may be NULL). */
+int cato_batch_download(cato_batch* b, int32_t slot, double* rho, double* rho_u, double* rho_v,
+                        double* rho_E, int64_t ld);
+
 /* Page-locked host memory for fast uploads/downloads (cudaHostAlloc / cudaFreeHost). */
 int cato_host_alloc(uint64_t bytes, void** out);
 int cato_host_free(void* p);
