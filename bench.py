@@ -18,6 +18,7 @@ grid and scheme; rank 0 only.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -33,9 +34,10 @@ METRIC = "cell-updates/s & HBM GB/s, plain FP64 vs mixed/batched; p99 solve late
 HBM_FALLBACK_GBS = 6800.0
 # algorithmic HBM bytes per cell and stage kernel launch (state in, state out), SSP-RK3:
 #   FP64 : stage 1 reads U^n, writes U1 (64 B); stages 2, 3 read U^n + U^k, write 32 B (96 B)
-#   mixed: stage 1 reads U^n, writes delta1 (32+16); stage 2 reads U^n + delta1, writes delta2
-#          (32+16+16); stage 3 reads U^n + delta2, writes U^{n+1} (32+16+32)
-BYTES_PER_CELL_STAGE = {"fp64": (64, 96, 96), "mixed": (48, 64, 80)}
+#   mixed: stage 1 reads the FP32 copy of U^n and writes delta1 (16+16); stage 2 reads it and
+#          delta1, writes delta2 (16+16+16); stage 3 reads it, delta2 and the FP64 U^n, writes the
+#          FP64 U^{n+1} and its FP32 copy (16+16+32+32+16)
+BYTES_PER_CELL_STAGE = {"fp64": (64, 96, 96), "mixed": (32, 48, 112)}
 
 
 def env_int(name, default):
@@ -279,6 +281,90 @@ def bench_e2e(args, cfg, prims):
             "sequence": "upload_primitive + K x integrate + download (pinned host buffers)"}
 
 
+def bench_batched(args):
+    """Config 3: 256 uneven grids (sides log-uniform [64,1024] rounded to 16, aspect U[1,4]),
+    random circles, SLAU + MLP5, SSP-RK2, CFL 0.5, 500 steps each, mixed precision, one
+    persistent launch per stage, CUDA-graph chunks, autotuned tile plan.  Error vs FP64 on a
+    sample of the instances."""
+    import numpy as np
+
+    from fvleg_2d_gb300 import ic
+    from fvleg_2d_gb300.batch import Batch
+
+    rng = np.random.default_rng(args.batch_seed)
+    sides = ic.batch_sides(args.batch_n, rng)
+    insts = [ic.random_circles(nx, ny, rng, precision="mixed") for nx, ny in sides]
+    cells = sum(c.ni * c.nj for c, _ in insts)
+    # autotune the shared tile plan on a scratch batch of the same instances
+    tune = Batch(len(insts), precision="mixed")
+    for cfg, prims in insts:
+        tune.add(cfg, prims)
+    table = {}
+    for threads, rows in [(64, 16), (128, 16), (128, 32), (256, 16), (256, 32)]:
+        tune.set_plan(threads, rows)
+        tune.step(16)
+        table[f"{threads}x{rows}"] = tune.step(16) / 16
+    tune.close()
+    best = min(table, key=table.get)
+    threads, rows = (int(x) for x in best.split("x"))
+    b = Batch(len(insts), precision="mixed")
+    b.set_plan(threads, rows)
+    slots = [b.add(cfg, prims, max_steps=args.batch_steps) for cfg, prims in insts]
+    ms = b.step(args.batch_steps)
+    n_run, _ = b.running()
+    updates = cells * args.batch_steps
+    value = updates / (ms / 1e3)
+    bytes_per_update = 144  # mixed SSP-RK2: 32 B (stage 1) + 112 B (stage 2) per cell
+    # FP64 reference on a sample: relative L1 density error of the mixed result
+    k = min(args.batch_ref, len(insts))
+    pick = sorted(rng.choice(len(insts), size=k, replace=False).tolist())
+    ref = Batch(k, precision="fp64")
+    rslots = []
+    for i in pick:
+        cfg, prims = insts[i]
+        c64 = dataclasses.replace(cfg, precision="fp64")
+        rslots.append(ref.add(c64, prims, max_steps=args.batch_steps))
+    ref.step(args.batch_steps)
+    errs = []
+    for i, rs in zip(pick, rslots):
+        g = insts[i][0].ghost_layers()
+        a = ref.state(rs)["rho"][g:-g, g:-g]
+        m = b.state(slots[i])["rho"][g:-g, g:-g]
+        errs.append(float(np.abs(m - a).sum() / np.abs(a).sum()))
+    ref.close()
+    b.close()
+    return {
+        "value": value, "unit": "cell-updates/s", "instances": len(insts), "cells": cells,
+        "steps_each": args.batch_steps, "device_ms": ms, "still_running": n_run,
+        "plan": {"threads": threads, "rows_per_cta": rows, "tuning_ms_per_step": table},
+        "launches_per_step": 4, "dtype": "f32 flux / f64 state",
+        "roofline": {"bound": "hbm", "achieved": value * bytes_per_update / 1e9,
+                     "unit": "GB/s", "algorithmic_bytes_per_cell_update": bytes_per_update},
+        "rel_l1_density_error_vs_fp64": {"max": max(errs), "mean": sum(errs) / len(errs),
+                                         "instances": k},
+        "scheme": "SLAU, MLP5 (3 ghost layers), SSP-RK2, CFL 0.5, zero-gradient BCs",
+    }
+
+
+def bench_serving(args):
+    """Config 4 stream through the continuous-batching server (mixed and FP64)."""
+    from fvleg_2d_gb300.serve import Server, make_requests
+
+    out = {}
+    for precision in ("mixed", "fp64"):
+        reqs = make_requests(args.serve_n, rate=args.serve_rate, seed=args.serve_seed,
+                             side=(args.serve_min_side, args.serve_max_side), precision=precision)
+        srv = Server(precision=precision, budget_gb=120.0, capacity=1024, chunk_steps=16)
+        st = srv.serve(reqs, max_wall_s=args.serve_max_wall)
+        srv.close()
+        out[precision] = st.summary()
+    out["stream"] = {"requests": args.serve_n, "rate_per_s": args.serve_rate,
+                     "side": [args.serve_min_side, args.serve_max_side], "t_end": [0.05, 0.3],
+                     "fluxes": "AUSM+-up, AUSMPW+, SLAU, HLLC, Roe (uniform)",
+                     "admission": "120 GB HBM budget"}
+    return out
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -288,6 +374,18 @@ def main() -> int:
     ap.add_argument("--n", type=int, default=4096)
     ap.add_argument("--cpu-baseline-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-n", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=500)
+    ap.add_argument("--batch-seed", type=int, default=2024)
+    ap.add_argument("--batch-ref", type=int, default=8)
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-n", type=int, default=100)
+    ap.add_argument("--serve-rate", type=float, default=100.0)
+    ap.add_argument("--serve-seed", type=int, default=7)
+    ap.add_argument("--serve-min-side", type=int, default=64)
+    ap.add_argument("--serve-max-side", type=int, default=256)
+    ap.add_argument("--serve-max-wall", type=float, default=90.0)
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":
@@ -309,6 +407,8 @@ def main() -> int:
         cpu = {"value": v, "unit": "cell-updates/s", "cores": used, "kind": "port",
                "sample": f"{args.cpu_baseline_steps} SSP-RK3 steps of the same {args.n}^2 grid "
                          f"({secs:.1f} s, OpenMP C restatement of the reference)"}
+    batched = None if args.no_batched else bench_batched(args)
+    serving = None if args.no_serving else bench_serving(args)
     if rank != 0:
         return 0
     launches = fp64["launches_per_step"] * args.steps
@@ -340,6 +440,8 @@ def main() -> int:
             "roofline": mixed["roofline"], "stage_ms_per_step": mixed["stage_ms_per_step"],
             "gpu_launches": mixed["launches_per_step"] * args.steps, "clocks": mixed["clocks"],
         },
+        "batched": batched,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
     return 0

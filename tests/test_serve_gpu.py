@@ -1,0 +1,40 @@
+"""Serving loop: requests admitted while others run give exactly the result they give alone,
+and admission respects the HBM budget."""
+import numpy as np
+import pytest
+
+from fvleg_2d_gb300.serve import Server, make_requests, run_alone
+
+pytestmark = pytest.mark.gpu
+
+
+def test_each_result_same_alone_and_in_mix(cato_lib):
+    reqs = make_requests(10, rate=400.0, seed=3, side=(32, 96), t_end=(0.01, 0.03))
+    srv = Server(precision="mixed", budget_gb=120.0, capacity=16, chunk_steps=8,
+                 keep_results=True)
+    stats = srv.serve(reqs)
+    srv.close()
+    assert len(stats.completed) == len(reqs) and stats.censored == 0
+    overlapped = sum(1 for r in reqs for o in reqs
+                     if r is not o and o.admitted < r.finished and r.admitted < o.finished)
+    assert overlapped > 0, "requests should share the GPU"
+    for r in reqs:
+        ref = run_alone(r)
+        assert r.steps == ref["steps"] and r.error_code == 0
+        for k in ("rho", "rho_u", "rho_v", "rho_E"):
+            np.testing.assert_array_equal(r.result[k], ref[k], err_msg=f"request {r.rid} {k}")
+
+
+def test_admission_respects_budget(cato_lib):
+    reqs = make_requests(6, rate=1000.0, seed=4, side=(48, 64), t_end=(0.01, 0.02))
+    from fvleg_2d_gb300.batch import instance_bytes
+
+    one = max(instance_bytes(r.config_and_ic()[0]) for r in reqs)
+    srv = Server(precision="mixed", budget_gb=2.5 * one / 1e9, capacity=16, chunk_steps=4)
+    stats = srv.serve(reqs)
+    srv.close()
+    assert len(stats.completed) == 6
+    # never more than two instances resident at once under a 2.5-instance budget
+    for r in reqs:
+        live = sum(1 for o in reqs if o.admitted <= r.admitted < o.finished)
+        assert live <= 2
