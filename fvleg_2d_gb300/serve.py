@@ -89,6 +89,7 @@ class ServeStats:
             return lat[min(len(lat) - 1, int(math.ceil(p / 100.0 * len(lat))) - 1)]
 
         return {"completed": len(self.completed), "censored": self.censored,
+                "ended_with_error": sum(1 for r in self.completed if r.error_code),
                 "p50_latency_s": pct(50), "p99_latency_s": pct(99),
                 "wall_s": self.wall_s, "device_s": self.device_ms / 1e3,
                 "cell_updates": self.cell_updates,
@@ -201,6 +202,7 @@ def run_alone(req: Request) -> dict:
     s = b.add(cfg, prims, t_end=req.t_end)
     b.run_until_done(chunk=64)
     out = b.state(s)
-    out["steps"] = b.query(s)["iteration"]
+    q = b.query(s)
+    out["steps"], out["error_code"] = q["iteration"], q["error_code"]
     b.close()
     return out
