@@ -58,12 +58,16 @@ def test_admission_respects_budget(cato_lib):
     reqs = make_requests(6, rate=1000.0, seed=4, side=(48, 64), t_end=(0.01, 0.02))
     from fvleg_2d_gb300.batch import instance_bytes
 
-    one = max(instance_bytes(r.config_and_ic()[0]) for r in reqs)
-    srv = Server(precision="mixed", budget_gb=2.5 * one / 1e9, capacity=16, chunk_steps=4)
+    need = {r.rid: instance_bytes(r.config_and_ic()[0]) for r in reqs}
+    budget = 2.5 * max(need.values())
+    srv = Server(precision="mixed", budget_gb=budget / 1e9, capacity=16, chunk_steps=4)
     stats = srv.serve(reqs)
     srv.close()
     assert len(stats.completed) == 6
-    # never more than two instances resident at once under a 2.5-instance budget
+    # at every admission the resident instances fit the budget, and the budget did bind
+    peak = 0
     for r in reqs:
-        live = sum(1 for o in reqs if o.admitted <= r.admitted < o.finished)
-        assert live <= 2
+        live = [o for o in reqs if o.admitted <= r.admitted < o.finished]
+        assert sum(need[o.rid] for o in live) <= budget
+        peak = max(peak, len(live))
+    assert peak < len(reqs)
