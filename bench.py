@@ -281,6 +281,40 @@ def bench_e2e(args, cfg, prims):
             "sequence": "upload_primitive + K x integrate + download (pinned host buffers)"}
 
 
+def bench_kh(args, peak_gbs):
+    """Roofline stress: Kelvin-Helmholtz shear layer on 8192^2 (Roe with Harten's entropy fix,
+    superbee, SSP-RK3, CFL 0.4, periodic x, symmetry y).  The mixed path runs the full 200-step
+    window; the FP64 path a bounded window of it (it is FP64-ALU bound, ~0.5 s per step)."""
+    from fvleg_2d_gb300 import ic
+    from fvleg_2d_gb300.fluid import Fluid
+
+    out = {}
+    for precision, steps in (("mixed", args.kh_steps), ("fp64", args.kh_fp64_steps)):
+        if steps <= 0:
+            continue
+        cfg, prims = ic.kelvin_helmholtz(args.kh_n, roe_entropy_fix="harten", precision=precision)
+        f = Fluid(cfg).initialize(*prims)
+        f.run_timed(3)
+        with ClockSampler(env_int("LOCAL_RANK", 0)) as clk:
+            total_ms, kernel_ms = f.run_timed(steps, per_kernel=True)
+        cells = cfg.ni * cfg.nj
+        per_stage = BYTES_PER_CELL_STAGE[precision]
+        achieved = sum(per_stage) * cells * steps / (sum(kernel_ms[1:]) / 1e3) / 1e9
+        out[precision] = {
+            "value": cells * steps / (total_ms / 1e3), "unit": "cell-updates/s",
+            "steps": steps, "ms_per_step": total_ms / steps,
+            "stage_ms_per_step": [m / steps for m in kernel_ms[1:]],
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+                         "frac": achieved / peak_gbs,
+                         "algorithmic_bytes_per_cell_update": sum(per_stage)},
+            "clocks": clk.summary(),
+        }
+        f.close()
+    out["workload"] = (f"Kelvin-Helmholtz {args.kh_n}x{args.kh_n}, Roe + Harten, superbee, "
+                       "SSP-RK3, CFL 0.4, periodic x / symmetry y; 3 warm-up steps")
+    return out
+
+
 def bench_batched(args):
     """Config 3: 256 uneven grids (sides log-uniform [64,1024] rounded to 16, aspect U[1,4]),
     random circles, SLAU + MLP5, SSP-RK2, CFL 0.5, 500 steps each, mixed precision, one
@@ -384,6 +418,10 @@ def main() -> int:
     ap.add_argument("--batch-steps", type=int, default=500)
     ap.add_argument("--batch-seed", type=int, default=2024)
     ap.add_argument("--batch-ref", type=int, default=8)
+    ap.add_argument("--no-kh", action="store_true")
+    ap.add_argument("--kh-n", type=int, default=8192)
+    ap.add_argument("--kh-steps", type=int, default=200)
+    ap.add_argument("--kh-fp64-steps", type=int, default=5)
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serve-n", type=int, default=100)
     ap.add_argument("--serve-rate", type=float, default=100.0)
@@ -412,6 +450,7 @@ def main() -> int:
         cpu = {"value": v, "unit": "cell-updates/s", "cores": used, "kind": "port",
                "sample": f"{args.cpu_baseline_steps} SSP-RK3 steps of the same {args.n}^2 grid "
                          f"({secs:.1f} s, OpenMP C restatement of the reference)"}
+    kh = None if args.no_kh else bench_kh(args, peak)
     batched = None if args.no_batched else bench_batched(args)
     serving = None if args.no_serving else bench_serving(args)
     if rank != 0:
@@ -445,6 +484,7 @@ def main() -> int:
             "roofline": mixed["roofline"], "stage_ms_per_step": mixed["stage_ms_per_step"],
             "gpu_launches": mixed["launches_per_step"] * args.steps, "clocks": mixed["clocks"],
         },
+        "kelvin_helmholtz": kh,
         "batched": batched,
         "serving": serving,
     }

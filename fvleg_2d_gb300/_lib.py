@@ -60,6 +60,8 @@ def load(build_if_missing: bool = False):
         "cato_gpu_set_time": (ctypes.c_int, [H, ctypes.c_double, i64]),
         "cato_gpu_get_time": (ctypes.c_int, [H, _dp, ctypes.POINTER(i64), _dp]),
         "cato_gpu_download": (ctypes.c_int, [H] + [_dp] * 8 + [i64]),
+        "cato_gpu_conservation_sums": (ctypes.c_int, [H, _dp]),
+        "cato_gpu_convergence": (ctypes.c_int, [H, _dp]),
         "cato_gpu_solve": (ctypes.c_int, [H] + [_dp] * 8 + [i64]),
         "cato_gpu_interpolate_edges": (ctypes.c_int, [H, _dp, i64, _dp, _dp]),
         "cato_gpu_status": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int32)]),

@@ -56,6 +56,8 @@ struct cato_handle {
   int cur = 0;               // mixed: which U holds U^n
   bool uploaded = false;
   bool raw_pending = false;  // next stage 1 uses prim_raw
+  bool stepped = false;      // a step ran since the last upload (its stage buffers are valid)
+  double* red = nullptr;     // reduction partials + results (lazy)
   Plan plan;
   FluxConsts<double> K64{};
   FluxConsts<float> K32{};
@@ -455,6 +457,7 @@ int cato_gpu_destroy(cato_handle* h) {
   for (int k = 0; k < 8; ++k) cudaFree(h->scratch[k]);
   for (int k = 0; k < 4; ++k) cudaFree(h->halo[k]);
   cudaFree(h->ctl);
+  cudaFree(h->red);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
   if (h->own_stream_saved) h->stream = h->own_stream_saved;
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -497,6 +500,7 @@ int cato_gpu_upload_primitive(cato_handle* h, const double* rho, const double* u
   if (rc) return rc;
   h->uploaded = true;
   h->raw_pending = true;
+  h->stepped = false;
   return status_code(h->ctl_host->status);
 }
 
@@ -527,6 +531,7 @@ int cato_gpu_integrate(cato_handle* h, double dt, double* dt_used, int32_t* erro
   }
   rc = pull_ctl(h);
   if (rc) return rc;
+  if (h->ctl_host->iter > c.iter) h->stepped = true;
   if (dt_used) *dt_used = h->ctl_host->dt;
   if (error_code) *error_code = status_code(h->ctl_host->status);
   return CATO_OK;
@@ -565,6 +570,7 @@ int cato_gpu_run(cato_handle* h, int64_t max_steps, double t_end, int64_t* steps
     }
     if (!h->ctl_host->active || h->ctl_host->status) break;
   }
+  if (h->ctl_host->iter > it0) h->stepped = true;
   if (steps_done) *steps_done = h->ctl_host->iter - it0;
   if (time) *time = h->ctl_host->time;
   if (error_code) *error_code = status_code(h->ctl_host->status);
@@ -780,6 +786,7 @@ int cato_gpu_run_timed(cato_handle* h, int64_t n_steps, float* total_ms, float* 
   if (rc) return rc;
   if (h->cfg.precision == CATO_MIXED)
     h->cur = (int)((parity0 + (h->ctl_host->iter - it0)) & 1);
+  if (h->ctl_host->iter > it0) h->stepped = true;
   return status_code(h->ctl_host->status);
 }
 
@@ -842,7 +849,81 @@ int cato_gpu_profile_step(cato_handle* h, float* kernel_ms, int32_t capacity, in
   for (int k = 0; k < nk; ++k) CK(cudaEventElapsedTime(&kernel_ms[k], ev[k], ev[k + 1]));
   for (auto& e : ev) cudaEventDestroy(e);
   if (n_kernels) *n_kernels = nk;
-  return pull_ctl(h);
+  rc = pull_ctl(h);
+  if (rc) return rc;
+  if (h->ctl_host->iter > c.iter) h->stepped = true;
+  return CATO_OK;
+}
+
+static int reduce(cato_handle* h, RedArgs R, double out[RED_Q]) {
+  if (!h->red) CK(cudaMalloc(&h->red, (RED_BLOCKS + 1) * RED_Q * sizeof(double)));
+  R.ni = h->ni;
+  R.nj = h->nj;
+  R.pitch = h->pitch;
+  R.partials = h->red;
+  reduce_partials_kernel<<<RED_BLOCKS, RED_THREADS, 0, h->stream>>>(R);
+  CK(cudaGetLastError());
+  reduce_final_kernel<<<1, RED_THREADS, 0, h->stream>>>(h->red, RED_BLOCKS,
+                                                       h->red + RED_BLOCKS * RED_Q);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, h->red + RED_BLOCKS * RED_Q, RED_Q * sizeof(double),
+                     cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return CATO_OK;
+}
+
+// U^n of the handle: FP64 U[0]; mixed U[cur]
+static double* const* state_now(cato_handle* h) {
+  return h->cfg.precision == CATO_FP64 ? h->U[0] : h->U[h->cur];
+}
+
+int cato_gpu_conservation_sums(cato_handle* h, double totals[4]) {
+  if (!h || !totals) return CATO_ERR_ARG;
+  if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  RedArgs R{};
+  R.mode = 0;
+  double* const* U = state_now(h);
+  for (int k = 0; k < 4; ++k) R.A[k] = U[k];
+  double out[RED_Q];
+  int rc = reduce(h, R, out);
+  if (rc) return rc;
+  for (int k = 0; k < 4; ++k) totals[k] = out[k] * h->G.vol;
+  return CATO_OK;
+}
+
+int cato_gpu_convergence(cato_handle* h, double l2[4]) {
+  if (!h || !l2) return CATO_ERR_ARG;
+  if (!h->uploaded || !h->stepped) return fail(h, CATO_ERR_STATE, "no step since the upload");
+  const int rk = h->cfg.rk;
+  const bool ssp = rk == CATO_RK_SSP2 || rk == CATO_RK_SSP3;
+  RedArgs R{};
+  R.mode = 1;
+  if (h->cfg.precision == CATO_FP64) {
+    // SSP: the first stage's output U_1 is still in S0; rk(m,n) compares with U^n, which the
+    // last stage overwrote in place
+    if (!ssp)
+      return fail(h, CATO_ERR_STATE, "FP64 rk(m,n) steps update U^n in place: no U_0 to compare");
+    for (int k = 0; k < 4; ++k) {
+      R.A[k] = h->S[0][k];
+      R.B[k] = h->U[0][k];
+    }
+  } else {
+    // U^n is in U[1-cur] after the step; U_1 = U^n + delta_1 for SSP, U_0 = U^n for rk(m,n)
+    for (int k = 0; k < 4; ++k) {
+      R.A[k] = h->U[1 - h->cur][k];
+      R.B[k] = h->U[h->cur][k];
+    }
+    R.d1 = ssp ? h->D[0] : nullptr;
+  }
+  double out[RED_Q];
+  int rc = reduce(h, R, out);
+  if (rc) return rc;
+  for (int k = 0; k < 4; ++k) {
+    double n0 = sqrt(out[4 + k]);
+    if (k == 1 || k == 2) n0 = n0 > 1.0 ? n0 : 1.0;
+    l2[k] = sqrt(out[k]) / n0;
+  }
+  return CATO_OK;
 }
 
 }  // extern "C"

@@ -166,4 +166,80 @@ static __global__ void interp_edges_kernel(int ni, int nj, int lim, const double
   }
 }
 
+// Deterministic FP64 reductions over the interior: a fixed partition (block b takes rows
+// b, b + RED_BLOCKS, ...; thread t takes columns t, t + RED_THREADS, ...) and a fixed summation
+// tree, so a result depends only on the data and the grid size, never on scheduling.
+constexpr int RED_BLOCKS = 304;  // 2 x 152 SMs
+constexpr int RED_THREADS = 256;
+constexpr int RED_Q = 8;         // quantities per reduction
+
+struct RedArgs {
+  int ni, nj, pitch;
+  int mode;               // 0: sums of A; 1: sums of (B - A1)^2 and A1^2, A1 = A (+ d1)
+  const double* A[4];
+  const double* B[4];
+  const float4* d1;       // mode 1, mixed path: first-stage increment (A1 = A + d1)
+  double* partials;       // RED_BLOCKS x RED_Q
+};
+
+__device__ __forceinline__ double block_sum(double x, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = x;
+  __syncthreads();
+  x = (threadIdx.x < (RED_THREADS >> 5)) ? sh[threadIdx.x] : 0.0;
+  if (w == 0) {
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  }
+  return x;  // valid in thread 0
+}
+
+static __global__ void __launch_bounds__(RED_THREADS) reduce_partials_kernel(RedArgs R) {
+  __shared__ double sh[RED_THREADS / 32];
+  double acc[RED_Q];
+#pragma unroll
+  for (int q = 0; q < RED_Q; ++q) acc[q] = 0.0;
+  for (int j = blockIdx.x; j < R.nj; j += gridDim.x) {
+    for (int i = threadIdx.x; i < R.ni; i += blockDim.x) {
+      const size_t idx = (size_t)j * R.pitch + i;
+      float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (R.mode == 1 && R.d1) d = R.d1[idx];
+      const float dd[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        double a = R.A[k][idx];
+        if (R.mode == 0) {
+          acc[k] += a;
+        } else {
+          if (R.d1) a = a + (double)dd[k];
+          const double df = R.B[k][idx] - a;
+          acc[k] += df * df;
+          acc[4 + k] += a * a;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < RED_Q; ++q) {
+    const double s = block_sum(acc[q], sh);
+    if (threadIdx.x == 0) R.partials[blockIdx.x * RED_Q + q] = s;
+  }
+}
+
+// one block: out[q] = sum over blocks of partials[b][q], in a fixed order
+static __global__ void __launch_bounds__(RED_THREADS) reduce_final_kernel(const double* partials,
+                                                                          int n_blocks,
+                                                                          double* out) {
+  __shared__ double sh[RED_THREADS / 32];
+  for (int q = 0; q < RED_Q; ++q) {
+    double x = 0.0;
+    for (int b = threadIdx.x; b < n_blocks; b += blockDim.x) x += partials[b * RED_Q + q];
+    x = block_sum(x, sh);
+    if (threadIdx.x == 0) out[q] = x;
+  }
+}
+
 }  // namespace cato

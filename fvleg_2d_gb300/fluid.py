@@ -164,6 +164,20 @@ class Fluid(_Handle):
                self.h, "download")
         return {k: v for k, v in out.items() if v is not None}
 
+    def conservation_sums(self) -> np.ndarray:
+        """Interior totals of rho, rho u, rho v, rho E times the cell volume (FP64, deterministic)."""
+        out = np.zeros(4)
+        _check(self.L.cato_gpu_conservation_sums(self.h, _lib.ptr(out)), self.h,
+               "conservation_sums")
+        return out
+
+    def convergence(self) -> np.ndarray:
+        """calculate_convergence (mod_fluid.f90:1162-1205) of the last step:
+        [rho, rho u, rho v, rho E] relative L2 change from the first to the last stage."""
+        out = np.zeros(4)
+        _check(self.L.cato_gpu_convergence(self.h, _lib.ptr(out)), self.h, "convergence")
+        return out
+
     def t(self):
         """Time derivative of the current state (fluid_t%t, mod_fluid.f90:460-516)."""
         s = self.state(("rho", "u", "v", "p"))

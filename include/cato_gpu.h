@@ -161,6 +161,20 @@ int cato_gpu_get_time(cato_handle* h, double* time, int64_t* iteration, double* 
 int cato_gpu_download(cato_handle* h, double* rho, double* rho_u, double* rho_v, double* rho_E,
                       double* u, double* v, double* p, double* cs, int64_t ld);
 
+/* Global totals of the current state in FP64: sum over the interior of rho, rho u, rho v, rho E
+ * times the cell volume (mass, momentum and energy in the domain; the reference sums rho_E for
+ * its energy check, mod_fluid.f90:808-811).  Deterministic: a fixed partition and summation
+ * tree, so repeated calls on the same state give the same bits. */
+int cato_gpu_conservation_sums(cato_handle* h, double totals[4]);
+
+/* calculate_convergence (mod_fluid.f90:1162-1205) of the last step: L2 norm of the change from
+ * the first to the last stage over the interior, divided by the first stage's norm (by
+ * max(norm, 1) for rho u and rho v): SSP-RK2 U_1 vs U_2, SSP-RK3 U_1 vs U_3, rk(m,n) U_0 vs
+ * U_curr.  Computed on demand from the stage buffers of the last step (no cost per step).
+ * CATO_ERR_STATE before the first step after an upload, and for FP64 rk(m,n), whose last stage
+ * overwrites U_0 in place. */
+int cato_gpu_convergence(cato_handle* h, double l2[4]);
+
 /* flux_solver_t%solve (flux_solver.f90:66-87) on caller-given primitive fields: applies the BCs
  * to the ghosts of rho/u/v/p (written back, as the reference's intent(inout)), reconstructs,
  * computes edge fluxes and the flux divergence into d_*_dt (halo-padded, ghosts zeroed as in

@@ -826,6 +826,8 @@ struct oracle_fluid {
   double* L[4];
   double time, dt;
   int64_t iteration;
+  double conv[4];   /* calculate_convergence of the last step */
+  int conv_valid;
 };
 
 static double* falloc(dims_t d) { return (double*)calloc(nfield(d), sizeof(double)); }
@@ -918,6 +920,7 @@ int oracle_set_primitive(oracle_fluid* f, const double* rho, const double* u, co
     }
   f->time = 0.0;
   f->iteration = 0;
+  f->conv_valid = 0;
   return 0;
 }
 
@@ -933,6 +936,7 @@ int oracle_set_conserved(oracle_fluid* f, const double* rho, const double* rho_u
     }
   double* U[4] = {f->rho, f->rhou, f->rhov, f->rhoE};
   derive_all(f, U, f->u, f->v, f->p, f->cs);
+  f->conv_valid = 0;
   return 0;
 }
 
@@ -992,6 +996,48 @@ static void stage_b(oracle_fluid* f, double* const out[4], double* const A[4], d
       }
 }
 
+/* calculate_convergence (mod_fluid.f90:1162-1205): L2 norm of the change from the first to the
+ * last stage over the interior, relative to the first stage's norm (for rho u and rho v relative to
+ * max(norm, 1)).  norm2 is restated as the square root of the plain sum of squares, summed in
+ * (i fastest, then j) order; the Fortran intrinsic may scale its sum, which changes only the
+ * last bits. */
+static void convergence(oracle_fluid* f, double* const first[4], double* const last[4]) {
+  dims_t d = f->d;
+  for (int k = 0; k < 4; ++k) {
+    double sd = 0.0, s0 = 0.0;
+    for (int j = 1; j <= d.nj; ++j)
+      for (int i = 1; i <= d.ni; ++i) {
+        double a = AT(first[k], i, j), df = AT(last[k], i, j) - a;
+        sd += df * df;
+        s0 += a * a;
+      }
+    double n0 = sqrt(s0);
+    if (k == 1 || k == 2) n0 = n0 > 1.0 ? n0 : 1.0;
+    f->conv[k] = sqrt(sd) / n0;
+  }
+  f->conv_valid = 1;
+}
+
+int oracle_convergence(oracle_fluid* f, double out[4]) {
+  if (!f->conv_valid) return CATO_ERR_STATE;
+  for (int k = 0; k < 4; ++k) out[k] = f->conv[k];
+  return CATO_OK;
+}
+
+/* Interior totals of the conserved variables (sum of U * cell volume): mass, x and y momentum
+ * and energy in the domain, summed in (i fastest, then j) order. */
+int oracle_conservation_sums(oracle_fluid* f, double out[4]) {
+  dims_t d = f->d;
+  double* U[4] = {f->rho, f->rhou, f->rhov, f->rhoE};
+  for (int k = 0; k < 4; ++k) {
+    double s = 0.0;
+    for (int j = 1; j <= d.nj; ++j)
+      for (int i = 1; i <= d.ni; ++i) s += AT(U[k], i, j);
+    out[k] = s * f->geo.vol;
+  }
+  return CATO_OK;
+}
+
 /* stage primitives (u, v, p, cs reused from the scratch solver arrays' neighbours) */
 typedef struct {
   double *u, *v, *p, *cs;
@@ -1016,6 +1062,7 @@ int oracle_integrate(oracle_fluid* f, double dt, int32_t* error_code) {
     derive_all(f, U1, su[0], sv[0], spp[0], scs[0]);
     rc |= residual(f, U1[0], su[0], sv[0], spp[0]);
     stage_b(f, U2, U, 0.5, U1, 0.5, 0.5 * dt);
+    convergence(f, U1, U2);
     for (int k = 0; k < 4; ++k) memcpy(U[k], U2[k], nfield(d) * sizeof(double));
   } else if (f->c.rk == CATO_RK_SSP3) {
     double* U1[4] = {f->st[0][0], f->st[0][1], f->st[0][2], f->st[0][3]};
@@ -1029,6 +1076,7 @@ int oracle_integrate(oracle_fluid* f, double dt, int32_t* error_code) {
     derive_all(f, U2, su[1], sv[1], spp[1], scs[1]);
     rc |= residual(f, U2[0], su[1], sv[1], spp[1]);
     stage_b(f, U3, U, 1.0 / 3.0, U2, 2.0 / 3.0, (2.0 / 3.0) * dt);
+    convergence(f, U1, U3);
     for (int k = 0; k < 4; ++k) memcpy(U[k], U3[k], nfield(d) * sizeof(double));
   } else {
     /* rk(m,n), mod_fluid.f90:926-966 */
@@ -1056,6 +1104,7 @@ int oracle_integrate(oracle_fluid* f, double dt, int32_t* error_code) {
       stage_a(f, Uc, U0, dt * alpha[m]);
       derive_all(f, Uc, su[0], sv[0], spp[0], scs[0]);
     }
+    convergence(f, U0, Uc);
     for (int k = 0; k < 4; ++k) memcpy(U[k], Uc[k], nfield(d) * sizeof(double));
   }
   f->time = f->time + dt;

@@ -52,6 +52,10 @@ int oracle_set_conserved(oracle_fluid* f, const double* rho, const double* rho_u
                          const double* rho_v, const double* rho_E);
 double oracle_time(oracle_fluid* f);
 int64_t oracle_iteration(oracle_fluid* f);
+/* calculate_convergence of the last step (CATO_ERR_STATE before the first step) */
+int oracle_convergence(oracle_fluid* f, double out[4]);
+/* interior totals of rho, rho u, rho v, rho E times the cell volume */
+int oracle_conservation_sums(oracle_fluid* f, double out[4]);
 
 #ifdef __cplusplus
 }

@@ -63,6 +63,9 @@ def lib():
         L.oracle_time.argtypes = [ctypes.c_void_p]
         L.oracle_iteration.restype = ctypes.c_int64
         L.oracle_iteration.argtypes = [ctypes.c_void_p]
+        for name in ("oracle_convergence", "oracle_conservation_sums"):
+            getattr(L, name).restype = ctypes.c_int
+            getattr(L, name).argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]
         _lib = L
     return _lib
 
@@ -187,6 +190,20 @@ class OracleFluid:
     @property
     def iteration(self) -> int:
         return lib().oracle_iteration(self._h)
+
+    def convergence(self) -> np.ndarray:
+        """calculate_convergence of the last step: [rho, rho u, rho v, rho E]."""
+        out = np.zeros(4)
+        rc = lib().oracle_convergence(self._h, _ptr(out))
+        if rc:
+            raise RuntimeError(f"oracle_convergence: {rc}")
+        return out
+
+    def conservation_sums(self) -> np.ndarray:
+        """Interior totals of rho, rho u, rho v, rho E times the cell volume."""
+        out = np.zeros(4)
+        lib().oracle_conservation_sums(self._h, _ptr(out))
+        return out
 
     def run(self, t_end: float, max_steps: int = 10**9) -> int:
         """The main.f90 time loop (CFL dt each step, no last-step trim); returns steps taken."""
