@@ -37,7 +37,8 @@ HBM_FALLBACK_GBS = 6800.0
 #   mixed: stage 1 reads the FP32 copy of U^n and writes delta1 (16+16); stage 2 reads it and
 #          delta1, writes delta2 (16+16+16); stage 3 reads it, delta2 and the FP64 U^n, writes the
 #          FP64 U^{n+1} and its FP32 copy (16+16+32+32+16)
-BYTES_PER_CELL_STAGE = {"fp64": (64, 96, 96), "mixed": (32, 48, 112)}
+#   mixed_df: the FP64 layout
+BYTES_PER_CELL_STAGE = {"fp64": (64, 96, 96), "mixed": (32, 48, 112), "mixed_df": (64, 96, 96)}
 
 
 def env_int(name, default):
@@ -289,7 +290,8 @@ def bench_kh(args, peak_gbs):
     from fvleg_2d_gb300.fluid import Fluid
 
     out = {}
-    for precision, steps in (("mixed", args.kh_steps), ("fp64", args.kh_fp64_steps)):
+    for precision, steps in (("mixed", args.kh_steps), ("mixed_df", args.kh_df_steps),
+                             ("fp64", args.kh_fp64_steps)):
         if steps <= 0:
             continue
         cfg, prims = ic.kelvin_helmholtz(args.kh_n, roe_entropy_fix="harten", precision=precision)
@@ -317,9 +319,9 @@ def bench_kh(args, peak_gbs):
 
 def bench_batched(args):
     """Config 3: 256 uneven grids (sides log-uniform [64,1024] rounded to 16, aspect U[1,4]),
-    random circles, SLAU + MLP5, SSP-RK2, CFL 0.5, 500 steps each, mixed precision, one
-    persistent launch per stage, CUDA-graph chunks, autotuned tile plan.  Error vs FP64 on a
-    sample of the instances."""
+    random circles, SLAU + MLP5, SSP-RK2, CFL 0.5, 500 steps each; one persistent launch per
+    stage, CUDA-graph chunks, autotuned tile plan.  Run in the two mixed precisions (FP32 flux,
+    double-float flux) with the relative L1 density error against FP64 on a sample of instances."""
     import numpy as np
 
     from fvleg_2d_gb300 import ic
@@ -327,62 +329,81 @@ def bench_batched(args):
 
     rng = np.random.default_rng(args.batch_seed)
     sides = ic.batch_sides(args.batch_n, rng)
-    insts = [ic.random_circles(nx, ny, rng, precision="mixed") for nx, ny in sides]
+    insts = [ic.random_circles(nx, ny, rng) for nx, ny in sides]
     cells = sum(c.ni * c.nj for c, _ in insts)
-    # autotune the shared tile plan on a scratch batch of the same instances
-    tune = Batch(len(insts), precision="mixed")
-    for cfg, prims in insts:
-        tune.add(cfg, prims)
-    table = {}
-    for threads, rows in [(64, 16), (128, 16), (128, 32), (256, 16), (256, 32)]:
-        tune.set_plan(threads, rows)
-        tune.step(16)
-        table[f"{threads}x{rows}"] = tune.step(16) / 16
-    tune.close()
-    best = min(table, key=table.get)
-    threads, rows = (int(x) for x in best.split("x"))
-    b = Batch(len(insts), precision="mixed")
-    b.set_plan(threads, rows)
-    slots = [b.add(cfg, prims, max_steps=args.batch_steps) for cfg, prims in insts]
-    ms = b.step(args.batch_steps)
-    n_run, _ = b.running()
-    qs = [b.query(s) for s in slots]
-    failed = sum(1 for q in qs if q["error_code"])
-    updates_done = sum(q["iteration"] * c.ni * c.nj for q, (c, _) in zip(qs, insts))
-    value = updates_done / (ms / 1e3)
-    bytes_per_update = 144  # mixed SSP-RK2: 32 B (stage 1) + 112 B (stage 2) per cell
-    # FP64 reference on a sample: relative L1 density error of the mixed result
-    ok = [i for i, q in enumerate(qs) if q["error_code"] == 0]
-    k = min(args.batch_ref, len(ok))
-    pick = sorted(rng.choice(ok, size=k, replace=False).tolist())
-    ref = Batch(k, precision="fp64")
-    rslots = []
-    for i in pick:
-        cfg, prims = insts[i]
-        c64 = dataclasses.replace(cfg, precision="fp64")
-        rslots.append(ref.add(c64, prims, max_steps=args.batch_steps))
-    ref.step(args.batch_steps)
-    errs = []
-    for i, rs in zip(pick, rslots):
-        g = insts[i][0].ghost_layers()
-        a = ref.state(rs)["rho"][g:-g, g:-g]
-        m = b.state(slots[i])["rho"][g:-g, g:-g]
-        errs.append(float(np.abs(m - a).sum() / np.abs(a).sum()))
-    ref.close()
-    b.close()
-    return {
-        "value": value, "unit": "cell-updates/s", "instances": len(insts), "cells": cells,
-        "steps_each": args.batch_steps, "device_ms": ms, "still_running": n_run,
-        "ended_with_error": failed, "cell_updates": updates_done,
-        "plan": {"threads": threads, "rows_per_cta": rows, "tuning_ms_per_step": table},
-        "launches_per_step": 4, "dtype": "f32 flux / f64 state",
-        "roofline": {"bound": "hbm", "achieved": value * bytes_per_update / 1e9,
-                     "unit": "GB/s", "algorithmic_bytes_per_cell_update": bytes_per_update},
-        "rel_l1_density_error_vs_fp64": {"max": max(errs, default=None),
-                                         "mean": sum(errs) / len(errs) if errs else None,
-                                         "instances": k},
+    pick_rng = np.random.default_rng(args.batch_seed + 1)
+    ref_states = {}
+
+    def fp64_reference(idx):
+        todo = [i for i in idx if i not in ref_states]
+        if not todo:
+            return
+        ref = Batch(len(todo), precision="fp64")
+        slots = [ref.add(insts[i][0], insts[i][1], max_steps=args.batch_steps) for i in todo]
+        ref.step(args.batch_steps)
+        for i, s in zip(todo, slots):
+            q = ref.query(s)
+            ref_states[i] = (q["error_code"], ref.state(s)["rho"])
+        ref.close()
+
+    out = {}
+    for precision in args.batch_precisions.split(","):
+        pinsts = [(dataclasses.replace(c, precision=precision), p) for c, p in insts]
+        # autotune the shared tile plan on a scratch batch of the same instances
+        tune = Batch(len(pinsts), precision=precision)
+        for cfg, prims in pinsts:
+            tune.add(cfg, prims)
+        table = {}
+        for threads, rows in [(64, 16), (128, 16), (128, 32), (256, 16), (256, 32)]:
+            tune.set_plan(threads, rows)
+            tune.step(4)
+            table[f"{threads}x{rows}"] = tune.step(8) / 8
+        tune.close()
+        best = min(table, key=table.get)
+        threads, rows = (int(x) for x in best.split("x"))
+        b = Batch(len(pinsts), precision=precision)
+        b.set_plan(threads, rows)
+        slots = [b.add(cfg, prims, max_steps=args.batch_steps) for cfg, prims in pinsts]
+        ms = b.step(args.batch_steps)
+        n_run, _ = b.running()
+        qs = [b.query(s) for s in slots]
+        failed = sum(1 for q in qs if q["error_code"])
+        updates_done = sum(q["iteration"] * c.ni * c.nj for q, (c, _) in zip(qs, pinsts))
+        value = updates_done / (ms / 1e3)
+        # algorithmic bytes per cell-update, SSP-RK2: FP32 mixed 32 + 112, FP64 layout 64 + 96
+        bytes_per_update = 144 if precision == "mixed" else 160
+        ok = [i for i, q in enumerate(qs) if q["error_code"] == 0]
+        k = min(args.batch_ref, len(ok))
+        pick = sorted(pick_rng.choice(ok, size=k, replace=False).tolist()) if k else []
+        fp64_reference(pick)
+        errs = []
+        for i in pick:
+            ec, a = ref_states[i]
+            if ec:
+                continue
+            g = insts[i][0].ghost_layers()
+            a = a[g:-g, g:-g]
+            m = b.state(slots[i])["rho"][g:-g, g:-g]
+            errs.append(float(np.abs(m - a).sum() / np.abs(a).sum()))
+        b.close()
+        out[precision] = {
+            "value": value, "unit": "cell-updates/s", "device_ms": ms, "still_running": n_run,
+            "ended_with_error": failed, "cell_updates": updates_done,
+            "plan": {"threads": threads, "rows_per_cta": rows, "tuning_ms_per_step": table},
+            "roofline": {"bound": "hbm", "achieved": value * bytes_per_update / 1e9,
+                         "unit": "GB/s", "algorithmic_bytes_per_cell_update": bytes_per_update},
+            "rel_l1_density_error_vs_fp64": {"max": max(errs, default=None),
+                                             "mean": sum(errs) / len(errs) if errs else None,
+                                             "instances": len(errs)},
+        }
+    out.update({
+        "instances": len(insts), "cells": cells, "steps_each": args.batch_steps,
+        "launches_per_step": 4,
         "scheme": "SLAU, MLP5 (3 ghost layers), SSP-RK2, CFL 0.5, zero-gradient BCs",
-    }
+        "precisions": {"mixed": "FP32 reconstruction/flux, FP64 state",
+                       "mixed_df": "double-float (FP32 pairs) reconstruction/flux, FP64 state"},
+    })
+    return out
 
 
 def bench_serving(args):
@@ -390,7 +411,7 @@ def bench_serving(args):
     from fvleg_2d_gb300.serve import Server, make_requests
 
     out = {}
-    for precision in ("mixed", "fp64"):
+    for precision in ("mixed", "mixed_df", "fp64"):
         reqs = make_requests(args.serve_n, rate=args.serve_rate, seed=args.serve_seed,
                              side=(args.serve_min_side, args.serve_max_side), precision=precision)
         srv = Server(precision=precision, budget_gb=120.0, capacity=1024, chunk_steps=16)
@@ -418,10 +439,12 @@ def main() -> int:
     ap.add_argument("--batch-steps", type=int, default=500)
     ap.add_argument("--batch-seed", type=int, default=2024)
     ap.add_argument("--batch-ref", type=int, default=8)
+    ap.add_argument("--batch-precisions", default="mixed,mixed_df")
     ap.add_argument("--no-kh", action="store_true")
     ap.add_argument("--kh-n", type=int, default=8192)
     ap.add_argument("--kh-steps", type=int, default=200)
     ap.add_argument("--kh-fp64-steps", type=int, default=5)
+    ap.add_argument("--kh-df-steps", type=int, default=20)
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serve-n", type=int, default=100)
     ap.add_argument("--serve-rate", type=float, default=100.0)
@@ -440,6 +463,7 @@ def main() -> int:
     peak, peak_kind = measured_peaks()
     fp64, cfg, prims = bench_precision(args, "fp64", dist, world, peak)
     mixed, _, _ = bench_precision(args, "mixed", dist, world, peak)
+    mixed_df, _, _ = bench_precision(args, "mixed_df", dist, world, peak)
     e2e = bench_e2e(args, cfg, prims)
     e2e_all = allreduce_max(dist, -e2e["value"])  # slowest replica
     e2e["value"] = -e2e_all * world
@@ -483,6 +507,15 @@ def main() -> int:
             "ms_per_step": mixed["ms_per_step"], "speedup_vs_fp64": mixed["value"] / fp64["value"],
             "roofline": mixed["roofline"], "stage_ms_per_step": mixed["stage_ms_per_step"],
             "gpu_launches": mixed["launches_per_step"] * args.steps, "clocks": mixed["clocks"],
+        },
+        "mixed_df": {
+            "value": mixed_df["value"], "unit": "cell-updates/s",
+            "dtype": "double-float (FP32 pairs) flux / f64 state",
+            "ms_per_step": mixed_df["ms_per_step"],
+            "speedup_vs_fp64": mixed_df["value"] / fp64["value"],
+            "roofline": mixed_df["roofline"], "stage_ms_per_step": mixed_df["stage_ms_per_step"],
+            "gpu_launches": mixed_df["launches_per_step"] * args.steps,
+            "clocks": mixed_df["clocks"],
         },
         "kelvin_helmholtz": kh,
         "batched": batched,

@@ -1,9 +1,11 @@
 """Build the sm_103a C-ABI library ``libcato_gpu.so`` in-tree (``fvleg_2d_gb300/_lib/``).
 
 The stage kernel family is instantiated once per (precision, flux) pair from ``stage_inst.cu``
-so the 16 translation units compile in parallel; the FP64 units and the helper kernels are built
-with ``--fmad=false`` (each reference operation rounds on its own), the mixed-precision units with
-FMA contraction enabled.  No CMake, no torch: nvcc and a C++ host compiler only.
+so the 24 translation units compile in parallel; the FP64 units and the helper kernels are built
+with ``--fmad=false`` (each reference operation rounds on its own), the FP32 mixed units with
+FMA contraction, fast square root and flush-to-zero, the double-float units with FMA contraction
+and IEEE FP32 semantics (their pair arithmetic is written with explicitly rounded intrinsics).
+No CMake, no torch: nvcc and a C++ host compiler only.
 """
 from __future__ import annotations
 
@@ -48,7 +50,8 @@ def _units() -> list[tuple[str, list[str]]]:
               "-I", INCLUDE]
     units = []
     for real, flags in (("double", ["--fmad=false"]),
-                        ("float", ["--fmad=true", "-prec-sqrt=false", "-ftz=true"])):
+                        ("float", ["--fmad=true", "-prec-sqrt=false", "-ftz=true"]),
+                        ("df", ["--fmad=true"])):
         for flux in range(N_FLUX):
             obj = os.path.join(BUILD_DIR, f"stage_{real}_{flux}.o")
             cmd = [nvcc(), *ARCH, *common, *flags, f"-DCATO_REAL={real}",

@@ -36,7 +36,7 @@ RK_IDS = {
     "rk(2,5)": 7,
 }
 BC_IDS = {"zero_gradient": 0, "symmetry": 1, "periodic": 2}
-PRECISION_IDS = {"fp64": 0, "mixed": 1}
+PRECISION_IDS = {"fp64": 0, "mixed": 1, "mixed_df": 2}
 # side order of cato_config.bc: the reference's application order (flux_solver.f90:165-183)
 SIDES = ("+x", "+y", "-x", "-y")
 

@@ -51,9 +51,16 @@ __global__ void batch_step_end(InstDesc* descs, int n) {
   if (i >= n) return;
   InstDesc& d = descs[i];
   if (d.in_use && d.ctl.active) {
-    if (d.prec == 1) d.cur = 1 - d.cur;
+    if (d.prec == 1) d.cur = 1 - d.cur;  // the mixed path writes U^{n+1} to the other buffer
     d.raw_pending = 0;
   }
+}
+
+cudaError_t launch_batch_prec(int prec, int flux, int recon, int threads, cudaStream_t s,
+                              const BatchStageArgs& B) {
+  if (prec == CATO_FP64) return launch_batch<double>(flux, recon, threads, s, B);
+  if (prec == CATO_MIXED_DF) return launch_batch<df>(flux, recon, threads, s, B);
+  return launch_batch<float>(flux, recon, threads, s, B);
 }
 
 struct StageSpec {
@@ -193,10 +200,7 @@ static int rebuild(cato_batch* b) {
   for (const auto& g : b->groups) {
     BatchStageArgs B;
     std::memset(&B, 0, sizeof(B));
-    cudaError_t e = b->prec == CATO_FP64
-                        ? launch_batch<double>(g.flux, g.recon, b->threads, b->stream, B)
-                        : launch_batch<float>(g.flux, g.recon, b->threads, b->stream, B);
-    BK(e);
+    BK(launch_batch_prec(b->prec, g.flux, g.recon, b->threads, b->stream, B));
   }
   BK(cudaStreamSynchronize(b->stream));
   drop_graph(b);
@@ -224,10 +228,7 @@ static int enqueue_batch_step(cato_batch* b) {
       B.a = b->stages[k].a;
       B.b = b->stages[k].b;
       B.coef = b->stages[k].coef;
-      cudaError_t e = b->prec == CATO_FP64
-                          ? launch_batch<double>(G.flux, G.recon, b->threads, b->stream, B)
-                          : launch_batch<float>(G.flux, G.recon, b->threads, b->stream, B);
-      BK(e);
+      BK(launch_batch_prec(b->prec, G.flux, G.recon, b->threads, b->stream, B));
     }
   }
   batch_step_end<<<(b->capacity + 127) / 128, 128, 0, b->stream>>>(b->d_descs, b->capacity);
@@ -241,13 +242,15 @@ int cato_batch_instance_bytes(const cato_config* cfg, uint64_t* bytes) {
   if (!cfg || !bytes) return CATO_ERR_ARG;
   const size_t pitch = (size_t)(cfg->ni + 31) / 32 * 32;
   const size_t cells = pitch * (size_t)cfg->nj;
-  *bytes = cfg->precision == CATO_FP64 ? cells * 8 * 12 : cells * (8 * 8 + 16 * 4);
+  // FP64 and mixed_df: U + two stage buffers; mixed: two U + two FP32 copies + two increments
+  *bytes = cfg->precision != CATO_MIXED ? cells * 8 * 12 : cells * (8 * 8 + 16 * 4);
   return CATO_OK;
 }
 
 int cato_batch_create(int32_t capacity, int32_t precision, int32_t rk, cato_batch** out) {
   if (!out || capacity < 1) return CATO_ERR_ARG;
-  if (precision != CATO_FP64 && precision != CATO_MIXED) return CATO_ERR_CONFIG;
+  if (precision != CATO_FP64 && precision != CATO_MIXED && precision != CATO_MIXED_DF)
+    return CATO_ERR_CONFIG;
   if (rk < CATO_RK_SSP2 || rk > CATO_RK_2_5) return CATO_ERR_CONFIG;
   *out = nullptr;
   cato_batch* b = new cato_batch();
@@ -338,19 +341,8 @@ int cato_batch_add(cato_batch* b, const cato_config* cfg, const double* rho, con
   d.K64.ausm_sigma = cfg->ausm_sigma;
   d.K64.low_mach_fix = cfg->apply_low_mach_fix ? 1 : 0;
   d.K64.harten = cfg->roe_entropy_fix == CATO_ROE_HARTEN ? 1 : 0;
-  d.K32.gamma = (float)d.K64.gamma;
-  d.K32.g_over_gm1 = (float)d.K64.g_over_gm1;
-  d.K32.gm1 = (float)d.K64.gm1;
-  d.K32.two_gm1_over_gp1 = (float)d.K64.two_gm1_over_gp1;
-  d.K32.gamma_factor = (float)d.K64.gamma_factor;
-  d.K32.hllc_gf = (float)d.K64.hllc_gf;
-  d.K32.harten_delta = (float)d.K64.harten_delta;
-  d.K32.ausm_beta = (float)d.K64.ausm_beta;
-  d.K32.ausm_kp = (float)d.K64.ausm_kp;
-  d.K32.ausm_ku = (float)d.K64.ausm_ku;
-  d.K32.ausm_sigma = (float)d.K64.ausm_sigma;
-  d.K32.low_mach_fix = d.K64.low_mach_fix;
-  d.K32.harten = d.K64.harten;
+  d.K32 = convert_consts<float>(d.K64);
+  d.Kdf = convert_consts<df>(d.K64);
   d.G.vol = (cfg->dx - 0.0) * (cfg->dy - 0.0) - (0.0 - 0.0) * (0.0 - 0.0);
   double l[4] = {cfg->dx, cfg->dy, cfg->dx, cfg->dy};
   double mx = l[0], mn = l[0];
@@ -363,7 +355,7 @@ int cato_batch_add(cato_batch* b, const cato_config* cfg, const double* rho, con
   bool ok = true;
   for (int k = 0; k < 4 && ok; ++k) {
     ok = cudaMalloc(&d.U[0][k], fb) == cudaSuccess;
-    if (ok && d.prec == CATO_FP64) {
+    if (ok && d.prec != CATO_MIXED) {
       ok = cudaMalloc(&d.S[0][k], fb) == cudaSuccess && cudaMalloc(&d.S[1][k], fb) == cudaSuccess;
       d.prim_raw[k] = d.S[1][k];
     } else if (ok) {
@@ -514,7 +506,7 @@ int cato_batch_download(cato_batch* b, int32_t slot, double* rho, double* rho_u,
   BK(cudaStreamSynchronize(b->stream));
   const InstDesc& d = b->h_pinned[slot];
   if (ld < d.ni + 2 * d.ng) return CATO_ERR_ARG;
-  double* const* U = d.prec == CATO_FP64 ? d.U[0] : d.U[d.cur];
+  double* const* U = d.prec != CATO_MIXED ? d.U[0] : d.U[d.cur];
   double* out[4] = {rho, rho_u, rho_v, rho_E};
   for (int k = 0; k < 4; ++k) {
     if (!out[k]) continue;

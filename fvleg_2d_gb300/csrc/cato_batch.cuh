@@ -17,12 +17,13 @@ struct InstDesc {
   int limiter, rows_per_cta, flux, recon;
   int cur;                 // mixed: which U buffer holds U^n
   int raw_pending;         // the first stage uses the uploaded primitives as is
-  int prec;                // 0 FP64, 1 mixed
+  int prec;                // 0 FP64, 1 mixed, 2 mixed_df (FP64 layout)
   int in_use;
   double gamma, cfl;
   Geom G;
   FluxConsts<double> K64;
   FluxConsts<float> K32;
+  FluxConsts<df> Kdf;
   double* U[2][4];
   double* S[2][4];
   float4* D[2];
@@ -64,7 +65,7 @@ __device__ __forceinline__ void batch_stage_args(InstDesc* d, const BatchStageAr
   A.cfl = d->cfl;
   A.G = d->G;
   const bool raw = (B.stage == 0) && d->raw_pending;
-  if constexpr (sizeof(R) == 8) {
+  if constexpr (Prec<R>::kind != 1) {
     double* const* prev = (B.stage == 0) ? d->U[0] : d->S[(B.stage - 1) & 1];
     double* const* out = B.last ? d->U[0] : d->S[B.stage & 1];
 #pragma unroll
@@ -111,10 +112,12 @@ __global__ void __launch_bounds__(256) batch_stage_kernel(const BatchStageArgs B
     StageArgs A;
     batch_stage_args<R>(d, B, A);
     A.rows_per_cta = w.w;
-    if constexpr (sizeof(R) == 8)
+    if constexpr (Prec<R>::kind == 0)
       stage_tile<R, NG, FLUX, RECON>(A, d->K64, w.y, w.z, smem_raw);
-    else
+    else if constexpr (Prec<R>::kind == 1)
       stage_tile<R, NG, FLUX, RECON>(A, d->K32, w.y, w.z, smem_raw);
+    else
+      stage_tile<R, NG, FLUX, RECON>(A, d->Kdf, w.y, w.z, smem_raw);
   }
 }
 

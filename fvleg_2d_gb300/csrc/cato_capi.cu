@@ -7,6 +7,8 @@
 //   mixed path: U^n double-buffered (2 x 4 x f64) with FP32 copies (2 x float4 per cell) and
 //               stage increments delta (2 x float4 per cell): U^k = U^n + delta_k,
 //               delta_{k+1} = b delta_k + c L(U^k), U^{n+1} = U^n + delta in FP64.
+//   mixed_df  : the FP64 layout; reconstruction, flux and divergence in double-float (pairs of
+//               FP32) and the stage combine in FP64.
 // The primitives of an upload are kept (in a buffer not needed before the first step) because
 // the first stage after an upload uses them as is, like the reference after initialize.
 #include <cstdio>
@@ -61,6 +63,7 @@ struct cato_handle {
   Plan plan;
   FluxConsts<double> K64{};
   FluxConsts<float> K32{};
+  FluxConsts<df> Kdf{};
   Geom G{};
   std::vector<Stage> stages;
   std::string err;
@@ -141,21 +144,8 @@ static void fill_consts(cato_handle* h) {
   K.low_mach_fix = c.apply_low_mach_fix ? 1 : 0;
   K.harten = c.roe_entropy_fix == CATO_ROE_HARTEN ? 1 : 0;
   h->K64 = K;
-  FluxConsts<float> F{};
-  F.gamma = (float)K.gamma;
-  F.g_over_gm1 = (float)K.g_over_gm1;
-  F.gm1 = (float)K.gm1;
-  F.two_gm1_over_gp1 = (float)K.two_gm1_over_gp1;
-  F.gamma_factor = (float)K.gamma_factor;
-  F.hllc_gf = (float)K.hllc_gf;
-  F.harten_delta = (float)K.harten_delta;
-  F.ausm_beta = (float)K.ausm_beta;
-  F.ausm_kp = (float)K.ausm_kp;
-  F.ausm_ku = (float)K.ausm_ku;
-  F.ausm_sigma = (float)K.ausm_sigma;
-  F.low_mach_fix = K.low_mach_fix;
-  F.harten = K.harten;
-  h->K32 = F;
+  h->K32 = convert_consts<float>(K);
+  h->Kdf = convert_consts<df>(K);
   // quad_cell_t metrics of a dx x dy axis-aligned cell (quad_cell.f90:69-229): volume dx*dy,
   // edge lengths dx, dy, dx, dy (all set to the largest when they differ by < 2 eps),
   // min_dx = dx, min_dy = dy.
@@ -209,6 +199,8 @@ static cudaError_t launch(cato_handle* h, const StageArgs& A) {
   const int recon = recon_of(h->cfg.limiter);
   if (h->cfg.precision == CATO_FP64)
     return launch_stage<double>(h->cfg.flux, recon, grid, T, h->stream, A, h->K64);
+  if (h->cfg.precision == CATO_MIXED_DF)
+    return launch_stage<df>(h->cfg.flux, recon, grid, T, h->stream, A, h->Kdf);
   return launch_stage<float>(h->cfg.flux, recon, grid, T, h->stream, A, h->K32);
 }
 
@@ -218,7 +210,7 @@ static int enqueue_step(cato_handle* h) {
   CK(cudaGetLastError());
   if (h->event_hook) CK(cudaEventRecord(h->event_hook[1], h->stream));
   const int ns = (int)h->stages.size();
-  const bool fp64 = h->cfg.precision == CATO_FP64;
+  const bool fp64 = h->cfg.precision != CATO_MIXED;  // FP64 stage-buffer layout
   for (int k = 0; k < ns; ++k) {
     const Stage& st = h->stages[k];
     StageArgs A = base_args(h);
@@ -371,7 +363,8 @@ int cato_config_check(const cato_config* c) {
     return CATO_ERR_CONFIG;
   if (!(c->gamma > 1.0) || !(c->cfl > 0.0) || !(c->dx > 0.0) || !(c->dy > 0.0))
     return CATO_ERR_CONFIG;
-  if (c->precision != CATO_FP64 && c->precision != CATO_MIXED) return CATO_ERR_CONFIG;
+  if (c->precision != CATO_FP64 && c->precision != CATO_MIXED && c->precision != CATO_MIXED_DF)
+    return CATO_ERR_CONFIG;
   if (c->roe_entropy_fix != CATO_ROE_REFERENCE && c->roe_entropy_fix != CATO_ROE_HARTEN)
     return CATO_ERR_CONFIG;
   if ((long long)c->ni > (1LL << 30) || (long long)c->nj > (1LL << 30)) return CATO_ERR_CONFIG;
@@ -401,7 +394,7 @@ int cato_gpu_create(const cato_config* cfg, cato_handle** out) {
   if (e != cudaSuccess) { delete h; return CATO_ERR_CUDA; }
   h->own_stream = true;
   const size_t fb = h->field_elems * sizeof(double);
-  const bool fp64 = cfg->precision == CATO_FP64;
+  const bool fp64 = cfg->precision != CATO_MIXED;  // FP64 stage-buffer layout
   auto dalloc = [&](void** p, size_t bytes) -> bool {
     cudaError_t ee = cudaMalloc(p, bytes);
     if (ee != cudaSuccess) { (void)cudaGetLastError(); return false; }
@@ -434,10 +427,13 @@ int cato_gpu_create(const cato_config* cfg, cato_handle** out) {
     return cleanup(CATO_ERR_CUDA);
   // prepare the kernel's shared-memory attribute outside any stream capture
   StageArgs A = base_args(h);
-  cudaError_t ee = fp64 ? launch_stage<double>(cfg->flux, recon_of(cfg->limiter), dim3(0, 0), 64,
-                                               h->stream, A, h->K64)
-                        : launch_stage<float>(cfg->flux, recon_of(cfg->limiter), dim3(0, 0), 64,
-                                              h->stream, A, h->K32);
+  const int rc0 = recon_of(cfg->limiter);
+  cudaError_t ee =
+      cfg->precision == CATO_FP64
+          ? launch_stage<double>(cfg->flux, rc0, dim3(0, 0), 64, h->stream, A, h->K64)
+      : cfg->precision == CATO_MIXED_DF
+          ? launch_stage<df>(cfg->flux, rc0, dim3(0, 0), 64, h->stream, A, h->Kdf)
+          : launch_stage<float>(cfg->flux, rc0, dim3(0, 0), 64, h->stream, A, h->K32);
   if (ee != cudaSuccess) return cleanup(CATO_ERR_CUDA);
   *out = h;
   return CATO_OK;
@@ -603,7 +599,7 @@ int cato_gpu_download(cato_handle* h, double* rho, double* rho_u, double* rho_v,
   if (!h) return CATO_ERR_ARG;
   if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
   if (ld < h->ni + 2 * h->ng) return fail(h, CATO_ERR_ARG, "leading dimension too small");
-  double** Un = h->U[h->cfg.precision == CATO_FP64 ? 0 : h->cur];
+  double** Un = h->U[h->cfg.precision != CATO_MIXED ? 0 : h->cur];
   double* cons_out[4] = {rho, rho_u, rho_v, rho_E};
   double* der_out[4] = {u, v, p, cs};
   int rc;
@@ -874,7 +870,7 @@ static int reduce(cato_handle* h, RedArgs R, double out[RED_Q]) {
 
 // U^n of the handle: FP64 U[0]; mixed U[cur]
 static double* const* state_now(cato_handle* h) {
-  return h->cfg.precision == CATO_FP64 ? h->U[0] : h->U[h->cur];
+  return h->cfg.precision != CATO_MIXED ? h->U[0] : h->U[h->cur];
 }
 
 int cato_gpu_conservation_sums(cato_handle* h, double totals[4]) {
@@ -898,11 +894,11 @@ int cato_gpu_convergence(cato_handle* h, double l2[4]) {
   const bool ssp = rk == CATO_RK_SSP2 || rk == CATO_RK_SSP3;
   RedArgs R{};
   R.mode = 1;
-  if (h->cfg.precision == CATO_FP64) {
+  if (h->cfg.precision != CATO_MIXED) {
     // SSP: the first stage's output U_1 is still in S0; rk(m,n) compares with U^n, which the
     // last stage overwrote in place
     if (!ssp)
-      return fail(h, CATO_ERR_STATE, "FP64 rk(m,n) steps update U^n in place: no U_0 to compare");
+      return fail(h, CATO_ERR_STATE, "rk(m,n) steps update U^n in place: no U_0 to compare");
     for (int k = 0; k < 4; ++k) {
       R.A[k] = h->S[0][k];
       R.B[k] = h->U[0][k];

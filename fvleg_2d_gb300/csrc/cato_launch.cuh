@@ -93,6 +93,9 @@ CATO_DECLARE_STAGE(double, 6) CATO_DECLARE_STAGE(double, 7)
 CATO_DECLARE_STAGE(float, 0) CATO_DECLARE_STAGE(float, 1) CATO_DECLARE_STAGE(float, 2)
 CATO_DECLARE_STAGE(float, 3) CATO_DECLARE_STAGE(float, 4) CATO_DECLARE_STAGE(float, 5)
 CATO_DECLARE_STAGE(float, 6) CATO_DECLARE_STAGE(float, 7)
+CATO_DECLARE_STAGE(df, 0) CATO_DECLARE_STAGE(df, 1) CATO_DECLARE_STAGE(df, 2)
+CATO_DECLARE_STAGE(df, 3) CATO_DECLARE_STAGE(df, 4) CATO_DECLARE_STAGE(df, 5)
+CATO_DECLARE_STAGE(df, 6) CATO_DECLARE_STAGE(df, 7)
 #undef CATO_DECLARE_STAGE
 
 template <typename R>

@@ -6,6 +6,8 @@
 // which makes the results bit-identical to the CPU restatement of the reference.
 // R = float: the mixed path's reconstruction and flux arithmetic (fast reciprocal division
 // and square root); state accumulation stays FP64 in the stage kernel.
+// R = df (cato_df.cuh): the mixed_df path, the same arithmetic in double-float pairs on the
+// FP32 pipe (~44-bit precision); state accumulation stays FP64.
 //
 // Reference citations are file:line in smillerc/fvleg_2d.
 #pragma once
@@ -13,6 +15,8 @@
 #include <cstdint>
 #include <cfloat>
 #include <cuda_runtime.h>
+
+#include "cato_df.cuh"
 
 namespace cato {
 
@@ -41,6 +45,13 @@ template <> struct Num<float> {
   static __device__ __forceinline__ float sqrt(float a) { return ::sqrtf(a); }
 };
 
+template <> struct Num<df> {
+  static constexpr df eps = df(2.220446049250313080847263336181640625e-16f, 0.0f);
+  static constexpr df tiny = df(FLT_MIN, 0.0f);
+  static __device__ __forceinline__ df div(df a, df b) { return df_div(a, b); }
+  static __device__ __forceinline__ df sqrt(df a) { return df_sqrt(a); }
+};
+
 // FP64: the reference's MAX/MIN as compare-and-select (identical signed-zero behaviour to the
 // CPU restatement).  FP32 (mixed path): single-instruction min/max.
 template <typename R> __device__ __forceinline__ R rmax(R a, R b) { return (a < b) ? b : a; }
@@ -48,8 +59,12 @@ template <typename R> __device__ __forceinline__ R rmin(R a, R b) { return (b < 
 template <> __device__ __forceinline__ float rmax<float>(float a, float b) { return fmaxf(a, b); }
 template <> __device__ __forceinline__ float rmin<float>(float a, float b) { return fminf(a, b); }
 template <typename R> __device__ __forceinline__ R rabs(R a) { return fabs(a); }
+template <> __device__ __forceinline__ df rabs<df>(df a) { return df_abs(a); }
 // Fortran SIGN(1.0, x)
 template <typename R> __device__ __forceinline__ R fsign1(R x) { return signbit(x) ? R(-1) : R(1); }
+template <> __device__ __forceinline__ df fsign1<df>(df x) {
+  return signbit(x.hi) ? df(-1.0f) : df(1.0f);
+}
 
 // |x| < c for c > 0 without an FP compare: bit patterns of non-negative IEEE values order like
 // unsigned integers and NaN compares false, as the reference's ABS(x) < c does.
@@ -58,6 +73,7 @@ __device__ __forceinline__ bool abs_lt(double x, double c) {
   return bx < (unsigned long long)__double_as_longlong(c);
 }
 __device__ __forceinline__ bool abs_lt(float x, float c) { return fabsf(x) < c; }
+__device__ __forceinline__ bool abs_lt(df x, df c) { return df_abs(x) < c; }
 
 // ---------------------------------------------------------------------------------------------
 // FP64 <-> FP32 conversion on the integer pipe (GB300's F2F shares the narrow FP64 pipe).
@@ -87,6 +103,14 @@ __device__ __forceinline__ double f2d_int(float f) {
   else hi = sign | ((e + 896u) << 20) | (m >> 3);
   return __hiloint2double((int)hi, (int)lo);
 }
+
+// FP64 <-> df: hi = the FP64 value rounded to FP32, lo = the (exact) remainder rounded to FP32;
+// one FP64 add, the conversions on the integer pipe.
+__device__ __forceinline__ df to_df(double d) {
+  const float h = d2f_int(d);
+  return df(h, d2f_int(d - f2d_int(h)));
+}
+__device__ __forceinline__ double from_df(df a) { return f2d_int(a.hi) + f2d_int(a.lo); }
 
 // ---------------------------------------------------------------------------------------------
 // Primitive recovery
@@ -126,6 +150,20 @@ __device__ __forceinline__ void prim_from_cons(float g, float g1, float r, float
   cs = sqrtf(g * p * ir);
   if (fabsf(v) < 1e-13f * cs) v = 0.0f;
   if (fabsf(u) < 1e-13f * cs) u = 0.0f;
+}
+
+// df (mixed_df path): as the FP32 variant, in double-float; the Mach filter compares against an
+// FP32 sound speed (it only decides whether a velocity below 1e-13 c is set to zero).
+__device__ __forceinline__ void prim_from_cons(df g, df g1, df r, df ru, df rv, df rE, df& u,
+                                               df& v, df& p, df& cs, bool want_cs) {
+  const df ir = df_div(df(1.0f), r);
+  u = ru * ir;
+  v = rv * ir;
+  p = g1 * (rE - df(0.5f) * r * (u * u + v * v));
+  const float csf = sqrtf(fmaxf(g.hi * p.hi * ir.hi, 0.0f));
+  if (want_cs) cs = df_sqrt(g * p * ir);
+  if (fabsf(v.hi) < 1e-13f * csf) v = df(0.0f);
+  if (fabsf(u.hi) < 1e-13f * csf) u = df(0.0f);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -209,6 +247,25 @@ template <typename R> struct FluxConsts {
   R ausm_beta, ausm_kp, ausm_ku, ausm_sigma;
   int low_mach_fix, harten;
 };
+
+// The FP64 constants carried to another compute type (host side).
+template <typename R> inline FluxConsts<R> convert_consts(const FluxConsts<double>& K) {
+  FluxConsts<R> C{};
+  C.gamma = R(K.gamma);
+  C.g_over_gm1 = R(K.g_over_gm1);
+  C.gm1 = R(K.gm1);
+  C.two_gm1_over_gp1 = R(K.two_gm1_over_gp1);
+  C.gamma_factor = R(K.gamma_factor);
+  C.hllc_gf = R(K.hllc_gf);
+  C.harten_delta = R(K.harten_delta);
+  C.ausm_beta = R(K.ausm_beta);
+  C.ausm_kp = R(K.ausm_kp);
+  C.ausm_ku = R(K.ausm_ku);
+  C.ausm_sigma = R(K.ausm_sigma);
+  C.low_mach_fix = K.low_mach_fix;
+  C.harten = K.harten;
+  return C;
+}
 
 template <typename R> struct Prim { R r, u, v, p; };
 

@@ -20,6 +20,16 @@
 
 namespace cato {
 
+// How a compute type keeps and reads the state.
+//   0 FP64    : structure-of-arrays FP64 state, stage buffers FP64 (bit-exact drop-in path)
+//   1 FP32    : stencil from an FP32 copy of U^n plus FP32 stage increments (mixed)
+//   2 df      : the FP64 layout (FP64 stage states, no FP32 rounding between stages) with the
+//               reconstruction, flux and divergence in double-float (mixed_df)
+template <typename R> struct Prec;
+template <> struct Prec<double> { static constexpr int kind = 0; };
+template <> struct Prec<float> { static constexpr int kind = 1; };
+template <> struct Prec<df> { static constexpr int kind = 2; };
+
 struct StageArgs {
   int ni, nj, pitch;       // interior cells, row pitch (cells) of the state arrays
   int bc[4];               // by side: +x, +y, -x, -y
@@ -164,6 +174,10 @@ template <> struct RowSrc<float> {
   float4 d;     // delta_k
   bool flipy;
 };
+template <> struct RowSrc<df> {
+  double c[4];  // conserved state of the stage (or the raw primitives)
+  bool flipy;
+};
 
 template <typename R>
 __device__ __forceinline__ void load_src(const StageArgs& A, int sx, int row, RowSrc<R>& s) {
@@ -171,7 +185,7 @@ __device__ __forceinline__ void load_src(const StageArgs& A, int sx, int row, Ro
   const int sy = map_index(row, A.nj, A.bc[SIDE_MY], A.bc[SIDE_PY], fy);
   s.flipy = fy;
   const size_t idx = (size_t)sy * A.pitch + sx;
-  if constexpr (sizeof(R) == 8) {
+  if constexpr (Prec<R>::kind != 1) {
     const double* const* src = A.Pin[0] ? A.Pin : A.Uk;
 #pragma unroll
     for (int k = 0; k < 4; ++k) s.c[k] = __ldg(src[k] + idx);
@@ -190,13 +204,21 @@ template <typename R>
 __device__ __forceinline__ void src_to_prim(const StageArgs& A, const RowSrc<R>& s, bool flipx,
                                             R g, R g1, R out[4]) {
   R r, u, v, p;
-  if constexpr (sizeof(R) == 8) {
+  if constexpr (Prec<R>::kind == 0) {
     if (A.Pin[0]) {
       r = s.c[0]; u = s.c[1]; v = s.c[2]; p = s.c[3];
     } else {
       R cs;
       r = s.c[0];
       prim_from_cons(g, g1, r, s.c[1], s.c[2], s.c[3], u, v, p, cs);
+    }
+  } else if constexpr (Prec<R>::kind == 2) {
+    if (A.Pin[0]) {
+      r = to_df(s.c[0]); u = to_df(s.c[1]); v = to_df(s.c[2]); p = to_df(s.c[3]);
+    } else {
+      R cs;
+      r = to_df(s.c[0]);
+      prim_from_cons(g, g1, r, to_df(s.c[1]), to_df(s.c[2]), to_df(s.c[3]), u, v, p, cs, false);
     }
   } else {
     if (A.Pin[0]) {
@@ -242,6 +264,13 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
   const double dt = *A.dt;
   const double cc = A.coef * dt;
   const R* rp[6];
+  // mixed_df constants of the update (unused by the other paths)
+  [[maybe_unused]] df dx_inv, dy_inv, cfl_df;
+  if constexpr (Prec<R>::kind == 2) {
+    dx_inv = to_df(1.0 / A.G.dx);
+    dy_inv = to_df(1.0 / A.G.dy);
+    cfl_df = to_df(A.cfl);
+  }
 
   // prologue: rows y0-NG .. y0+NG-1
   for (int r = y0 - NG; r < y0 + NG; ++r) {
@@ -275,7 +304,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
     double ua[4], uk[4];
     float4 dkc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (in_cell) {
-      if constexpr (sizeof(R) == 8) {
+      if constexpr (Prec<R>::kind != 1) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           ua[k] = A.Ua[k] ? A.Ua[k][cidx] : 0.0;  // may alias Uo: plain load, read before write
@@ -316,13 +345,17 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
     __syncthreads();
     if (in_cell) {
       double un[4];
-      if constexpr (sizeof(R) == 8) {
+      if constexpr (Prec<R>::kind != 1) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          double Fi = sfi[k * T + t], Fim = sfi[k * T + t - 1];
-          double Fj = sfj[((j & 1) * 4 + k) * T + t];
-          double Fjm = sfj[(((j - 1) & 1) * 4 + k) * T + t];
-          double L = divergence_fp64(Fi, Fim, Fj, Fjm, A.G);
+          const R Fi = sfi[k * T + t], Fim = sfi[k * T + t - 1];
+          const R Fj = sfj[((j & 1) * 4 + k) * T + t];
+          const R Fjm = sfj[(((j - 1) & 1) * 4 + k) * T + t];
+          double L;
+          if constexpr (Prec<R>::kind == 0)
+            L = divergence_fp64(Fi, Fim, Fj, Fjm, A.G);
+          else  // double-float flux differences, the result carried to FP64
+            L = from_df(-((Fi - Fim) * dx_inv + (Fj - Fjm) * dy_inv));
           double r;
           if (A.kind == 2) {
             r = L;
@@ -362,7 +395,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
       }
       if (A.last) {
         // CFL dt of the new state (get_timestep, mod_fluid.f90:554-558) and the sanity checks
-        if constexpr (sizeof(R) == 8) {
+        if constexpr (Prec<R>::kind == 0) {
           double u, v, p, cs;
           prim_from_cons(A.gamma, A.gamma - 1.0, un[0], un[1], un[2], un[3], u, v, p, cs);
           double d = A.cfl / (((fabs(u) + cs) / A.G.dx) + ((fabs(v) + cs) / A.G.dy));
@@ -370,6 +403,16 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
           if (isnan(un[0]) || isnan(u) || isnan(v) || isnan(p)) st_loc |= ST_NAN;
           if (un[0] < 0.0) st_loc |= ST_NEG_DENSITY;
           if (p < 0.0) st_loc |= ST_NEG_PRESSURE;
+        } else if constexpr (Prec<R>::kind == 2) {
+          df u, v, p, cs;
+          prim_from_cons(g, g1, to_df(un[0]), to_df(un[1]), to_df(un[2]), to_df(un[3]), u, v,
+                         p, cs, true);
+          const df d = df_div(cfl_df, (df_abs(u) + cs) * dx_inv + (df_abs(v) + cs) * dy_inv);
+          const double dd = from_df(d);
+          if (dd > 0.0 && dd < dt_loc) dt_loc = dd;
+          if (isnan(un[0]) || isnan(u.hi) || isnan(v.hi) || isnan(p.hi)) st_loc |= ST_NAN;
+          if (un[0] < 0.0) st_loc |= ST_NEG_DENSITY;
+          if (p.hi < 0.0f) st_loc |= ST_NEG_PRESSURE;
         } else {
           const float4 uf = make_float4(d2f_int(un[0]), d2f_int(un[1]), d2f_int(un[2]),
                                         d2f_int(un[3]));

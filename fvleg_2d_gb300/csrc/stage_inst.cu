@@ -1,10 +1,10 @@
 // One (precision, flux) instantiation of the stage kernel family.  The build compiles this file
-// once per pair with -DCATO_REAL=double|float -DCATO_FLUX=<0..7>; the FP64 objects are built
+// once per pair with -DCATO_REAL=double|float|df -DCATO_FLUX=<0..7>; the FP64 objects are built
 // with --fmad=false so that every reference operation rounds on its own.
 #include "cato_launch.cuh"
 
 #ifndef CATO_REAL
-#error "CATO_REAL must be defined (double or float)"
+#error "CATO_REAL must be defined (double, float or df)"
 #endif
 #ifndef CATO_FLUX
 #error "CATO_FLUX must be defined (0..7)"

@@ -35,7 +35,7 @@ def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("workload", choices=["sod", "quadrant", "kh", "circles"])
     ap.add_argument("--n", type=int, default=1024)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed_df"])
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--seed", type=int, default=0)
     a = ap.parse_args(argv)

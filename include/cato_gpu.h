@@ -83,7 +83,9 @@ enum cato_side { CATO_PLUS_X = 0, CATO_PLUS_Y = 1, CATO_MINUS_X = 2, CATO_MINUS_
 
 enum cato_precision {
   CATO_FP64 = 0,   /* the drop-in path: IEEE FP64 throughout, reference operation order */
-  CATO_MIXED = 1   /* FP32 reconstruction + flux arithmetic, FP64 conserved state and RK update */
+  CATO_MIXED = 1,  /* FP32 reconstruction + flux arithmetic, FP64 conserved state and RK update */
+  CATO_MIXED_DF = 2 /* double-float (pairs of FP32, ~44-bit) reconstruction, flux and divergence
+                       on the FP32 pipe; FP64 conserved and stage states and RK combine */
 };
 
 enum cato_roe_fix {
@@ -171,8 +173,8 @@ int cato_gpu_conservation_sums(cato_handle* h, double totals[4]);
  * the first to the last stage over the interior, divided by the first stage's norm (by
  * max(norm, 1) for rho u and rho v): SSP-RK2 U_1 vs U_2, SSP-RK3 U_1 vs U_3, rk(m,n) U_0 vs
  * U_curr.  Computed on demand from the stage buffers of the last step (no cost per step).
- * CATO_ERR_STATE before the first step after an upload, and for FP64 rk(m,n), whose last stage
- * overwrites U_0 in place. */
+ * CATO_ERR_STATE before the first step after an upload, and for rk(m,n) outside the mixed
+ * path (the last stage overwrites U_0 in place there). */
 int cato_gpu_convergence(cato_handle* h, double l2[4]);
 
 /* flux_solver_t%solve (flux_solver.f90:66-87) on caller-given primitive fields: applies the BCs

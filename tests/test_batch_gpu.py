@@ -23,7 +23,7 @@ def _instances(precision, n=6, seed=5):
     return out
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_df"])
 def test_batch_instances_match_single_handles(cato_lib, precision):
     insts = _instances(precision)
     steps = [7, 12, 3, 20, 9, 15]
@@ -44,7 +44,7 @@ def test_batch_instances_match_single_handles(cato_lib, precision):
             np.testing.assert_array_equal(got[k], ref[k], err_msg=f"slot {slot} {k}")
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_df"])
 def test_alone_equals_in_mix(cato_lib, precision):
     insts = _instances(precision, n=5, seed=9)
     mix = Batch(8, precision=precision)

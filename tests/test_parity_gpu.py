@@ -120,3 +120,43 @@ def test_mixed_sod_density_error(oracle, cato_lib):
     r32 = interior(cfg_m, mx.state(("rho",))["rho"])
     l1 = np.abs(r32 - r64).sum() / np.abs(r64).sum()
     assert l1 <= 1e-6, l1
+
+
+@pytest.mark.parametrize("flux", FLUXES)
+def test_mixed_df_steps_close_to_oracle(oracle, cato_lib, flux):
+    """mixed_df (double-float reconstruction/flux, FP64 state): after 8 CFL steps every
+    conserved variable within 1e-10 relative L1 of the FP64 oracle (each double-float operation
+    carries ~1e-13 relative error)."""
+    limiter = {"SLAU": "MLP5", "SD-SLAU": "MLP3", "Roe": "superbee", "HLLC": "van_leer"}.get(flux, "minmod")
+    bc = ["zg", "zg_sym", "per_sym", "per", "sym_per"][FLUXES.index(flux) % 5]
+    cfg = _cfg(flux, limiter, bc, ni=70, nj=41, integration_strategy="ssp_rk3")
+    prims = random_prims(cfg, np.random.default_rng(13))
+    ref = oracle.OracleFluid(cfg)
+    ref.set_primitive(*prims)
+    cfg_df = _cfg(flux, limiter, bc, ni=70, nj=41, integration_strategy="ssp_rk3",
+                  precision="mixed_df")
+    gpu = Fluid(cfg_df).initialize(*prims)
+    for _ in range(8):
+        assert ref.integrate() == 0
+        gpu.integrate()
+    assert abs(gpu.time - ref.time) <= 1e-12 * ref.time
+    a, b = ref.state(), gpu.state()
+    for k in ("rho", "rho_u", "rho_v", "rho_E"):
+        x, y = interior(cfg, a[k]), interior(cfg, b[k])
+        l1 = np.abs(y - x).sum() / np.abs(x).sum()
+        assert l1 <= 1e-10, (k, l1)
+
+
+def test_mixed_df_sod_density_error(oracle, cato_lib):
+    """mixed_df on the full Sod run: same step count, relative L1 density error <= 1e-10."""
+    cfg, prims = ic.sod()
+    fp = Fluid(cfg).initialize(*prims)
+    n64 = fp.run(0.2)
+    cfg_d, _ = ic.sod(precision="mixed_df")
+    md = Fluid(cfg_d).initialize(*prims)
+    nd = md.run(0.2)
+    assert nd == n64
+    r64 = interior(cfg, fp.state(("rho",))["rho"])
+    rdf = interior(cfg_d, md.state(("rho",))["rho"])
+    l1 = np.abs(rdf - r64).sum() / np.abs(r64).sum()
+    assert l1 <= 1e-10, l1
