@@ -178,61 +178,73 @@ __device__ __forceinline__ R tvd_phi(int lim, R r) {
   return Num<R>::div(r + rabs(r), R(1) + rabs(r)); // "vanleer" (muscl_tvd2.fypp:199-200)
 }
 
+// The limiter's own arithmetic (slope ratios, limiter functions, MLP coefficients) runs in
+// Lim<R>: the compute type itself, except for the double-float path, which takes its slope
+// differences in double-float, rounds them to FP32 for the limiter and adds the limited slope
+// term back in double-float.  The limiter only scales the slope term, so its FP32 rounding moves
+// a face value by ~1e-7 of that term, never of the value itself.
+template <typename R> struct Lim { using type = R; };
+template <> struct Lim<df> { using type = float; };
+template <typename R> __device__ __forceinline__ typename Lim<R>::type lim_of(R x) { return x; }
+template <> __device__ __forceinline__ float lim_of<df>(df x) { return x.hi; }
+
 template <typename R>
 __device__ __forceinline__ void recon_tvd2(int lim, R qm1, R q0, R qp1, R qp2, R& L, R& Rr) {
-  const R EPS = Num<R>::eps;
-  R dm = q0 - qm1, d0 = qp1 - q0, dp = qp2 - qp1;
-  if (abs_lt(dm, EPS)) dm = R(0);
-  if (abs_lt(d0, EPS)) d0 = R(0);
-  if (abs_lt(dp, EPS)) dp = R(0);
+  using T = typename Lim<R>::type;
+  const T EPS = Num<T>::eps;
+  T dm = lim_of(q0 - qm1), d0 = lim_of(qp1 - q0), dp = lim_of(qp2 - qp1);
+  if (abs_lt(dm, EPS)) dm = T(0);
+  if (abs_lt(d0, EPS)) d0 = T(0);
+  if (abs_lt(dp, EPS)) dp = T(0);
   // d0 == 0 gives r = 0 exactly (0/x); skip the division
-  R rL = (d0 == R(0)) ? R(0) * (dm + R(1e-16)) : Num<R>::div(d0, dm + R(1e-16));
-  R rR = (d0 == R(0)) ? R(0) * (dp + R(1e-16)) : Num<R>::div(d0, dp + R(1e-16));
-  R phi = tvd_phi(lim, rL);
-  L = q0 + R(0.5) * phi * dm;
+  T rL = (d0 == T(0)) ? T(0) * (dm + T(1e-16)) : Num<T>::div(d0, dm + T(1e-16));
+  T rR = (d0 == T(0)) ? T(0) * (dp + T(1e-16)) : Num<T>::div(d0, dp + T(1e-16));
+  T phi = tvd_phi(lim, rL);
+  L = q0 + R(T(0.5) * phi * dm);
   phi = tvd_phi(lim, rR);
-  Rr = qp1 - R(0.5) * phi * dp;
+  Rr = qp1 - R(T(0.5) * phi * dp);
 }
 
 template <typename R, int ORDER>
 __device__ __forceinline__ void recon_mlp(R qm2, R qm1, R q0, R qp1, R qp2, R qp3, R t0p, R t0m,
                                           R t1p, R t1m, R& L, R& Rr) {
-  const R EPS = Num<R>::eps;
-  const R S = R(1e-30);  // SMALL_NUM, muscl_mlp.fypp:122
-  R dm = q0 - qm1, d0 = qp1 - q0, dp = qp2 - qp1;
-  if (abs_lt(dm, EPS)) dm = R(0);
-  if (abs_lt(d0, EPS)) d0 = R(0);
-  if (abs_lt(dp, EPS)) dp = R(0);
-  R rR_p1 = Num<R>::div(d0, dp + S);
-  R rL = Num<R>::div(d0, dm + S);
-  R bL, bR;
+  using T = typename Lim<R>::type;
+  const T EPS = Num<T>::eps;
+  const T S = T(1e-30);  // SMALL_NUM, muscl_mlp.fypp:122
+  T dm = lim_of(q0 - qm1), d0 = lim_of(qp1 - q0), dp = lim_of(qp2 - qp1);
+  if (abs_lt(dm, EPS)) dm = T(0);
+  if (abs_lt(d0, EPS)) d0 = T(0);
+  if (abs_lt(dp, EPS)) dp = T(0);
+  T rR_p1 = Num<T>::div(d0, dp + S);
+  T rL = Num<T>::div(d0, dm + S);
+  T bL, bR;
   if (ORDER == 5) {
-    R dm3 = qm1 - qm2, dp5 = qp3 - qp2;
-    if (abs_lt(dm3, EPS)) dm3 = R(0);
-    if (abs_lt(dp5, EPS)) dp5 = R(0);
-    R rL_m1 = Num<R>::div(dm, dm3 + S);
-    R rL_p1 = Num<R>::div(dp, d0 + S);
-    R rR_p2 = Num<R>::div(dp, dp5 + S);
-    R rR = Num<R>::div(dm, d0 + S);
-    bL = Num<R>::div((((Num<R>::div(R(-2), rL_m1 + S)) + R(11)) + R(24) * rL) - R(3) * rL * rL_p1,
-                     R(30));
-    bR = Num<R>::div((((Num<R>::div(R(-2), rR_p2 + S)) + R(11)) + R(24) * rR_p1) -
-                         R(3) * rR_p1 * rR,
-                     R(30));
+    T dm3 = lim_of(qm1 - qm2), dp5 = lim_of(qp3 - qp2);
+    if (abs_lt(dm3, EPS)) dm3 = T(0);
+    if (abs_lt(dp5, EPS)) dp5 = T(0);
+    T rL_m1 = Num<T>::div(dm, dm3 + S);
+    T rL_p1 = Num<T>::div(dp, d0 + S);
+    T rR_p2 = Num<T>::div(dp, dp5 + S);
+    T rR = Num<T>::div(dm, d0 + S);
+    bL = Num<T>::div((((Num<T>::div(T(-2), rL_m1 + S)) + T(11)) + T(24) * rL) - T(3) * rL * rL_p1,
+                     T(30));
+    bR = Num<T>::div((((Num<T>::div(T(-2), rR_p2 + S)) + T(11)) + T(24) * rR_p1) -
+                         T(3) * rR_p1 * rR,
+                     T(30));
   } else {
-    bL = Num<R>::div(R(1) + R(2) * rL, R(3));
-    bR = Num<R>::div(R(1) + R(2) * rR_p1, R(3));
+    bL = Num<T>::div(T(1) + T(2) * rL, T(3));
+    bR = Num<T>::div(T(1) + T(2) * rR_p1, T(3));
   }
-  R tt = Num<R>::div(rabs(t0p - t0m), rabs(qp1 - qm1) + S);
-  R tt1 = Num<R>::div(rabs(t1p - t1m), rabs(qp2 - q0) + S);
-  R aLt = Num<R>::div(R(2) * rmax(R(1), rL) * (R(1) + rmax(R(0), Num<R>::div(tt1, rR_p1 + S))),
-                      R(1) + tt);
-  R aRt = Num<R>::div(R(2) * rmax(R(1), rR_p1) * (R(1) + rmax(R(0), Num<R>::div(tt, rL + S))),
-                      R(1) + tt1);
-  R aL = rmax(R(1), rmin(R(2), aLt));
-  R aR = rmax(R(1), rmin(R(2), aRt));
-  L = q0 + R(0.5) * rmax(R(0), rmin(rmin(aL * rL, aL), bL)) * dm;
-  Rr = qp1 - R(0.5) * rmax(R(0), rmin(rmin(aR * rR_p1, aR), bR)) * dp;
+  T tt = Num<T>::div(rabs(lim_of(t0p - t0m)), rabs(lim_of(qp1 - qm1)) + S);
+  T tt1 = Num<T>::div(rabs(lim_of(t1p - t1m)), rabs(lim_of(qp2 - q0)) + S);
+  T aLt = Num<T>::div(T(2) * rmax(T(1), rL) * (T(1) + rmax(T(0), Num<T>::div(tt1, rR_p1 + S))),
+                      T(1) + tt);
+  T aRt = Num<T>::div(T(2) * rmax(T(1), rR_p1) * (T(1) + rmax(T(0), Num<T>::div(tt, rL + S))),
+                      T(1) + tt1);
+  T aL = rmax(T(1), rmin(T(2), aLt));
+  T aR = rmax(T(1), rmin(T(2), aRt));
+  L = q0 + R(T(0.5) * rmax(T(0), rmin(rmin(aL * rL, aL), bL)) * dm);
+  Rr = qp1 - R(T(0.5) * rmax(T(0), rmin(rmin(aR * rR_p1, aR), bR)) * dp);
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -1186,7 +1186,8 @@ int oracle_config_check(const cato_config* c) {
     return CATO_ERR_CONFIG;
   if (!(c->gamma > 1.0) || !(c->cfl > 0.0) || !(c->dx > 0.0) || !(c->dy > 0.0))
     return CATO_ERR_CONFIG;
-  if (c->precision != CATO_FP64 && c->precision != CATO_MIXED) return CATO_ERR_CONFIG;
+  /* the oracle computes in FP64 whatever the precision asks of the GPU path */
+  if (c->precision < CATO_FP64 || c->precision > CATO_MIXED_DF) return CATO_ERR_CONFIG;
   if (c->roe_entropy_fix != CATO_ROE_REFERENCE && c->roe_entropy_fix != CATO_ROE_HARTEN)
     return CATO_ERR_CONFIG;
   return CATO_OK;
