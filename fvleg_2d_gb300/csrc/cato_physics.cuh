@@ -178,73 +178,169 @@ __device__ __forceinline__ R tvd_phi(int lim, R r) {
   return Num<R>::div(r + rabs(r), R(1) + rabs(r)); // "vanleer" (muscl_tvd2.fypp:199-200)
 }
 
-// The limiter's own arithmetic (slope ratios, limiter functions, MLP coefficients) runs in
-// Lim<R>: the compute type itself, except for the double-float path, which takes its slope
-// differences in double-float, rounds them to FP32 for the limiter and adds the limited slope
-// term back in double-float.  The limiter only scales the slope term, so its FP32 rounding moves
-// a face value by ~1e-7 of that term, never of the value itself.
-template <typename R> struct Lim { using type = R; };
-template <> struct Lim<df> { using type = float; };
-template <typename R> __device__ __forceinline__ typename Lim<R>::type lim_of(R x) { return x; }
-template <> __device__ __forceinline__ float lim_of<df>(df x) { return x.hi; }
-
 template <typename R>
 __device__ __forceinline__ void recon_tvd2(int lim, R qm1, R q0, R qp1, R qp2, R& L, R& Rr) {
-  using T = typename Lim<R>::type;
-  const T EPS = Num<T>::eps;
-  T dm = lim_of(q0 - qm1), d0 = lim_of(qp1 - q0), dp = lim_of(qp2 - qp1);
-  if (abs_lt(dm, EPS)) dm = T(0);
-  if (abs_lt(d0, EPS)) d0 = T(0);
-  if (abs_lt(dp, EPS)) dp = T(0);
+  const R EPS = Num<R>::eps;
+  R dm = q0 - qm1, d0 = qp1 - q0, dp = qp2 - qp1;
+  if (abs_lt(dm, EPS)) dm = R(0);
+  if (abs_lt(d0, EPS)) d0 = R(0);
+  if (abs_lt(dp, EPS)) dp = R(0);
   // d0 == 0 gives r = 0 exactly (0/x); skip the division
-  T rL = (d0 == T(0)) ? T(0) * (dm + T(1e-16)) : Num<T>::div(d0, dm + T(1e-16));
-  T rR = (d0 == T(0)) ? T(0) * (dp + T(1e-16)) : Num<T>::div(d0, dp + T(1e-16));
-  T phi = tvd_phi(lim, rL);
-  L = q0 + R(T(0.5) * phi * dm);
+  R rL = (d0 == R(0)) ? R(0) * (dm + R(1e-16)) : Num<R>::div(d0, dm + R(1e-16));
+  R rR = (d0 == R(0)) ? R(0) * (dp + R(1e-16)) : Num<R>::div(d0, dp + R(1e-16));
+  R phi = tvd_phi(lim, rL);
+  L = q0 + R(0.5) * phi * dm;
   phi = tvd_phi(lim, rR);
-  Rr = qp1 - R(T(0.5) * phi * dp);
+  Rr = qp1 - R(0.5) * phi * dp;
 }
 
 template <typename R, int ORDER>
 __device__ __forceinline__ void recon_mlp(R qm2, R qm1, R q0, R qp1, R qp2, R qp3, R t0p, R t0m,
                                           R t1p, R t1m, R& L, R& Rr) {
-  using T = typename Lim<R>::type;
-  const T EPS = Num<T>::eps;
-  const T S = T(1e-30);  // SMALL_NUM, muscl_mlp.fypp:122
-  T dm = lim_of(q0 - qm1), d0 = lim_of(qp1 - q0), dp = lim_of(qp2 - qp1);
-  if (abs_lt(dm, EPS)) dm = T(0);
-  if (abs_lt(d0, EPS)) d0 = T(0);
-  if (abs_lt(dp, EPS)) dp = T(0);
-  T rR_p1 = Num<T>::div(d0, dp + S);
-  T rL = Num<T>::div(d0, dm + S);
-  T bL, bR;
+  const R EPS = Num<R>::eps;
+  const R S = R(1e-30);  // SMALL_NUM, muscl_mlp.fypp:122
+  R dm = q0 - qm1, d0 = qp1 - q0, dp = qp2 - qp1;
+  if (abs_lt(dm, EPS)) dm = R(0);
+  if (abs_lt(d0, EPS)) d0 = R(0);
+  if (abs_lt(dp, EPS)) dp = R(0);
+  R rR_p1 = Num<R>::div(d0, dp + S);
+  R rL = Num<R>::div(d0, dm + S);
+  R bL, bR;
   if (ORDER == 5) {
-    T dm3 = lim_of(qm1 - qm2), dp5 = lim_of(qp3 - qp2);
-    if (abs_lt(dm3, EPS)) dm3 = T(0);
-    if (abs_lt(dp5, EPS)) dp5 = T(0);
-    T rL_m1 = Num<T>::div(dm, dm3 + S);
-    T rL_p1 = Num<T>::div(dp, d0 + S);
-    T rR_p2 = Num<T>::div(dp, dp5 + S);
-    T rR = Num<T>::div(dm, d0 + S);
-    bL = Num<T>::div((((Num<T>::div(T(-2), rL_m1 + S)) + T(11)) + T(24) * rL) - T(3) * rL * rL_p1,
-                     T(30));
-    bR = Num<T>::div((((Num<T>::div(T(-2), rR_p2 + S)) + T(11)) + T(24) * rR_p1) -
-                         T(3) * rR_p1 * rR,
-                     T(30));
+    R dm3 = qm1 - qm2, dp5 = qp3 - qp2;
+    if (abs_lt(dm3, EPS)) dm3 = R(0);
+    if (abs_lt(dp5, EPS)) dp5 = R(0);
+    R rL_m1 = Num<R>::div(dm, dm3 + S);
+    R rL_p1 = Num<R>::div(dp, d0 + S);
+    R rR_p2 = Num<R>::div(dp, dp5 + S);
+    R rR = Num<R>::div(dm, d0 + S);
+    bL = Num<R>::div((((Num<R>::div(R(-2), rL_m1 + S)) + R(11)) + R(24) * rL) - R(3) * rL * rL_p1,
+                     R(30));
+    bR = Num<R>::div((((Num<R>::div(R(-2), rR_p2 + S)) + R(11)) + R(24) * rR_p1) -
+                         R(3) * rR_p1 * rR,
+                     R(30));
   } else {
-    bL = Num<T>::div(T(1) + T(2) * rL, T(3));
-    bR = Num<T>::div(T(1) + T(2) * rR_p1, T(3));
+    bL = Num<R>::div(R(1) + R(2) * rL, R(3));
+    bR = Num<R>::div(R(1) + R(2) * rR_p1, R(3));
   }
-  T tt = Num<T>::div(rabs(lim_of(t0p - t0m)), rabs(lim_of(qp1 - qm1)) + S);
-  T tt1 = Num<T>::div(rabs(lim_of(t1p - t1m)), rabs(lim_of(qp2 - q0)) + S);
-  T aLt = Num<T>::div(T(2) * rmax(T(1), rL) * (T(1) + rmax(T(0), Num<T>::div(tt1, rR_p1 + S))),
-                      T(1) + tt);
-  T aRt = Num<T>::div(T(2) * rmax(T(1), rR_p1) * (T(1) + rmax(T(0), Num<T>::div(tt, rL + S))),
-                      T(1) + tt1);
-  T aL = rmax(T(1), rmin(T(2), aLt));
-  T aR = rmax(T(1), rmin(T(2), aRt));
-  L = q0 + R(T(0.5) * rmax(T(0), rmin(rmin(aL * rL, aL), bL)) * dm);
-  Rr = qp1 - R(T(0.5) * rmax(T(0), rmin(rmin(aR * rR_p1, aR), bR)) * dp);
+  R tt = Num<R>::div(rabs(t0p - t0m), rabs(qp1 - qm1) + S);
+  R tt1 = Num<R>::div(rabs(t1p - t1m), rabs(qp2 - q0) + S);
+  R aLt = Num<R>::div(R(2) * rmax(R(1), rL) * (R(1) + rmax(R(0), Num<R>::div(tt1, rR_p1 + S))),
+                      R(1) + tt);
+  R aRt = Num<R>::div(R(2) * rmax(R(1), rR_p1) * (R(1) + rmax(R(0), Num<R>::div(tt, rL + S))),
+                      R(1) + tt1);
+  R aL = rmax(R(1), rmin(R(2), aLt));
+  R aR = rmax(R(1), rmin(R(2), aRt));
+  L = q0 + R(0.5) * rmax(R(0), rmin(rmin(aL * rL, aL), bL)) * dm;
+  Rr = qp1 - R(0.5) * rmax(R(0), rmin(rmin(aR * rR_p1, aR), bR)) * dp;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Double-float reconstruction (mixed_df).  The limited slope phi(r) * dq is, for each branch of
+// the limiter, an algebraic combination of the slope differences themselves: with r = d0/dm,
+// r * dm = d0, (1 + 2r)/3 * dm = (dm + 2 d0)/3, and the MLP5 coefficient times dm is the
+// fifth-order combination (-2 dm3 + 11 dm + 24 d0 - 3 dp)/30.  So the branch is chosen in FP32
+// (only a near-tie can go the other way, where both branches agree to FP32 rounding) and the
+// chosen slope is evaluated in double-float from the double-float differences, without the
+// ratio divisions.  The reference's 1e-16 / 1e-30 regularisations only matter for differences
+// at the epsilon flush threshold, where the slope term is itself ~1e-16.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ df df_half(df a) { return df(a.hi * 0.5f, a.lo * 0.5f); }  // exact
+__device__ __forceinline__ df df_twice(df a) { return df(a.hi * 2.0f, a.lo * 2.0f); }  // exact
+__device__ __forceinline__ df df_scale(df a, float c) { return a * df(c); }
+
+// TVD2 slope phi(r) * dq for r = d0 / dq (dq = dm for the left state, dp for the right)
+__device__ __forceinline__ df tvd_slope_df(int lim, df D0, df Dq) {
+  const float d0 = D0.hi, dq = Dq.hi;
+  if (d0 == 0.0f || dq == 0.0f || ((d0 > 0.0f) != (dq > 0.0f))) return df(0.0f);  // r <= 0
+  const float a0 = fabsf(d0), aq = fabsf(dq);  // r = a0 / aq > 0
+  if (lim == LIM_MINMOD) return a0 < aq ? D0 : Dq;            // min(r, 1) * dq
+  if (lim == LIM_SUPERBEE) {                                    // max(min(2r, 1), min(r, 2)) * dq
+    if (2.0f * a0 <= aq) return df_twice(D0);
+    if (a0 <= aq) return Dq;
+    if (a0 <= 2.0f * aq) return D0;
+    return df_twice(Dq);
+  }
+  // van Leer: 2r / (1 + r) * dq = 2 d0 dq / (dq + d0)
+  return df_div(df_twice(D0 * Dq), Dq + D0);
+}
+
+__device__ __forceinline__ df flushed(df d) {
+  return fabsf(d.hi) < 2.220446049250313080847263336181640625e-16f ? df(0.0f) : d;
+}
+
+template <>
+__device__ __forceinline__ void recon_tvd2<df>(int lim, df qm1, df q0, df qp1, df qp2, df& L,
+                                               df& Rr) {
+  const df Dm = flushed(q0 - qm1), D0 = flushed(qp1 - q0), Dp = flushed(qp2 - qp1);
+  L = q0 + df_half(tvd_slope_df(lim, D0, Dm));
+  Rr = qp1 - df_half(tvd_slope_df(lim, D0, Dp));
+}
+
+// MLP slope: phi * dq with phi = max(0, min(alpha r, alpha, beta)); candidates
+// alpha * d0, alpha * dq and beta * dq (the latter given in double-float as bdq).
+__device__ __forceinline__ df mlp_slope_df(float r, float alpha, float beta, df D0, df Dq,
+                                           df bdq) {
+  const float c1 = alpha * r, c2 = alpha;
+  float m = fminf(c1, c2);
+  int pick = c1 <= c2 ? 1 : 2;
+  if (beta < m) { m = beta; pick = 3; }
+  if (!(m > 0.0f)) return df(0.0f);
+  if (pick == 1) return df_scale(D0, alpha);
+  if (pick == 2) return df_scale(Dq, alpha);
+  return bdq;
+}
+
+template <int ORDER>
+__device__ __forceinline__ void recon_mlp_df(df qm2, df qm1, df q0, df qp1, df qp2, df qp3,
+                                             df t0p, df t0m, df t1p, df t1m, df& L, df& Rr) {
+  const float S = 1e-30f;
+  const df Dm = flushed(q0 - qm1), D0 = flushed(qp1 - q0), Dp = flushed(qp2 - qp1);
+  const float dm = Dm.hi, d0 = D0.hi, dp = Dp.hi;
+  const float rR_p1 = __fdividef(d0, dp + S), rL = __fdividef(d0, dm + S);
+  float bL, bR;
+  df bdL, bdR;  // beta * dm (left), beta * dp (right) in double-float
+  if (ORDER == 5) {
+    const df Dm3 = flushed(qm1 - qm2), Dp5 = flushed(qp3 - qp2);
+    const float dm3 = Dm3.hi, dp5 = Dp5.hi;
+    const float rL_m1 = __fdividef(dm, dm3 + S), rL_p1 = __fdividef(dp, d0 + S);
+    const float rR_p2 = __fdividef(dp, dp5 + S), rR = __fdividef(dm, d0 + S);
+    bL = ((__fdividef(-2.0f, rL_m1 + S) + 11.0f) + 24.0f * rL - 3.0f * rL * rL_p1) * (1.0f / 30.0f);
+    bR = ((__fdividef(-2.0f, rR_p2 + S) + 11.0f) + 24.0f * rR_p1 - 3.0f * rR_p1 * rR) *
+         (1.0f / 30.0f);
+    // beta_L dm = (-2 dm3 + 11 dm + 24 d0 - 3 rL rL_p1 dm)/30 with rL rL_p1 dm = dp (0 if d0 = 0)
+    const df t3L = d0 == 0.0f ? df(0.0f) : Dp, t3R = d0 == 0.0f ? df(0.0f) : Dm;
+    bdL = (df_scale(Dm3, -2.0f) + df_scale(Dm, 11.0f) + df_scale(D0, 24.0f) - df_scale(t3L, 3.0f)) *
+          df(1.0 / 30.0);
+    // beta_R dp = (-2 dp5 + 11 dp + 24 d0 - 3 rR_p1 rR dp)/30 with rR_p1 rR dp = dm
+    bdR = (df_scale(Dp5, -2.0f) + df_scale(Dp, 11.0f) + df_scale(D0, 24.0f) - df_scale(t3R, 3.0f)) *
+          df(1.0 / 30.0);
+  } else {
+    bL = (1.0f + 2.0f * rL) * (1.0f / 3.0f);
+    bR = (1.0f + 2.0f * rR_p1) * (1.0f / 3.0f);
+    bdL = (Dm + df_twice(D0)) * df(1.0 / 3.0);
+    bdR = (Dp + df_twice(D0)) * df(1.0 / 3.0);
+  }
+  const float tt = __fdividef(fabsf((t0p - t0m).hi), fabsf((qp1 - qm1).hi) + S);
+  const float tt1 = __fdividef(fabsf((t1p - t1m).hi), fabsf((qp2 - q0).hi) + S);
+  const float aLt = __fdividef(2.0f * fmaxf(1.0f, rL) * (1.0f + fmaxf(0.0f, __fdividef(tt1, rR_p1 + S))),
+                               1.0f + tt);
+  const float aRt = __fdividef(2.0f * fmaxf(1.0f, rR_p1) * (1.0f + fmaxf(0.0f, __fdividef(tt, rL + S))),
+                               1.0f + tt1);
+  const float aL = fmaxf(1.0f, fminf(2.0f, aLt)), aR = fmaxf(1.0f, fminf(2.0f, aRt));
+  L = dm == 0.0f ? q0 : q0 + df_half(mlp_slope_df(rL, aL, bL, D0, Dm, bdL));
+  Rr = dp == 0.0f ? qp1 : qp1 - df_half(mlp_slope_df(rR_p1, aR, bR, D0, Dp, bdR));
+}
+
+template <>
+__device__ __forceinline__ void recon_mlp<df, 3>(df qm2, df qm1, df q0, df qp1, df qp2, df qp3,
+                                                 df t0p, df t0m, df t1p, df t1m, df& L, df& Rr) {
+  recon_mlp_df<3>(qm2, qm1, q0, qp1, qp2, qp3, t0p, t0m, t1p, t1m, L, Rr);
+}
+template <>
+__device__ __forceinline__ void recon_mlp<df, 5>(df qm2, df qm1, df q0, df qp1, df qp2, df qp3,
+                                                 df t0p, df t0m, df t1p, df t1m, df& L, df& Rr) {
+  recon_mlp_df<5>(qm2, qm1, q0, qp1, qp2, qp3, t0p, t0m, t1p, t1m, L, Rr);
 }
 
 // ---------------------------------------------------------------------------------------------
