@@ -119,7 +119,14 @@ struct cato_batch {
   std::vector<Group> groups;
   int* d_counters = nullptr;
   int n_counters_cap = 0;
-  int threads = 128, rows = 32;
+  int threads = 128, rows = 32;  // plan: CTA width, largest rows per tile
+  int tile_rows = 32;            // rows per tile chosen by the last rebuild
+  int sms = 0;
+  // one stream per (flux, reconstruction) group: the groups touch disjoint instances, so their
+  // stage chains run concurrently between the step's begin and end kernels
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> side_done;
+  cudaEvent_t fork = nullptr;
   bool dirty = true;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -168,10 +175,29 @@ static int rebuild(cato_batch* b) {
     return (long long)b->h_descs[x].ni * b->h_descs[x].nj >
            (long long)b->h_descs[y].ni * b->h_descs[y].nj;
   });
+  if (!b->sms) {
+    int dev = 0;
+    BK(cudaGetDevice(&dev));
+    BK(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  // Rows per tile: the plan's, halved (down to 4) while the batch would give fewer than two
+  // tiles per SM, so that a batch of small grids still fills the GPU.
+  auto n_tiles = [&](int r) {
+    long long n = 0;
+    for (int i : order) {
+      const InstDesc& d = b->h_descs[i];
+      const int W = b->threads - 2 * d.ng, rr = std::min(r, d.nj);
+      n += (long long)((d.ni + W - 1) / W) * ((d.nj + rr - 1) / rr);
+    }
+    return n;
+  };
+  int tile_rows = b->rows;
+  while (tile_rows > 4 && n_tiles(tile_rows) < 2LL * b->sms) tile_rows = std::max(4, tile_rows / 2);
+  b->tile_rows = tile_rows;
   for (int i : order) {
     const InstDesc& d = b->h_descs[i];
     const int W = b->threads - 2 * d.ng;
-    const int rows = std::min(b->rows, d.nj);
+    const int rows = std::min(tile_rows, d.nj);
     const int tx = (d.ni + W - 1) / W, ty = (d.nj + rows - 1) / rows;
     auto& L = lists[{d.flux, d.recon}];
     for (int y = 0; y < ty; ++y)
@@ -196,6 +222,15 @@ static int rebuild(cato_batch* b) {
     BK(cudaMalloc(&b->d_counters, sizeof(int) * need));
     b->n_counters_cap = need;
   }
+  while (b->side.size() < b->groups.size()) {
+    cudaStream_t st;
+    cudaEvent_t ev;
+    BK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    BK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    b->side.push_back(st);
+    b->side_done.push_back(ev);
+  }
+  if (!b->fork) BK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
   // set each kernel's shared-memory attribute outside any stream capture
   for (const auto& g : b->groups) {
     BatchStageArgs B;
@@ -214,21 +249,30 @@ static int enqueue_batch_step(cato_batch* b) {
                                               b->n_counters_cap);
   BK(cudaGetLastError());
   const int ns = (int)b->stages.size();
-  for (int k = 0; k < ns; ++k) {
-    for (size_t g = 0; g < b->groups.size(); ++g) {
-      const Group& G = b->groups[g];
+  const int ng = (int)b->groups.size();
+  const bool fan = ng > 1;
+  if (fan) BK(cudaEventRecord(b->fork, b->stream));
+  for (int g = 0; g < ng; ++g) {
+    const Group& G = b->groups[g];
+    cudaStream_t st = fan ? b->side[g] : b->stream;
+    if (fan) BK(cudaStreamWaitEvent(st, b->fork, 0));
+    for (int k = 0; k < ns; ++k) {
       BatchStageArgs B;
       B.descs = b->d_descs;
       B.items = G.d_items;
       B.n_items = G.n_items;
-      B.counter = b->d_counters + k * (int)b->groups.size() + (int)g;
+      B.counter = b->d_counters + k * ng + g;
       B.stage = k;
       B.kind = b->stages[k].kind;
       B.last = (k == ns - 1);
       B.a = b->stages[k].a;
       B.b = b->stages[k].b;
       B.coef = b->stages[k].coef;
-      BK(launch_batch_prec(b->prec, G.flux, G.recon, b->threads, b->stream, B));
+      BK(launch_batch_prec(b->prec, G.flux, G.recon, b->threads, st, B));
+    }
+    if (fan) {
+      BK(cudaEventRecord(b->side_done[g], st));
+      BK(cudaStreamWaitEvent(b->stream, b->side_done[g], 0));
     }
   }
   batch_step_end<<<(b->capacity + 127) / 128, 128, 0, b->stream>>>(b->d_descs, b->capacity);
@@ -284,6 +328,11 @@ int cato_batch_destroy(cato_batch* b) {
   for (auto& d : b->h_descs)
     if (d.in_use) free_instance(d);
   for (auto& g : b->groups) cudaFree(g.d_items);
+  for (size_t k = 0; k < b->side.size(); ++k) {
+    cudaStreamDestroy(b->side[k]);
+    cudaEventDestroy(b->side_done[k]);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
   cudaFree(b->d_counters);
   cudaFree(b->d_descs);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);
