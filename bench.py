@@ -464,9 +464,15 @@ def main() -> int:
     fp64, cfg, prims = bench_precision(args, "fp64", dist, world, peak)
     mixed, _, _ = bench_precision(args, "mixed", dist, world, peak)
     mixed_df, _, _ = bench_precision(args, "mixed_df", dist, world, peak)
-    e2e = bench_e2e(args, cfg, prims)
-    e2e_all = allreduce_max(dist, -e2e["value"])  # slowest replica
-    e2e["value"] = -e2e_all * world
+    def e2e_of(precision):
+        c = dataclasses.replace(cfg, precision=precision)
+        r = bench_e2e(args, c, prims)
+        r["value"] = -allreduce_max(dist, -r["value"]) * world  # slowest replica
+        return r
+
+    e2e = e2e_of("fp64")
+    e2e_mixed = e2e_of("mixed")
+    e2e_df = e2e_of("mixed_df")
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -507,6 +513,7 @@ def main() -> int:
             "ms_per_step": mixed["ms_per_step"], "speedup_vs_fp64": mixed["value"] / fp64["value"],
             "roofline": mixed["roofline"], "stage_ms_per_step": mixed["stage_ms_per_step"],
             "gpu_launches": mixed["launches_per_step"] * args.steps, "clocks": mixed["clocks"],
+            "e2e": e2e_mixed,
         },
         "mixed_df": {
             "value": mixed_df["value"], "unit": "cell-updates/s",
@@ -515,7 +522,7 @@ def main() -> int:
             "speedup_vs_fp64": mixed_df["value"] / fp64["value"],
             "roofline": mixed_df["roofline"], "stage_ms_per_step": mixed_df["stage_ms_per_step"],
             "gpu_launches": mixed_df["launches_per_step"] * args.steps,
-            "clocks": mixed_df["clocks"],
+            "clocks": mixed_df["clocks"], "e2e": e2e_df,
         },
         "kelvin_helmholtz": kh,
         "batched": batched,
