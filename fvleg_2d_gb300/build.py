@@ -48,6 +48,8 @@ def _sources_digest(extra: list[str]) -> str:
 def _units() -> list[tuple[str, list[str]]]:
     common = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", INCLUDE]
+    # developer knob: extra nvcc flags for every unit (e.g. -DCATO_DF_MIN_BLOCKS=2)
+    common += os.environ.get("CATO_NVCC_FLAGS", "").split()
     units = []
     for real, flags in (("double", ["--fmad=false"]),
                         ("float", ["--fmad=true", "-prec-sqrt=false", "-ftz=true"]),

@@ -448,8 +448,15 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
   }
 }
 
+// Minimum resident 256-thread CTAs per SM requested from the register allocator for the
+// double-float kernels (their pair arithmetic is latency-bound; more warps hide it).
+#ifndef CATO_DF_MIN_BLOCKS
+#define CATO_DF_MIN_BLOCKS 1
+#endif
+
 template <typename R, int NG, int FLUX, int RECON>
-__global__ void __launch_bounds__(256) stage_kernel(const StageArgs A, const FluxConsts<R> K) {
+__global__ void __launch_bounds__(256, (Prec<R>::kind == 2 ? CATO_DF_MIN_BLOCKS : 1))
+    stage_kernel(const StageArgs A, const FluxConsts<R> K) {
   if (A.active && *A.active == 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   stage_tile<R, NG, FLUX, RECON>(A, K, blockIdx.x, blockIdx.y, smem_raw);
