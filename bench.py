@@ -183,7 +183,9 @@ def run_reference(args, world, rank, dist):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": workload_config(args, world),
+        "config": dict(workload_config(args, world),
+                       window="steps from the initial state: the restatement does the same "
+                              "arithmetic for every cell whatever the data"),
         "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": used,
                          "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
@@ -199,14 +201,42 @@ def workload_config(args, world):
             "gamma": 1.4, "bc": "zero_gradient (transmissive) on all sides",
             "cells": args.n * args.n, "n_ghost": 2,
             "l2": "state of 4 x 8 B x 16.8M cells = 537 MB per copy > 129 MB L2 (no flush needed)",
+            "window": (f"steps from the developed flow at t = {args.t_start} (state advanced with "
+                       "the mixed path, then uploaded as primitives)" if args.t_start > 0
+                       else "steps from the initial state"),
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
 
 
-def bench_precision(args, precision, dist, world, peak_gbs):
+_DEVELOPED = {}
+
+
+def quadrant_state(args):
+    """The quadrant problem's state at t = args.t_start (primitives, halo-padded): the timed
+    window is taken from the developed flow rather than from the piecewise-constant initial
+    state, whose uniform regions make every path's data-dependent shortcuts unrepresentatively
+    cheap.  The state is advanced with the mixed path (its accuracy is irrelevant to a
+    throughput window) and cached for all legs."""
     from fvleg_2d_gb300 import ic
     from fvleg_2d_gb300.fluid import Fluid
 
-    cfg, prims = ic.riemann_quadrant(args.n, precision=precision)
+    key = (args.n, args.t_start)
+    if key not in _DEVELOPED:
+        cfg, prims = ic.riemann_quadrant(args.n)
+        if args.t_start > 0:
+            f = Fluid(dataclasses.replace(cfg, precision="mixed")).initialize(*prims)
+            f.run(args.t_start)
+            s = f.state(("rho", "u", "v", "p"))
+            prims = [s["rho"], s["u"], s["v"], s["p"]]
+            f.close()
+        _DEVELOPED[key] = (cfg, prims)
+    return _DEVELOPED[key]
+
+
+def bench_precision(args, precision, dist, world, peak_gbs):
+    from fvleg_2d_gb300.fluid import Fluid
+
+    cfg, prims = quadrant_state(args)
+    cfg = dataclasses.replace(cfg, precision=precision)
     f = Fluid(cfg).initialize(*prims)
     f.run_timed(args.warmup)
     barrier(dist)
@@ -432,6 +462,8 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=4096)
+    ap.add_argument("--t-start", type=float, default=0.15,
+                    help="start the timed window from the quadrant flow at this time")
     ap.add_argument("--cpu-baseline-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")

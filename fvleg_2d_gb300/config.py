@@ -35,7 +35,9 @@ RK_IDS = {
     "rk(2,4)": 6,
     "rk(2,5)": 7,
 }
-BC_IDS = {"zero_gradient": 0, "symmetry": 1, "periodic": 2}
+# bc_factory.f90:46-59 names
+BC_IDS = {"zero_gradient": 0, "symmetry": 1, "mirror": 1, "reflection": 1, "periodic": 2,
+          "outlet": 3, "outflow": 3}
 PRECISION_IDS = {"fp64": 0, "mixed": 1, "mixed_df": 2}
 # side order of cato_config.bc: the reference's application order (flux_solver.f90:165-183)
 SIDES = ("+x", "+y", "-x", "-y")
@@ -89,6 +91,7 @@ class CatoConfig(ctypes.Structure):
         ("ausm_kp", ctypes.c_double),
         ("ausm_ku", ctypes.c_double),
         ("ausm_sigma", ctypes.c_double),
+        ("bc_pressure", ctypes.c_double),
     ]
 
 
@@ -118,6 +121,7 @@ class SchemeConfig:
     ausm_kp: float = 0.25
     ausm_ku: float = 0.75
     ausm_sigma: float = 1.0
+    outflow_ambient_pressure: float = 0.0  # [boundary_conditions], for 'outflow' sides
     n_ghost: int | None = None
 
     def ghost_layers(self) -> int:
@@ -145,6 +149,7 @@ class SchemeConfig:
         c.harten_delta = self.harten_delta
         c.ausm_beta, c.ausm_kp = self.ausm_beta, self.ausm_kp
         c.ausm_ku, c.ausm_sigma = self.ausm_ku, self.ausm_sigma
+        c.bc_pressure = self.outflow_ambient_pressure
         return c
 
     @property

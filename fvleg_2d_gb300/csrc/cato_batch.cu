@@ -374,6 +374,7 @@ int cato_batch_add(cato_batch* b, const cato_config* cfg, const double* rho, con
   d.recon = recon_id(cfg->limiter);
   d.prec = cfg->precision;
   d.gamma = cfg->gamma;
+  d.bc_p = cfg->bc_pressure;
   d.cfl = cfg->cfl;
   // the same constants and uniform geometry as a single-instance handle
   const double g = cfg->gamma;

@@ -19,7 +19,7 @@ struct InstDesc {
   int raw_pending;         // the first stage uses the uploaded primitives as is
   int prec;                // 0 FP64, 1 mixed, 2 mixed_df (FP64 layout)
   int in_use;
-  double gamma, cfl;
+  double gamma, cfl, bc_p;
   Geom G;
   FluxConsts<double> K64;
   FluxConsts<float> K32;
@@ -62,6 +62,7 @@ __device__ __forceinline__ void batch_stage_args(InstDesc* d, const BatchStageAr
   A.dt_min = &d->ctl.dt_min;
   A.status = &d->ctl.status;
   A.gamma = d->gamma;
+  A.bc_p = d->bc_p;
   A.cfl = d->cfl;
   A.G = d->G;
   const bool raw = (B.stage == 0) && d->raw_pending;

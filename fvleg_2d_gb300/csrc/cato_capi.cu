@@ -187,6 +187,7 @@ static StageArgs base_args(cato_handle* h) {
   A.dt_min = &h->ctl->dt_min;
   A.status = &h->ctl->status;
   A.gamma = h->cfg.gamma;
+  A.bc_p = h->cfg.bc_pressure;
   A.cfl = h->cfg.cfl;
   A.G = h->G;
   return A;
@@ -354,8 +355,13 @@ int cato_config_check(const cato_config* c) {
   const int need = (c->limiter == CATO_LIM_MLP5) ? 3 : 2;  // mod_input.f90:320-338
   if (c->n_ghost != need) return CATO_ERR_CONFIG;
   if (c->ni < c->n_ghost || c->nj < c->n_ghost) return CATO_ERR_CONFIG;
-  for (int s = 0; s < 4; ++s)
-    if (c->bc[s] < CATO_BC_ZERO_GRADIENT || c->bc[s] > CATO_BC_PERIODIC) return CATO_ERR_CONFIG;
+  bool outlet = false;
+  for (int s = 0; s < 4; ++s) {
+    if (c->bc[s] < CATO_BC_ZERO_GRADIENT || c->bc[s] > CATO_BC_OUTLET) return CATO_ERR_CONFIG;
+    outlet |= c->bc[s] == CATO_BC_OUTLET;
+  }
+  // outlet_bc_constructor stops on an ambient pressure <= 0 (outlet_bc.f90:54-59)
+  if (outlet && !(c->bc_pressure > 0.0)) return CATO_ERR_CONFIG;
   // periodic must be paired on an axis: an unpaired periodic side leaves ghost corners unset
   if ((c->bc[CATO_PLUS_X] == CATO_BC_PERIODIC) != (c->bc[CATO_MINUS_X] == CATO_BC_PERIODIC))
     return CATO_ERR_CONFIG;
@@ -660,8 +666,9 @@ int cato_gpu_solve(cato_handle* h, double* rho, double* u, double* v, double* p,
   const int4 bc = make_int4(h->cfg.bc[0], h->cfg.bc[1], h->cfg.bc[2], h->cfg.bc[3]);
   const long long hld = h->ni + 2 * h->ng;
   fill_ghosts_kernel<<<grid_for((long long)h->halo_elems), 256, 0, h->stream>>>(
-      h->ni, h->nj, h->pitch, h->ng, bc, h->scratch[0], h->scratch[1], h->scratch[2],
-      h->scratch[3], h->halo[0], h->halo[1], h->halo[2], h->halo[3], hld);
+      h->ni, h->nj, h->pitch, h->ng, bc, h->cfg.gamma, h->cfg.bc_pressure, h->scratch[0],
+      h->scratch[1], h->scratch[2], h->scratch[3], h->halo[0], h->halo[1], h->halo[2],
+      h->halo[3], hld);
   CK(cudaGetLastError());
   for (int k = 0; k < 4; ++k)
     CK(cudaMemcpy2DAsync(prim[k], (size_t)ld * sizeof(double), h->halo[k], (size_t)hld * sizeof(double),

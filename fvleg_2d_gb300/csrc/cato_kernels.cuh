@@ -108,6 +108,7 @@ static __global__ void derive_kernel(int ni, int nj, int pitch, double gamma, in
 // Halo-padded primitive fields with every ghost cell filled by the boundary conditions, as after
 // flux_solver_t%apply_primitive_bc (flux_solver.f90:138-185).
 static __global__ void fill_ghosts_kernel(int ni, int nj, int pitch, int ng, int4 bc,
+                                   double gamma, double bc_p,
                                    const double* __restrict__ r_, const double* __restrict__ u_,
                                    const double* __restrict__ v_, const double* __restrict__ p_,
                                    double* ro, double* uo, double* vo, double* po, long long ld) {
@@ -121,10 +122,12 @@ static __global__ void fill_ghosts_kernel(int ni, int nj, int pitch, int ng, int
     const int sy = map_index(jj - ng, nj, bcs[SIDE_MY], bcs[SIDE_PY], fy);
     const size_t s = (size_t)sy * pitch + sx;
     const size_t o = (size_t)jj * ld + ii;
-    ro[o] = r_[s];
-    uo[o] = fx ? -u_[s] : u_[s];
-    vo[o] = fy ? -v_[s] : v_[s];
-    po[o] = p_[s];
+    double r = r_[s], u = fx ? -u_[s] : u_[s], v = fy ? -v_[s] : v_[s], p = p_[s];
+    if (bcs[SIDE_PX] == BC_OUTLET && ii - ng >= ni) outlet_ghost<double>(gamma, bc_p, r, u, v, p);
+    ro[o] = r;
+    uo[o] = u;
+    vo[o] = v;
+    po[o] = p;
   }
 }
 

@@ -47,7 +47,8 @@ double* g_scratch_dev[kMaxDevices] = {};
 size_t round_up(size_t n) { return (n + kAlign - 1) / kAlign * kAlign; }
 
 // the BC-filled halo-padded primitives written back to the caller (flux_solver.f90:138-185)
-__global__ void noalloc_fill_ghosts(int ni, int nj, int pitch, int ng, int4 bc,
+__global__ void noalloc_fill_ghosts(int ni, int nj, int pitch, int ng, int4 bc, double gamma,
+                                    double bc_p,
                                     const double* __restrict__ r_, const double* __restrict__ u_,
                                     const double* __restrict__ v_, const double* __restrict__ p_,
                                     double* ro, double* uo, double* vo, double* po, long long ld) {
@@ -61,10 +62,12 @@ __global__ void noalloc_fill_ghosts(int ni, int nj, int pitch, int ng, int4 bc,
     const int sy = map_index(jj - ng, nj, bcs[SIDE_MY], bcs[SIDE_PY], fy);
     const size_t s = (size_t)sy * pitch + sx;
     const size_t o = (size_t)jj * ld + ii;
-    ro[o] = r_[s];
-    uo[o] = fx ? -u_[s] : u_[s];
-    vo[o] = fy ? -v_[s] : v_[s];
-    po[o] = p_[s];
+    double r = r_[s], u = fx ? -u_[s] : u_[s], v = fy ? -v_[s] : v_[s], p = p_[s];
+    if (bcs[SIDE_PX] == BC_OUTLET && ii - ng >= ni) outlet_ghost<double>(gamma, bc_p, r, u, v, p);
+    ro[o] = r;
+    uo[o] = u;
+    vo[o] = v;
+    po[o] = p;
   }
 }
 
@@ -170,6 +173,7 @@ extern "C" int cato_gpu_solve_noalloc(const cato_config* cfg, double* rho, doubl
   A.dt_min = reinterpret_cast<unsigned long long*>(ctl + 1);
   A.status = reinterpret_cast<int*>(ctl + 2);
   A.gamma = cfg->gamma;
+  A.bc_p = cfg->bc_pressure;
   A.cfl = cfg->cfl;
   A.G = G;
   for (int k = 0; k < 4; ++k) {
@@ -186,8 +190,9 @@ extern "C" int cato_gpu_solve_noalloc(const cato_config* cfg, double* rho, doubl
   const long long nh = hld * (nj + 2 * ng);
   int blocks = (int)((nh + 255) / 256);
   blocks = blocks > 4864 ? 4864 : blocks;
-  noalloc_fill_ghosts<<<blocks, 256, 0, s>>>(ni, nj, pitch, ng, bc, prim[0], prim[1], prim[2],
-                                             prim[3], gh[0], gh[1], gh[2], gh[3], hld);
+  noalloc_fill_ghosts<<<blocks, 256, 0, s>>>(ni, nj, pitch, ng, bc, cfg->gamma, cfg->bc_pressure,
+                                             prim[0], prim[1], prim[2], prim[3], gh[0], gh[1],
+                                             gh[2], gh[3], hld);
   NA_CK(cudaGetLastError());
   for (int k = 0; k < 4; ++k)
     NA_CK(cudaMemcpy2DAsync(host_prim[k], (size_t)ld * sizeof(double), gh[k],

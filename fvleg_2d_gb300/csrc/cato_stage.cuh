@@ -56,6 +56,7 @@ struct StageArgs {
   int* status;
   // physics
   double gamma, cfl;
+  double bc_p;             // outlet pressure (CATO_BC_OUTLET)
   Geom G;
 };
 
@@ -74,6 +75,27 @@ __device__ __forceinline__ int map_index(int g, int n, int bc_lo, int bc_hi, boo
     return n - 1;
   }
   return g;
+}
+
+// Outlet ghost state on the +x side (outlet_bc.f90:101-123) from the primitives of the boundary
+// cell it maps to (after the other sides' BCs, as the outlet has the lowest priority): copied
+// when the boundary cell is supersonic, else the characteristic subsonic outflow state at the
+// ambient pressure p_b.  The reference leaves the ghost unchanged when p_b or the boundary
+// density is below tiny (p_b > 0 is enforced by the configuration check); here it keeps the copy.
+template <typename R>
+__device__ __forceinline__ void outlet_ghost(R gamma, R p_b, R& r, R& u, R& v, R& p) {
+  const R r0 = r, p_d = p;
+  if (!(p_b > Num<R>::tiny) || !(r0 > Num<R>::tiny)) return;
+  const R cs = Num<R>::sqrt(gamma * rabs(Num<R>::div(p_d, r0)));
+  const R vel = Num<R>::sqrt(u * u + v * v);
+  const R mach = Num<R>::div(vel, cs);
+  const R nx = Num<R>::div(u, vel + R(1e-30));
+  const R ny = Num<R>::div(v, vel + R(1e-30));
+  if (mach > R(1)) return;
+  r = r0 + Num<R>::div(p_b - p_d, cs * cs);
+  u = u + Num<R>::div(nx * (p_d - p_b), r0 * cs);
+  v = v + Num<R>::div(ny * (p_d - p_b), r0 * cs);
+  p = p_b;
 }
 
 template <int RING> __device__ __forceinline__ int slot_of(int row) {
@@ -202,7 +224,7 @@ __device__ __forceinline__ void load_src(const StageArgs& A, int sx, int row, Ro
 
 template <typename R>
 __device__ __forceinline__ void src_to_prim(const StageArgs& A, const RowSrc<R>& s, bool flipx,
-                                            R g, R g1, R out[4]) {
+                                            bool outlet_x, R g, R g1, R out[4]) {
   R r, u, v, p;
   if constexpr (Prec<R>::kind == 0) {
     if (A.Pin[0]) {
@@ -229,9 +251,12 @@ __device__ __forceinline__ void src_to_prim(const StageArgs& A, const RowSrc<R>&
       prim_from_cons(g, g1, r, s.c.y + s.d.y, s.c.z + s.d.z, s.c.w + s.d.w, u, v, p, cs);
     }
   }
+  u = flipx ? -u : u;
+  v = s.flipy ? -v : v;
+  if (outlet_x) outlet_ghost<R>(g, R(A.bc_p), r, u, v, p);
   out[0] = r;
-  out[1] = flipx ? -u : u;
-  out[2] = s.flipy ? -v : v;
+  out[1] = u;
+  out[2] = v;
   out[3] = p;
 }
 
@@ -259,6 +284,8 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
   const R g = R(A.gamma), g1 = R(A.gamma - 1.0);
   bool flipx;
   const int sx = map_index(min(gx, A.ni + NG - 1), A.ni, A.bc[SIDE_MX], A.bc[SIDE_PX], flipx);
+  // +x outlet ghost columns get the characteristic outflow state (lowest-priority BC)
+  const bool outlet_x = (A.bc[SIDE_PX] == BC_OUTLET) && (gx >= A.ni);
   const bool in_i_edge = (t >= NG - 1) && (t <= NG + W - 1) && (gx <= A.ni - 1);
   const bool in_cell = (t >= NG) && (t <= NG + W - 1) && (gx < A.ni);
   const double dt = *A.dt;
@@ -277,7 +304,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
     RowSrc<R> s;
     load_src<R>(A, sx, r, s);
     R q[4];
-    src_to_prim<R>(A, s, flipx, g, g1, q);
+    src_to_prim<R>(A, s, flipx, outlet_x, g, g1, q);
     R* row = ring + slot_of<RING>(r) * 4 * T;
 #pragma unroll
     for (int k = 0; k < 4; ++k) row[k * T + t] = q[k];
@@ -322,7 +349,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
     if (j + 1 < y1) load_src<R>(A, sx, j + 1 + NG, nxt);
     {
       R q[4];
-      src_to_prim<R>(A, pre, flipx, g, g1, q);
+      src_to_prim<R>(A, pre, flipx, outlet_x, g, g1, q);
       R* row = ring + slot_of<RING>(j + NG) * 4 * T;
 #pragma unroll
       for (int k = 0; k < 4; ++k) row[k * T + t] = q[k];
@@ -451,7 +478,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
 // Minimum resident 256-thread CTAs per SM requested from the register allocator for the
 // double-float kernels (their pair arithmetic is latency-bound; more warps hide it).
 #ifndef CATO_DF_MIN_BLOCKS
-#define CATO_DF_MIN_BLOCKS 1
+#define CATO_DF_MIN_BLOCKS 2
 #endif
 
 template <typename R, int NG, int FLUX, int RECON>

@@ -75,7 +75,9 @@ enum cato_rk {
 enum cato_bc {
   CATO_BC_ZERO_GRADIENT = 0, /* priority 1, zero_gradient_bc.f90:54-121 */
   CATO_BC_SYMMETRY = 1,      /* priority 1, symmetry_bc.f90:56-133 */
-  CATO_BC_PERIODIC = 2       /* priority 2, periodic_bc.fypp:78-283 */
+  CATO_BC_PERIODIC = 2,      /* priority 2, periodic_bc.fypp:78-283 */
+  CATO_BC_OUTLET = 3         /* priority 0, outlet_bc.f90:63-176: characteristic subsonic outflow
+                                to bc_pressure on +x, line copies on the other sides */
 };
 
 /* Sides in the reference's application order within one priority (flux_solver.f90:165-183). */
@@ -112,6 +114,7 @@ typedef struct cato_config {
   double ausm_kp;             /* [ausm] pressure_diffusion_coeff, default 0.25 */
   double ausm_ku;             /* K_u, default 0.75 (not read from the deck by the reference) */
   double ausm_sigma;          /* [ausm] sonic_point_sigma, default 1 */
+  double bc_pressure;         /* [boundary_conditions] outflow_ambient_pressure (CATO_BC_OUTLET) */
 } cato_config;
 
 typedef struct cato_handle cato_handle;

@@ -148,8 +148,46 @@ double oracle_limiter(int32_t lim, double r) {
 /* zero_gradient_bc.f90:64-119 (full-length rows/columns), symmetry_bc.f90:75-131,
  * periodic_bc.fypp:138-278 on a single image (x: rows jlo:jhi; y: columns ilo:ihi; corners
  * only when all four sides are periodic, periodic_bc.fypp:68-74). */
-static void apply_one_bc(dims_t d, int type, int side, int do_corners, double* f[4]) {
+/* outlet_bc.f90:83-175: on +x every ghost column (all j of the halo) takes the characteristic
+ * outflow state computed from the boundary column ihi; -x, +y, -y copy the boundary line
+ * (full length). */
+static void apply_outlet_px(dims_t d, double gamma, double p_b, double* f[4]) {
   const int ng = d.ng, ni = d.ni, nj = d.nj;
+  double *rho = f[0], *u = f[1], *v = f[2], *p = f[3];
+  for (int i = ni + 1; i <= ni + ng; ++i)
+    for (int j = 1 - ng; j <= nj + ng; ++j) {
+      double p_d = AT(p, ni, j), rho_0 = AT(rho, ni, j);
+      if (p_b > TINY && rho_0 > TINY) {
+        double cs = sqrt(gamma * fabs(p_d / rho_0));
+        double vel = sqrt(AT(u, ni, j) * AT(u, ni, j) + AT(v, ni, j) * AT(v, ni, j));
+        double mach = vel / cs;
+        double nx = AT(u, ni, j) / (vel + 1e-30);
+        double ny = AT(v, ni, j) / (vel + 1e-30);
+        if (mach > 1.0) {
+          AT(rho, i, j) = AT(rho, ni, j);
+          AT(u, i, j) = AT(u, ni, j);
+          AT(v, i, j) = AT(v, ni, j);
+          AT(p, i, j) = AT(p, ni, j);
+        } else {
+          AT(rho, i, j) = AT(rho, ni, j) + (p_b - p_d) / (cs * cs);
+          AT(u, i, j) = AT(u, ni, j) + nx * (p_d - p_b) / (rho_0 * cs);
+          AT(v, i, j) = AT(v, ni, j) + ny * (p_d - p_b) / (rho_0 * cs);
+          AT(p, i, j) = p_b;
+        }
+      }
+    }
+}
+
+static void apply_one_bc(dims_t d, int type, int side, int do_corners, double gamma,
+                         double p_b, double* f[4]) {
+  const int ng = d.ng, ni = d.ni, nj = d.nj;
+  if (type == CATO_BC_OUTLET) {
+    if (side == CATO_PLUS_X) {
+      apply_outlet_px(d, gamma, p_b, f);
+      return;
+    }
+    type = CATO_BC_ZERO_GRADIENT; /* the line copies of outlet_bc.f90:126-164 */
+  }
   for (int g = 1; g <= ng; ++g) {
     if (type == CATO_BC_ZERO_GRADIENT) {
       for (int k = 0; k < 4; ++k) {
@@ -213,7 +251,10 @@ static void apply_one_bc(dims_t d, int type, int side, int do_corners, double* f
   }
 }
 
-static int bc_priority(int type) { return type == CATO_BC_PERIODIC ? 2 : 1; }
+/* periodic 2, zero-gradient / symmetry 1, outlet 0 (boundary_conditions.f90, the constructors) */
+static int bc_priority(int type) {
+  return type == CATO_BC_PERIODIC ? 2 : (type == CATO_BC_OUTLET ? 0 : 1);
+}
 
 /* flux_solver_t%apply_primitive_bc, flux_solver.f90:138-185: priority high -> low and, within
  * one priority, +x, +y, -x, -y. */
@@ -226,7 +267,8 @@ int oracle_apply_bc(const cato_config* c, double* rho, double* u, double* v, dou
   for (int s = 0; s < 4; ++s) maxp = bc_priority(c->bc[s]) > maxp ? bc_priority(c->bc[s]) : maxp;
   for (int prio = maxp; prio >= 0; --prio)
     for (int s = 0; s < 4; ++s)
-      if (bc_priority(c->bc[s]) == prio) apply_one_bc(d, c->bc[s], s, all_periodic, f);
+      if (bc_priority(c->bc[s]) == prio)
+        apply_one_bc(d, c->bc[s], s, all_periodic, c->gamma, c->bc_pressure, f);
   return 0;
 }
 
@@ -236,7 +278,7 @@ int oracle_apply_bc_side(const cato_config* c, int side, int type, int do_corner
                          double* u, double* v, double* p) {
   dims_t d = mkdims(c);
   double* f[4] = {rho, u, v, p};
-  apply_one_bc(d, type, side, do_corners, f);
+  apply_one_bc(d, type, side, do_corners, c->gamma, c->bc_pressure, f);
   return 0;
 }
 
@@ -1177,8 +1219,12 @@ int oracle_config_check(const cato_config* c) {
   int need = (c->limiter == CATO_LIM_MLP5) ? 3 : 2; /* mod_input.f90:320-338 */
   if (c->n_ghost != need) return CATO_ERR_CONFIG;
   if (c->ni < c->n_ghost || c->nj < c->n_ghost) return CATO_ERR_CONFIG;
-  for (int s = 0; s < 4; ++s)
-    if (c->bc[s] < CATO_BC_ZERO_GRADIENT || c->bc[s] > CATO_BC_PERIODIC) return CATO_ERR_CONFIG;
+  int outlet = 0;
+  for (int s = 0; s < 4; ++s) {
+    if (c->bc[s] < CATO_BC_ZERO_GRADIENT || c->bc[s] > CATO_BC_OUTLET) return CATO_ERR_CONFIG;
+    outlet |= c->bc[s] == CATO_BC_OUTLET;
+  }
+  if (outlet && !(c->bc_pressure > 0.0)) return CATO_ERR_CONFIG; /* outlet_bc.f90:54-59 */
   /* periodic must be paired on an axis (an unpaired side leaves ghost cells unset) */
   if ((c->bc[CATO_PLUS_X] == CATO_BC_PERIODIC) != (c->bc[CATO_MINUS_X] == CATO_BC_PERIODIC))
     return CATO_ERR_CONFIG;

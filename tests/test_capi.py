@@ -33,7 +33,8 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_struct_layout():
-    assert ctypes.sizeof(CatoConfig) == 128
+    assert ctypes.sizeof(CatoConfig) == 136
+    assert CatoConfig.bc_pressure.offset == 128
     assert CatoConfig.gamma.offset == 56
 
 
