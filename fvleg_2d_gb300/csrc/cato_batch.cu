@@ -393,14 +393,7 @@ int cato_batch_add(cato_batch* b, const cato_config* cfg, const double* rho, con
   d.K64.harten = cfg->roe_entropy_fix == CATO_ROE_HARTEN ? 1 : 0;
   d.K32 = convert_consts<float>(d.K64);
   d.Kdf = convert_consts<df>(d.K64);
-  d.G.vol = (cfg->dx - 0.0) * (cfg->dy - 0.0) - (0.0 - 0.0) * (0.0 - 0.0);
-  double l[4] = {cfg->dx, cfg->dy, cfg->dx, cfg->dy};
-  double mx = l[0], mn = l[0];
-  for (int k = 1; k < 4; ++k) { mx = l[k] > mx ? l[k] : mx; mn = l[k] < mn ? l[k] : mn; }
-  if (mx - mn < 2.0 * 2.220446049250313080847263336181640625e-16) l[0] = l[1] = l[2] = l[3] = mx;
-  d.G.l1 = l[0]; d.G.l2 = l[1]; d.G.l3 = l[2]; d.G.l4 = l[3];
-  d.G.dx = cfg->dx;
-  d.G.dy = cfg->dy;
+  d.G = uniform_geom(cfg->dx, cfg->dy);
   const size_t cells = (size_t)d.pitch * d.nj, fb = cells * sizeof(double);
   bool ok = true;
   for (int k = 0; k < 4 && ok; ++k) {

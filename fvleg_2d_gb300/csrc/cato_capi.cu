@@ -146,18 +146,7 @@ static void fill_consts(cato_handle* h) {
   h->K64 = K;
   h->K32 = convert_consts<float>(K);
   h->Kdf = convert_consts<df>(K);
-  // quad_cell_t metrics of a dx x dy axis-aligned cell (quad_cell.f90:69-229): volume dx*dy,
-  // edge lengths dx, dy, dx, dy (all set to the largest when they differ by < 2 eps),
-  // min_dx = dx, min_dy = dy.
-  Geom G{};
-  G.vol = (c.dx - 0.0) * (c.dy - 0.0) - (0.0 - 0.0) * (0.0 - 0.0);
-  double l[4] = {c.dx, c.dy, c.dx, c.dy};
-  double mx = l[0], mn = l[0];
-  for (int k = 1; k < 4; ++k) { mx = l[k] > mx ? l[k] : mx; mn = l[k] < mn ? l[k] : mn; }
-  if (mx - mn < 2.0 * 2.220446049250313080847263336181640625e-16) l[0] = l[1] = l[2] = l[3] = mx;
-  G.l1 = l[0]; G.l2 = l[1]; G.l3 = l[2]; G.l4 = l[3];
-  G.dx = c.dx;
-  G.dy = c.dy;
+  const Geom G = uniform_geom(c.dx, c.dy);
   h->G = G;
 }
 

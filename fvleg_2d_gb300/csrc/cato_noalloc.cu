@@ -148,15 +148,7 @@ extern "C" int cato_gpu_solve_noalloc(const cato_config* cfg, double* rho, doubl
   K.ausm_sigma = cfg->ausm_sigma;
   K.low_mach_fix = cfg->apply_low_mach_fix ? 1 : 0;
   K.harten = cfg->roe_entropy_fix == CATO_ROE_HARTEN ? 1 : 0;
-  Geom G{};
-  G.vol = (cfg->dx - 0.0) * (cfg->dy - 0.0) - (0.0 - 0.0) * (0.0 - 0.0);
-  double l[4] = {cfg->dx, cfg->dy, cfg->dx, cfg->dy};
-  double mx = l[0], mn = l[0];
-  for (int k = 1; k < 4; ++k) { mx = l[k] > mx ? l[k] : mx; mn = l[k] < mn ? l[k] : mn; }
-  if (mx - mn < 2.0 * 2.220446049250313080847263336181640625e-16) l[0] = l[1] = l[2] = l[3] = mx;
-  G.l1 = l[0]; G.l2 = l[1]; G.l3 = l[2]; G.l4 = l[3];
-  G.dx = cfg->dx;
-  G.dy = cfg->dy;
+  const Geom G = uniform_geom(cfg->dx, cfg->dy);
 
   StageArgs A;
   std::memset(&A, 0, sizeof(A));

@@ -12,8 +12,9 @@
 // Reference citations are file:line in smillerc/fvleg_2d.
 #pragma once
 
-#include <cstdint>
 #include <cfloat>
+#include <cmath>
+#include <cstdint>
 #include <cuda_runtime.h>
 
 #include "cato_df.cuh"
@@ -34,7 +35,17 @@ template <typename R> struct Num;
 template <> struct Num<double> {
   static constexpr double eps = 2.220446049250313080847263336181640625e-16;  // epsilon(1.0_rk)
   static constexpr double tiny = 2.2250738585072013830902327173324040642e-308; // tiny(1.0_rk)
-  static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+  // IEEE a / b.  Two exact cases are decided on the integer pipe (GB300's FP64 pipe is its
+  // narrowest and a division costs ~10 of its instructions): a signed zero over a finite
+  // non-zero b is the zero with the sign of the product, and a / 1 is a.
+  static __device__ __forceinline__ double div(double a, double b) {
+    const unsigned long long ua = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long ub = (unsigned long long)__double_as_longlong(b);
+    if ((ua << 1) == 0ULL && (ub << 1) != 0ULL && ((ub >> 52) & 0x7ffULL) != 0x7ffULL)
+      return __longlong_as_double((long long)((ua ^ ub) & 0x8000000000000000ULL));
+    if (ub == 0x3ff0000000000000ULL) return a;
+    return a / b;
+  }
   static __device__ __forceinline__ double sqrt(double a) { return ::sqrt(a); }
 };
 
@@ -57,6 +68,30 @@ template <> struct Num<df> {
 template <typename R> __device__ __forceinline__ R rmax(R a, R b) { return (a < b) ? b : a; }
 template <typename R> __device__ __forceinline__ R rmin(R a, R b) { return (b < a) ? b : a; }
 template <> __device__ __forceinline__ float rmax<float>(float a, float b) { return fmaxf(a, b); }
+// FP64 compare-and-select on the integer pipe: the sign-magnitude bits map to a monotone signed
+// key (+0 and -0 share key 0); a NaN operand makes the comparison false, as in IEEE.
+__device__ __forceinline__ bool d_isnan(double x) {
+  return ((unsigned long long)__double_as_longlong(x) << 1) > 0xffe0000000000000ULL;
+}
+__device__ __forceinline__ long long d_key(double x) {
+  const long long b = __double_as_longlong(x);
+  return b >= 0 ? b : -(b & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool d_less(double a, double b) {
+  return d_key(a) < d_key(b) && !d_isnan(a) && !d_isnan(b);
+}
+template <> __device__ __forceinline__ double rmax<double>(double a, double b) {
+  return d_less(a, b) ? b : a;
+}
+template <> __device__ __forceinline__ double rmin<double>(double a, double b) {
+  return d_less(b, a) ? b : a;
+}
+// x <= 0 (false for NaN)
+template <typename R> __device__ __forceinline__ bool nonpos(R x) { return x <= R(0); }
+template <> __device__ __forceinline__ bool nonpos<double>(double x) {
+  const long long b = __double_as_longlong(x);
+  return (b < 0 || (b << 1) == 0) && !d_isnan(x);
+}
 template <> __device__ __forceinline__ float rmin<float>(float a, float b) { return fminf(a, b); }
 template <typename R> __device__ __forceinline__ R rabs(R a) { return fabs(a); }
 template <> __device__ __forceinline__ df rabs<df>(df a) { return df_abs(a); }
@@ -175,7 +210,10 @@ template <typename R>
 __device__ __forceinline__ R tvd_phi(int lim, R r) {
   if (lim == LIM_MINMOD) return rmax(R(0), rmin(r, R(1)));
   if (lim == LIM_SUPERBEE) return rmax(rmax(R(0), rmin(R(2) * r, R(1))), rmin(r, R(2)));
-  return Num<R>::div(r + rabs(r), R(1) + rabs(r)); // "vanleer" (muscl_tvd2.fypp:199-200)
+  // "vanleer" (muscl_tvd2.fypp:199-200); for r <= 0 the numerator r + |r| is +0 and so is
+  // the quotient (1 + |r| >= 1): skip the division
+  if (nonpos(r)) return R(0);
+  return Num<R>::div(r + rabs(r), R(1) + rabs(r));
 }
 
 template <typename R>
@@ -185,9 +223,8 @@ __device__ __forceinline__ void recon_tvd2(int lim, R qm1, R q0, R qp1, R qp2, R
   if (abs_lt(dm, EPS)) dm = R(0);
   if (abs_lt(d0, EPS)) d0 = R(0);
   if (abs_lt(dp, EPS)) dp = R(0);
-  // d0 == 0 gives r = 0 exactly (0/x); skip the division
-  R rL = (d0 == R(0)) ? R(0) * (dm + R(1e-16)) : Num<R>::div(d0, dm + R(1e-16));
-  R rR = (d0 == R(0)) ? R(0) * (dp + R(1e-16)) : Num<R>::div(d0, dp + R(1e-16));
+  R rL = Num<R>::div(d0, dm + R(1e-16));
+  R rR = Num<R>::div(d0, dp + R(1e-16));
   R phi = tvd_phi(lim, rL);
   L = q0 + R(0.5) * phi * dm;
   phi = tvd_phi(lim, rR);
@@ -721,7 +758,29 @@ __device__ __forceinline__ void flux_hllc(const FluxConsts<R>& K, const Prim<R>&
 struct Geom {
   double vol, l1, l2, l3, l4;  // volume, edge lengths (bottom, right, top, left)
   double dx, dy;               // min_dx / min_dy for the CFL step
+  double inv_vol;              // 1/vol when vol is a power of two (x/vol == x*inv_vol exactly), else 0
 };
+
+// quad_cell_t metrics of a dx x dy axis-aligned cell (quad_cell.f90:69-229): volume dx*dy,
+// edge lengths dx, dy, dx, dy (all set to the largest when they differ by < 2 eps),
+// min_dx = dx, min_dy = dy.
+inline Geom uniform_geom(double dx, double dy) {
+  Geom G{};
+  G.vol = (dx - 0.0) * (dy - 0.0) - (0.0 - 0.0) * (0.0 - 0.0);
+  double l[4] = {dx, dy, dx, dy};
+  double mx = l[0], mn = l[0];
+  for (int k = 1; k < 4; ++k) { mx = l[k] > mx ? l[k] : mx; mn = l[k] < mn ? l[k] : mn; }
+  if (mx - mn < 2.0 * 2.220446049250313080847263336181640625e-16) l[0] = l[1] = l[2] = l[3] = mx;
+  G.l1 = l[0]; G.l2 = l[1]; G.l3 = l[2]; G.l4 = l[3];
+  G.dx = dx;
+  G.dy = dy;
+  // a division by a power of two is the multiplication by its reciprocal, which is exactly
+  // representable: both round the same real number (power-of-two grids, e.g. 4096^2 on [0,1]^2)
+  int e = 0;
+  const double m = std::frexp(G.vol, &e);
+  G.inv_vol = (m == 0.5 && e > -1020 && e < 1020) ? 1.0 / G.vol : 0.0;
+  return G;
+}
 
 __device__ __forceinline__ double divergence_fp64(double Fi, double Fim, double Fj, double Fjm,
                                                   const Geom& G) {
@@ -739,7 +798,7 @@ __device__ __forceinline__ double divergence_fp64(double Fi, double Fim, double 
   if (rabs(b) < mj * REL_TOL) b = 0.0;
   double s = a + b;
   if (abs_lt(s, NEAR0)) s = 0.0;
-  return (-s) / G.vol;
+  return G.inv_vol != 0.0 ? (-s) * G.inv_vol : (-s) / G.vol;
 }
 
 }  // namespace cato
