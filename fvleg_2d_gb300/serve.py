@@ -206,3 +206,47 @@ def run_alone(req: Request) -> dict:
     out["steps"], out["error_code"] = q["iteration"], q["error_code"]
     b.close()
     return out
+
+
+def main(argv=None) -> int:
+    """Rate sweep of the request stream, one JSON line per rate:
+
+        python -m fvleg_2d_gb300.serve --rates 10,20,50,100,200,500 --requests 200 \\
+            --side 128,2048 --max-wall 30 --precision mixed
+    """
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--rates", default="10,20,50,100,200,500")
+    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--side", default="128,2048")
+    ap.add_argument("--t-end", default="0.05,0.3")
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed", "mixed_df"])
+    ap.add_argument("--budget-gb", type=float, default=120.0)
+    ap.add_argument("--capacity", type=int, default=1024)
+    ap.add_argument("--chunk", type=int, default=16)
+    ap.add_argument("--max-wall", type=float, default=30.0)
+    ap.add_argument("--seed", type=int, default=7)
+    a = ap.parse_args(argv)
+    side = tuple(int(x) for x in a.side.split(","))
+    t_end = tuple(float(x) for x in a.t_end.split(","))
+    for rate in (float(x) for x in a.rates.split(",")):
+        reqs = make_requests(a.requests, rate=rate, seed=a.seed, side=side, t_end=t_end,
+                             precision=a.precision)
+        srv = Server(precision=a.precision, budget_gb=a.budget_gb, capacity=a.capacity,
+                     chunk_steps=a.chunk)
+        st = srv.serve(reqs, max_wall_s=a.max_wall)
+        srv.close()
+        out = st.summary()
+        offered = sum(r.n * r.n for r in reqs if r.arrival <= st.wall_s)
+        out.update({"rate_per_s": rate, "precision": a.precision, "side": list(side),
+                    "arrived": sum(1 for r in reqs if r.arrival <= st.wall_s),
+                    "completed_per_s": len(st.completed) / st.wall_s if st.wall_s else None,
+                    "arrived_cells": offered})
+        print(json.dumps(out), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
