@@ -480,9 +480,16 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
 #ifndef CATO_DF_MIN_BLOCKS
 #define CATO_DF_MIN_BLOCKS 2
 #endif
+// the same for the FP32 (mixed) kernels
+#ifndef CATO_F32_MIN_BLOCKS
+#define CATO_F32_MIN_BLOCKS 1
+#endif
+template <typename R> constexpr int min_blocks() {
+  return Prec<R>::kind == 2 ? CATO_DF_MIN_BLOCKS : (Prec<R>::kind == 1 ? CATO_F32_MIN_BLOCKS : 1);
+}
 
 template <typename R, int NG, int FLUX, int RECON>
-__global__ void __launch_bounds__(256, (Prec<R>::kind == 2 ? CATO_DF_MIN_BLOCKS : 1))
+__global__ void __launch_bounds__(256, min_blocks<R>())
     stage_kernel(const StageArgs A, const FluxConsts<R> K) {
   if (A.active && *A.active == 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];

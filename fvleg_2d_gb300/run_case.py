@@ -39,6 +39,7 @@ def main(argv=None) -> int:
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed_df"])
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--plan", default="", help="threads,rows_per_cta (default: the handle's)")
     ap.add_argument("--t-start", type=float, default=0.0,
                     help="first advance the flow to this time with the mixed path")
     a = ap.parse_args(argv)
@@ -50,6 +51,8 @@ def main(argv=None) -> int:
         prims = [s["rho"], s["u"], s["v"], s["p"]]
         g.close()
     f = Fluid(cfg).initialize(*prims)
+    if a.plan:
+        f.set_plan(*(int(x) for x in a.plan.split(",")))
     ms, kern = f.run_timed(a.steps, per_kernel=True)
     cells = cfg.ni * cfg.nj
     print(json.dumps({"workload": a.workload, "ni": cfg.ni, "nj": cfg.nj,
