@@ -1,0 +1,251 @@
+"""Input decks: the reference's ``.ini`` format read into the hot path's configuration.
+
+Follows ``input_t%read_from_ini`` (``src/lib/io/mod_input.f90:194-445``): the same sections,
+keys and defaults (``mod_input.f90:34-155``).  Values may be quoted with single or double quotes,
+``;`` and ``#`` start comments, logicals are ``true``/``.true.``/``t`` (any case) and reals may
+use a Fortran ``d`` exponent.
+
+A deck whose initial conditions come from an HDF5 file (``read_from_file = true``) needs the grid
+size and spacing from that file: pass ``ni, nj, dx, dy`` to :meth:`Deck.scheme` and upload the
+file's primitives through :class:`fvleg_2d_gb300.fluid.Fluid` (there is no HDF5 library in this
+build).  A deck with ``read_from_file = false`` is complete: its uniform initial state and grid
+come from the deck (``[initial_conditions] init_*``, ``[grid] ni_nodes ... ymax``).
+"""
+from __future__ import annotations
+
+import configparser
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .config import BC_IDS, FLUX_IDS, LIMITER_IDS, RK_IDS, SchemeConfig
+
+_TRUE = {"true", ".true.", "t", "yes", "on", "1"}
+_FALSE = {"false", ".false.", "f", "no", "off", "0"}
+
+
+class DeckError(ValueError):
+    """An invalid deck (the reference stops with error_msg in the same situations)."""
+
+
+def _strip(v: str) -> str:
+    v = v.strip()
+    if len(v) >= 2 and v[0] == v[-1] and v[0] in "'\"":
+        v = v[1:-1]
+    return v.strip()
+
+
+def _real(v: str) -> float:
+    return float(_strip(v).replace("d", "e").replace("D", "e"))
+
+
+def _logical(v: str) -> bool:
+    s = _strip(v).lower()
+    if s in _TRUE:
+        return True
+    if s in _FALSE:
+        return False
+    raise DeckError(f"not a logical: {v!r}")
+
+
+@dataclass
+class Deck:
+    # [general]
+    title: str = ""
+    units: str = "cgs"
+    # [reference_state]
+    non_dimensionalize: bool = True
+    reference_length: float = 1.0
+    reference_density: float = 1.0
+    reference_velocity: float = 1.0
+    # [time]
+    max_time: float = 1.0
+    initial_delta_t: float = 0.0
+    use_constant_delta_t: bool = False
+    cfl: float = 0.1
+    integration_strategy: str = ""
+    max_iterations: int = 2**31 - 1
+    allow_subcycle: bool = False
+    # [physics]
+    polytropic_index: float = 5.0 / 3.0
+    # [scheme]
+    flux_solver: str = "AUSMPW+"
+    spatial_reconstruction: str = "MUSCL"
+    limiter: str = "minmod"
+    apply_low_mach_fix: bool = True
+    # [ausm] (read only for AUSM+-up, mod_input.f90:262-267)
+    ausm_beta: float = 1.0 / 8.0
+    ausm_pressure_diffusion_coeff: float = 0.25
+    ausm_pressure_flux_coeff: float = 0.75
+    ausm_sonic_point_sigma: float = 1.0
+    # [initial_conditions]
+    read_from_file: bool = True
+    initial_condition_file: str = ""
+    init_density: float = 0.0
+    init_x_velocity: float = 0.0
+    init_y_velocity: float = 0.0
+    init_pressure: float = 0.0
+    # [grid]
+    n_ghost_layers: int = 2
+    grid_type: str = "2d_regular"
+    ni_nodes: int = 0
+    nj_nodes: int = 0
+    xmin: float = 0.0
+    xmax: float = 0.0
+    ymin: float = 0.0
+    ymax: float = 0.0
+    # [boundary_conditions]
+    bc: dict = field(default_factory=lambda: {s: "periodic" for s in ("+x", "-x", "+y", "-y")})
+    outflow_ambient_pressure: float = 0.0
+    # [io]
+    contour_interval_dt: float = 0.1
+    contour_format: str = "xdmf"
+
+    def scheme(self, ni: int | None = None, nj: int | None = None, dx: float | None = None,
+               dy: float | None = None, precision: str = "fp64") -> SchemeConfig:
+        """The hot path's configuration of this deck on an ni x nj grid of dx x dy cells (from
+        the deck's own grid keys when the initial state is not read from a file)."""
+        if ni is None:
+            ni, nj, dx, dy = self.grid()
+        strategy = self.integration_strategy
+        if strategy not in RK_IDS:
+            raise DeckError(f"integration_strategy {strategy!r} is not supported "
+                            f"(one of {sorted(RK_IDS)}; 'ssp_rk43' is a no-op in the reference)")
+        if self.flux_solver not in FLUX_IDS:
+            raise DeckError(f"flux_solver {self.flux_solver!r} is not supported ({sorted(FLUX_IDS)})")
+        if self.limiter not in LIMITER_IDS:
+            raise DeckError(f"limiter {self.limiter!r} is not supported ({sorted(LIMITER_IDS)})")
+        for side, name in self.bc.items():
+            if name not in BC_IDS:
+                raise DeckError(f"boundary condition {name!r} at {side} is not supported")
+        return SchemeConfig(
+            ni=int(ni), nj=int(nj), dx=float(dx), dy=float(dy), flux_solver=self.flux_solver,
+            limiter=self.limiter, integration_strategy=strategy, bc=dict(self.bc),
+            gamma=self.polytropic_index, cfl=self.cfl,
+            apply_low_mach_fix=self.apply_low_mach_fix, precision=precision,
+            ausm_beta=self.ausm_beta, ausm_kp=self.ausm_pressure_diffusion_coeff,
+            ausm_ku=self.ausm_pressure_flux_coeff, ausm_sigma=self.ausm_sonic_point_sigma,
+            outflow_ambient_pressure=self.outflow_ambient_pressure,
+            n_ghost=self.n_ghost_layers)
+
+    def grid(self) -> tuple[int, int, float, float]:
+        """(ni, nj, dx, dy) of a deck-defined uniform grid: nodes - 1 cells per direction."""
+        if self.read_from_file:
+            raise DeckError("the grid comes from the initial condition file; pass ni, nj, dx, dy")
+        if self.ni_nodes < 2 or self.nj_nodes < 2:
+            raise DeckError("[grid] ni_nodes and nj_nodes must be >= 2")
+        ni, nj = self.ni_nodes - 1, self.nj_nodes - 1
+        return ni, nj, (self.xmax - self.xmin) / ni, (self.ymax - self.ymin) / nj
+
+    def initial_primitives(self, cfg: SchemeConfig) -> list[np.ndarray]:
+        """The uniform initial state of [initial_conditions] init_* (halo-padded, ghosts 0)."""
+        if self.read_from_file:
+            raise DeckError("the initial state comes from a file: upload its primitives")
+        g = cfg.ghost_layers()
+        out = []
+        for val in (self.init_density, self.init_x_velocity, self.init_y_velocity,
+                    self.init_pressure):
+            a = np.zeros(cfg.halo_shape, order="F")
+            a[g:g + cfg.ni, g:g + cfg.nj] = val
+            out.append(a)
+        return out
+
+
+def _ghost_layers_for(limiter: str) -> int:
+    """mod_input.f90:318-338: the ghost layers an edge interpolation scheme needs."""
+    if limiter in ("minmod", "superbee", "van_leer", "vanleer", "none", "TVD2", "TVD3", "MLP3",
+                   "eMLP3"):
+        return 2
+    if limiter in ("TVD5", "MLP5", "eMLP5"):
+        return 3
+    raise DeckError("Unknown edge interpolation scheme, must be one of the following: "
+                    "'TVD2', 'TVD3', 'TVD5', 'MLP3', or 'MLP5'")
+
+
+def parse_deck(text: str) -> Deck:
+    """Parse the text of an input deck."""
+    cp = configparser.ConfigParser(inline_comment_prefixes=(";", "#"),
+                                   comment_prefixes=(";", "#"), interpolation=None, strict=False)
+    cp.read_string(text)
+
+    def get(sec, key, conv=_strip, default=None, required=False):
+        if cp.has_option(sec, key):
+            return conv(cp.get(sec, key))
+        if required:
+            raise DeckError(f"[{sec}] {key} is required")
+        return default
+
+    d = Deck()
+    d.title = get("general", "title", default="")
+    d.units = get("general", "units", default="cgs")
+    d.non_dimensionalize = get("reference_state", "non_dimensionalize", _logical, True)
+    if d.non_dimensionalize:
+        d.reference_length = get("reference_state", "reference_length", _real, 1.0)
+        d.reference_density = get("reference_state", "reference_density", _real, 1.0)
+        d.reference_velocity = get("reference_state", "reference_velocity", _real, 1.0)
+    d.max_time = get("time", "max_time", _real, required=True)
+    d.initial_delta_t = get("time", "initial_delta_t", _real, 0.0)
+    d.use_constant_delta_t = get("time", "use_constant_delta_t", _logical, False)
+    d.cfl = get("time", "cfl", _real, 0.1)
+    d.integration_strategy = get("time", "integration_strategy", required=True)
+    d.max_iterations = get("time", "max_iterations", lambda v: int(_real(v)), 2**31 - 1)
+    d.allow_subcycle = get("time", "allow_subcycle", _logical, False)
+    d.polytropic_index = get("physics", "polytropic_index", _real, required=True)
+    d.flux_solver = get("scheme", "flux_solver", required=True)
+    if d.flux_solver == "AUSM+-up":
+        d.ausm_beta = get("ausm", "beta", _real, 1.0 / 8.0)
+        d.ausm_pressure_diffusion_coeff = get("ausm", "pressure_diffusion_coeff", _real, 0.25)
+        d.ausm_pressure_flux_coeff = get("ausm", "pressure_flux_coeff", _real, 0.75)
+        d.ausm_sonic_point_sigma = get("ausm", "sonic_point_sigma", _real, 1.0)
+    d.spatial_reconstruction = get("scheme", "spatial_reconstruction", default="MUSCL")
+    d.limiter = get("scheme", "limiter", default="minmod")
+    d.apply_low_mach_fix = get("scheme", "apply_low_mach_fix", _logical, True)
+    d.read_from_file = get("initial_conditions", "read_from_file", _logical, True)
+    if d.read_from_file:
+        d.initial_condition_file = get("initial_conditions", "initial_condition_file",
+                                       required=True)
+    d.init_density = get("initial_conditions", "init_density", _real, 0.0)
+    d.init_x_velocity = get("initial_conditions", "init_x_velocity", _real, 0.0)
+    d.init_y_velocity = get("initial_conditions", "init_y_velocity", _real, 0.0)
+    d.init_pressure = get("initial_conditions", "init_pressure", _real, 0.0)
+    need = _ghost_layers_for(d.limiter)
+    d.n_ghost_layers = get("grid", "n_ghost_layers", lambda v: int(_real(v)), need)
+    if d.n_ghost_layers != need:
+        raise DeckError("The number of required ghost cell layers doesn't match the edge "
+                        "interpolation order")
+    d.grid_type = get("grid", "grid_type", default="2d_regular")
+    if not d.read_from_file:
+        d.ni_nodes = get("grid", "ni_nodes", lambda v: int(_real(v)), required=True)
+        d.nj_nodes = get("grid", "nj_nodes", lambda v: int(_real(v)), required=True)
+        d.xmin = get("grid", "xmin", _real, required=True)
+        d.xmax = get("grid", "xmax", _real, required=True)
+        d.ymin = get("grid", "ymin", _real, required=True)
+        d.ymax = get("grid", "ymax", _real, required=True)
+    for side, key in (("+x", "plus_x"), ("-x", "minus_x"), ("+y", "plus_y"), ("-y", "minus_y")):
+        d.bc[side] = get("boundary_conditions", key, default="periodic")
+    if "outflow" in d.bc.values():
+        d.outflow_ambient_pressure = get("boundary_conditions", "outflow_ambient_pressure", _real,
+                                         required=True)
+    d.contour_format = get("io", "format", default=get("io", "contour_format", default="xdmf"))
+    d.contour_interval_dt = get("io", "contour_interval_dt", _real, 0.1)
+    return d
+
+
+def read_deck(path: str) -> Deck:
+    """Read an input deck file (``cato.x input.ini``'s argument)."""
+    with open(path) as f:
+        return parse_deck(f.read())
+
+
+def run_deck(deck: Deck, precision: str = "fp64", prims=None, grid=None):
+    """The main.f90 time loop for a deck: returns (fluid, steps).  For a deck that reads its
+    initial state from a file, pass that state as ``prims`` (rho, u, v, p, halo-padded) and its
+    grid as ``grid=(ni, nj, dx, dy)``."""
+    from .fluid import Fluid
+
+    cfg = deck.scheme(*(grid or (None, None, None, None)), precision=precision)
+    if prims is None:
+        prims = deck.initial_primitives(cfg)
+    fluid = Fluid(cfg).initialize(*prims)
+    steps = fluid.run(deck.max_time, deck.max_iterations)
+    return fluid, steps
