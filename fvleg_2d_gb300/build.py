@@ -1,7 +1,8 @@
 """Build the sm_103a C-ABI library ``libcato_gpu.so`` in-tree (``fvleg_2d_gb300/_lib/``).
 
 The stage kernel family is instantiated once per (precision, flux) pair from ``stage_inst.cu``
-so the 24 translation units compile in parallel; the FP64 units and the helper kernels are built
+(the double-float ones once per reconstruction and kernel kind) so that the units compile in
+parallel; the FP64 units and the helper kernels are built
 with ``--fmad=false`` (each reference operation rounds on its own), the FP32 mixed units with
 FMA contraction, fast square root and flush-to-zero, the double-float units with FMA contraction
 and IEEE FP32 semantics (their pair arithmetic is written with explicitly rounded intrinsics).
@@ -23,7 +24,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "libcato_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-N_FLUX = 8
+N_FLUX = 9
 
 
 def nvcc() -> str:
@@ -51,14 +52,25 @@ def _units() -> list[tuple[str, list[str]]]:
     # developer knob: extra nvcc flags for every unit (e.g. -DCATO_DF_MIN_BLOCKS=2)
     common += os.environ.get("CATO_NVCC_FLAGS", "").split()
     units = []
+    src = os.path.join(CSRC, "stage_inst.cu")
     for real, flags in (("double", ["--fmad=false"]),
                         ("float", ["--fmad=true", "-prec-sqrt=false", "-ftz=true"]),
                         ("df", ["--fmad=true"])):
         for flux in range(N_FLUX):
-            obj = os.path.join(BUILD_DIR, f"stage_{real}_{flux}.o")
-            cmd = [nvcc(), *ARCH, *common, *flags, f"-DCATO_REAL={real}",
-                   f"-DCATO_FLUX={flux}", "-c", os.path.join(CSRC, "stage_inst.cu"), "-o", obj]
-            units.append((obj, cmd))
+            # the double-float kernels take ~10x longer in ptxas: one unit per reconstruction
+            # and kernel kind keeps every unit under a minute
+            parts = ([(rc, part) for rc in (0, 3, 5) for part in (1, 2)] if real == "df"
+                     else [(None, 0)])
+            for rc, part in parts:
+                tag = f"stage_{real}_{flux}" + ("" if rc is None else f"_r{rc}_k{part}")
+                obj = os.path.join(BUILD_DIR, tag + ".o")
+                defs = [f"-DCATO_REAL={real}", f"-DCATO_FLUX={flux}"]
+                if rc is not None:
+                    defs += [f"-DCATO_RECON={rc}", f"-DCATO_PART={part}"]
+                cmd = [nvcc(), *ARCH, *common, *flags, *defs, "-c", src, "-o", obj]
+                units.append((obj, cmd))
+    # longest first, so that the slow double-float units start before the rest
+    units.sort(key=lambda u: 0 if "-DCATO_REAL=df" in u[1] else 1)
     for src in ("cato_capi.cu", "cato_batch.cu", "cato_noalloc.cu"):
         path = os.path.join(CSRC, src)
         if not os.path.exists(path):

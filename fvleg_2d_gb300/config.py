@@ -22,6 +22,7 @@ FLUX_IDS = {
     "Roe": 5,
     "AUSM+-up": 6,
     "HLLC": 7,
+    "M-AUSMPW+": 8,
 }
 LIMITER_IDS = {"minmod": 0, "superbee": 1, "van_leer": 2, "vanleer": 2, "MLP3": 3, "MLP5": 4}
 RK_IDS = {

@@ -338,7 +338,7 @@ int cato_config_default(cato_config* c, int32_t ni, int32_t nj) {
 int cato_config_check(const cato_config* c) {
   if (!c) return CATO_ERR_ARG;
   if (c->ni < 1 || c->nj < 1) return CATO_ERR_CONFIG;
-  if (c->flux < CATO_FLUX_AUSMPW_PLUS || c->flux > CATO_FLUX_HLLC) return CATO_ERR_CONFIG;
+  if (c->flux < CATO_FLUX_AUSMPW_PLUS || c->flux > CATO_FLUX_M_AUSMPW_PLUS) return CATO_ERR_CONFIG;
   if (c->limiter < CATO_LIM_MINMOD || c->limiter > CATO_LIM_MLP5) return CATO_ERR_CONFIG;
   if (c->rk < CATO_RK_SSP2 || c->rk > CATO_RK_2_5) return CATO_ERR_CONFIG;
   const int need = (c->limiter == CATO_LIM_MLP5) ? 3 : 2;  // mod_input.f90:320-338

@@ -10,10 +10,6 @@
 
 namespace cato {
 
-// recon: 0 = TVD2 (minmod / superbee / van Leer), 3 = MLP3, 5 = MLP5
-template <typename R, int FLUX>
-cudaError_t launch_stage_flux(int recon, dim3 grid, int threads, cudaStream_t stream,
-                              const StageArgs& A, const FluxConsts<R>& K);
 
 template <typename R, int NG, int FLUX, int RECON>
 cudaError_t launch_stage_one(dim3 grid, int threads, cudaStream_t stream, const StageArgs& A,
@@ -32,9 +28,10 @@ cudaError_t launch_stage_one(dim3 grid, int threads, cudaStream_t stream, const 
   return cudaGetLastError();
 }
 
+// recon: 0 = TVD2 (minmod / superbee / van Leer), 3 = MLP3, 5 = MLP5
 template <typename R, int FLUX>
-cudaError_t launch_stage_flux(int recon, dim3 grid, int threads, cudaStream_t stream,
-                              const StageArgs& A, const FluxConsts<R>& K) {
+inline cudaError_t launch_stage_flux(int recon, dim3 grid, int threads, cudaStream_t stream,
+                                     const StageArgs& A, const FluxConsts<R>& K) {
   switch (recon) {
     case 0: return launch_stage_one<R, 2, FLUX, 0>(grid, threads, stream, A, K);
     case 3: return launch_stage_one<R, 2, FLUX, 3>(grid, threads, stream, A, K);
@@ -72,8 +69,8 @@ cudaError_t launch_batch_one(int threads, cudaStream_t stream, const BatchStageA
 }
 
 template <typename R, int FLUX>
-cudaError_t launch_batch_flux(int recon, int threads, cudaStream_t stream,
-                              const BatchStageArgs& B) {
+inline cudaError_t launch_batch_flux(int recon, int threads, cudaStream_t stream,
+                                     const BatchStageArgs& B) {
   switch (recon) {
     case 0: return launch_batch_one<R, 2, FLUX, 0>(threads, stream, B);
     case 3: return launch_batch_one<R, 2, FLUX, 3>(threads, stream, B);
@@ -82,21 +79,27 @@ cudaError_t launch_batch_flux(int recon, int threads, cudaStream_t stream,
   }
 }
 
-#define CATO_DECLARE_STAGE(R, F)                                                             \
-  extern template cudaError_t launch_stage_flux<R, F>(int, dim3, int, cudaStream_t,         \
-                                                      const StageArgs&, const FluxConsts<R>&); \
-  extern template cudaError_t launch_batch_flux<R, F>(int, int, cudaStream_t,               \
-                                                      const BatchStageArgs&);
-CATO_DECLARE_STAGE(double, 0) CATO_DECLARE_STAGE(double, 1) CATO_DECLARE_STAGE(double, 2)
-CATO_DECLARE_STAGE(double, 3) CATO_DECLARE_STAGE(double, 4) CATO_DECLARE_STAGE(double, 5)
-CATO_DECLARE_STAGE(double, 6) CATO_DECLARE_STAGE(double, 7)
-CATO_DECLARE_STAGE(float, 0) CATO_DECLARE_STAGE(float, 1) CATO_DECLARE_STAGE(float, 2)
-CATO_DECLARE_STAGE(float, 3) CATO_DECLARE_STAGE(float, 4) CATO_DECLARE_STAGE(float, 5)
-CATO_DECLARE_STAGE(float, 6) CATO_DECLARE_STAGE(float, 7)
-CATO_DECLARE_STAGE(df, 0) CATO_DECLARE_STAGE(df, 1) CATO_DECLARE_STAGE(df, 2)
-CATO_DECLARE_STAGE(df, 3) CATO_DECLARE_STAGE(df, 4) CATO_DECLARE_STAGE(df, 5)
-CATO_DECLARE_STAGE(df, 6) CATO_DECLARE_STAGE(df, 7)
+// Every (precision, NG, flux, reconstruction) kernel is instantiated in exactly one translation
+// unit (stage_inst.cu, compiled once per precision and flux, and for the slow double-float units
+// once per reconstruction and kernel kind); everywhere else these are extern.
+#define CATO_DECLARE_ONE(R, F, NG, RC)                                                         \
+  extern template cudaError_t launch_stage_one<R, NG, F, RC>(dim3, int, cudaStream_t,          \
+                                                             const StageArgs&,                 \
+                                                             const FluxConsts<R>&);            \
+  extern template cudaError_t launch_batch_one<R, NG, F, RC>(int, cudaStream_t,               \
+                                                             const BatchStageArgs&);
+#define CATO_DECLARE_STAGE(R, F) \
+  CATO_DECLARE_ONE(R, F, 2, 0) CATO_DECLARE_ONE(R, F, 2, 3) CATO_DECLARE_ONE(R, F, 3, 5)
+#define CATO_DECLARE_PREC(R)                                                      \
+  CATO_DECLARE_STAGE(R, 0) CATO_DECLARE_STAGE(R, 1) CATO_DECLARE_STAGE(R, 2)      \
+  CATO_DECLARE_STAGE(R, 3) CATO_DECLARE_STAGE(R, 4) CATO_DECLARE_STAGE(R, 5)      \
+  CATO_DECLARE_STAGE(R, 6) CATO_DECLARE_STAGE(R, 7) CATO_DECLARE_STAGE(R, 8)
+CATO_DECLARE_PREC(double)
+CATO_DECLARE_PREC(float)
+CATO_DECLARE_PREC(df)
+#undef CATO_DECLARE_PREC
 #undef CATO_DECLARE_STAGE
+#undef CATO_DECLARE_ONE
 
 template <typename R>
 inline cudaError_t launch_stage(int flux, int recon, dim3 grid, int threads, cudaStream_t s,
@@ -110,6 +113,7 @@ inline cudaError_t launch_stage(int flux, int recon, dim3 grid, int threads, cud
     case 5: return launch_stage_flux<R, 5>(recon, grid, threads, s, A, K);
     case 6: return launch_stage_flux<R, 6>(recon, grid, threads, s, A, K);
     case 7: return launch_stage_flux<R, 7>(recon, grid, threads, s, A, K);
+    case 8: return launch_stage_flux<R, 8>(recon, grid, threads, s, A, K);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -126,6 +130,7 @@ inline cudaError_t launch_batch(int flux, int recon, int threads, cudaStream_t s
     case 5: return launch_batch_flux<R, 5>(recon, threads, s, B);
     case 6: return launch_batch_flux<R, 6>(recon, threads, s, B);
     case 7: return launch_batch_flux<R, 7>(recon, threads, s, B);
+    case 8: return launch_batch_flux<R, 8>(recon, threads, s, B);
     default: return cudaErrorInvalidValue;
   }
 }

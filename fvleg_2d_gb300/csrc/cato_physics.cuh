@@ -22,7 +22,7 @@
 namespace cato {
 
 enum { FLUX_AUSMPW = 0, FLUX_SLAU = 1, FLUX_SLAU2 = 2, FLUX_SD_SLAU = 3, FLUX_SD_SLAU2 = 4,
-       FLUX_ROE = 5, FLUX_AUSM_UP = 6, FLUX_HLLC = 7 };
+       FLUX_ROE = 5, FLUX_AUSM_UP = 6, FLUX_HLLC = 7, FLUX_M_AUSMPW = 8 };
 enum { LIM_MINMOD = 0, LIM_SUPERBEE = 1, LIM_VANLEER = 2, LIM_MLP3 = 3, LIM_MLP5 = 4 };
 enum { BC_ZERO_GRADIENT = 0, BC_SYMMETRY = 1, BC_PERIODIC = 2, BC_OUTLET = 3 };
 enum { SIDE_PX = 0, SIDE_PY = 1, SIDE_MX = 2, SIDE_MY = 3 };
@@ -503,6 +503,120 @@ __device__ __forceinline__ void flux_ausmpw(const FluxConsts<R>& K, const Prim<R
     F[2] = (mL * v_LHS) + (mR * v_RHS) + pterm;
   }
   F[3] = (mL * H_L) + (mR * H_R);
+}
+
+// M-AUSMPW+, the active code of m_ausmpw_plus_solver.fypp:437-708: AUSMPW+'s interface Mach
+// number and w sensor, pressure splitting without the alpha term (:600-610), the shock sensor f
+// with 1e-10 cuts (get_f, :804-843), interface states blended towards the superbee edge states
+// (phi_L_half / phi_R_half, :768-800; As, Bs) and flux cuts at epsilon*1e3 (:369, :684-705).
+// U_L/U_R/V_L/V_R are taken before the low-Mach fix, as in the reference.
+template <typename R>
+__device__ __forceinline__ R mausm_p_plus(R M) {
+  if (rabs(M) > R(1)) return R(0.5) * (R(1) + fsign1(M));
+  return R(0.25) * ((M + R(1)) * (M + R(1))) * (R(2) - M);
+}
+template <typename R>
+__device__ __forceinline__ R mausm_p_minus(R M) {
+  if (rabs(M) > R(1)) return R(0.5) * (R(1) - fsign1(M));
+  return R(0.25) * ((M - R(1)) * (M - R(1))) * (R(2) + M);
+}
+template <typename R>
+__device__ __forceinline__ R mausm_phi_L(R pL, R pR, R pLsb, R a) {
+  if (rabs(pR - pL) < R(1) || rabs(pLsb - pL) < Num<R>::eps) return pL;
+  return pL + Num<R>::div(rmax(R(0), (pR - pL) * (pLsb - pL)), (pR - pL) * rabs(pLsb - pL)) *
+                  rmin(rmin(a, R(0.5) * rabs(pR - pL)), rabs(pLsb - pL));
+}
+template <typename R>
+__device__ __forceinline__ R mausm_phi_R(R pL, R pR, R pRsb, R a) {
+  if (rabs(pL - pR) < Num<R>::eps || rabs(pRsb - pR) < R(1)) return pR;
+  return pR + Num<R>::div(rmax(R(0), (pL - pR) * (pRsb - pR)), (pL - pR) * rabs(pRsb - pR)) *
+                  rmin(rmin(a, R(0.5) * rabs(pL - pR)), rabs(pRsb - pR));
+}
+
+template <typename R, int DIR>
+__device__ __forceinline__ void flux_mausmpw(const FluxConsts<R>& K, const Prim<R>& A,
+                                             const Prim<R>& B, const Prim<R>& As,
+                                             const Prim<R>& Bs, const R pc[4], R F[4]) {
+  const R g = R(K.gamma);
+  const R EPSF = R(2.220446049250313080847263336181640625e-13);  // epsilon(1.0_rk) * 1e3_rk
+  const R CUT = R(1e-10);
+  R rho_L = A.r, u_LHS = A.u, v_LHS = A.v, p_L = A.p;
+  R rho_R = B.r, u_RHS = B.u, v_RHS = B.v, p_R = B.p;
+  const R U_L = DIR == 0 ? u_LHS : v_LHS, U_R = DIR == 0 ? u_RHS : v_RHS;
+  const R V_L = DIR == 0 ? v_LHS : u_LHS, V_R = DIR == 0 ? v_RHS : u_RHS;
+  R cs_L = Num<R>::sqrt(Num<R>::div(g * p_L, rho_L));
+  R cs_R = Num<R>::sqrt(Num<R>::div(g * p_R, rho_R));
+  R M_LHS = Num<R>::div(Num<R>::sqrt(u_LHS * u_LHS + v_LHS * v_LHS), cs_L);
+  R M_RHS = Num<R>::div(Num<R>::sqrt(u_RHS * u_RHS + v_RHS * v_RHS), cs_R);
+  if (K.low_mach_fix && (rabs(M_LHS) < R(0.1) || rabs(M_RHS) < R(0.1))) {  // LOW_MACH
+    R f_M = rmin(R(1), rmax(M_LHS, M_RHS));
+    R uLf = R(0.5) * (u_LHS + u_RHS) + f_M * R(0.5) * (u_LHS - u_RHS);
+    R uRf = R(0.5) * (u_LHS + u_RHS) - f_M * R(0.5) * (u_LHS - u_RHS);
+    R vLf = R(0.5) * (v_LHS + v_RHS) + f_M * R(0.5) * (v_LHS - v_RHS);
+    R vRf = R(0.5) * (v_LHS + v_RHS) - f_M * R(0.5) * (v_LHS - v_RHS);
+    u_LHS = uLf; u_RHS = uRf; v_LHS = vLf; v_RHS = vRf;
+  }
+  const R gg = R(K.g_over_gm1);
+  R H_L = gg * Num<R>::div(p_L, rho_L) + R(0.5) * (u_LHS * u_LHS + v_LHS * v_LHS);
+  R H_R = gg * Num<R>::div(p_R, rho_R) + R(0.5) * (u_RHS * u_RHS + v_RHS * v_RHS);
+  R H_normal = rmin(H_L - R(0.5) * (V_L * V_L), H_R - R(0.5) * (V_R * V_R));
+  R c_s = Num<R>::sqrt(R(K.two_gm1_over_gp1) * H_normal);
+  R c_half;
+  if (R(0.5) * (U_L + U_R) < R(0)) c_half = Num<R>::div(c_s * c_s, rmax(rabs(U_R), c_s));
+  else c_half = Num<R>::div(c_s * c_s, rmax(rabs(U_L), c_s));
+  R M_L = Num<R>::div(U_L, c_half);
+  R M_R = Num<R>::div(U_R, c_half);
+  R M_L_plus = aw_m_plus(M_L);
+  R M_R_minus = aw_m_minus(M_R);
+  R P_R_minus = mausm_p_minus(M_R);
+  R P_L_plus = mausm_p_plus(M_L);
+  R p_s = p_L * P_L_plus + p_R * P_R_minus;
+  R mt = rmin(Num<R>::div(p_L, p_R), Num<R>::div(p_R, p_L));
+  R w = R(1) - (mt * mt * mt);
+  R f_L, f_R;
+  if (abs_lt(p_s, Num<R>::tiny)) {
+    f_L = R(0);
+    f_R = R(0);
+  } else {
+    R t = rmin(R(1), Num<R>::div(rmin(rmin(rmin(pc[0], pc[1]), pc[2]), pc[3]), rmin(p_L, p_R)));
+    R min_term = t * t;
+    if (rabs(R(1) - min_term) < CUT) min_term = R(1);
+    R fl = Num<R>::div(p_L, p_s) - R(1);
+    if (rabs(fl) < CUT) fl = R(0);
+    f_L = fl * min_term;
+    R fr = Num<R>::div(p_R, p_s) - R(1);
+    if (rabs(fr) < CUT) fr = R(0);
+    f_R = fr * min_term;
+  }
+  R Mb_L, Mb_R;
+  if (M_L_plus + M_R_minus < R(0)) {
+    Mb_L = M_L_plus * w * (R(1) + f_L);
+    Mb_R = M_R_minus + M_L_plus * ((R(1) - w) * (R(1) + f_L) - f_R);
+  } else {
+    Mb_L = M_L_plus + M_R_minus * ((R(1) - w) * (R(1) + f_R) - f_L);
+    Mb_R = M_R_minus * w * (R(1) + f_R);
+  }
+  R t2 = rmin(R(1), rmax(rabs(M_L), rabs(M_R)));
+  R a = R(1) - t2 * t2;
+  R rLh = mausm_phi_L(rho_L, rho_R, As.r, a), rRh = mausm_phi_R(rho_L, rho_R, Bs.r, a);
+  R uLh = mausm_phi_L(u_LHS, u_RHS, As.u, a), uRh = mausm_phi_R(u_LHS, u_RHS, Bs.u, a);
+  R vLh = mausm_phi_L(v_LHS, v_RHS, As.v, a), vRh = mausm_phi_R(v_LHS, v_RHS, Bs.v, a);
+  R pLh = mausm_phi_L(p_L, p_R, As.p, a), pRh = mausm_phi_R(p_L, p_R, Bs.p, a);
+  R H_Lh = gg * Num<R>::div(pLh, rLh) + R(0.5) * (uLh * uLh + vLh * vLh);
+  R H_Rh = gg * Num<R>::div(pRh, rRh) + R(0.5) * (uRh * uRh + vRh * vRh);
+  R mL = Mb_L * c_half * rLh;
+  R mR = Mb_R * c_half * rRh;
+  if (rabs(mL + mR) < EPSF) { mL = R(0); mR = R(0); }
+  F[0] = mL + mR;
+  // pressure terms carry n_x = 1 (DIR 0) or n_y = 1 (DIR 1); the other is an exact zero
+  const R pn = (P_L_plus * p_L) + (P_R_minus * p_R);
+  const R pz = (P_L_plus * R(0) * p_L) + (P_R_minus * R(0) * p_R);
+  const R px = DIR == 0 ? pn : pz, py = DIR == 0 ? pz : pn;
+  const R tx = (mL * uLh) + (mR * uRh), ty = (mL * vLh) + (mR * vRh);
+  F[1] = rabs(tx) < EPSF ? px : tx + px;
+  F[2] = rabs(ty) < EPSF ? py : ty + py;
+  F[3] = (mL * H_Lh) + (mR * H_Rh);
+  if (rabs(F[3]) < EPSF) F[3] = R(0);
 }
 
 // SLAU / SLAU2 / SD-SLAU / SD-SLAU2, slau_solver.fypp:332-490.  dpair[6][2]: delta_p1..6 cells.

@@ -134,11 +134,21 @@ __device__ __forceinline__ void edge_flux(const R* const rp[6], int T, int lim, 
   Prim<R> A = {Lv[0], Lv[1], Lv[2], Lv[3]}, B = {Rv[0], Rv[1], Rv[2], Rv[3]};
   // cell pressures in reference (i, j) terms: P(di, dj) = p(i+di, j+dj), (i, j) = left cell
   auto P = [&](int di, int dj) -> R { return DIR == 0 ? Q(3, di, dj) : Q(3, dj, di); };
-  if (FLUX == FLUX_AUSMPW) {
+  if (FLUX == FLUX_AUSMPW || FLUX == FLUX_M_AUSMPW) {
     R pc[4];
     if (DIR == 0) { pc[0] = P(0, -1); pc[1] = P(1, -1); pc[2] = P(0, 1); pc[3] = P(1, 1); }
     else { pc[0] = P(1, 0); pc[1] = P(1, 1); pc[2] = P(-1, 0); pc[3] = P(-1, 1); }
-    flux_ausmpw<R, DIR>(K, A, B, pc, F);
+    if constexpr (FLUX == FLUX_M_AUSMPW) {
+      // the superbee edge states of the second interpolator (m_ausmpw_plus_solver.fypp:163-167)
+      R Ls[4], Rs[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        recon_tvd2<R>(LIM_SUPERBEE, Q(k, -1, 0), Q(k, 0, 0), Q(k, 1, 0), Q(k, 2, 0), Ls[k], Rs[k]);
+      Prim<R> As = {Ls[0], Ls[1], Ls[2], Ls[3]}, Bs = {Rs[0], Rs[1], Rs[2], Rs[3]};
+      flux_mausmpw<R, DIR>(K, A, B, As, Bs, pc, F);
+    } else {
+      flux_ausmpw<R, DIR>(K, A, B, pc, F);
+    }
   } else if (FLUX == FLUX_SLAU || FLUX == FLUX_SLAU2 || FLUX == FLUX_SD_SLAU ||
              FLUX == FLUX_SD_SLAU2) {
     R pa[6], pb[6];
@@ -480,12 +490,20 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
 #ifndef CATO_DF_MIN_BLOCKS
 #define CATO_DF_MIN_BLOCKS 2
 #endif
-// the same for the FP32 (mixed) kernels
+// the same for the FP32 (mixed) kernels: the single-grid kernels run best unconstrained, the
+// persistent batch kernels (whose MLP5 instances need ~180 registers) at 3 CTAs per SM
 #ifndef CATO_F32_MIN_BLOCKS
 #define CATO_F32_MIN_BLOCKS 1
 #endif
+#ifndef CATO_F32_BATCH_MIN_BLOCKS
+#define CATO_F32_BATCH_MIN_BLOCKS 3
+#endif
 template <typename R> constexpr int min_blocks() {
   return Prec<R>::kind == 2 ? CATO_DF_MIN_BLOCKS : (Prec<R>::kind == 1 ? CATO_F32_MIN_BLOCKS : 1);
+}
+template <typename R> constexpr int batch_min_blocks() {
+  return Prec<R>::kind == 2 ? CATO_DF_MIN_BLOCKS
+                            : (Prec<R>::kind == 1 ? CATO_F32_BATCH_MIN_BLOCKS : 1);
 }
 
 template <typename R, int NG, int FLUX, int RECON>

@@ -47,7 +47,9 @@ enum cato_flux {
   CATO_FLUX_SD_SLAU2 = 4,     /* 'SD-SLAU2' */
   CATO_FLUX_ROE = 5,          /* 'Roe'       roe_solver.fypp:229-515 */
   CATO_FLUX_AUSM_PLUS_UP = 6, /* 'AUSM+-up'  ausm_plus_solver.f90:394-643 (driver restated) */
-  CATO_FLUX_HLLC = 7          /* 'HLLC'      Toro HLLC, PVRS wave speeds (reference is a stub) */
+  CATO_FLUX_HLLC = 7,         /* 'HLLC'      Toro HLLC, PVRS wave speeds (reference is a stub) */
+  CATO_FLUX_M_AUSMPW_PLUS = 8 /* 'M-AUSMPW+' m_ausmpw_plus_solver.fypp:437-708 (superbee-blended
+                                 interface states) */
 };
 
 /* Edge reconstruction (src/lib/spatial_reconstruction/muscl_factory.f90:54-94). */

@@ -462,6 +462,108 @@ static void flux_ausmpw(const cato_config* c, int dir, double nx, double ny, pri
   F[3] = (mL * H_L) + (mR * H_R);
 }
 
+/* M-AUSMPW+ (m_ausmpw_plus_solver.fypp, the active code of get_iflux/get_jflux :437-708): the
+ * AUSMPW+ interface Mach and pressure splitting without the alpha term (:600-610), the shock
+ * sensor f of get_f (:804-843, 1e-10 cuts), and interface states blended towards the superbee
+ * states by phi_L_half / phi_R_half (:768-800); flux cuts at epsilon*1e3 (:369, :684-705). */
+static double mausm_p_plus(double M) {
+  if (fabs(M) > 1.0) return 0.5 * (1.0 + (signbit(M) ? -1.0 : 1.0));
+  return 0.25 * ((M + 1.0) * (M + 1.0)) * (2.0 - M);
+}
+static double mausm_p_minus(double M) {
+  if (fabs(M) > 1.0) return 0.5 * (1.0 - (signbit(M) ? -1.0 : 1.0));
+  return 0.25 * ((M - 1.0) * (M - 1.0)) * (2.0 + M);
+}
+static double mausm_phi_L(double pL, double pR, double pLsb, double a) {
+  if (fabs(pR - pL) < 1.0 || fabs(pLsb - pL) < EPS) return pL;
+  return pL + dmax(0.0, (pR - pL) * (pLsb - pL)) / ((pR - pL) * fabs(pLsb - pL)) *
+                  dmin(dmin(a, 0.5 * fabs(pR - pL)), fabs(pLsb - pL));
+}
+static double mausm_phi_R(double pL, double pR, double pRsb, double a) {
+  if (fabs(pL - pR) < EPS || fabs(pRsb - pR) < 1.0) return pR;
+  return pR + dmax(0.0, (pL - pR) * (pRsb - pR)) / ((pL - pR) * fabs(pRsb - pR)) *
+                  dmin(dmin(a, 0.5 * fabs(pL - pR)), fabs(pRsb - pR));
+}
+static void flux_mausmpw(const cato_config* c, int dir, double nx, double ny, prim_t Lq,
+                         prim_t Rq, prim_t Ls, prim_t Rs, const double pc[4], double F[4]) {
+  const double g = c->gamma;
+  const double EPSF = EPS * 1e3; /* epsilon(1.0_rk) * 1e3_rk */
+  double rho_L = Lq.r, u_LHS = Lq.u, v_LHS = Lq.v, p_L = Lq.p;
+  double rho_R = Rq.r, u_RHS = Rq.u, v_RHS = Rq.v, p_R = Rq.p;
+  double U_L, U_R, V_L, V_R; /* taken before the low-Mach fix */
+  if (dir == 0) { U_L = u_LHS; U_R = u_RHS; V_L = v_LHS; V_R = v_RHS; }
+  else { U_L = v_LHS; U_R = v_RHS; V_L = u_LHS; V_R = u_RHS; }
+  double cs_L = sqrt(g * p_L / rho_L);
+  double cs_R = sqrt(g * p_R / rho_R);
+  double M_LHS = sqrt(u_LHS * u_LHS + v_LHS * v_LHS) / cs_L;
+  double M_RHS = sqrt(u_RHS * u_RHS + v_RHS * v_RHS) / cs_R;
+  if (c->apply_low_mach_fix && (fabs(M_LHS) < 0.1 || fabs(M_RHS) < 0.1)) { /* LOW_MACH */
+    double f_M = dmin(1.0, dmax(M_LHS, M_RHS));
+    double uLf = 0.5 * (u_LHS + u_RHS) + f_M * 0.5 * (u_LHS - u_RHS);
+    double uRf = 0.5 * (u_LHS + u_RHS) - f_M * 0.5 * (u_LHS - u_RHS);
+    double vLf = 0.5 * (v_LHS + v_RHS) + f_M * 0.5 * (v_LHS - v_RHS);
+    double vRf = 0.5 * (v_LHS + v_RHS) - f_M * 0.5 * (v_LHS - v_RHS);
+    u_LHS = uLf; u_RHS = uRf; v_LHS = vLf; v_RHS = vRf;
+  }
+  double H_L = (g / (g - 1.0)) * (p_L / rho_L) + 0.5 * (u_LHS * u_LHS + v_LHS * v_LHS);
+  double H_R = (g / (g - 1.0)) * (p_R / rho_R) + 0.5 * (u_RHS * u_RHS + v_RHS * v_RHS);
+  double H_normal = dmin(H_L - 0.5 * (V_L * V_L), H_R - 0.5 * (V_R * V_R));
+  double c_s = sqrt(2.0 * ((g - 1.0) / (g + 1.0)) * H_normal);
+  double c_half;
+  if (0.5 * (U_L + U_R) < 0.0) c_half = (c_s * c_s) / dmax(fabs(U_R), c_s);
+  else c_half = (c_s * c_s) / dmax(fabs(U_L), c_s);
+  double M_L = U_L / c_half;
+  double M_R = U_R / c_half;
+  double M_L_plus = ausmpw_m_plus(M_L);
+  double M_R_minus = ausmpw_m_minus(M_R);
+  double P_R_minus = mausm_p_minus(M_R);
+  double P_L_plus = mausm_p_plus(M_L);
+  double p_s = p_L * P_L_plus + p_R * P_R_minus;
+  double mt = dmin(p_L / p_R, p_R / p_L);
+  double w = 1.0 - (mt * mt * mt);
+  double f_L, f_R;
+  if (fabs(p_s) < TINY) {
+    f_L = 0.0;
+    f_R = 0.0;
+  } else {
+    double t = dmin(1.0, dmin(dmin(dmin(pc[0], pc[1]), pc[2]), pc[3]) / dmin(p_L, p_R));
+    double min_term = t * t;
+    if (fabs(1.0 - min_term) < 1e-10) min_term = 1.0;
+    double fl = (p_L / p_s) - 1.0;
+    if (fabs(fl) < 1e-10) fl = 0.0;
+    f_L = fl * min_term;
+    double fr = (p_R / p_s) - 1.0;
+    if (fabs(fr) < 1e-10) fr = 0.0;
+    f_R = fr * min_term;
+  }
+  double Mb_L, Mb_R;
+  if (M_L_plus + M_R_minus < 0.0) {
+    Mb_L = M_L_plus * w * (1.0 + f_L);
+    Mb_R = M_R_minus + M_L_plus * ((1.0 - w) * (1.0 + f_L) - f_R);
+  } else {
+    Mb_L = M_L_plus + M_R_minus * ((1.0 - w) * (1.0 + f_R) - f_L);
+    Mb_R = M_R_minus * w * (1.0 + f_R);
+  }
+  double t2 = dmin(1.0, dmax(fabs(M_L), fabs(M_R)));
+  double a = 1.0 - t2 * t2;
+  double rLh = mausm_phi_L(rho_L, rho_R, Ls.r, a), rRh = mausm_phi_R(rho_L, rho_R, Rs.r, a);
+  double uLh = mausm_phi_L(u_LHS, u_RHS, Ls.u, a), uRh = mausm_phi_R(u_LHS, u_RHS, Rs.u, a);
+  double vLh = mausm_phi_L(v_LHS, v_RHS, Ls.v, a), vRh = mausm_phi_R(v_LHS, v_RHS, Rs.v, a);
+  double pLh = mausm_phi_L(p_L, p_R, Ls.p, a), pRh = mausm_phi_R(p_L, p_R, Rs.p, a);
+  double H_Lh = (g / (g - 1.0)) * (pLh / rLh) + 0.5 * (uLh * uLh + vLh * vLh);
+  double H_Rh = (g / (g - 1.0)) * (pRh / rRh) + 0.5 * (uRh * uRh + vRh * vRh);
+  double mL = Mb_L * c_half * rLh;
+  double mR = Mb_R * c_half * rRh;
+  if (fabs(mL + mR) < EPSF) { mL = 0.0; mR = 0.0; }
+  F[0] = mL + mR;
+  double tx = (mL * uLh) + (mR * uRh), px = (P_L_plus * nx * p_L) + (P_R_minus * nx * p_R);
+  F[1] = fabs(tx) < EPSF ? px : tx + px;
+  double ty = (mL * vLh) + (mR * vRh), py = (P_L_plus * ny * p_L) + (P_R_minus * ny * p_R);
+  F[2] = fabs(ty) < EPSF ? py : ty + py;
+  F[3] = (mL * H_Lh) + (mR * H_Rh);
+  if (fabs(F[3]) < EPSF) F[3] = 0.0;
+}
+
 /* SLAU family, slau_solver.fypp:332-490.  pc (SD variants) = delta_p1..6 cell pairs:
  * pc[0..5] = first cell of each pair, pc[6..11] = second cell. */
 static void flux_slau(const cato_config* c, double nx, double ny, prim_t Lq, prim_t Rq,
@@ -725,13 +827,15 @@ static void flux_hllc(const cato_config* c, int dir, prim_t Lq, prim_t Rq, doubl
  * shock sensors.  Edge (i,j) sits between cells (i,j) and (i+1,j) [dir 0] or (i,j+1) [dir 1]. */
 #define PN(n, t) (dir == 0 ? AT(p, i + (n), j + (t)) : AT(p, i + (t), j + (n)))
 static void edge_flux(dims_t d, const cato_config* c, int dir, const double* p, int i, int j,
-                      prim_t Lq, prim_t Rq, double F[4]) {
+                      prim_t Lq, prim_t Rq, prim_t Ls, prim_t Rs, double F[4]) {
   /* Cartesian edge normals: exactly (1,0) for i-edges and (0,1) for j-edges
    * (quad_cell.f90:193-229 evaluated on axis-aligned cells) */
   double nx = dir == 0 ? 1.0 : 0.0, ny = dir == 0 ? 0.0 : 1.0;
   switch (c->flux) {
-    case CATO_FLUX_AUSMPW_PLUS: {
-      /* get_f arguments, ausmpw_plus_solver.fypp:430-442 */
+    case CATO_FLUX_AUSMPW_PLUS:
+    case CATO_FLUX_M_AUSMPW_PLUS: {
+      /* get_f arguments, ausmpw_plus_solver.fypp:430-442 (the same cells in
+       * m_ausmpw_plus_solver.fypp:669-679) */
       double pc[4];
       if (dir == 0) {
         pc[0] = AT(p, i, j - 1); pc[1] = AT(p, i + 1, j - 1);
@@ -740,7 +844,8 @@ static void edge_flux(dims_t d, const cato_config* c, int dir, const double* p, 
         pc[0] = AT(p, i + 1, j); pc[1] = AT(p, i + 1, j + 1);
         pc[2] = AT(p, i - 1, j); pc[3] = AT(p, i - 1, j + 1);
       }
-      flux_ausmpw(c, dir, nx, ny, Lq, Rq, pc, F);
+      if (c->flux == CATO_FLUX_M_AUSMPW_PLUS) flux_mausmpw(c, dir, nx, ny, Lq, Rq, Ls, Rs, pc, F);
+      else flux_ausmpw(c, dir, nx, ny, Lq, Rq, pc, F);
       break;
     }
     case CATO_FLUX_SLAU:
@@ -825,19 +930,25 @@ int oracle_solve(const cato_config* c, double* rho, double* u, double* v, double
 #pragma omp parallel for schedule(static)
   for (int j = 1; j <= d.nj; ++j)
     for (int i = 0; i <= d.ni; ++i) {
-      double L[4], R[4];
+      double L[4], R[4], Ls[4] = {0}, Rs[4] = {0};
       for (int k = 0; k < 4; ++k) edge_recon(d, c->limiter, q[k], 0, i, j, &L[k], &R[k]);
+      if (c->flux == CATO_FLUX_M_AUSMPW_PLUS) /* the superbee edge states, :163-167 */
+        for (int k = 0; k < 4; ++k) edge_recon(d, CATO_LIM_SUPERBEE, q[k], 0, i, j, &Ls[k], &Rs[k]);
       prim_t Lq = {L[0], L[1], L[2], L[3]}, Rq = {R[0], R[1], R[2], R[3]};
-      edge_flux(d, c, 0, p, i, j, Lq, Rq, &IF(iflux, 0, i, j));
+      prim_t Lsq = {Ls[0], Ls[1], Ls[2], Ls[3]}, Rsq = {Rs[0], Rs[1], Rs[2], Rs[3]};
+      edge_flux(d, c, 0, p, i, j, Lq, Rq, Lsq, Rsq, &IF(iflux, 0, i, j));
     }
   /* j-direction edges (1:ni, 0:nj) */
 #pragma omp parallel for schedule(static)
   for (int j = 0; j <= d.nj; ++j)
     for (int i = 1; i <= d.ni; ++i) {
-      double L[4], R[4];
+      double L[4], R[4], Ls[4] = {0}, Rs[4] = {0};
       for (int k = 0; k < 4; ++k) edge_recon(d, c->limiter, q[k], 1, i, j, &L[k], &R[k]);
+      if (c->flux == CATO_FLUX_M_AUSMPW_PLUS)
+        for (int k = 0; k < 4; ++k) edge_recon(d, CATO_LIM_SUPERBEE, q[k], 1, i, j, &Ls[k], &Rs[k]);
       prim_t Lq = {L[0], L[1], L[2], L[3]}, Rq = {R[0], R[1], R[2], R[3]};
-      edge_flux(d, c, 1, p, i, j, Lq, Rq, &JF(jflux, 0, i, j));
+      prim_t Lsq = {Ls[0], Ls[1], Ls[2], Ls[3]}, Rsq = {Rs[0], Rs[1], Rs[2], Rs[3]};
+      edge_flux(d, c, 1, p, i, j, Lq, Rq, Lsq, Rsq, &JF(jflux, 0, i, j));
     }
   double* out[4] = {drho, drhou, drhov, drhoE};
   size_t n = nfield(d);
@@ -1213,7 +1324,7 @@ int oracle_config_default(cato_config* c, int32_t ni, int32_t nj) {
 int oracle_config_check(const cato_config* c) {
   if (!c) return CATO_ERR_ARG;
   if (c->ni < 1 || c->nj < 1) return CATO_ERR_CONFIG;
-  if (c->flux < CATO_FLUX_AUSMPW_PLUS || c->flux > CATO_FLUX_HLLC) return CATO_ERR_CONFIG;
+  if (c->flux < CATO_FLUX_AUSMPW_PLUS || c->flux > CATO_FLUX_M_AUSMPW_PLUS) return CATO_ERR_CONFIG;
   if (c->limiter < CATO_LIM_MINMOD || c->limiter > CATO_LIM_MLP5) return CATO_ERR_CONFIG;
   if (c->rk < CATO_RK_SSP2 || c->rk > CATO_RK_2_5) return CATO_ERR_CONFIG;
   int need = (c->limiter == CATO_LIM_MLP5) ? 3 : 2; /* mod_input.f90:320-338 */

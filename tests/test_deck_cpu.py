@@ -100,7 +100,7 @@ def test_reference_integrated_decks_parse():
         c = cfg.to_c()
         assert _lib.load(build_if_missing=True).cato_config_check(ctypes.byref(c)) == 0, path
         supported += 1
-    assert supported >= 7
+    assert supported >= 15
     with open(os.path.join(os.path.dirname(REF_DECKS[0]), "..", "sod_1d", "input.ini")) as f:
         sod = parse_deck(f.read())
     assert (sod.flux_solver, sod.limiter, sod.integration_strategy) == ("Roe", "MLP5", "ssp_rk2")

@@ -170,10 +170,11 @@ def _sod_exact(x, t, gamma=1.4, left=(1.0, 0.0, 1.0), right=(0.125, 0.0, 0.1), x
     return rho
 
 
-def test_oracle_sod_against_exact_solution(oracle):
+@pytest.mark.parametrize("flux", ["AUSMPW+", "M-AUSMPW+"])
+def test_oracle_sod_against_exact_solution(oracle, flux):
     """Physical sanity bound (tests/integrated/sod_1d compares against an exact Riemann solver):
     the 400x40 Sod run at t ~ 0.2 is within 1 % L1 of the exact density and y-uniform."""
-    cfg, prims = ic.sod()
+    cfg, prims = ic.sod(flux_solver=flux)
     f = oracle.OracleFluid(cfg)
     f.set_primitive(*prims)
     f.run(0.2)

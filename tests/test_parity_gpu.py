@@ -16,7 +16,7 @@ from fvleg_2d_gb300.fluid import Fluid, FluxSolver, MusclInterpolator
 
 pytestmark = pytest.mark.gpu
 
-FLUXES = ["AUSMPW+", "SLAU", "SLAU2", "SD-SLAU", "SD-SLAU2", "Roe", "AUSM+-up", "HLLC"]
+FLUXES = ["AUSMPW+", "SLAU", "SLAU2", "SD-SLAU", "SD-SLAU2", "Roe", "AUSM+-up", "HLLC", "M-AUSMPW+"]
 LIMITERS = ["minmod", "superbee", "van_leer", "MLP3", "MLP5"]
 BCS = {
     "zg": {"+x": "zero_gradient", "-x": "zero_gradient", "+y": "zero_gradient", "-y": "zero_gradient"},
