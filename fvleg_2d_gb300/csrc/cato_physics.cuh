@@ -31,6 +31,10 @@ enum { SIDE_PX = 0, SIDE_PY = 1, SIDE_MX = 2, SIDE_MY = 3 };
 enum { ST_NEG_DENSITY = 1, ST_NEG_PRESSURE = 2, ST_NAN = 4 };
 
 template <typename R> struct Num;
+// the mixed path's FP32 compute type (its arithmetic skips the reference's FP64-scale epsilon
+// flushes, which cannot fire at FP32 resolution for data of normal magnitude)
+template <typename R> constexpr bool kFP32 = false;
+template <> constexpr bool kFP32<float> = true;
 
 template <> struct Num<double> {
   static constexpr double eps = 2.220446049250313080847263336181640625e-16;  // epsilon(1.0_rk)
@@ -220,9 +224,11 @@ template <typename R>
 __device__ __forceinline__ void recon_tvd2(int lim, R qm1, R q0, R qp1, R qp2, R& L, R& Rr) {
   const R EPS = Num<R>::eps;
   R dm = q0 - qm1, d0 = qp1 - q0, dp = qp2 - qp1;
-  if (abs_lt(dm, EPS)) dm = R(0);
-  if (abs_lt(d0, EPS)) d0 = R(0);
-  if (abs_lt(dp, EPS)) dp = R(0);
+  if constexpr (!kFP32<R>) {  // FP32 differences below 2.2e-16 need |q| < 1e-9: no flush
+    if (abs_lt(dm, EPS)) dm = R(0);
+    if (abs_lt(d0, EPS)) d0 = R(0);
+    if (abs_lt(dp, EPS)) dp = R(0);
+  }
   R rL = Num<R>::div(d0, dm + R(1e-16));
   R rR = Num<R>::div(d0, dp + R(1e-16));
   R phi = tvd_phi(lim, rL);
@@ -237,16 +243,20 @@ __device__ __forceinline__ void recon_mlp(R qm2, R qm1, R q0, R qp1, R qp2, R qp
   const R EPS = Num<R>::eps;
   const R S = R(1e-30);  // SMALL_NUM, muscl_mlp.fypp:122
   R dm = q0 - qm1, d0 = qp1 - q0, dp = qp2 - qp1;
-  if (abs_lt(dm, EPS)) dm = R(0);
-  if (abs_lt(d0, EPS)) d0 = R(0);
-  if (abs_lt(dp, EPS)) dp = R(0);
+  if constexpr (!kFP32<R>) {
+    if (abs_lt(dm, EPS)) dm = R(0);
+    if (abs_lt(d0, EPS)) d0 = R(0);
+    if (abs_lt(dp, EPS)) dp = R(0);
+  }
   R rR_p1 = Num<R>::div(d0, dp + S);
   R rL = Num<R>::div(d0, dm + S);
   R bL, bR;
   if (ORDER == 5) {
     R dm3 = qm1 - qm2, dp5 = qp3 - qp2;
-    if (abs_lt(dm3, EPS)) dm3 = R(0);
-    if (abs_lt(dp5, EPS)) dp5 = R(0);
+    if constexpr (!kFP32<R>) {
+      if (abs_lt(dm3, EPS)) dm3 = R(0);
+      if (abs_lt(dp5, EPS)) dp5 = R(0);
+    }
     R rL_m1 = Num<R>::div(dm, dm3 + S);
     R rL_p1 = Num<R>::div(dp, d0 + S);
     R rR_p2 = Num<R>::div(dp, dp5 + S);

@@ -39,6 +39,15 @@ def test_batch_instances_match_single_handles(cato_lib, precision):
             f.integrate()
         ref = f.state(("rho", "rho_u", "rho_v", "rho_E"))
         got = b.state(slot)
+        if precision == "mixed":
+            # FP32 arithmetic built with FMA contraction: the batch kernel (compiled for 3 CTAs
+            # per SM) and the single-grid kernel may contract differently, so they agree to
+            # FP32 rounding, not bitwise.  (Alone and in a mix, the batch is bitwise: below.)
+            assert abs(f.time - q["time"]) <= 1e-6 * q["time"]
+            for k in ref:
+                np.testing.assert_allclose(got[k], ref[k], rtol=1e-5, atol=1e-6,
+                                           err_msg=f"slot {slot} {k}")
+            continue
         assert f.time == q["time"]
         for k in ref:
             np.testing.assert_array_equal(got[k], ref[k], err_msg=f"slot {slot} {k}")
