@@ -31,6 +31,10 @@ enum { SIDE_PX = 0, SIDE_PY = 1, SIDE_MX = 2, SIDE_MY = 3 };
 enum { ST_NEG_DENSITY = 1, ST_NEG_PRESSURE = 2, ST_NAN = 4 };
 
 template <typename R> struct Num;
+// the mixed path's FP32 compute type (its arithmetic skips the reference's FP64-scale epsilon
+// flushes, which cannot fire at FP32 resolution for data of normal magnitude)
+template <typename R> constexpr bool kFP32 = false;
+template <> constexpr bool kFP32<float> = true;
 
 template <> struct Num<double> {
   static constexpr double eps = 2.220446049250313080847263336181640625e-16;  // epsilon(1.0_rk)
@@ -220,9 +224,11 @@ template <typename R>
 __device__ __forceinline__ void recon_tvd2(int lim, R qm1, R q0, R qp1, R qp2, R& L, R& Rr) {
   const R EPS = Num<R>::eps;
   R dm = q0 - qm1, d0 = qp1 - q0, dp = qp2 - qp1;
-  if (abs_lt(dm, EPS)) dm = R(0);
-  if (abs_lt(d0, EPS)) d0 = R(0);
-  if (abs_lt(dp, EPS)) dp = R(0);
+  if constexpr (!kFP32<R>) {  // FP32 differences below 2.2e-16 need |q| < 1e-9: no flush
+    if (abs_lt(dm, EPS)) dm = R(0);
+    if (abs_lt(d0, EPS)) d0 = R(0);
+    if (abs_lt(dp, EPS)) dp = R(0);
+  }
   R rL = Num<R>::div(d0, dm + R(1e-16));
   R rR = Num<R>::div(d0, dp + R(1e-16));
   R phi = tvd_phi(lim, rL);
@@ -237,16 +243,20 @@ __device__ __forceinline__ void recon_mlp(R qm2, R qm1, R q0, R qp1, R qp2, R qp
   const R EPS = Num<R>::eps;
   const R S = R(1e-30);  // SMALL_NUM, muscl_mlp.fypp:122
   R dm = q0 - qm1, d0 = qp1 - q0, dp = qp2 - qp1;
-  if (abs_lt(dm, EPS)) dm = R(0);
-  if (abs_lt(d0, EPS)) d0 = R(0);
-  if (abs_lt(dp, EPS)) dp = R(0);
+  if constexpr (!kFP32<R>) {
+    if (abs_lt(dm, EPS)) dm = R(0);
+    if (abs_lt(d0, EPS)) d0 = R(0);
+    if (abs_lt(dp, EPS)) dp = R(0);
+  }
   R rR_p1 = Num<R>::div(d0, dp + S);
   R rL = Num<R>::div(d0, dm + S);
   R bL, bR;
   if (ORDER == 5) {
     R dm3 = qm1 - qm2, dp5 = qp3 - qp2;
-    if (abs_lt(dm3, EPS)) dm3 = R(0);
-    if (abs_lt(dp5, EPS)) dp5 = R(0);
+    if constexpr (!kFP32<R>) {
+      if (abs_lt(dm3, EPS)) dm3 = R(0);
+      if (abs_lt(dp5, EPS)) dp5 = R(0);
+    }
     R rL_m1 = Num<R>::div(dm, dm3 + S);
     R rL_p1 = Num<R>::div(dp, d0 + S);
     R rR_p2 = Num<R>::div(dp, dp5 + S);
@@ -273,146 +283,111 @@ __device__ __forceinline__ void recon_mlp(R qm2, R qm1, R q0, R qp1, R qp2, R qp
 }
 
 // ---------------------------------------------------------------------------------------------
-// Reconstruction of the mixed paths (V = float for mixed, df for mixed_df).  The limited slope
-// phi(r) * dq is, for each branch of a limiter, an algebraic combination of the slope
-// differences themselves: with r = d0/dm, r * dm = d0, (1 + 2r)/3 * dm = (dm + 2 d0)/3, the MLP5
-// coefficient times dm is the fifth-order combination (-2 dm3 + 11 dm + 24 d0 - 3 dp)/30, and
-// van Leer's 2r/(1+r) * dm = 2 d0 dm / (dm + d0).  So the branch is chosen in FP32 in slope space
+// Double-float reconstruction (mixed_df).  The limited slope phi(r) * dq is, for each branch of
+// the limiter, an algebraic combination of the slope differences themselves: with r = d0/dm,
+// r * dm = d0, (1 + 2r)/3 * dm = (dm + 2 d0)/3, and the MLP5 coefficient times dm is the
+// fifth-order combination (-2 dm3 + 11 dm + 24 d0 - 3 dp)/30.  So the branch is chosen in FP32
 // (only a near-tie can go the other way, where both branches agree to FP32 rounding) and the
-// chosen slope is evaluated in V from the differences, without the ratio divisions.  The
-// reference's 1e-16 / 1e-30 regularisations only matter for differences at the epsilon flush
-// threshold, where the slope term is itself ~1e-16.  The FP64 path keeps the reference's ratio
-// form above (bit-exact parity).
+// chosen slope is evaluated in double-float from the double-float differences, without the
+// ratio divisions.  The reference's 1e-16 / 1e-30 regularisations only matter for differences
+// at the epsilon flush threshold, where the slope term is itself ~1e-16.
 // ---------------------------------------------------------------------------------------------
 __device__ __forceinline__ df df_half(df a) { return df(a.hi * 0.5f, a.lo * 0.5f); }  // exact
 __device__ __forceinline__ df df_twice(df a) { return df(a.hi * 2.0f, a.lo * 2.0f); }  // exact
-
-__device__ __forceinline__ float lo_of(float x) { return x; }
-__device__ __forceinline__ float lo_of(df x) { return x.hi; }
-__device__ __forceinline__ float vhalf(float x) { return 0.5f * x; }
-__device__ __forceinline__ df vhalf(df x) { return df_half(x); }
-__device__ __forceinline__ float vtwice(float x) { return 2.0f * x; }
-__device__ __forceinline__ df vtwice(df x) { return df_twice(x); }
-__device__ __forceinline__ float vscale(float x, float c) { return x * c; }
-__device__ __forceinline__ df vscale(df x, float c) { return x * df(c); }
-__device__ __forceinline__ float vdiv(float a, float b) { return __fdividef(a, b); }
-__device__ __forceinline__ df vdiv(df a, df b) { return df_div(a, b); }
-// the reference's |difference| < epsilon flush: FP32 differences that small need |q| < 1e-9
-__device__ __forceinline__ float vflushed(float d) { return d; }
-__device__ __forceinline__ df vflushed(df d) {
-  return fabsf(d.hi) < 2.220446049250313080847263336181640625e-16f ? df(0.0f) : d;
-}
+__device__ __forceinline__ df df_scale(df a, float c) { return a * df(c); }
 
 // TVD2 slope phi(r) * dq for r = d0 / dq (dq = dm for the left state, dp for the right)
-template <typename V>
-__device__ __forceinline__ V tvd_slope(int lim, V D0, V Dq) {
-  const float d0 = lo_of(D0), dq = lo_of(Dq);
-  if (d0 == 0.0f || dq == 0.0f || ((d0 > 0.0f) != (dq > 0.0f))) return V(0.0f);  // r <= 0
+__device__ __forceinline__ df tvd_slope_df(int lim, df D0, df Dq) {
+  const float d0 = D0.hi, dq = Dq.hi;
+  if (d0 == 0.0f || dq == 0.0f || ((d0 > 0.0f) != (dq > 0.0f))) return df(0.0f);  // r <= 0
   const float a0 = fabsf(d0), aq = fabsf(dq);  // r = a0 / aq > 0
   if (lim == LIM_MINMOD) return a0 < aq ? D0 : Dq;            // min(r, 1) * dq
   if (lim == LIM_SUPERBEE) {                                    // max(min(2r, 1), min(r, 2)) * dq
-    if (2.0f * a0 <= aq) return vtwice(D0);
+    if (2.0f * a0 <= aq) return df_twice(D0);
     if (a0 <= aq) return Dq;
     if (a0 <= 2.0f * aq) return D0;
-    return vtwice(Dq);
+    return df_twice(Dq);
   }
-  return vdiv(vtwice(D0 * Dq), Dq + D0);  // van Leer
+  // van Leer: 2r / (1 + r) * dq = 2 d0 dq / (dq + d0)
+  return df_div(df_twice(D0 * Dq), Dq + D0);
 }
 
-template <typename V>
-__device__ __forceinline__ void recon_tvd2_sel(int lim, V qm1, V q0, V qp1, V qp2, V& L, V& Rr) {
-  const V Dm = vflushed(q0 - qm1), D0 = vflushed(qp1 - q0), Dp = vflushed(qp2 - qp1);
-  L = q0 + vhalf(tvd_slope(lim, D0, Dm));
-  Rr = qp1 - vhalf(tvd_slope(lim, D0, Dp));
+__device__ __forceinline__ df flushed(df d) {
+  return fabsf(d.hi) < 2.220446049250313080847263336181640625e-16f ? df(0.0f) : d;
 }
-template <>
-__device__ __forceinline__ void recon_tvd2<float>(int lim, float qm1, float q0, float qp1,
-                                                  float qp2, float& L, float& Rr) {
-  recon_tvd2_sel<float>(lim, qm1, q0, qp1, qp2, L, Rr);
-}
+
 template <>
 __device__ __forceinline__ void recon_tvd2<df>(int lim, df qm1, df q0, df qp1, df qp2, df& L,
                                                df& Rr) {
-  recon_tvd2_sel<df>(lim, qm1, q0, qp1, qp2, L, Rr);
+  const df Dm = flushed(q0 - qm1), D0 = flushed(qp1 - q0), Dp = flushed(qp2 - qp1);
+  L = q0 + df_half(tvd_slope_df(lim, D0, Dm));
+  Rr = qp1 - df_half(tvd_slope_df(lim, D0, Dp));
 }
 
-// MLP slope phi * dq, phi = max(0, min(alpha r, alpha, beta)), chosen in slope space: with
-// r dq = d0 the candidates are alpha d0, alpha dq and beta dq (bdq); for dq > 0 the slope is
-// max(0, min(...)) and for dq < 0 min(0, max(...)).
-template <typename V>
-__device__ __forceinline__ V mlp_pick(float alpha, V D0, V Dq, V bdq) {
-  const float dq = lo_of(Dq);
-  const float s1 = alpha * lo_of(D0), s2 = alpha * dq, s3 = lo_of(bdq);
-  float m = s1;
-  int pick = 1;
-  if (dq > 0.0f) {
-    if (s2 < m) { m = s2; pick = 2; }
-    if (s3 < m) { m = s3; pick = 3; }
-    if (!(m > 0.0f)) return V(0.0f);
-  } else {
-    if (s2 > m) { m = s2; pick = 2; }
-    if (s3 > m) { m = s3; pick = 3; }
-    if (!(m < 0.0f)) return V(0.0f);
-  }
-  if (pick == 1) return vscale(D0, alpha);
-  if (pick == 2) return vscale(Dq, alpha);
+// MLP slope: phi * dq with phi = max(0, min(alpha r, alpha, beta)); candidates
+// alpha * d0, alpha * dq and beta * dq (the latter given in double-float as bdq).
+__device__ __forceinline__ df mlp_slope_df(float r, float alpha, float beta, df D0, df Dq,
+                                           df bdq) {
+  const float c1 = alpha * r, c2 = alpha;
+  float m = fminf(c1, c2);
+  int pick = c1 <= c2 ? 1 : 2;
+  if (beta < m) { m = beta; pick = 3; }
+  if (!(m > 0.0f)) return df(0.0f);
+  if (pick == 1) return df_scale(D0, alpha);
+  if (pick == 2) return df_scale(Dq, alpha);
   return bdq;
 }
 
-template <int ORDER, typename V>
-__device__ __forceinline__ void recon_mlp_sel(V qm2, V qm1, V q0, V qp1, V qp2, V qp3, V t0p,
-                                              V t0m, V t1p, V t1m, V& L, V& Rr) {
+template <int ORDER>
+__device__ __forceinline__ void recon_mlp_df(df qm2, df qm1, df q0, df qp1, df qp2, df qp3,
+                                             df t0p, df t0m, df t1p, df t1m, df& L, df& Rr) {
   const float S = 1e-30f;
-  const V Dm = vflushed(q0 - qm1), D0 = vflushed(qp1 - q0), Dp = vflushed(qp2 - qp1);
-  const float dm = lo_of(Dm), d0 = lo_of(D0), dp = lo_of(Dp);
-  V bdL, bdR;  // beta * dm (left), beta * dp (right)
-  if (ORDER == 5) {
-    const V Dm3 = vflushed(qm1 - qm2), Dp5 = vflushed(qp3 - qp2);
-    // beta_L dm = (-2 dm3 + 11 dm + 24 d0 - 3 rL rL_p1 dm)/30 with rL rL_p1 dm = dp (0 if d0 = 0);
-    // beta_R dp = (-2 dp5 + 11 dp + 24 d0 - 3 rR_p1 rR dp)/30 with rR_p1 rR dp = dm
-    const V t3L = d0 == 0.0f ? V(0.0f) : Dp, t3R = d0 == 0.0f ? V(0.0f) : Dm;
-    bdL = (vscale(Dm3, -2.0f) + vscale(Dm, 11.0f) + vscale(D0, 24.0f) - vscale(t3L, 3.0f)) *
-          V(1.0 / 30.0);
-    bdR = (vscale(Dp5, -2.0f) + vscale(Dp, 11.0f) + vscale(D0, 24.0f) - vscale(t3R, 3.0f)) *
-          V(1.0 / 30.0);
-  } else {
-    bdL = (Dm + vtwice(D0)) * V(1.0 / 3.0);
-    bdR = (Dp + vtwice(D0)) * V(1.0 / 3.0);
-  }
-  // alpha: the multi-dimensional limiting factor (muscl_mlp.fypp:241-264), in FP32
+  const df Dm = flushed(q0 - qm1), D0 = flushed(qp1 - q0), Dp = flushed(qp2 - qp1);
+  const float dm = Dm.hi, d0 = D0.hi, dp = Dp.hi;
   const float rR_p1 = __fdividef(d0, dp + S), rL = __fdividef(d0, dm + S);
-  const float tt = __fdividef(fabsf(lo_of(t0p - t0m)), fabsf(lo_of(qp1 - qm1)) + S);
-  const float tt1 = __fdividef(fabsf(lo_of(t1p - t1m)), fabsf(lo_of(qp2 - q0)) + S);
+  float bL, bR;
+  df bdL, bdR;  // beta * dm (left), beta * dp (right) in double-float
+  if (ORDER == 5) {
+    const df Dm3 = flushed(qm1 - qm2), Dp5 = flushed(qp3 - qp2);
+    const float dm3 = Dm3.hi, dp5 = Dp5.hi;
+    const float rL_m1 = __fdividef(dm, dm3 + S), rL_p1 = __fdividef(dp, d0 + S);
+    const float rR_p2 = __fdividef(dp, dp5 + S), rR = __fdividef(dm, d0 + S);
+    bL = ((__fdividef(-2.0f, rL_m1 + S) + 11.0f) + 24.0f * rL - 3.0f * rL * rL_p1) * (1.0f / 30.0f);
+    bR = ((__fdividef(-2.0f, rR_p2 + S) + 11.0f) + 24.0f * rR_p1 - 3.0f * rR_p1 * rR) *
+         (1.0f / 30.0f);
+    // beta_L dm = (-2 dm3 + 11 dm + 24 d0 - 3 rL rL_p1 dm)/30 with rL rL_p1 dm = dp (0 if d0 = 0)
+    const df t3L = d0 == 0.0f ? df(0.0f) : Dp, t3R = d0 == 0.0f ? df(0.0f) : Dm;
+    bdL = (df_scale(Dm3, -2.0f) + df_scale(Dm, 11.0f) + df_scale(D0, 24.0f) - df_scale(t3L, 3.0f)) *
+          df(1.0 / 30.0);
+    // beta_R dp = (-2 dp5 + 11 dp + 24 d0 - 3 rR_p1 rR dp)/30 with rR_p1 rR dp = dm
+    bdR = (df_scale(Dp5, -2.0f) + df_scale(Dp, 11.0f) + df_scale(D0, 24.0f) - df_scale(t3R, 3.0f)) *
+          df(1.0 / 30.0);
+  } else {
+    bL = (1.0f + 2.0f * rL) * (1.0f / 3.0f);
+    bR = (1.0f + 2.0f * rR_p1) * (1.0f / 3.0f);
+    bdL = (Dm + df_twice(D0)) * df(1.0 / 3.0);
+    bdR = (Dp + df_twice(D0)) * df(1.0 / 3.0);
+  }
+  const float tt = __fdividef(fabsf((t0p - t0m).hi), fabsf((qp1 - qm1).hi) + S);
+  const float tt1 = __fdividef(fabsf((t1p - t1m).hi), fabsf((qp2 - q0).hi) + S);
   const float aLt = __fdividef(2.0f * fmaxf(1.0f, rL) * (1.0f + fmaxf(0.0f, __fdividef(tt1, rR_p1 + S))),
                                1.0f + tt);
   const float aRt = __fdividef(2.0f * fmaxf(1.0f, rR_p1) * (1.0f + fmaxf(0.0f, __fdividef(tt, rL + S))),
                                1.0f + tt1);
   const float aL = fmaxf(1.0f, fminf(2.0f, aLt)), aR = fmaxf(1.0f, fminf(2.0f, aRt));
-  L = dm == 0.0f ? q0 : q0 + vhalf(mlp_pick(aL, D0, Dm, bdL));
-  Rr = dp == 0.0f ? qp1 : qp1 - vhalf(mlp_pick(aR, D0, Dp, bdR));
+  L = dm == 0.0f ? q0 : q0 + df_half(mlp_slope_df(rL, aL, bL, D0, Dm, bdL));
+  Rr = dp == 0.0f ? qp1 : qp1 - df_half(mlp_slope_df(rR_p1, aR, bR, D0, Dp, bdR));
 }
 
 template <>
-__device__ __forceinline__ void recon_mlp<float, 3>(float qm2, float qm1, float q0, float qp1,
-                                                    float qp2, float qp3, float t0p, float t0m,
-                                                    float t1p, float t1m, float& L, float& Rr) {
-  recon_mlp_sel<3, float>(qm2, qm1, q0, qp1, qp2, qp3, t0p, t0m, t1p, t1m, L, Rr);
-}
-template <>
-__device__ __forceinline__ void recon_mlp<float, 5>(float qm2, float qm1, float q0, float qp1,
-                                                    float qp2, float qp3, float t0p, float t0m,
-                                                    float t1p, float t1m, float& L, float& Rr) {
-  recon_mlp_sel<5, float>(qm2, qm1, q0, qp1, qp2, qp3, t0p, t0m, t1p, t1m, L, Rr);
-}
-template <>
 __device__ __forceinline__ void recon_mlp<df, 3>(df qm2, df qm1, df q0, df qp1, df qp2, df qp3,
                                                  df t0p, df t0m, df t1p, df t1m, df& L, df& Rr) {
-  recon_mlp_sel<3, df>(qm2, qm1, q0, qp1, qp2, qp3, t0p, t0m, t1p, t1m, L, Rr);
+  recon_mlp_df<3>(qm2, qm1, q0, qp1, qp2, qp3, t0p, t0m, t1p, t1m, L, Rr);
 }
 template <>
 __device__ __forceinline__ void recon_mlp<df, 5>(df qm2, df qm1, df q0, df qp1, df qp2, df qp3,
                                                  df t0p, df t0m, df t1p, df t1m, df& L, df& Rr) {
-  recon_mlp_sel<5, df>(qm2, qm1, q0, qp1, qp2, qp3, t0p, t0m, t1p, t1m, L, Rr);
+  recon_mlp_df<5>(qm2, qm1, q0, qp1, qp2, qp3, t0p, t0m, t1p, t1m, L, Rr);
 }
 
 // ---------------------------------------------------------------------------------------------
