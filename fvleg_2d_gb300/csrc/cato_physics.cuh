@@ -237,6 +237,34 @@ __device__ __forceinline__ void recon_tvd2(int lim, R qm1, R q0, R qp1, R qp2, R
   Rr = qp1 - R(0.5) * phi * dp;
 }
 
+// FP32 (mixed path): the limited slope phi(r) * dq without the ratio.  For r = d0/dq > 0,
+// minmod gives min(r, 1) dq = (|d0| < |dq| ? d0 : dq), superbee picks one of 2 d0, dq, d0, 2 dq,
+// and van Leer's 2r/(1+r) dq = 2 d0 dq / (dq + d0); r <= 0 gives 0.  Written with selects (no
+// data-dependent branches: the warp stays converged); the limiter id is uniform.
+__device__ __forceinline__ float tvd_slope_f32(int lim, float d0, float dq) {
+  const bool pos = d0 * dq > 0.0f;
+  const float a0 = fabsf(d0), aq = fabsf(dq);
+  float s;
+  if (lim == LIM_MINMOD) {
+    s = a0 < aq ? d0 : dq;
+  } else if (lim == LIM_SUPERBEE) {
+    const float lo = (2.0f * a0 <= aq) ? 2.0f * d0 : dq;   // r <= 1
+    const float hi = (a0 <= 2.0f * aq) ? d0 : 2.0f * dq;   // r > 1
+    s = (a0 <= aq) ? lo : hi;
+  } else {
+    s = __fdividef(2.0f * d0 * dq, dq + d0);
+  }
+  return pos ? s : 0.0f;
+}
+
+template <>
+__device__ __forceinline__ void recon_tvd2<float>(int lim, float qm1, float q0, float qp1,
+                                                  float qp2, float& L, float& Rr) {
+  const float dm = q0 - qm1, d0 = qp1 - q0, dp = qp2 - qp1;
+  L = q0 + 0.5f * tvd_slope_f32(lim, d0, dm);
+  Rr = qp1 - 0.5f * tvd_slope_f32(lim, d0, dp);
+}
+
 template <typename R, int ORDER>
 __device__ __forceinline__ void recon_mlp(R qm2, R qm1, R q0, R qp1, R qp2, R qp3, R t0p, R t0m,
                                           R t1p, R t1m, R& L, R& Rr) {
