@@ -498,12 +498,17 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
 #ifndef CATO_F32_BATCH_MIN_BLOCKS
 #define CATO_F32_BATCH_MIN_BLOCKS 3
 #endif
+// and for the FP64 kernels
+#ifndef CATO_F64_MIN_BLOCKS
+#define CATO_F64_MIN_BLOCKS 1
+#endif
 template <typename R> constexpr int min_blocks() {
-  return Prec<R>::kind == 2 ? CATO_DF_MIN_BLOCKS : (Prec<R>::kind == 1 ? CATO_F32_MIN_BLOCKS : 1);
+  return Prec<R>::kind == 2 ? CATO_DF_MIN_BLOCKS
+                            : (Prec<R>::kind == 1 ? CATO_F32_MIN_BLOCKS : CATO_F64_MIN_BLOCKS);
 }
 template <typename R> constexpr int batch_min_blocks() {
   return Prec<R>::kind == 2 ? CATO_DF_MIN_BLOCKS
-                            : (Prec<R>::kind == 1 ? CATO_F32_BATCH_MIN_BLOCKS : 1);
+                            : (Prec<R>::kind == 1 ? CATO_F32_BATCH_MIN_BLOCKS : CATO_F64_MIN_BLOCKS);
 }
 
 template <typename R, int NG, int FLUX, int RECON>
