@@ -269,8 +269,32 @@ def bench_precision(args, precision, dist, world, peak_gbs):
         },
         "clocks": clk.summary(),
     }
+    if precision == "fp64":
+        # The FP64 kernel is bound by GB300's FP64 pipe (2 FP64 thread-instructions per SM and
+        # cycle), not by HBM: FP64-pipe instructions per cell and stage from the ncu capture of
+        # the same kernel on the developed flow, over the stage time, against 2 x SMs x the SM
+        # clock sampled during the timed region.
+        ipc = profile_traffic().get("fp64_pipe_inst_per_cell_stage")
+        mhz = res["clocks"].get("sm_mhz") or res["clocks"].get("sm_max_mhz")
+        if ipc and mhz:
+            sms = _sm_count()
+            got = ipc * cells * len(per_stage) * args.steps / (sum(stage_ms) / 1e3) / 1e9
+            peak = 2 * sms * mhz / 1e3
+            res["roofline"]["fp64_pipe"] = {
+                "achieved": got, "peak": peak, "unit": "G FP64 thread-instructions/s",
+                "frac": got / peak, "instructions_per_cell_stage": ipc,
+                "source": "profiles/stage_kernel_fp64_quadrant2048_developed.md"}
     f.close()
     return res, cfg, prims
+
+
+def _sm_count() -> int:
+    try:
+        import torch
+
+        return torch.cuda.get_device_properties(env_int("LOCAL_RANK", 0)).multi_processor_count
+    except Exception:
+        return 152
 
 
 def bench_e2e(args, cfg, prims):
