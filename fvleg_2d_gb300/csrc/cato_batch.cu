@@ -432,7 +432,8 @@ int cato_batch_add(cato_batch* b, const cato_config* cfg, const double* rho, con
   long long n = (long long)d.ni * d.nj;
   int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 32);
   upload_init_kernel<<<blocks, 256, 0, b->stream>>>(
-      d.ni, d.nj, d.pitch, d.gamma, d.cfl, d.G.dx, d.G.dy, d.prim_raw[0], d.prim_raw[1],
+      d.ni, d.nj, d.pitch, d.gamma, d.cfl, d.G.dx, d.G.dy, nullptr, nullptr, d.prim_raw[0],
+      d.prim_raw[1],
       d.prim_raw[2], d.prim_raw[3], d.U[0][0], d.U[0][1], d.U[0][2], d.U[0][3],
       &b->d_descs[s].ctl);
   BK(cudaGetLastError());

@@ -11,6 +11,8 @@
 //               FP32) and the stage combine in FP64.
 // The primitives of an upload are kept (in a buffer not needed before the first step) because
 // the first stage after an upload uses them as is, like the reference after initialize.
+#include <cmath>
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -59,6 +61,8 @@ struct cato_handle {
   bool uploaded = false;
   bool raw_pending = false;  // next stage 1 uses prim_raw
   bool stepped = false;      // a step ran since the last upload (its stage buffers are valid)
+  double* rect[6] = {};      // rectilinear grid: dx, lx, 1/dx per column; dy, ly, 1/dy per row
+  float* rectf[2] = {};      // FP32 1/dx per column, 1/dy per row
   double* red = nullptr;     // reduction partials + results (lazy)
   Plan plan;
   FluxConsts<double> K64{};
@@ -449,6 +453,8 @@ int cato_gpu_destroy(cato_handle* h) {
   for (int k = 0; k < 4; ++k) cudaFree(h->halo[k]);
   cudaFree(h->ctl);
   cudaFree(h->red);
+  for (int k = 0; k < 6; ++k) cudaFree(h->rect[k]);
+  for (int k = 0; k < 2; ++k) cudaFree(h->rectf[k]);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
   if (h->own_stream_saved) h->stream = h->own_stream_saved;
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -479,7 +485,8 @@ int cato_gpu_upload_primitive(cato_handle* h, const double* rho, const double* u
   h->cur = 0;
   double** Un = h->U[0];
   upload_init_kernel<<<grid_for((long long)h->ni * h->nj), 256, 0, h->stream>>>(
-      h->ni, h->nj, h->pitch, h->cfg.gamma, h->cfg.cfl, h->G.dx, h->G.dy, h->prim_raw[0],
+      h->ni, h->nj, h->pitch, h->cfg.gamma, h->cfg.cfl, h->G.dx, h->G.dy, h->G.dxc, h->G.dyc,
+      h->prim_raw[0],
       h->prim_raw[1], h->prim_raw[2], h->prim_raw[3], Un[0], Un[1], Un[2], Un[3], h->ctl);
   CK(cudaGetLastError());
   if (h->cfg.precision == CATO_MIXED) {
@@ -847,6 +854,64 @@ int cato_gpu_profile_step(cato_handle* h, float* kernel_ms, int32_t capacity, in
   return CATO_OK;
 }
 
+// Per-column (or per-row) metrics of a rectilinear grid from its n + 1 nodes, with the
+// quad_cell.f90 formulas on an axis-aligned cell: width x(i+1) - x(i), edge length
+// sqrt(width^2 + 0^2) and the reciprocal width (FP64 and FP32).
+static __global__ void rect_metrics_kernel(const double* __restrict__ nodes, int n, double* d,
+                                           double* l, double* r, float* rf) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double w = nodes[i + 1] - nodes[i];
+    d[i] = w;
+    l[i] = sqrt(w * w + 0.0 * 0.0);
+    r[i] = 1.0 / w;
+    rf[i] = d2f_int(1.0 / w);
+  }
+}
+
+int cato_gpu_set_rectilinear(cato_handle* h, const double* x_nodes, const double* y_nodes) {
+  if (!h) return CATO_ERR_ARG;
+  if (!x_nodes != !y_nodes) return fail(h, CATO_ERR_ARG, "give both node arrays or neither");
+  CK(cudaStreamSynchronize(h->stream));
+  h->uploaded = false;  // the stored CFL dt and state were for the previous geometry
+  h->stepped = false;
+  if (!x_nodes) {  // back to the uniform dx x dy grid of the configuration
+    h->G.dxc = h->G.lxc = h->G.rdxc = h->G.dyc = h->G.lyc = h->G.rdyc = nullptr;
+    h->G.rdxf = h->G.rdyf = nullptr;
+    return CATO_OK;
+  }
+  const int n[2] = {h->ni, h->nj};
+  const double* nodes[2] = {x_nodes, y_nodes};
+  for (int a = 0; a < 2; ++a)
+    for (int k = 0; k < n[a]; ++k)
+      if (!(nodes[a][k + 1] > nodes[a][k]) || !std::isfinite(nodes[a][k + 1] - nodes[a][k]))
+        return fail(h, CATO_ERR_ARG, "node coordinates must be finite and strictly increasing");
+  for (int a = 0; a < 2; ++a) {
+    for (int k = 0; k < 3; ++k)
+      if (!h->rect[3 * a + k]) CK(cudaMalloc(&h->rect[3 * a + k], (n[a] + 1) * sizeof(double)));
+    if (!h->rectf[a]) CK(cudaMalloc(&h->rectf[a], (n[a] + 1) * sizeof(float)));
+  }
+  double* tmp = nullptr;
+  CK(cudaMalloc(&tmp, (std::max(h->ni, h->nj) + 1) * sizeof(double)));
+  for (int a = 0; a < 2; ++a) {
+    cudaError_t e = cudaMemcpyAsync(tmp, nodes[a], (n[a] + 1) * sizeof(double),
+                                    cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) {
+      rect_metrics_kernel<<<grid_for(n[a]), 256, 0, h->stream>>>(
+          tmp, n[a], h->rect[3 * a], h->rect[3 * a + 1], h->rect[3 * a + 2], h->rectf[a]);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+      cudaFree(tmp);
+      return cuda_fail(h, e, "cato_gpu_set_rectilinear");
+    }
+  }
+  cudaFree(tmp);
+  h->G.dxc = h->rect[0]; h->G.lxc = h->rect[1]; h->G.rdxc = h->rect[2]; h->G.rdxf = h->rectf[0];
+  h->G.dyc = h->rect[3]; h->G.lyc = h->rect[4]; h->G.rdyc = h->rect[5]; h->G.rdyf = h->rectf[1];
+  return CATO_OK;
+}
+
 static int reduce(cato_handle* h, RedArgs R, double out[RED_Q]) {
   if (!h->red) CK(cudaMalloc(&h->red, (RED_BLOCKS + 1) * RED_Q * sizeof(double)));
   R.ni = h->ni;
@@ -876,10 +941,12 @@ int cato_gpu_conservation_sums(cato_handle* h, double totals[4]) {
   R.mode = 0;
   double* const* U = state_now(h);
   for (int k = 0; k < 4; ++k) R.A[k] = U[k];
+  R.dxc = h->G.dxc;
+  R.dyc = h->G.dyc;
   double out[RED_Q];
   int rc = reduce(h, R, out);
   if (rc) return rc;
-  for (int k = 0; k < 4; ++k) totals[k] = out[k] * h->G.vol;
+  for (int k = 0; k < 4; ++k) totals[k] = h->G.dxc ? out[k] : out[k] * h->G.vol;
   return CATO_OK;
 }
 

@@ -23,7 +23,8 @@ static __global__ void step_begin_kernel(StepCtl* c) {
 // initialize_from_hdf5 + eos%primitive_to_conserved (equation_of_state.f90:316-324 through the
 // field operators) and the CFL dt of the raw primitives (mod_fluid.f90:249, 518-562).
 static __global__ void upload_init_kernel(int ni, int nj, int pitch, double gamma, double cfl, double dx,
-                                   double dy, const double* __restrict__ r_,
+                                   double dy, const double* __restrict__ dxc,
+                                   const double* __restrict__ dyc, const double* __restrict__ r_,
                                    const double* __restrict__ u_, const double* __restrict__ v_,
                                    const double* __restrict__ p_, double* rho, double* rhou,
                                    double* rhov, double* rhoE, StepCtl* ctl) {
@@ -46,7 +47,9 @@ static __global__ void upload_init_kernel(int ni, int nj, int pitch, double gamm
     rhoE[idx] = E;
     const double pr = abs_lt(p, TINY) ? 0.0 : p / r;
     const double cs = sqrt(gamma * pr);
-    const double d = cfl / (((fabs(u) + cs) / dx) + ((fabs(v) + cs) / dy));
+    // min_dx / min_dy of the cell: per column / row on a rectilinear grid
+    const double cdx = dxc ? dxc[i] : dx, cdy = dyc ? dyc[j] : dy;
+    const double d = cfl / (((fabs(u) + cs) / cdx) + ((fabs(v) + cs) / cdy));
     if (d < dmin) dmin = d;
     if (isnan(r) || isnan(u) || isnan(v) || isnan(p)) st |= ST_NAN;
     // initialize_from_hdf5 refuses ~0 density or pressure (mod_fluid.f90:352-360)
@@ -182,6 +185,8 @@ struct RedArgs {
   const double* A[4];
   const double* B[4];
   const float4* d1;       // mode 1, mixed path: first-stage increment (A1 = A + d1)
+  const double* dxc;      // mode 0 on a rectilinear grid: the sums are of A * dx_i * dy_j
+  const double* dyc;
   double* partials;       // RED_BLOCKS x RED_Q
 };
 
@@ -215,7 +220,7 @@ static __global__ void __launch_bounds__(RED_THREADS) reduce_partials_kernel(Red
       for (int k = 0; k < 4; ++k) {
         double a = R.A[k][idx];
         if (R.mode == 0) {
-          acc[k] += a;
+          acc[k] += R.dxc ? a * (R.dxc[i] * R.dyc[j] - 0.0 * 0.0) : a;
         } else {
           if (R.d1) a = a + (double)dd[k];
           const double df = R.B[k][idx] - a;

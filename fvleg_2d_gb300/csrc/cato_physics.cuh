@@ -911,7 +911,37 @@ struct Geom {
   double vol, l1, l2, l3, l4;  // volume, edge lengths (bottom, right, top, left)
   double dx, dy;               // min_dx / min_dy for the CFL step
   double inv_vol;              // 1/vol when vol is a power of two (x/vol == x*inv_vol exactly), else 0
+  // Rectilinear grids (null pointers on a uniform grid): per column i the cell width
+  // x(i+1) - x(i), its edge length and reciprocal; per row j the same in y.  Every pycato grid
+  // (uniform and layered, generate_initial_grids.py) is a tensor product of 1-D node arrays.
+  const double* dxc;
+  const double* lxc;
+  const double* rdxc;
+  const float* rdxf;
+  const double* dyc;
+  const double* lyc;
+  const double* rdyc;
+  const float* rdyf;
 };
+
+// quad_cell_t metrics of interior cell (i, j) (0-based) of a rectilinear grid, with the formulas
+// of quad_cell.f90 on the cell's four corners (x_i, y_j) .. (x_i+1, y_j+1): volume
+// dx dy - 0 * 0, edge lengths lx, ly, lx, ly snapped to the largest when they differ by
+// < 2 eps, min_dx = dx, min_dy = dy.  A uniform grid returns its constant metrics.
+__device__ __forceinline__ Geom cell_geom(const Geom& G, int i, int j) {
+  if (!G.dxc) return G;
+  Geom c = G;
+  const double dx = G.dxc[i], dy = G.dyc[j];
+  double lx = G.lxc[i], ly = G.lyc[j];
+  const double mx = rmax(rmax(rmax(lx, ly), lx), ly), mn = rmin(rmin(rmin(lx, ly), lx), ly);
+  if (mx - mn < 2.0 * 2.220446049250313080847263336181640625e-16) lx = ly = mx;
+  c.l1 = lx; c.l2 = ly; c.l3 = lx; c.l4 = ly;
+  c.vol = dx * dy - 0.0 * 0.0;
+  c.dx = dx;
+  c.dy = dy;
+  c.inv_vol = 0.0;
+  return c;
+}
 
 // quad_cell_t metrics of a dx x dy axis-aligned cell (quad_cell.f90:69-229): volume dx*dy,
 // edge lengths dx, dy, dx, dy (all set to the largest when they differ by < 2 eps),

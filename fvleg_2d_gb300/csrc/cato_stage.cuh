@@ -304,10 +304,13 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
   // mixed_df constants of the update (unused by the other paths)
   [[maybe_unused]] df dx_inv, dy_inv, cfl_df;
   if constexpr (Prec<R>::kind == 2) {
-    dx_inv = to_df(1.0 / A.G.dx);
+    dx_inv = to_df(A.G.rdxc ? A.G.rdxc[min(max(gx, 0), A.ni - 1)] : 1.0 / A.G.dx);
     dy_inv = to_df(1.0 / A.G.dy);
     cfl_df = to_df(A.cfl);
   }
+  // FP32 reciprocal cell width of this thread's column (mixed path)
+  [[maybe_unused]] const float idx_col =
+      A.G.rdxf ? A.G.rdxf[min(max(gx, 0), A.ni - 1)] : (float)(1.0 / A.G.dx);
 
   // prologue: rows y0-NG .. y0+NG-1
   for (int r = y0 - NG; r < y0 + NG; ++r) {
@@ -382,6 +385,11 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
     __syncthreads();
     if (in_cell) {
       double un[4];
+      // the cell's metrics (constants on a uniform grid)
+      const Geom cg = cell_geom(A.G, gx, j);
+      if constexpr (Prec<R>::kind == 2) {
+        if (A.G.rdyc) dy_inv = to_df(A.G.rdyc[j]);
+      }
       if constexpr (Prec<R>::kind != 1) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -390,7 +398,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
           const R Fjm = sfj[(((j - 1) & 1) * 4 + k) * T + t];
           double L;
           if constexpr (Prec<R>::kind == 0)
-            L = divergence_fp64(Fi, Fim, Fj, Fjm, A.G);
+            L = divergence_fp64(Fi, Fim, Fj, Fjm, cg);
           else  // double-float flux differences, the result carried to FP64
             L = from_df(-((Fi - Fim) * dx_inv + (Fj - Fjm) * dy_inv));
           double r;
@@ -410,7 +418,8 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
         }
       } else {
         const float ccf = (float)cc, bf = (float)A.b;
-        const float idx_f = (float)(1.0 / A.G.dx), idy_f = (float)(1.0 / A.G.dy);
+        const float idx_f = idx_col;
+        const float idy_f = A.G.rdyf ? A.G.rdyf[j] : (float)(1.0 / A.G.dy);
         float dn[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -435,7 +444,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
         if constexpr (Prec<R>::kind == 0) {
           double u, v, p, cs;
           prim_from_cons(A.gamma, A.gamma - 1.0, un[0], un[1], un[2], un[3], u, v, p, cs);
-          double d = A.cfl / (((fabs(u) + cs) / A.G.dx) + ((fabs(v) + cs) / A.G.dy));
+          double d = A.cfl / (((fabs(u) + cs) / cg.dx) + ((fabs(v) + cs) / cg.dy));
           if (d < dt_loc) dt_loc = d;
           if (isnan(un[0]) || isnan(u) || isnan(v) || isnan(p)) st_loc |= ST_NAN;
           if (un[0] < 0.0) st_loc |= ST_NEG_DENSITY;
@@ -457,8 +466,9 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
           float u, v, p, cs;
           prim_from_cons((float)A.gamma, (float)(A.gamma - 1.0), uf.x, uf.y, uf.z, uf.w, u, v,
                          p, cs);
-          float d = (float)A.cfl / ((fabsf(u) + cs) * (float)(1.0 / A.G.dx) +
-                                    (fabsf(v) + cs) * (float)(1.0 / A.G.dy));
+          float d = (float)A.cfl / ((fabsf(u) + cs) * idx_col +
+                                    (fabsf(v) + cs) * (A.G.rdyf ? A.G.rdyf[j]
+                                                                : (float)(1.0 / A.G.dy)));
           double dd = f2d_int(d);
           if (__double_as_longlong(dd) < __double_as_longlong(dt_loc) && d > 0.0f) dt_loc = dd;
           if (isnan(uf.x) || isnan(u) || isnan(v) || isnan(p)) st_loc |= ST_NAN;

@@ -71,6 +71,24 @@ class _Handle:
     def ld(self) -> int:
         return self.cfg.halo_shape[0]
 
+    def set_rectilinear(self, x_nodes, y_nodes):
+        """Non-uniform tensor-product grid: interior node coordinates x(1..ni+1), y(1..nj+1),
+        strictly increasing (the uniform and layered grids of pycato's
+        generate_initial_grids.py:43-380, whose cells are axis-aligned).  ``None, None`` returns
+        to the configuration's uniform dx x dy.  Call before ``initialize``."""
+        if x_nodes is None and y_nodes is None:
+            xs = ys = None
+        else:
+            xs = np.ascontiguousarray(x_nodes, dtype=np.float64)
+            ys = np.ascontiguousarray(y_nodes, dtype=np.float64)
+            if xs.shape != (self.cfg.ni + 1,) or ys.shape != (self.cfg.nj + 1,):
+                raise ValueError(f"expected {self.cfg.ni + 1} x nodes and {self.cfg.nj + 1} "
+                                 f"y nodes, got {xs.shape} and {ys.shape}")
+        _check(self.L.cato_gpu_set_rectilinear(self.h, _lib.ptr(xs), _lib.ptr(ys)), self.h,
+               "set_rectilinear")
+        self.nodes = None if xs is None else (xs, ys)
+        return self
+
 
 class Fluid(_Handle):
     """fluid_t on the GPU.  ``Fluid(cfg).initialize(rho, u, v, p)`` replaces
@@ -181,7 +199,10 @@ class Fluid(_Handle):
     def t(self):
         """Time derivative of the current state (fluid_t%t, mod_fluid.f90:460-516)."""
         s = self.state(("rho", "u", "v", "p"))
-        return FluxSolver(self.cfg).solve(s["rho"], s["u"], s["v"], s["p"])
+        fs = FluxSolver(self.cfg)
+        if getattr(self, "nodes", None) is not None:
+            fs.set_rectilinear(*self.nodes)
+        return fs.solve(s["rho"], s["u"], s["v"], s["p"])
 
 
 class FluxSolver(_Handle):

@@ -144,6 +144,15 @@ const char* cato_gpu_last_error(const cato_handle* h);
 int cato_gpu_upload_primitive(cato_handle* h, const double* rho, const double* u,
                               const double* v, const double* p, int64_t ld);
 
+/* Rectilinear (tensor-product) grid: the interior node coordinates x(1..ni+1) and y(1..nj+1),
+ * strictly increasing, in place of the configuration's uniform dx x dy.  Covers the uniform and
+ * the layered grids of pycato (generate_initial_grids.py:43-113, 166-380), whose cells are
+ * axis-aligned; the cell metrics follow quad_cell.f90:69-229 (volume, edge lengths with their
+ * 2-eps snap, min_dx / min_dy per cell).  Replaces the grid part of
+ * grid_block_2d_t%initialize (grid_block_2d.f90:54-151) for such grids.  Both pointers NULL
+ * returns to the uniform grid.  The state must be uploaded (again) afterwards. */
+int cato_gpu_set_rectilinear(cato_handle* h, const double* x_nodes, const double* y_nodes);
+
 /* CFL time step of the current state.  Replaces fluid_t%get_timestep (mod_fluid.f90:518-562). */
 int cato_gpu_get_timestep(cato_handle* h, double* dt);
 

@@ -130,6 +130,29 @@ static geom_t uniform_geom(const cato_config* c) {
   return g;
 }
 
+/* Per-cell metrics of a rectilinear grid with node coordinates x(1..ni+1), y(1..nj+1): the
+ * quad_cell_t of every interior cell on its corners in the order of
+ * grid_block_2d_t%populate_element_specifications (grid_block_2d.f90:370-387):
+ * (x_i, y_j), (x_i+1, y_j), (x_i+1, y_j+1), (x_i, y_j+1).  Cell (i, j) is entry
+ * (j-1)*ni + (i-1).  NULL on a bad grid (nodes not strictly increasing). */
+static geom_t* rect_cells(int ni, int nj, const double* xn, const double* yn) {
+  for (int i = 0; i < ni; ++i)
+    if (!(xn[i + 1] > xn[i])) return NULL;
+  for (int j = 0; j < nj; ++j)
+    if (!(yn[j + 1] > yn[j])) return NULL;
+  geom_t* g = (geom_t*)malloc(sizeof(geom_t) * (size_t)ni * nj);
+  if (!g) return NULL;
+  for (int j = 0; j < nj; ++j)
+    for (int i = 0; i < ni; ++i) {
+      double x[4] = {xn[i], xn[i + 1], xn[i + 1], xn[i]};
+      double y[4] = {yn[j], yn[j], yn[j + 1], yn[j + 1]};
+      double nv[8];
+      geom_t* c = &g[(size_t)j * ni + i];
+      oracle_quad_metrics(x, y, &c->vol, c->l, nv, &c->dx, &c->dy);
+    }
+  return g;
+}
+
 /* ------------------------------------------------------------------------------------------ */
 /* limiters as inlined in muscl_tvd2.fypp:195-213                                              */
 /* ------------------------------------------------------------------------------------------ */
@@ -916,9 +939,11 @@ static double divergence(double Fi, double Fim, double Fj, double Fjm, const geo
 }
 
 /* flux_solver_t%solve for the edge-split solvers (e.g. slau_solver.fypp:123-249): BCs on the
- * primitives, reconstruction, edge fluxes, flux divergence.  d_* are halo-padded, ghosts 0. */
-int oracle_solve(const cato_config* c, double* rho, double* u, double* v, double* p,
-                 double* drho, double* drhou, double* drhov, double* drhoE) {
+ * primitives, reconstruction, edge fluxes, flux divergence.  d_* are halo-padded, ghosts 0.
+ * `cells` holds per-cell metrics (rect_cells) or is NULL for the uniform dx x dy grid. */
+static int solve_geo(const cato_config* c, const geom_t* cells, double* rho, double* u,
+                     double* v, double* p, double* drho, double* drhou, double* drhov,
+                     double* drhoE) {
   dims_t d = mkdims(c);
   geom_t geo = uniform_geom(c);
   oracle_apply_bc(c, rho, u, v, p);
@@ -958,10 +983,27 @@ int oracle_solve(const cato_config* c, double* rho, double* u, double* v, double
     for (int i = 1; i <= d.ni; ++i)
       for (int k = 0; k < 4; ++k)
         AT(out[k], i, j) = divergence(IF(iflux, k, i, j), IF(iflux, k, i - 1, j),
-                                      JF(jflux, k, i, j), JF(jflux, k, i, j - 1), &geo);
+                                      JF(jflux, k, i, j), JF(jflux, k, i, j - 1),
+                                      cells ? &cells[(size_t)(j - 1) * d.ni + (i - 1)] : &geo);
   free(iflux);
   free(jflux);
   return 0;
+}
+
+int oracle_solve(const cato_config* c, double* rho, double* u, double* v, double* p,
+                 double* drho, double* drhou, double* drhov, double* drhoE) {
+  return solve_geo(c, NULL, rho, u, v, p, drho, drhou, drhov, drhoE);
+}
+
+int oracle_solve_rect(const cato_config* c, const double* x_nodes, const double* y_nodes,
+                      double* rho, double* u, double* v, double* p, double* drho, double* drhou,
+                      double* drhov, double* drhoE) {
+  if (oracle_config_check(c) != CATO_OK) return CATO_ERR_CONFIG;
+  geom_t* cells = rect_cells(c->ni, c->nj, x_nodes, y_nodes);
+  if (!cells) return CATO_ERR_ARG;
+  int rc = solve_geo(c, cells, rho, u, v, p, drho, drhou, drhov, drhoE);
+  free(cells);
+  return rc;
 }
 
 /* ------------------------------------------------------------------------------------------ */
@@ -971,6 +1013,7 @@ struct oracle_fluid {
   cato_config c;
   dims_t d;
   geom_t geo;
+  geom_t* cells; /* per-cell metrics of a rectilinear grid (rect_cells), NULL if uniform */
   /* conserved (U) and derived (u, v, p, cs) of the current state */
   double *rho, *rhou, *rhov, *rhoE, *u, *v, *p, *cs;
   /* scratch: stage states, primitive copies for the solver, residuals */
@@ -1006,6 +1049,7 @@ void oracle_destroy(oracle_fluid* f) {
   for (int s = 0; s < 3; ++s)
     for (int k = 0; k < 4; ++k) free(f->st[s][k]);
   for (int k = 0; k < 4; ++k) { free(f->sp[k]); free(f->L[k]); }
+  free(f->cells);
   free(f);
 }
 
@@ -1097,10 +1141,14 @@ int oracle_set_conserved(oracle_fluid* f, const double* rho, const double* rho_u
 double oracle_get_timestep(oracle_fluid* f) {
   dims_t d = f->d;
   double m = INFINITY;
-  const double cfl = f->c.cfl, dx = f->geo.dx, dy = f->geo.dy;
+  const double cfl = f->c.cfl;
+  const geom_t* cells = f->cells;
+  const geom_t geo = f->geo;
 #pragma omp parallel for reduction(min : m) schedule(static)
   for (int j = 1; j <= d.nj; ++j)
     for (int i = 1; i <= d.ni; ++i) {
+      const geom_t* g = cells ? &cells[(size_t)(j - 1) * d.ni + (i - 1)] : &geo;
+      const double dx = g->dx, dy = g->dy;
       double cs = AT(f->cs, i, j);
       double t = cfl / (((fabs(AT(f->u, i, j)) + cs) / dx) + ((fabs(AT(f->v, i, j)) + cs) / dy));
       if (t < m) m = t;
@@ -1116,8 +1164,8 @@ static int residual(oracle_fluid* f, const double* pr, const double* pu, const d
   memcpy(f->sp[1], pu, n);
   memcpy(f->sp[2], pv, n);
   memcpy(f->sp[3], pp, n);
-  return oracle_solve(&f->c, f->sp[0], f->sp[1], f->sp[2], f->sp[3], f->L[0], f->L[1], f->L[2],
-                      f->L[3]);
+  return solve_geo(&f->c, f->cells, f->sp[0], f->sp[1], f->sp[2], f->sp[3], f->L[0], f->L[1],
+                   f->L[2], f->L[3]);
 }
 
 /* out = A + L*c with the field '+' flush (fluid operators mod_fluid.f90:609-669) */
@@ -1185,9 +1233,24 @@ int oracle_conservation_sums(oracle_fluid* f, double out[4]) {
   for (int k = 0; k < 4; ++k) {
     double s = 0.0;
     for (int j = 1; j <= d.nj; ++j)
-      for (int i = 1; i <= d.ni; ++i) s += AT(U[k], i, j);
-    out[k] = s * f->geo.vol;
+      for (int i = 1; i <= d.ni; ++i)
+        s += f->cells ? AT(U[k], i, j) * f->cells[(size_t)(j - 1) * d.ni + (i - 1)].vol
+                      : AT(U[k], i, j);
+    out[k] = f->cells ? s : s * f->geo.vol;
   }
+  return CATO_OK;
+}
+
+/* Rectilinear grid of node coordinates x(1..ni+1), y(1..nj+1); both NULL = uniform again. */
+int oracle_set_rectilinear(oracle_fluid* f, const double* x_nodes, const double* y_nodes) {
+  if (!x_nodes != !y_nodes) return CATO_ERR_ARG;
+  geom_t* cells = NULL;
+  if (x_nodes) {
+    cells = rect_cells(f->d.ni, f->d.nj, x_nodes, y_nodes);
+    if (!cells) return CATO_ERR_ARG;
+  }
+  free(f->cells);
+  f->cells = cells;
   return CATO_OK;
 }
 

@@ -38,6 +38,10 @@ int oracle_interpolate_edges(const cato_config* cfg, const double* q, double* i_
                              double* j_edges);
 int oracle_solve(const cato_config* cfg, double* rho, double* u, double* v, double* p,
                  double* d_rho_dt, double* d_rho_u_dt, double* d_rho_v_dt, double* d_rho_E_dt);
+/* oracle_solve on the rectilinear grid of node coordinates x(1..ni+1), y(1..nj+1). */
+int oracle_solve_rect(const cato_config* cfg, const double* x_nodes, const double* y_nodes,
+                      double* rho, double* u, double* v, double* p, double* d_rho_dt,
+                      double* d_rho_u_dt, double* d_rho_v_dt, double* d_rho_E_dt);
 
 /* Whole fluid_t. */
 oracle_fluid* oracle_create(const cato_config* cfg);
@@ -56,6 +60,7 @@ int64_t oracle_iteration(oracle_fluid* f);
 int oracle_convergence(oracle_fluid* f, double out[4]);
 /* interior totals of rho, rho u, rho v, rho E times the cell volume */
 int oracle_conservation_sums(oracle_fluid* f, double out[4]);
+int oracle_set_rectilinear(oracle_fluid* f, const double* x_nodes, const double* y_nodes);
 
 #ifdef __cplusplus
 }

@@ -49,6 +49,8 @@ def lib():
                                            _dp, _dp, _dp, _dp]
         L.oracle_interpolate_edges.argtypes = [cfgp, _dp, _dp, _dp]
         L.oracle_solve.argtypes = [cfgp] + [_dp] * 8
+        L.oracle_solve_rect.argtypes = [cfgp] + [_dp] * 10
+        L.oracle_set_rectilinear.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.oracle_create.restype = ctypes.c_void_p
         L.oracle_create.argtypes = [cfgp]
         L.oracle_destroy.argtypes = [ctypes.c_void_p]
@@ -130,11 +132,18 @@ def interpolate_edges(cfg: SchemeConfig, q):
     return ie, je
 
 
-def solve(cfg: SchemeConfig, rho, u, v, p):
-    """flux_solver_t%solve: BCs written into the ghosts of rho/u/v/p; returns d/dt of U."""
+def solve(cfg: SchemeConfig, rho, u, v, p, nodes=None):
+    """flux_solver_t%solve: BCs written into the ghosts of rho/u/v/p; returns d/dt of U.
+    ``nodes = (x(1..ni+1), y(1..nj+1))`` selects a rectilinear grid."""
     out = [empty_field(cfg) for _ in range(4)]
-    rc = lib().oracle_solve(_cfg(cfg), _ptr(rho), _ptr(u), _ptr(v), _ptr(p),
-                            *(_ptr(a) for a in out))
+    if nodes is None:
+        rc = lib().oracle_solve(_cfg(cfg), _ptr(rho), _ptr(u), _ptr(v), _ptr(p),
+                                *(_ptr(a) for a in out))
+    else:
+        xs, ys = (np.ascontiguousarray(a, dtype=np.float64) for a in nodes)
+        rc = lib().oracle_solve_rect(_cfg(cfg), xs.ctypes.data_as(_dp), ys.ctypes.data_as(_dp),
+                                     _ptr(rho), _ptr(u), _ptr(v), _ptr(p),
+                                     *(_ptr(a) for a in out))
     if rc != 0:
         raise RuntimeError(f"oracle_solve failed: {rc}")
     return out
@@ -155,6 +164,14 @@ class OracleFluid:
         if h:
             lib().oracle_destroy(h)
             self._h = None
+
+    def set_rectilinear(self, x_nodes, y_nodes) -> None:
+        """Rectilinear grid of node coordinates x(1..ni+1), y(1..nj+1)."""
+        xs, ys = (np.ascontiguousarray(a, dtype=np.float64) for a in (x_nodes, y_nodes))
+        rc = lib().oracle_set_rectilinear(self._h, xs.ctypes.data_as(_dp),
+                                          ys.ctypes.data_as(_dp))
+        if rc:
+            raise ValueError(f"oracle_set_rectilinear: {rc}")
 
     def set_primitive(self, rho, u, v, p) -> None:
         arrs = [np.asfortranarray(a, dtype=np.float64) for a in (rho, u, v, p)]
