@@ -371,6 +371,45 @@ def bench_kh(args, peak_gbs):
     return out
 
 
+def layered_grid_nodes(n: int) -> tuple:
+    """Interior nodes of an n x n pycato-style grid on [0,1]^2: x in three constant-spacing
+    layers (n/8 cells over 0.05, n/4 over 0.2, the rest over 0.75, stitched like
+    make_2d_layered_grid), y from numpy.linspace (make_uniform_grid)."""
+    import numpy as np
+
+    counts = (n // 8, n // 4, n - n // 8 - n // 4)
+    parts, start = [], 0.0
+    for thickness, count in zip((0.05, 0.2, 0.75), counts):
+        parts.append(np.linspace(start, start + thickness, count + 1))
+        start += thickness
+    return np.unique(np.concatenate(parts)), np.linspace(0.0, 1.0, n + 1)
+
+
+def bench_rectilinear(args, uniform_values):
+    """The rectilinear-grid path (per-column / per-row metrics, per-cell volume and division):
+    the developed quadrant state on a layered n x n grid, each precision against its
+    uniform-grid value."""
+    from fvleg_2d_gb300.fluid import Fluid
+
+    cfg0, prims = quadrant_state(args)
+    xs, ys = layered_grid_nodes(args.n)
+    out = {"workload": (f"developed quadrant state on a {args.n}x{args.n} layered grid "
+                        "(x: 3 constant-spacing layers, cell widths 1 : 2 : 3, y: linspace)")}
+    for precision in ("fp64", "mixed", "mixed_df"):
+        cfg = dataclasses.replace(cfg0, precision=precision)
+        f = Fluid(cfg).set_rectilinear(xs, ys).initialize(*prims)
+        f.run_timed(args.warmup)
+        with ClockSampler(env_int("LOCAL_RANK", 0)) as clk:
+            total_ms, _ = f.run_timed(args.steps, per_kernel=False)
+        value = cfg.ni * cfg.nj * args.steps / (total_ms / 1e3)
+        out[precision] = {"value": value, "unit": "cell-updates/s",
+                          "ms_per_step": total_ms / args.steps,
+                          "vs_uniform_grid": value / uniform_values[precision],
+                          "clocks": clk.summary()}
+        f.close()
+    return out
+
+
 def bench_batched(args):
     """Config 3: 256 uneven grids (sides log-uniform [64,1024] rounded to 16, aspect U[1,4]),
     random circles, SLAU + MLP5, SSP-RK2, CFL 0.5, 500 steps each; one persistent launch per
@@ -496,6 +535,7 @@ def main() -> int:
     ap.add_argument("--batch-seed", type=int, default=2024)
     ap.add_argument("--batch-ref", type=int, default=8)
     ap.add_argument("--batch-precisions", default="mixed,mixed_df")
+    ap.add_argument("--no-rectilinear", action="store_true")
     ap.add_argument("--no-kh", action="store_true")
     ap.add_argument("--kh-n", type=int, default=8192)
     ap.add_argument("--kh-steps", type=int, default=200)
@@ -536,6 +576,8 @@ def main() -> int:
         cpu = {"value": v, "unit": "cell-updates/s", "cores": used, "kind": "port",
                "sample": f"{args.cpu_baseline_steps} SSP-RK3 steps of the same {args.n}^2 grid "
                          f"({secs:.1f} s, OpenMP C restatement of the reference)"}
+    rect = None if args.no_rectilinear else bench_rectilinear(
+        args, {"fp64": fp64["value"], "mixed": mixed["value"], "mixed_df": mixed_df["value"]})
     kh = None if args.no_kh else bench_kh(args, peak)
     batched = None if args.no_batched else bench_batched(args)
     serving = None if args.no_serving else bench_serving(args)
@@ -580,6 +622,7 @@ def main() -> int:
             "gpu_launches": mixed_df["launches_per_step"] * args.steps,
             "clocks": mixed_df["clocks"], "e2e": e2e_df,
         },
+        "rectilinear": rect,
         "kelvin_helmholtz": kh,
         "batched": batched,
         "serving": serving,

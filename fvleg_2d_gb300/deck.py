@@ -5,15 +5,16 @@ keys and defaults (``mod_input.f90:34-155``).  Values may be quoted with single 
 ``;`` and ``#`` start comments, logicals are ``true``/``.true.``/``t`` (any case) and reals may
 use a Fortran ``d`` exponent.
 
-A deck whose initial conditions come from an HDF5 file (``read_from_file = true``) needs the grid
-size and spacing from that file: pass ``ni, nj, dx, dy`` to :meth:`Deck.scheme` and upload the
-file's primitives through :class:`fvleg_2d_gb300.fluid.Fluid` (there is no HDF5 library in this
-build).  A deck with ``read_from_file = false`` is complete: its uniform initial state and grid
-come from the deck (``[initial_conditions] init_*``, ``[grid] ni_nodes ... ymax``).
+A deck whose initial conditions come from a file (``read_from_file = true``) takes its grid and
+state from that file in pycato's layout (:mod:`.icfile`; ``.npz`` stands in for HDF5, which has
+no library in this build): :func:`run_deck` loads it.  A deck with ``read_from_file = false`` is
+complete: its uniform initial state and grid come from the deck (``[initial_conditions] init_*``,
+``[grid] ni_nodes ... ymax``).
 """
 from __future__ import annotations
 
 import configparser
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -237,15 +238,44 @@ def read_deck(path: str) -> Deck:
         return parse_deck(f.read())
 
 
-def run_deck(deck: Deck, precision: str = "fp64", prims=None, grid=None):
-    """The main.f90 time loop for a deck: returns (fluid, steps).  For a deck that reads its
-    initial state from a file, pass that state as ``prims`` (rho, u, v, p, halo-padded) and its
-    grid as ``grid=(ni, nj, dx, dy)``."""
+def load_initial_condition(deck: Deck, base_dir: str = "."):
+    """The deck's initial-condition file (pycato layout, see :mod:`.icfile`) in the reference's
+    non-dimensional units."""
+    from .icfile import read_ic
+
+    path = deck.initial_condition_file
+    if not os.path.isabs(path):
+        path = os.path.join(base_dir, path)
+    return read_ic(path, deck.n_ghost_layers, deck.reference_length, deck.reference_density,
+                   deck.reference_velocity, deck.non_dimensionalize)
+
+
+def t_to_nondim(deck: Deck) -> float:
+    """1 / t_ref with t_ref = reference_length / reference_velocity
+    (``non_dimensional.f90:95-118``); 1 without non-dimensionalization."""
+    if not deck.non_dimensionalize:
+        return 1.0
+    return 1.0 / (deck.reference_length / deck.reference_velocity)
+
+
+def run_deck(deck: Deck, precision: str = "fp64", prims=None, grid=None, base_dir: str = "."):
+    """The main.f90 time loop for a deck: returns (fluid, steps).  A deck that reads its
+    initial state from a file loads it (grid included) from ``initial_condition_file`` relative
+    to ``base_dir``; alternatively pass that state as ``prims`` (rho, u, v, p, halo-padded) and
+    a uniform grid as ``grid=(ni, nj, dx, dy)``.  ``max_time`` is scaled by ``t_to_nondim``
+    as in ``main.f90:98``."""
     from .fluid import Fluid
 
+    ic = None
+    if deck.read_from_file and prims is None:
+        ic = load_initial_condition(deck, base_dir)
+        grid, prims = ic.scheme_grid(), ic.primitives
     cfg = deck.scheme(*(grid or (None, None, None, None)), precision=precision)
     if prims is None:
         prims = deck.initial_primitives(cfg)
-    fluid = Fluid(cfg).initialize(*prims)
-    steps = fluid.run(deck.max_time, deck.max_iterations)
+    fluid = Fluid(cfg)
+    if ic is not None:
+        ic.apply_grid(fluid)
+    fluid.initialize(*prims)
+    steps = fluid.run(deck.max_time * t_to_nondim(deck), deck.max_iterations)
     return fluid, steps

@@ -4,7 +4,8 @@ import numpy as np
 import pytest
 
 from conftest import interior
-from fvleg_2d_gb300.deck import parse_deck, run_deck
+from fvleg_2d_gb300.deck import load_initial_condition, parse_deck, run_deck, t_to_nondim
+from test_icfile_cpu import layered_nodes, make_file, uniform_nodes
 
 pytestmark = pytest.mark.gpu
 
@@ -54,3 +55,49 @@ def test_run_deck_matches_oracle(oracle, cato_lib):
         np.testing.assert_array_equal(interior(cfg, b[k]), interior(cfg, a[k]), err_msg=k)
     # the outflow boundary at 2.0 < 2.5 drives an expansion into the box
     assert interior(cfg, b["rho"]).min() < 1.2
+
+
+FILE_DECK = """
+[reference_state]
+reference_length = 0.5
+reference_density = 1.5
+reference_velocity = 2.0e5
+[time]
+max_time = 1.5e-6
+integration_strategy = 'ssp_rk2'
+cfl = 0.5
+[physics]
+polytropic_index = 1.6667
+[scheme]
+flux_solver = 'SLAU2'
+limiter = 'MLP5'
+[initial_conditions]
+read_from_file = true
+initial_condition_file = 'layered.npz'
+[boundary_conditions]
+plus_x = 'zero_gradient'
+minus_x = 'symmetry'
+plus_y = 'periodic'
+minus_y = 'periodic'
+"""
+
+
+def test_run_deck_from_layered_file_matches_oracle(oracle, cato_lib, tmp_path):
+    """A file-driven deck (read_from_file) on a pycato layered grid: the GPU run and the oracle
+    on the file's rectilinear grid agree bit for bit."""
+    ng = 3
+    xn = layered_nodes([(0.05, 12), (0.2, 20), (0.75, 40)], ng)
+    make_file(str(tmp_path / "layered.npz"), xn, uniform_nodes(24, 0.0, 0.3, ng), ng, seed=4)
+    deck = parse_deck(FILE_DECK)
+    fluid, steps = run_deck(deck, base_dir=str(tmp_path))
+    ic = load_initial_condition(deck, str(tmp_path))
+    assert ic.uniform is None
+    cfg = deck.scheme(*ic.scheme_grid())
+    ref = oracle.OracleFluid(cfg)
+    ref.set_rectilinear(ic.x_nodes, ic.y_nodes)
+    ref.set_primitive(*ic.primitives)
+    n = ref.run(deck.max_time * t_to_nondim(deck))
+    assert steps == n > 3 and fluid.time == ref.time
+    a, b = ref.state(), fluid.state()
+    for k in ("rho", "rho_u", "rho_v", "rho_E"):
+        np.testing.assert_array_equal(interior(cfg, b[k]), interior(cfg, a[k]), err_msg=k)
