@@ -53,6 +53,7 @@ def load(build_if_missing: bool = False):
         "cato_gpu_last_error": (ctypes.c_char_p, [H]),
         "cato_gpu_upload_primitive": (ctypes.c_int, [H, _dp, _dp, _dp, _dp, i64]),
         "cato_gpu_set_rectilinear": (ctypes.c_int, [H, _dp, _dp]),
+        "cato_gpu_set_bc_table": (ctypes.c_int, [H, ctypes.c_int32, _dp, _dp, _dp]),
         "cato_gpu_get_timestep": (ctypes.c_int, [H, _dp]),
         "cato_gpu_integrate": (ctypes.c_int, [H, ctypes.c_double, _dp,
                                               ctypes.POINTER(ctypes.c_int32)]),

@@ -71,7 +71,7 @@ def _units() -> list[tuple[str, list[str]]]:
                 units.append((obj, cmd))
     # longest first, so that the slow double-float units start before the rest
     units.sort(key=lambda u: 0 if "-DCATO_REAL=df" in u[1] else 1)
-    for src in ("cato_capi.cu", "cato_batch.cu", "cato_noalloc.cu"):
+    for src in ("cato_capi.cu", "cato_batch.cu", "cato_noalloc.cu", "cato_pbc.cu"):
         path = os.path.join(CSRC, src)
         if not os.path.exists(path):
             continue

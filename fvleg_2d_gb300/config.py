@@ -38,7 +38,7 @@ RK_IDS = {
 }
 # bc_factory.f90:46-59 names
 BC_IDS = {"zero_gradient": 0, "symmetry": 1, "mirror": 1, "reflection": 1, "periodic": 2,
-          "outlet": 3, "outflow": 3}
+          "outlet": 3, "outflow": 3, "pressure_input": 4}
 PRECISION_IDS = {"fp64": 0, "mixed": 1, "mixed_df": 2}
 # side order of cato_config.bc: the reference's application order (flux_solver.f90:165-183)
 SIDES = ("+x", "+y", "-x", "-y")
@@ -54,6 +54,8 @@ CATO_ERR_CUDA = 12
 CATO_ERR_ARG = 13
 CATO_ERR_TIMEOUT = 14
 CATO_ERR_STATE = 15
+CATO_ERR_CAPACITY = 16
+CATO_ERR_BC_INPUT = 17
 STATUS_NAMES = {
     0: "ALL_OK",
     1: "NEG_DENSITY",
@@ -65,6 +67,8 @@ STATUS_NAMES = {
     13: "ERR_ARG",
     14: "ERR_TIMEOUT",
     15: "ERR_STATE",
+    16: "ERR_CAPACITY",
+    17: "ERR_BC_INPUT",
 }
 
 
@@ -93,6 +97,7 @@ class CatoConfig(ctypes.Structure):
         ("ausm_ku", ctypes.c_double),
         ("ausm_sigma", ctypes.c_double),
         ("bc_pressure", ctypes.c_double),
+        ("bc_density", ctypes.c_double),
     ]
 
 
@@ -123,6 +128,11 @@ class SchemeConfig:
     ausm_ku: float = 0.75
     ausm_sigma: float = 1.0
     outflow_ambient_pressure: float = 0.0  # [boundary_conditions], for 'outflow' sides
+    # constant target of a 'pressure_input' side (non-dimensional; a table replaces both,
+    # Fluid.set_bc_table).  The reference keeps the outflow pressure and this one in the same
+    # variable, the outflow value winning when both BCs are present (mod_input.f90:366-390).
+    constant_bc_pressure: float = 0.0
+    bc_density: float = 0.0
     n_ghost: int | None = None
 
     def ghost_layers(self) -> int:
@@ -150,7 +160,9 @@ class SchemeConfig:
         c.harten_delta = self.harten_delta
         c.ausm_beta, c.ausm_kp = self.ausm_beta, self.ausm_kp
         c.ausm_ku, c.ausm_sigma = self.ausm_ku, self.ausm_sigma
-        c.bc_pressure = self.outflow_ambient_pressure
+        outlet = any(BC_IDS[self.bc[s]] == 3 for s in SIDES)
+        c.bc_pressure = self.outflow_ambient_pressure if outlet else self.constant_bc_pressure
+        c.bc_density = self.bc_density
         return c
 
     @property

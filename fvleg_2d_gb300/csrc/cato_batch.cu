@@ -356,6 +356,8 @@ int cato_batch_add(cato_batch* b, const cato_config* cfg, const double* rho, con
   int rc = cato_config_check(cfg);
   if (rc != CATO_OK) return rc;
   if (cfg->precision != b->prec || cfg->rk != b->rk) return CATO_ERR_CONFIG;
+  // the pressure-input boundary runs per-stage kernels of its own: single handles only
+  if (cfg->bc[CATO_PLUS_X] == CATO_BC_PRESSURE_INPUT) return CATO_ERR_CONFIG;
   if (ld < cfg->ni + 2 * cfg->n_ghost) return CATO_ERR_ARG;
   int s = -1;
   for (int i = 0; i < b->capacity; ++i)

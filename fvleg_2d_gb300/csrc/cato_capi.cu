@@ -22,6 +22,7 @@
 #include "../../include/cato_gpu.h"
 #include "cato_kernels.cuh"
 #include "cato_launch.cuh"
+#include "cato_pbc.cuh"
 
 using namespace cato;
 
@@ -64,6 +65,10 @@ struct cato_handle {
   double* rect[6] = {};      // rectilinear grid: dx, lx, 1/dx per column; dy, ly, 1/dy per row
   float* rectf[2] = {};      // FP32 1/dx per column, 1/dy per row
   double* red = nullptr;     // reduction partials + results (lazy)
+  // +x pressure input: per-row edge states + the column maximum (lazy), the target table
+  double* pbc = nullptr;
+  double* pbc_tab = nullptr;
+  int pbc_n = 0, pbc_cap = 0;
   Plan plan;
   FluxConsts<double> K64{};
   FluxConsts<float> K32{};
@@ -198,6 +203,51 @@ static cudaError_t launch(cato_handle* h, const StageArgs& A) {
   return launch_stage<float>(h->cfg.flux, recon, grid, T, h->stream, A, h->K32);
 }
 
+static bool has_pbc(const cato_handle* h) {
+  return h->cfg.bc[CATO_PLUS_X] == CATO_BC_PRESSURE_INPUT;
+}
+
+// The pressure-input target must be usable before a step: a table, or the constant pressure
+// and density of the configuration (get_desired_pressure / get_desired_density stop the
+// reference on values below tiny, pressure_input_bc.f90:211-253).
+static int pbc_prepare(cato_handle* h) {
+  if (!has_pbc(h)) return CATO_OK;
+  const double tiny = 2.2250738585072014e-308;
+  if (h->pbc_n == 0 && !(h->cfg.bc_pressure >= tiny && h->cfg.bc_density >= tiny))
+    return fail(h, CATO_ERR_CONFIG,
+                "pressure_input: bc_pressure and bc_density must be >= tiny without a table");
+  if (!h->pbc) {
+    const size_t n = 3 * (size_t)(h->nj + 2 * h->ng) + 1;
+    CK(cudaMalloc(&h->pbc, n * sizeof(double)));
+    CK(cudaMemsetAsync(h->pbc, 0, n * sizeof(double), h->stream));
+  }
+  return CATO_OK;
+}
+
+// The two boundary kernels before a stage.  The boundary time of a stage is its flux solver's
+// time: t_n + dt (the step control has already advanced the time), except for the first stage
+// of an rk(m,n) step (rk_first), whose solver is a copy of the persistent fluid's and keeps its
+// creation time: t_create + dt.
+static int enqueue_pbc(cato_handle* h, StageArgs& A, bool rk_first) {
+  if (!has_pbc(h)) return CATO_OK;
+  PbcArgs P{};
+  P.table.n = h->pbc_n;
+  P.table.t = h->pbc_tab;
+  P.table.p = h->pbc_tab ? h->pbc_tab + h->pbc_n : nullptr;
+  P.table.rho = h->pbc_tab ? h->pbc_tab + 2 * h->pbc_n : nullptr;
+  P.table.p_const = h->cfg.bc_pressure;
+  P.table.rho_const = h->cfg.bc_density;
+  P.edge = h->pbc;
+  P.max_p = h->pbc + 3 * (size_t)(h->nj + 2 * h->ng);
+  P.ctl = h->ctl;
+  P.t_mode = rk_first ? 1 : 0;
+  P.ng = h->ng;
+  A.pbc_edge = h->pbc;
+  A.pbc_ng = h->ng;
+  CK(launch_pbc(h->cfg.precision, A, P, h->stream));
+  return CATO_OK;
+}
+
 // Enqueue one full time step (step control + every stage) on the handle's stream.
 static int enqueue_step(cato_handle* h) {
   step_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctl);
@@ -240,6 +290,8 @@ static int enqueue_step(cato_handle* h) {
       A.ufo = A.last ? h->Uf[1 - h->cur] : nullptr;
       if (st.kind == 0) A.b = 0.0;  // rk(m,n): U_curr = U_0 + c L(U_prev)
     }
+    const int rcb = enqueue_pbc(h, A, k == 0 && h->cfg.rk >= CATO_RK_1_3);
+    if (rcb) return rcb;
     CK(launch(h, A));
     if (h->event_hook) CK(cudaEventRecord(h->event_hook[k + 2], h->stream));
   }
@@ -255,6 +307,8 @@ static int pull_ctl(cato_handle* h) {
 }
 
 static int status_code(int bits) {
+  // the reference stops inside the boundary condition, before the state is ever checked
+  if (bits & ST_BC_INPUT) return CATO_ERR_BC_INPUT;
   if (bits & ST_NEG_DENSITY) return CATO_NEG_DENSITY;
   if (bits & ST_NEG_PRESSURE) return CATO_NEG_PRESSURE;
   if (bits & ST_NAN) return CATO_NANS_FOUND;
@@ -350,8 +404,11 @@ int cato_config_check(const cato_config* c) {
   if (c->ni < c->n_ghost || c->nj < c->n_ghost) return CATO_ERR_CONFIG;
   bool outlet = false;
   for (int s = 0; s < 4; ++s) {
-    if (c->bc[s] < CATO_BC_ZERO_GRADIENT || c->bc[s] > CATO_BC_OUTLET) return CATO_ERR_CONFIG;
+    if (c->bc[s] < CATO_BC_ZERO_GRADIENT || c->bc[s] > CATO_BC_PRESSURE_INPUT)
+      return CATO_ERR_CONFIG;
     outlet |= c->bc[s] == CATO_BC_OUTLET;
+    // apply_pressure_input_primitive_var_bc only implements +x (pressure_input_bc.f90:404-409)
+    if (c->bc[s] == CATO_BC_PRESSURE_INPUT && s != CATO_PLUS_X) return CATO_ERR_CONFIG;
   }
   // outlet_bc_constructor stops on an ambient pressure <= 0 (outlet_bc.f90:54-59)
   if (outlet && !(c->bc_pressure > 0.0)) return CATO_ERR_CONFIG;
@@ -453,6 +510,8 @@ int cato_gpu_destroy(cato_handle* h) {
   for (int k = 0; k < 4; ++k) cudaFree(h->halo[k]);
   cudaFree(h->ctl);
   cudaFree(h->red);
+  cudaFree(h->pbc);
+  cudaFree(h->pbc_tab);
   for (int k = 0; k < 6; ++k) cudaFree(h->rect[k]);
   for (int k = 0; k < 2; ++k) cudaFree(h->rectf[k]);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
@@ -515,7 +574,9 @@ int cato_gpu_integrate(cato_handle* h, double dt, double* dt_used, int32_t* erro
   if (!h) return CATO_ERR_ARG;
   if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
   // one step regardless of t_end; fixed dt when dt > 0
-  int rc = pull_ctl(h);
+  int rc = pbc_prepare(h);
+  if (rc) return rc;
+  rc = pull_ctl(h);
   if (rc) return rc;
   StepCtl c = *h->ctl_host;
   c.t_end = INFINITY;
@@ -539,7 +600,9 @@ int cato_gpu_run(cato_handle* h, int64_t max_steps, double t_end, int64_t* steps
                  double* time, int32_t* error_code) {
   if (!h) return CATO_ERR_ARG;
   if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
-  int rc = pull_ctl(h);
+  int rc = pbc_prepare(h);
+  if (rc) return rc;
+  rc = pull_ctl(h);
   if (rc) return rc;
   StepCtl c = *h->ctl_host;
   const long long it0 = c.iter;
@@ -580,6 +643,7 @@ int cato_gpu_set_time(cato_handle* h, double time, int64_t iteration) {
   int rc = pull_ctl(h);
   if (rc) return rc;
   h->ctl_host->time = time;
+  h->ctl_host->t_create = time;  // as a fluid created at this time (new_fluid(..., time))
   h->ctl_host->iter = iteration;
   CK(cudaMemcpyAsync(h->ctl, h->ctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -638,6 +702,7 @@ int cato_gpu_solve(cato_handle* h, double* rho, double* u, double* v, double* p,
   if (h->cfg.precision != CATO_FP64)
     return fail(h, CATO_ERR_CONFIG, "solve is the FP64 reference boundary");
   int rc;
+  if ((rc = pbc_prepare(h))) return rc;
   if ((rc = ensure_scratch(h))) return rc;
   if ((rc = ensure_halo(h))) return rc;
   double* prim[4] = {rho, u, v, p};
@@ -657,12 +722,14 @@ int cato_gpu_solve(cato_handle* h, double* rho, double* u, double* v, double* p,
     A.Ua[k] = nullptr;
     A.Uo[k] = h->scratch[4 + k];
   }
+  // a table target is evaluated at the handle's time (cato_gpu_set_time)
+  if ((rc = enqueue_pbc(h, A, false))) return rc;
   CK(launch(h, A));
   // write the BC-filled ghosts back into the caller's primitive arrays (intent(inout))
   const int4 bc = make_int4(h->cfg.bc[0], h->cfg.bc[1], h->cfg.bc[2], h->cfg.bc[3]);
   const long long hld = h->ni + 2 * h->ng;
   fill_ghosts_kernel<<<grid_for((long long)h->halo_elems), 256, 0, h->stream>>>(
-      h->ni, h->nj, h->pitch, h->ng, bc, h->cfg.gamma, h->cfg.bc_pressure, h->scratch[0],
+      h->ni, h->nj, h->pitch, h->ng, bc, h->cfg.gamma, h->cfg.bc_pressure, h->pbc, h->scratch[0],
       h->scratch[1], h->scratch[2], h->scratch[3], h->halo[0], h->halo[1], h->halo[2],
       h->halo[3], hld);
   CK(cudaGetLastError());
@@ -676,6 +743,11 @@ int cato_gpu_solve(cato_handle* h, double* rho, double* u, double* v, double* p,
     if ((rc = d2h_interior(h, dout[k], h->scratch[4 + k], ld))) return rc;
   }
   CK(cudaStreamSynchronize(h->stream));
+  if (has_pbc(h)) {
+    if ((rc = pull_ctl(h))) return rc;
+    if (h->ctl_host->status & ST_BC_INPUT)
+      return fail(h, CATO_ERR_BC_INPUT, "pressure_input target below tiny at the solve time");
+  }
   return CATO_OK;
 }
 
@@ -748,7 +820,9 @@ int cato_gpu_run_timed(cato_handle* h, int64_t n_steps, float* total_ms, float* 
   if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
   const int nk = 1 + (int)h->stages.size();
   if (kernel_ms && capacity < nk) return fail(h, CATO_ERR_ARG, "capacity too small");
-  int rc = pull_ctl(h);
+  int rc = pbc_prepare(h);
+  if (rc) return rc;
+  rc = pull_ctl(h);
   if (rc) return rc;
   StepCtl c = *h->ctl_host;
   const long long it0 = c.iter;
@@ -820,7 +894,8 @@ int cato_host_free(void* p) { return cudaFreeHost(p) == cudaSuccess ? CATO_OK : 
 
 int cato_gpu_launches_per_step(const cato_handle* h, int32_t* n) {
   if (!h || !n) return CATO_ERR_ARG;
-  *n = 1 + (int32_t)h->stages.size();
+  // step control + per stage: the stage kernel (+ the two pressure-input boundary kernels)
+  *n = 1 + (int32_t)h->stages.size() * (has_pbc(h) ? 3 : 1);
   return CATO_OK;
 }
 
@@ -829,7 +904,9 @@ int cato_gpu_profile_step(cato_handle* h, float* kernel_ms, int32_t capacity, in
   if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
   const int nk = 1 + (int)h->stages.size();
   if (capacity < nk) return fail(h, CATO_ERR_ARG, "capacity too small");
-  int rc = pull_ctl(h);
+  int rc = pbc_prepare(h);
+  if (rc) return rc;
+  rc = pull_ctl(h);
   if (rc) return rc;
   StepCtl c = *h->ctl_host;
   c.t_end = INFINITY;
@@ -851,6 +928,41 @@ int cato_gpu_profile_step(cato_handle* h, float* kernel_ms, int32_t capacity, in
   rc = pull_ctl(h);
   if (rc) return rc;
   if (h->ctl_host->iter > c.iter) h->stepped = true;
+  return CATO_OK;
+}
+
+int cato_gpu_set_bc_table(cato_handle* h, int32_t n, const double* time, const double* pressure,
+                          const double* density) {
+  if (!h) return CATO_ERR_ARG;
+  if (n == 0) {  // back to the constant target of the configuration
+    h->pbc_n = 0;
+    return CATO_OK;
+  }
+  if (!time || !pressure || !density) return fail(h, CATO_ERR_ARG, "null table pointer");
+  // linear_interp_1d%initialize: at least two points, strictly increasing times (finterp
+  // linear_interpolation_module.f90:451-478, 1743-1810)
+  if (n < 2) return fail(h, CATO_ERR_ARG, "a table needs at least two points");
+  for (int k = 0; k < n; ++k) {
+    if (!std::isfinite(time[k]) || !std::isfinite(pressure[k]) || !std::isfinite(density[k]))
+      return fail(h, CATO_ERR_ARG, "non-finite table entry");
+    if (k > 0 && !(time[k] > time[k - 1]))
+      return fail(h, CATO_ERR_ARG, "table times must be strictly increasing");
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  if (h->pbc_tab && n > h->pbc_cap) {
+    CK(cudaFree(h->pbc_tab));
+    h->pbc_tab = nullptr;
+    h->pbc_cap = 0;
+  }
+  if (!h->pbc_tab) {
+    CK(cudaMalloc(&h->pbc_tab, 3 * (size_t)n * sizeof(double)));
+    h->pbc_cap = n;
+  }
+  const double* src[3] = {time, pressure, density};
+  for (int k = 0; k < 3; ++k)
+    CK(cudaMemcpy(h->pbc_tab + (size_t)k * n, src[k], n * sizeof(double),
+                  cudaMemcpyHostToDevice));
+  h->pbc_n = n;
   return CATO_OK;
 }
 

@@ -17,6 +17,8 @@ struct StepCtl {
   unsigned long long dt_min;  // CFL dt of the current state (bits; ~0 = none)
   int active;
   int status;         // ST_* bits of the current state
+  double t_create;    // time the state was created at (upload / set_time): the flux solver of
+                      // the persistent fluid keeps it under rk(m,n) (pressure-input table time)
 };
 
 __device__ __forceinline__ double decode_dt(unsigned long long b) {

@@ -111,7 +111,7 @@ static __global__ void derive_kernel(int ni, int nj, int pitch, double gamma, in
 // Halo-padded primitive fields with every ghost cell filled by the boundary conditions, as after
 // flux_solver_t%apply_primitive_bc (flux_solver.f90:138-185).
 static __global__ void fill_ghosts_kernel(int ni, int nj, int pitch, int ng, int4 bc,
-                                   double gamma, double bc_p,
+                                   double gamma, double bc_p, const double* __restrict__ pbc_edge,
                                    const double* __restrict__ r_, const double* __restrict__ u_,
                                    const double* __restrict__ v_, const double* __restrict__ p_,
                                    double* ro, double* uo, double* vo, double* po, long long ld) {
@@ -127,6 +127,13 @@ static __global__ void fill_ghosts_kernel(int ni, int nj, int pitch, int ng, int
     const size_t o = (size_t)jj * ld + ii;
     double r = r_[s], u = fx ? -u_[s] : u_[s], v = fy ? -v_[s] : v_[s], p = p_[s];
     if (bcs[SIDE_PX] == BC_OUTLET && ii - ng >= ni) outlet_ghost<double>(gamma, bc_p, r, u, v, p);
+    if (bcs[SIDE_PX] == BC_PRESSURE_INPUT && ii - ng >= ni) {  // the row's edge state
+      const double* e = pbc_edge + 3 * (size_t)jj;
+      r = e[0];
+      u = e[1];
+      v = 0.0;
+      p = e[2];
+    }
     ro[o] = r;
     uo[o] = u;
     vo[o] = v;

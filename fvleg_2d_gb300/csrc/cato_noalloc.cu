@@ -81,6 +81,8 @@ extern "C" int cato_gpu_solve_noalloc(const cato_config* cfg, double* rho, doubl
   int rc = cato_config_check(cfg);
   if (rc != CATO_OK) return rc;
   if (cfg->precision != CATO_FP64) return CATO_ERR_CONFIG;
+  // the pressure-input boundary needs per-row device state: handle entry points only
+  if (cfg->bc[CATO_PLUS_X] == CATO_BC_PRESSURE_INPUT) return CATO_ERR_CONFIG;
   const int ni = cfg->ni, nj = cfg->nj, ng = cfg->n_ghost;
   if (ld < ni + 2 * ng) return CATO_ERR_ARG;
   const int pitch = (ni + 31) / 32 * 32;

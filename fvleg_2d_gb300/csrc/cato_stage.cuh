@@ -57,6 +57,10 @@ struct StageArgs {
   // physics
   double gamma, cfl;
   double bc_p;             // outlet pressure (CATO_BC_OUTLET)
+  // +x pressure input (CATO_BC_PRESSURE_INPUT): the ghost state (rho, u, p; v = 0) of rows
+  // -pbc_ng .. nj+pbc_ng-1, written for this stage by pbc_edge_kernel
+  const double* pbc_edge;
+  int pbc_ng;
   Geom G;
 };
 
@@ -200,15 +204,18 @@ template <typename R> struct RowSrc;
 template <> struct RowSrc<double> {
   double c[4];  // conserved (or raw primitives) as loaded
   bool flipy;
+  int row;      // the (possibly ghost) row this sample stands for
 };
 template <> struct RowSrc<float> {
   float4 c;     // FP32 copy of U^n (or the raw primitives)
   float4 d;     // delta_k
   bool flipy;
+  int row;
 };
 template <> struct RowSrc<df> {
   double c[4];  // conserved state of the stage (or the raw primitives)
   bool flipy;
+  int row;
 };
 
 template <typename R>
@@ -216,6 +223,7 @@ __device__ __forceinline__ void load_src(const StageArgs& A, int sx, int row, Ro
   bool fy;
   const int sy = map_index(row, A.nj, A.bc[SIDE_MY], A.bc[SIDE_PY], fy);
   s.flipy = fy;
+  s.row = row;
   const size_t idx = (size_t)sy * A.pitch + sx;
   if constexpr (Prec<R>::kind != 1) {
     const double* const* src = A.Pin[0] ? A.Pin : A.Uk;
@@ -232,9 +240,23 @@ __device__ __forceinline__ void load_src(const StageArgs& A, int sx, int row, Ro
   }
 }
 
+template <typename R> __device__ __forceinline__ R from_double(double x);
+template <> __device__ __forceinline__ double from_double<double>(double x) { return x; }
+template <> __device__ __forceinline__ float from_double<float>(double x) { return d2f_int(x); }
+template <> __device__ __forceinline__ df from_double<df>(double x) { return to_df(x); }
+
+// xmode: 0 interior / mapped ghost, 1 +x outlet ghost column, 2 +x pressure-input ghost column
 template <typename R>
 __device__ __forceinline__ void src_to_prim(const StageArgs& A, const RowSrc<R>& s, bool flipx,
-                                            bool outlet_x, R g, R g1, R out[4]) {
+                                            int xmode, R g, R g1, R out[4]) {
+  if (xmode == 2) {  // lowest-priority BC: the row's edge state replaces the mapped value
+    const double* e = A.pbc_edge + 3 * (size_t)(s.row + A.pbc_ng);
+    out[0] = from_double<R>(e[0]);
+    out[1] = from_double<R>(e[1]);
+    out[2] = R(0);
+    out[3] = from_double<R>(e[2]);
+    return;
+  }
   R r, u, v, p;
   if constexpr (Prec<R>::kind == 0) {
     if (A.Pin[0]) {
@@ -263,7 +285,7 @@ __device__ __forceinline__ void src_to_prim(const StageArgs& A, const RowSrc<R>&
   }
   u = flipx ? -u : u;
   v = s.flipy ? -v : v;
-  if (outlet_x) outlet_ghost<R>(g, R(A.bc_p), r, u, v, p);
+  if (xmode == 1) outlet_ghost<R>(g, R(A.bc_p), r, u, v, p);
   out[0] = r;
   out[1] = u;
   out[2] = v;
@@ -294,8 +316,10 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
   const R g = R(A.gamma), g1 = R(A.gamma - 1.0);
   bool flipx;
   const int sx = map_index(min(gx, A.ni + NG - 1), A.ni, A.bc[SIDE_MX], A.bc[SIDE_PX], flipx);
-  // +x outlet ghost columns get the characteristic outflow state (lowest-priority BC)
-  const bool outlet_x = (A.bc[SIDE_PX] == BC_OUTLET) && (gx >= A.ni);
+  // +x outlet / pressure-input ghost columns get the boundary state (lowest-priority BCs)
+  const int xmode = gx < A.ni ? 0
+                    : (A.bc[SIDE_PX] == BC_OUTLET ? 1
+                                                  : (A.bc[SIDE_PX] == BC_PRESSURE_INPUT ? 2 : 0));
   const bool in_i_edge = (t >= NG - 1) && (t <= NG + W - 1) && (gx <= A.ni - 1);
   const bool in_cell = (t >= NG) && (t <= NG + W - 1) && (gx < A.ni);
   const double dt = *A.dt;
@@ -317,7 +341,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
     RowSrc<R> s;
     load_src<R>(A, sx, r, s);
     R q[4];
-    src_to_prim<R>(A, s, flipx, outlet_x, g, g1, q);
+    src_to_prim<R>(A, s, flipx, xmode, g, g1, q);
     R* row = ring + slot_of<RING>(r) * 4 * T;
 #pragma unroll
     for (int k = 0; k < 4; ++k) row[k * T + t] = q[k];
@@ -362,7 +386,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
     if (j + 1 < y1) load_src<R>(A, sx, j + 1 + NG, nxt);
     {
       R q[4];
-      src_to_prim<R>(A, pre, flipx, outlet_x, g, g1, q);
+      src_to_prim<R>(A, pre, flipx, xmode, g, g1, q);
       R* row = ring + slot_of<RING>(j + NG) * 4 * T;
 #pragma unroll
       for (int k = 0; k < 4; ++k) row[k * T + t] = q[k];

@@ -98,6 +98,13 @@ class Deck:
     # [boundary_conditions]
     bc: dict = field(default_factory=lambda: {s: "periodic" for s in ("+x", "-x", "+y", "-y")})
     outflow_ambient_pressure: float = 0.0
+    # pressure_input sides (mod_input.f90:366-382); the outflow pressure and the constant
+    # pressure are one variable there (constant_bc_pressure_value), the outflow key read last
+    apply_constant_bc_pressure: bool = False
+    bc_density: float = 0.0
+    constant_bc_pressure_value: float = 0.0
+    bc_pressure_input_file: str = ""
+    bc_pressure_scale_factor: float = 1.0
     # [io]
     contour_interval_dt: float = 0.1
     contour_format: str = "xdmf"
@@ -119,6 +126,7 @@ class Deck:
         for side, name in self.bc.items():
             if name not in BC_IDS:
                 raise DeckError(f"boundary condition {name!r} at {side} is not supported")
+        f = nondim_factors(self)
         return SchemeConfig(
             ni=int(ni), nj=int(nj), dx=float(dx), dy=float(dy), flux_solver=self.flux_solver,
             limiter=self.limiter, integration_strategy=strategy, bc=dict(self.bc),
@@ -126,7 +134,11 @@ class Deck:
             apply_low_mach_fix=self.apply_low_mach_fix, precision=precision,
             ausm_beta=self.ausm_beta, ausm_kp=self.ausm_pressure_diffusion_coeff,
             ausm_ku=self.ausm_pressure_flux_coeff, ausm_sigma=self.ausm_sonic_point_sigma,
-            outflow_ambient_pressure=self.outflow_ambient_pressure,
+            # outlet_bc.f90:55 and pressure_input_bc.f90:82-89 (the density there is scaled
+            # with density_to_dim)
+            outflow_ambient_pressure=self.outflow_ambient_pressure * f["press_to_nondim"],
+            constant_bc_pressure=self.constant_bc_pressure_value * f["press_to_nondim"],
+            bc_density=self.bc_density * f["density_to_dim"],
             n_ghost=self.n_ghost_layers)
 
     def grid(self) -> tuple[int, int, float, float]:
@@ -224,9 +236,22 @@ def parse_deck(text: str) -> Deck:
         d.ymax = get("grid", "ymax", _real, required=True)
     for side, key in (("+x", "plus_x"), ("-x", "minus_x"), ("+y", "plus_y"), ("-y", "minus_y")):
         d.bc[side] = get("boundary_conditions", key, default="periodic")
+    if "pressure_input" in d.bc.values():
+        d.apply_constant_bc_pressure = get("boundary_conditions", "apply_constant_bc_pressure",
+                                           _logical, False)
+        d.bc_density = get("boundary_conditions", "bc_density", _real, 0.0)
+        if d.apply_constant_bc_pressure:
+            d.constant_bc_pressure_value = get("boundary_conditions",
+                                               "constant_bc_pressure_value", _real, required=True)
+        else:
+            d.bc_pressure_input_file = get("boundary_conditions", "bc_pressure_input_file",
+                                           required=True)
+        d.bc_pressure_scale_factor = get("boundary_conditions", "bc_pressure_scale_factor",
+                                         _real, 1.0)
     if "outflow" in d.bc.values():
         d.outflow_ambient_pressure = get("boundary_conditions", "outflow_ambient_pressure", _real,
                                          required=True)
+        d.constant_bc_pressure_value = d.outflow_ambient_pressure
     d.contour_format = get("io", "format", default=get("io", "contour_format", default="xdmf"))
     d.contour_interval_dt = get("io", "contour_interval_dt", _real, 0.1)
     return d
@@ -250,12 +275,60 @@ def load_initial_condition(deck: Deck, base_dir: str = "."):
                    deck.reference_velocity, deck.non_dimensionalize)
 
 
+def nondim_factors(deck: Deck) -> dict:
+    """The scale factors of ``set_refrence_quantities`` (``non_dimensional.f90:95-135``), all 1
+    without non-dimensionalization."""
+    names = ("len_to_nondim", "t_to_nondim", "density_to_nondim", "density_to_dim",
+             "vel_to_nondim", "press_to_nondim")
+    if not deck.non_dimensionalize:
+        return dict.fromkeys(names, 1.0)
+    L, R, V = deck.reference_length, deck.reference_density, deck.reference_velocity
+    t_ref = L / V
+    press_ref = R * (V * V)
+    return {"len_to_nondim": 1.0 / L, "t_to_nondim": 1.0 / t_ref, "density_to_nondim": 1.0 / R,
+            "density_to_dim": R, "vel_to_nondim": 1.0 / V, "press_to_nondim": 1.0 / press_ref}
+
+
 def t_to_nondim(deck: Deck) -> float:
     """1 / t_ref with t_ref = reference_length / reference_velocity
     (``non_dimensional.f90:95-118``); 1 without non-dimensionalization."""
-    if not deck.non_dimensionalize:
-        return 1.0
-    return 1.0 / (deck.reference_length / deck.reference_velocity)
+    return nondim_factors(deck)["t_to_nondim"]
+
+
+def read_bc_pressure_table(deck: Deck, base_dir: str = "."):
+    """The pressure-input table of ``bc_pressure_input_file`` as read_pressure_input reads it
+    (``pressure_input_bc.f90:92-181``): an optional first line starting with '#', then rows of
+    time [s], pressure [barye], density [g/cc] (list-directed, reading stops at the first row
+    that does not parse); scaled to time x t_to_nondim, pressure x press_to_nondim x
+    bc_pressure_scale_factor and density x density_to_nondim x bc_pressure_scale_factor."""
+    path = deck.bc_pressure_input_file
+    if not os.path.isabs(path):
+        path = os.path.join(base_dir, path)
+    if not os.path.exists(path):
+        raise DeckError(f"Pressure input file '{path}' not found")
+    rows = []
+    with open(path) as fh:
+        lines = fh.read().splitlines()
+    if lines and lines[0].lstrip().startswith("#"):
+        lines = lines[1:]
+    for line in lines:
+        parts = line.replace(",", " ").split()
+        if not parts:
+            continue
+        try:
+            row = [_real(x) for x in parts[:3]]
+        except ValueError:
+            break
+        if len(row) < 3:
+            break
+        rows.append(row)
+    if len(rows) < 2:
+        raise DeckError(f"{path}: the pressure input table needs at least two rows")
+    a = np.array(rows, dtype=np.float64)
+    f = nondim_factors(deck)
+    scale = deck.bc_pressure_scale_factor
+    return (a[:, 0] * f["t_to_nondim"], (a[:, 1] * f["press_to_nondim"]) * scale,
+            (a[:, 2] * f["density_to_nondim"]) * scale)
 
 
 def run_deck(deck: Deck, precision: str = "fp64", prims=None, grid=None, base_dir: str = "."):
@@ -276,6 +349,8 @@ def run_deck(deck: Deck, precision: str = "fp64", prims=None, grid=None, base_di
     fluid = Fluid(cfg)
     if ic is not None:
         ic.apply_grid(fluid)
+    if "pressure_input" in deck.bc.values() and not deck.apply_constant_bc_pressure:
+        fluid.set_bc_table(*read_bc_pressure_table(deck, base_dir))
     fluid.initialize(*prims)
     steps = fluid.run(deck.max_time * t_to_nondim(deck), deck.max_iterations)
     return fluid, steps

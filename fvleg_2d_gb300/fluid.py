@@ -89,6 +89,41 @@ class _Handle:
         self.nodes = None if xs is None else (xs, ys)
         return self
 
+    def set_bc_table(self, time=None, pressure=None, density=None):
+        """Target of the +x 'pressure_input' side as a table in time (non-dimensional time,
+        pressure and density as read_pressure_input leaves them, pressure_input_bc.f90:92-181);
+        no arguments returns to the configuration's constant target."""
+        if time is None:
+            _check(self.L.cato_gpu_set_bc_table(self.h, 0, None, None, None), self.h,
+                   "set_bc_table")
+            self.bc_table = None
+            return self
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (time, pressure, density)]
+        n = arrs[0].shape[0]
+        if any(a.shape != (n,) for a in arrs):
+            raise ValueError("time, pressure and density must be 1-D arrays of one length")
+        _check(self.L.cato_gpu_set_bc_table(self.h, n, *(_lib.ptr(a) for a in arrs)), self.h,
+               "set_bc_table")
+        self.bc_table = tuple(arrs)
+        return self
+
+    def set_time(self, time: float, iteration: int) -> None:
+        """fluid_t%set_time (mod_fluid.f90:400-409); also the time at which a FluxSolver
+        evaluates a tabulated pressure-input target."""
+        _check(self.L.cato_gpu_set_time(self.h, float(time), int(iteration)), self.h, "set_time")
+
+    @property
+    def time(self) -> float:
+        t = ctypes.c_double()
+        _check(self.L.cato_gpu_get_time(self.h, ctypes.byref(t), None, None), self.h)
+        return t.value
+
+    @property
+    def iteration(self) -> int:
+        it = ctypes.c_int64()
+        _check(self.L.cato_gpu_get_time(self.h, None, ctypes.byref(it), None), self.h)
+        return it.value
+
 
 class Fluid(_Handle):
     """fluid_t on the GPU.  ``Fluid(cfg).initialize(rho, u, v, p)`` replaces
@@ -159,21 +194,6 @@ class Fluid(_Handle):
         _check(self.L.cato_gpu_profile_step(self.h, ks, n, ctypes.byref(got)), self.h, "profile")
         return list(ks)[: got.value]
 
-    def set_time(self, time: float, iteration: int) -> None:
-        _check(self.L.cato_gpu_set_time(self.h, float(time), int(iteration)), self.h, "set_time")
-
-    @property
-    def time(self) -> float:
-        t = ctypes.c_double()
-        _check(self.L.cato_gpu_get_time(self.h, ctypes.byref(t), None, None), self.h)
-        return t.value
-
-    @property
-    def iteration(self) -> int:
-        it = ctypes.c_int64()
-        _check(self.L.cato_gpu_get_time(self.h, None, ctypes.byref(it), None), self.h)
-        return it.value
-
     def state(self, names=("rho", "rho_u", "rho_v", "rho_E", "u", "v", "p", "cs")) -> dict:
         """Download conserved and derived fields (halo-padded, ghosts zero)."""
         all_names = ("rho", "rho_u", "rho_v", "rho_E", "u", "v", "p", "cs")
@@ -202,6 +222,9 @@ class Fluid(_Handle):
         fs = FluxSolver(self.cfg)
         if getattr(self, "nodes", None) is not None:
             fs.set_rectilinear(*self.nodes)
+        if getattr(self, "bc_table", None) is not None:
+            fs.set_bc_table(*self.bc_table)
+        fs.set_time(self.time, self.iteration)
         return fs.solve(s["rho"], s["u"], s["v"], s["p"])
 
 

@@ -34,7 +34,9 @@ enum cato_status {
   CATO_ERR_ARG = 13,      /* bad argument (null pointer, too-small leading dimension, ...) */
   CATO_ERR_TIMEOUT = 14,  /* a bounded device-side wait gave up */
   CATO_ERR_STATE = 15,    /* call out of order (e.g. integrate before upload) */
-  CATO_ERR_CAPACITY = 16  /* the request exceeds a fixed-size device buffer (no-alloc entry) */
+  CATO_ERR_CAPACITY = 16, /* the request exceeds a fixed-size device buffer (no-alloc entry) */
+  CATO_ERR_BC_INPUT = 17  /* the pressure-input target pressure or density is below tiny at a
+                             stage's time (the reference stops, pressure_input_bc.f90:225-253) */
 };
 
 /* Flux solvers.  Names as accepted by the reference deck key [scheme] flux_solver
@@ -78,8 +80,12 @@ enum cato_bc {
   CATO_BC_ZERO_GRADIENT = 0, /* priority 1, zero_gradient_bc.f90:54-121 */
   CATO_BC_SYMMETRY = 1,      /* priority 1, symmetry_bc.f90:56-133 */
   CATO_BC_PERIODIC = 2,      /* priority 2, periodic_bc.fypp:78-283 */
-  CATO_BC_OUTLET = 3         /* priority 0, outlet_bc.f90:63-176: characteristic subsonic outflow
+  CATO_BC_OUTLET = 3,        /* priority 0, outlet_bc.f90:63-176: characteristic subsonic outflow
                                 to bc_pressure on +x, line copies on the other sides */
+  CATO_BC_PRESSURE_INPUT = 4 /* priority 0, +x only, pressure_input_bc.f90:256-414: the
+                                characteristic inlet/outlet state toward a target pressure and
+                                density, constant (bc_pressure, bc_density) or tabulated in time
+                                (cato_gpu_set_bc_table) */
 };
 
 /* Sides in the reference's application order within one priority (flux_solver.f90:165-183). */
@@ -116,7 +122,11 @@ typedef struct cato_config {
   double ausm_kp;             /* [ausm] pressure_diffusion_coeff, default 0.25 */
   double ausm_ku;             /* K_u, default 0.75 (not read from the deck by the reference) */
   double ausm_sigma;          /* [ausm] sonic_point_sigma, default 1 */
-  double bc_pressure;         /* [boundary_conditions] outflow_ambient_pressure (CATO_BC_OUTLET) */
+  double bc_pressure;         /* [boundary_conditions] outflow_ambient_pressure (CATO_BC_OUTLET) or
+                                 constant_bc_pressure_value x press_to_nondim (constant
+                                 CATO_BC_PRESSURE_INPUT); the reference keeps both in one value */
+  double bc_density;          /* [boundary_conditions] bc_density x density_to_dim: the constant
+                                 CATO_BC_PRESSURE_INPUT target density */
 } cato_config;
 
 typedef struct cato_handle cato_handle;
@@ -153,6 +163,17 @@ int cato_gpu_upload_primitive(cato_handle* h, const double* rho, const double* u
  * returns to the uniform grid.  The state must be uploaded (again) afterwards. */
 int cato_gpu_set_rectilinear(cato_handle* h, const double* x_nodes, const double* y_nodes);
 
+/* Target of a CATO_BC_PRESSURE_INPUT side as a table in time: n >= 2 points (time strictly
+ * increasing), pressure and density already scaled as read_pressure_input does
+ * (pressure_input_bc.f90:92-181: time x t_to_nondim, pressure x press_to_nondim x
+ * bc_pressure_scale_factor, density x density_to_nondim x bc_pressure_scale_factor).  Evaluated
+ * per stage as linear_interp_1d (finterp) at the stage's flux-solver time: t_n + dt, or for the
+ * first stage of an rk(m,n) step the creation time (upload: 0, or cato_gpu_set_time) + dt; a
+ * single cato_gpu_solve evaluates it at the handle's time.  n = 0 returns to the constant
+ * target of the configuration. */
+int cato_gpu_set_bc_table(cato_handle* h, int32_t n, const double* time, const double* pressure,
+                          const double* density);
+
 /* CFL time step of the current state.  Replaces fluid_t%get_timestep (mod_fluid.f90:518-562). */
 int cato_gpu_get_timestep(cato_handle* h, double* dt);
 
@@ -168,7 +189,9 @@ int cato_gpu_integrate(cato_handle* h, double dt, double* dt_used, int32_t* erro
 int cato_gpu_run(cato_handle* h, int64_t max_steps, double t_end, int64_t* steps_done,
                  double* time, int32_t* error_code);
 
-/* Time bookkeeping (fluid_t%set_time, mod_fluid.f90:400-409). */
+/* Time bookkeeping (fluid_t%set_time, mod_fluid.f90:400-409).  set_time also sets the creation
+ * time of the state, as a fluid_t created at that time (restart: new_fluid(..., time),
+ * master_puppeteer.f90:132). */
 int cato_gpu_set_time(cato_handle* h, double time, int64_t iteration);
 int cato_gpu_get_time(cato_handle* h, double* time, int64_t* iteration, double* last_dt);
 

@@ -201,9 +201,209 @@ static void apply_outlet_px(dims_t d, double gamma, double p_b, double* f[4]) {
     }
 }
 
+/* Target of a pressure-input side: a table in time (read_pressure_input, already scaled) or
+ * the constants of the configuration; `time` is the boundary's time (its flux solver's). */
+typedef struct {
+  int n;
+  const double *t, *p, *rho;
+  double time;
+} pbc_ctx_t;
+
+/* linear_interp_1d%evaluate (finterp linear_interpolation_module.f90:730-762 with dintrv
+ * :1189-1323): the interval [t(il), t(il+1)] holding x, the first / last interval outside. */
+static double interp_1d(int n, const double* xt, const double* f, double x) {
+  int il;
+  if (x >= xt[n - 1]) il = n - 2;
+  else if (x < xt[0]) il = 0;
+  else {
+    il = 0;
+    while (il + 1 < n - 1 && xt[il + 1] <= x) ++il;
+  }
+  double q1 = (x - xt[il]) / (xt[il + 1] - xt[il]);
+  double p1 = 1.0 - q1;
+  return p1 * f[il] + q1 * f[il + 1];
+}
+
+/* Powers of the subsonic inlet.  The reference calls libm's pow (Fortran '**' on reals), which
+ * is not always correctly rounded: glibc's pow has < 0.52 ulp of error, so an exact value very
+ * close to a rounding midpoint can round the other way.  Mode 0 (default) calls pow as the
+ * reference does; mode 1 returns the correctly rounded power from double-double arithmetic
+ * (Dekker products via fma, Knuth sums; exp by a degree-9 Taylor series after k ln2 and 2^10
+ * reductions, log by one Newton step on exp), the arithmetic the CUDA path uses. */
+static int g_pow_mode = 0;
+
+int oracle_set_pow_mode(int mode) {
+  g_pow_mode = mode;
+  return 0;
+}
+
+typedef struct {
+  double hi, lo;
+} ddo_t;
+
+static ddo_t ddo_quick_two_sum(double a, double b) {
+  double s = a + b;
+  ddo_t r = {s, b - (s - a)};
+  return r;
+}
+static ddo_t ddo_two_sum(double a, double b) {
+  double s = a + b, bb = s - a;
+  ddo_t r = {s, (a - (s - bb)) + (b - bb)};
+  return r;
+}
+static ddo_t ddo_add(ddo_t a, ddo_t b) {
+  ddo_t s = ddo_two_sum(a.hi, b.hi), t = ddo_two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = ddo_quick_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return ddo_quick_two_sum(s.hi, s.lo);
+}
+static ddo_t ddo_add_d(ddo_t a, double b) {
+  ddo_t s = ddo_two_sum(a.hi, b);
+  s.lo += a.lo;
+  return ddo_quick_two_sum(s.hi, s.lo);
+}
+static ddo_t ddo_mul(ddo_t a, ddo_t b) {
+  double p = a.hi * b.hi;
+  double e = fma(a.hi, b.hi, -p);
+  e += a.hi * b.lo + a.lo * b.hi;
+  return ddo_quick_two_sum(p, e);
+}
+static ddo_t ddo_mul_d(ddo_t a, double b) {
+  double p = a.hi * b;
+  double e = fma(a.hi, b, -p);
+  e += a.lo * b;
+  return ddo_quick_two_sum(p, e);
+}
+static ddo_t ddo_recip(double n) {
+  double h = 1.0 / n;
+  ddo_t r = {h, fma(-h, n, 1.0) / n};
+  return r;
+}
+static ddo_t ddo_exp(ddo_t a) {
+  const ddo_t ln2 = {0x1.62e42fefa39efp-1, 0x1.abc9e3b39803fp-56};
+  double k = rint(a.hi / ln2.hi);
+  ddo_t r = ddo_add(a, ddo_mul_d(ln2, -k));
+  r.hi = ldexp(r.hi, -10);
+  r.lo = ldexp(r.lo, -10);
+  ddo_t e = {1.0, 0.0};
+  for (int n = 9; n >= 2; --n) e = ddo_add_d(ddo_mul(ddo_mul(e, r), ddo_recip((double)n)), 1.0);
+  e = ddo_mul(e, r);
+  for (int n = 0; n < 10; ++n) e = ddo_mul(e, ddo_add_d(e, 2.0));
+  ddo_t y = ddo_add_d(e, 1.0);
+  ddo_t out = {ldexp(y.hi, (int)k), ldexp(y.lo, (int)k)};
+  return out;
+}
+static double pow_cr(double x, double y) {
+  if (!(x > 0.0) || !isfinite(x)) return pow(x, y);
+  if (x == 1.0) return 1.0;
+  double y0 = log(x);
+  ddo_t m = {-y0, 0.0};
+  ddo_t lx = ddo_add_d(ddo_add_d(ddo_mul_d(ddo_exp(m), x), -1.0), y0);
+  ddo_t e = ddo_exp(ddo_mul_d(lx, y));
+  return e.hi + e.lo;
+}
+
+double oracle_pow(int mode, double x, double y) { return mode ? pow_cr(x, y) : pow(x, y); }
+
+static double bc_pow(double x, double y) { return g_pow_mode ? pow_cr(x, y) : pow(x, y); }
+
+/* subsonic_inlet, inlet_outlet.f90:60-165, for the +x normal (1, 0), flow angle 0 */
+static void subsonic_inlet(double gamma, const double dom[4], double inlet_density,
+                           double inlet_total_press, double out[4]) {
+  const double rho = dom[0], u = dom[1], v = dom[2], p = dom[3];
+  const double n_x = 1.0, n_y = 0.0, theta = 0.0;
+  double cos_theta = 0.0;
+  double v_dot_n = u * (-n_x) + v * (-n_y);
+  double v_tot_d = sqrt(u * u + v * v);
+  if (v_tot_d > 0.0) cos_theta = -v_dot_n / v_tot_d;
+  double cs_d = sqrt(gamma * p / rho);
+  double cs_0_sq = cs_d * cs_d + ((gamma - 1.0) / 2.0) * (v_tot_d * v_tot_d);
+  double R_minus = v_dot_n - (2.0 * cs_d / (gamma - 1.0));
+  double first_term = -R_minus * (gamma - 1.0) / ((gamma - 1.0) * (cos_theta * cos_theta) + 2.0);
+  double cs_b;
+  if (fabs(cos_theta) > 0.0) {
+    double second_term = (((gamma - 1.0) * (cos_theta * cos_theta) + 2.0) * cs_0_sq) /
+                         ((gamma - 1.0) * (R_minus * R_minus));
+    double third_term = (gamma - 1.0) / 2.0;
+    cs_b = first_term * (1.0 + cos_theta * sqrt(second_term - third_term));
+  } else {
+    cs_b = first_term;
+  }
+  double R_plus = v_dot_n + (2.0 * cs_b / (gamma - 1.0));
+  double v_tot_b = (2.0 * cs_b / (gamma - 1.0)) - R_plus;
+  double mach_b = v_tot_b / cs_b;
+  double u_b = v_tot_b * cos(theta);
+  double v_b = v_tot_b * sin(theta);
+  double p_b = inlet_total_press *
+               bc_pow(1.0 + 0.5 * (gamma - 1.0) * (mach_b * mach_b), -gamma / (gamma - 1.0));
+  double rho_b = inlet_density *
+                 bc_pow(1.0 + 0.5 * (gamma - 1.0) * (mach_b * mach_b), -1.0 / (gamma - 1.0));
+  out[0] = rho_b; out[1] = u_b; out[2] = v_b; out[3] = p_b;
+}
+
+/* apply_pressure_input_primitive_var_bc on +x, pressure_input_bc.f90:256-404: edge states of
+ * every row bottom_ghost..top_ghost from the boundary column ihi, then every ghost column. */
+static void apply_pressure_input_px(dims_t d, double gamma, double p_const, double rho_const,
+                                    const pbc_ctx_t* pc, double* f[4]) {
+  const int ng = d.ng, ni = d.ni, nj = d.nj, nrow = nj + 2 * ng;
+  double *rho = f[0], *u = f[1], *v = f[2], *p = f[3];
+  double p_des = p_const, rho_des = rho_const;
+  if (pc && pc->n > 0) {
+    p_des = interp_1d(pc->n, pc->t, pc->p, pc->time);
+    rho_des = interp_1d(pc->n, pc->t, pc->rho, pc->time);
+  }
+  double* edge = (double*)malloc(sizeof(double) * 3 * (size_t)nrow);
+  /* maxval(domain_p(bottom:top)): gfortran skips NaNs unless all are NaN */
+  double maxp = NAN;
+  for (int j = 1 - ng; j <= nj + ng; ++j) {
+    double x = AT(p, ni, j);
+    if (maxp != maxp || x > maxp) maxp = (x != x) ? maxp : x;
+  }
+  for (int j = 1 - ng; j <= nj + ng; ++j) {
+    double dom[4] = {AT(rho, ni, j), AT(u, ni, j), 0.0, AT(p, ni, j)};
+    double b[4];
+    double cs = sqrt(gamma * dom[3] / dom[0]);
+    double mach_u = dom[1] / cs;
+    if (mach_u > 0.0) {
+      if (mach_u <= 1.0 || maxp < p_des) {
+        /* subsonic_outlet, inlet_outlet.f90:167-196 with the normal (1, 0) */
+        double cs_d = sqrt(gamma * dom[3] / dom[0]);
+        b[3] = p_des;
+        b[0] = dom[0] + (b[3] - dom[3]) / (cs_d * cs_d);
+        b[1] = dom[1] + 1.0 * (dom[3] - b[3]) / (dom[0] * cs_d);
+        b[2] = dom[2] + 0.0 * (dom[3] - b[3]) / (dom[0] * cs_d);
+      } else {
+        for (int k = 0; k < 4; ++k) b[k] = dom[k]; /* supersonic_outlet */
+      }
+    } else {
+      if (fabs(mach_u) > 1.0) {
+        b[0] = rho_des; b[1] = dom[1]; b[2] = dom[2]; b[3] = p_des;
+      } else {
+        subsonic_inlet(gamma, dom, rho_des, p_des, b);
+      }
+    }
+    double* e = edge + 3 * (size_t)(j + ng - 1);
+    e[0] = b[0]; e[1] = b[1]; e[2] = b[3];
+  }
+  for (int i = ni + 1; i <= ni + ng; ++i)
+    for (int j = 1 - ng; j <= nj + ng; ++j) {
+      const double* e = edge + 3 * (size_t)(j + ng - 1);
+      AT(rho, i, j) = e[0];
+      AT(u, i, j) = e[1];
+      AT(v, i, j) = 0.0;
+      AT(p, i, j) = e[2];
+    }
+  free(edge);
+}
+
 static void apply_one_bc(dims_t d, int type, int side, int do_corners, double gamma,
-                         double p_b, double* f[4]) {
+                         double p_b, double rho_b, const pbc_ctx_t* pc, double* f[4]) {
   const int ng = d.ng, ni = d.ni, nj = d.nj;
+  if (type == CATO_BC_PRESSURE_INPUT) {
+    if (side == CATO_PLUS_X) apply_pressure_input_px(d, gamma, p_b, rho_b, pc, f);
+    return;
+  }
   if (type == CATO_BC_OUTLET) {
     if (side == CATO_PLUS_X) {
       apply_outlet_px(d, gamma, p_b, f);
@@ -274,14 +474,16 @@ static void apply_one_bc(dims_t d, int type, int side, int do_corners, double ga
   }
 }
 
-/* periodic 2, zero-gradient / symmetry 1, outlet 0 (boundary_conditions.f90, the constructors) */
+/* periodic 2, zero-gradient / symmetry 1, outlet and pressure input 0 (the constructors) */
 static int bc_priority(int type) {
-  return type == CATO_BC_PERIODIC ? 2 : (type == CATO_BC_OUTLET ? 0 : 1);
+  return type == CATO_BC_PERIODIC ? 2
+         : (type == CATO_BC_OUTLET || type == CATO_BC_PRESSURE_INPUT ? 0 : 1);
 }
 
 /* flux_solver_t%apply_primitive_bc, flux_solver.f90:138-185: priority high -> low and, within
  * one priority, +x, +y, -x, -y. */
-int oracle_apply_bc(const cato_config* c, double* rho, double* u, double* v, double* p) {
+static int apply_bc_at(const cato_config* c, const pbc_ctx_t* pc, double* rho, double* u,
+                       double* v, double* p) {
   dims_t d = mkdims(c);
   double* f[4] = {rho, u, v, p};
   int all_periodic = 1;
@@ -291,8 +493,13 @@ int oracle_apply_bc(const cato_config* c, double* rho, double* u, double* v, dou
   for (int prio = maxp; prio >= 0; --prio)
     for (int s = 0; s < 4; ++s)
       if (bc_priority(c->bc[s]) == prio)
-        apply_one_bc(d, c->bc[s], s, all_periodic, c->gamma, c->bc_pressure, f);
+        apply_one_bc(d, c->bc[s], s, all_periodic, c->gamma, c->bc_pressure, c->bc_density,
+                     pc, f);
   return 0;
+}
+
+int oracle_apply_bc(const cato_config* c, double* rho, double* u, double* v, double* p) {
+  return apply_bc_at(c, NULL, rho, u, v, p);
 }
 
 /* One boundary_condition_t%apply on one side (used to replay the reference's own BC unit tests,
@@ -301,7 +508,7 @@ int oracle_apply_bc_side(const cato_config* c, int side, int type, int do_corner
                          double* u, double* v, double* p) {
   dims_t d = mkdims(c);
   double* f[4] = {rho, u, v, p};
-  apply_one_bc(d, type, side, do_corners, c->gamma, c->bc_pressure, f);
+  apply_one_bc(d, type, side, do_corners, c->gamma, c->bc_pressure, c->bc_density, NULL, f);
   return 0;
 }
 
@@ -941,12 +1148,12 @@ static double divergence(double Fi, double Fim, double Fj, double Fjm, const geo
 /* flux_solver_t%solve for the edge-split solvers (e.g. slau_solver.fypp:123-249): BCs on the
  * primitives, reconstruction, edge fluxes, flux divergence.  d_* are halo-padded, ghosts 0.
  * `cells` holds per-cell metrics (rect_cells) or is NULL for the uniform dx x dy grid. */
-static int solve_geo(const cato_config* c, const geom_t* cells, double* rho, double* u,
-                     double* v, double* p, double* drho, double* drhou, double* drhov,
+static int solve_geo(const cato_config* c, const geom_t* cells, const pbc_ctx_t* pc, double* rho,
+                     double* u, double* v, double* p, double* drho, double* drhou, double* drhov,
                      double* drhoE) {
   dims_t d = mkdims(c);
   geom_t geo = uniform_geom(c);
-  oracle_apply_bc(c, rho, u, v, p);
+  apply_bc_at(c, pc, rho, u, v, p);
   double* iflux = (double*)malloc(sizeof(double) * 4 * (size_t)(d.ni + 1) * d.nj);
   double* jflux = (double*)malloc(sizeof(double) * 4 * (size_t)d.ni * (d.nj + 1));
   if (!iflux || !jflux) { free(iflux); free(jflux); return CATO_ERR_OOM; }
@@ -992,7 +1199,15 @@ static int solve_geo(const cato_config* c, const geom_t* cells, double* rho, dou
 
 int oracle_solve(const cato_config* c, double* rho, double* u, double* v, double* p,
                  double* drho, double* drhou, double* drhov, double* drhoE) {
-  return solve_geo(c, NULL, rho, u, v, p, drho, drhou, drhov, drhoE);
+  return solve_geo(c, NULL, NULL, rho, u, v, p, drho, drhou, drhov, drhoE);
+}
+
+int oracle_solve_pbc(const cato_config* c, int32_t n, const double* t, const double* pt,
+                     const double* rhot, double time, double* rho, double* u, double* v, double* p,
+                     double* drho, double* drhou, double* drhov, double* drhoE) {
+  if (oracle_config_check(c) != CATO_OK) return CATO_ERR_CONFIG;
+  pbc_ctx_t pc = {n, t, pt, rhot, time};
+  return solve_geo(c, NULL, &pc, rho, u, v, p, drho, drhou, drhov, drhoE);
 }
 
 int oracle_solve_rect(const cato_config* c, const double* x_nodes, const double* y_nodes,
@@ -1001,7 +1216,7 @@ int oracle_solve_rect(const cato_config* c, const double* x_nodes, const double*
   if (oracle_config_check(c) != CATO_OK) return CATO_ERR_CONFIG;
   geom_t* cells = rect_cells(c->ni, c->nj, x_nodes, y_nodes);
   if (!cells) return CATO_ERR_ARG;
-  int rc = solve_geo(c, cells, rho, u, v, p, drho, drhou, drhov, drhoE);
+  int rc = solve_geo(c, cells, NULL, rho, u, v, p, drho, drhou, drhov, drhoE);
   free(cells);
   return rc;
 }
@@ -1014,6 +1229,14 @@ struct oracle_fluid {
   dims_t d;
   geom_t geo;
   geom_t* cells; /* per-cell metrics of a rectilinear grid (rect_cells), NULL if uniform */
+  /* pressure-input table (NULL: the configuration's constants) and the flux-solver clock of the
+   * persistent fluid (flux solvers add dt to their time before applying the BCs, e.g.
+   * slau_solver.fypp:168; copies of a fluid re-initialise theirs to the fluid's time,
+   * assign_fluid mod_fluid.f90:706) */
+  double* pbc_tab;
+  int pbc_n;
+  double solver_time;
+  double bc_time;    /* boundary time of the residual being evaluated */
   /* conserved (U) and derived (u, v, p, cs) of the current state */
   double *rho, *rhou, *rhov, *rhoE, *u, *v, *p, *cs;
   /* scratch: stage states, primitive copies for the solver, residuals */
@@ -1050,6 +1273,7 @@ void oracle_destroy(oracle_fluid* f) {
     for (int k = 0; k < 4; ++k) free(f->st[s][k]);
   for (int k = 0; k < 4; ++k) { free(f->sp[k]); free(f->L[k]); }
   free(f->cells);
+  free(f->pbc_tab);
   free(f);
 }
 
@@ -1116,8 +1340,35 @@ int oracle_set_primitive(oracle_fluid* f, const double* rho, const double* u, co
       AT(f->cs, i, j) = sqrt(f->c.gamma * pr);
     }
   f->time = 0.0;
+  f->solver_time = 0.0;
   f->iteration = 0;
   f->conv_valid = 0;
+  return 0;
+}
+
+/* fluid_t%set_time; as a fluid created at `time` (new_fluid(..., time)), its solver clock too */
+int oracle_set_time(oracle_fluid* f, double time, int64_t iteration) {
+  f->time = time;
+  f->solver_time = time;
+  f->iteration = iteration;
+  return 0;
+}
+
+/* pressure-input target table (n = 0: the configuration's constants) */
+int oracle_set_bc_table(oracle_fluid* f, int32_t n, const double* t, const double* p,
+                        const double* rho) {
+  free(f->pbc_tab);
+  f->pbc_tab = NULL;
+  f->pbc_n = 0;
+  if (n <= 0) return 0;
+  if (n < 2) return CATO_ERR_ARG;
+  for (int k = 1; k < n; ++k)
+    if (!(t[k] > t[k - 1])) return CATO_ERR_ARG;
+  f->pbc_tab = (double*)malloc(sizeof(double) * 3 * (size_t)n);
+  memcpy(f->pbc_tab, t, sizeof(double) * n);
+  memcpy(f->pbc_tab + n, p, sizeof(double) * n);
+  memcpy(f->pbc_tab + 2 * n, rho, sizeof(double) * n);
+  f->pbc_n = n;
   return 0;
 }
 
@@ -1164,8 +1415,10 @@ static int residual(oracle_fluid* f, const double* pr, const double* pu, const d
   memcpy(f->sp[1], pu, n);
   memcpy(f->sp[2], pv, n);
   memcpy(f->sp[3], pp, n);
-  return solve_geo(&f->c, f->cells, f->sp[0], f->sp[1], f->sp[2], f->sp[3], f->L[0], f->L[1],
-                   f->L[2], f->L[3]);
+  pbc_ctx_t pc = {f->pbc_n, f->pbc_tab, f->pbc_tab ? f->pbc_tab + f->pbc_n : NULL,
+                  f->pbc_tab ? f->pbc_tab + 2 * f->pbc_n : NULL, f->bc_time};
+  return solve_geo(&f->c, f->cells, &pc, f->sp[0], f->sp[1], f->sp[2], f->sp[3], f->L[0],
+                   f->L[1], f->L[2], f->L[3]);
 }
 
 /* out = A + L*c with the field '+' flush (fluid operators mod_fluid.f90:609-669) */
@@ -1270,12 +1523,18 @@ int oracle_integrate(oracle_fluid* f, double dt, int32_t* error_code) {
   /* per-stage derived quantities (u, v, p, cs), allocated on demand */
   for (int s = 0; s < 4; ++s) { su[s] = falloc(d); sv[s] = falloc(d); spp[s] = falloc(d); scs[s] = falloc(d); }
   int rc = 0;
+  /* boundary times: U%t advances the persistent fluid's solver clock; the stage copies U_1, U_2
+   * (assigned from expressions led by U) restart theirs at U%time before adding dt */
+  const double t_copy = f->time + dt;
   if (f->c.rk == CATO_RK_SSP2) {
     double* U1[4] = {f->st[0][0], f->st[0][1], f->st[0][2], f->st[0][3]};
     double* U2[4] = {f->st[1][0], f->st[1][1], f->st[1][2], f->st[1][3]};
+    f->solver_time = f->solver_time + dt;
+    f->bc_time = f->solver_time;
     rc |= residual(f, f->rho, f->u, f->v, f->p);
     stage_a(f, U1, U, dt);
     derive_all(f, U1, su[0], sv[0], spp[0], scs[0]);
+    f->bc_time = t_copy;
     rc |= residual(f, U1[0], su[0], sv[0], spp[0]);
     stage_b(f, U2, U, 0.5, U1, 0.5, 0.5 * dt);
     convergence(f, U1, U2);
@@ -1284,9 +1543,12 @@ int oracle_integrate(oracle_fluid* f, double dt, int32_t* error_code) {
     double* U1[4] = {f->st[0][0], f->st[0][1], f->st[0][2], f->st[0][3]};
     double* U2[4] = {f->st[1][0], f->st[1][1], f->st[1][2], f->st[1][3]};
     double* U3[4] = {f->st[2][0], f->st[2][1], f->st[2][2], f->st[2][3]};
+    f->solver_time = f->solver_time + dt;
+    f->bc_time = f->solver_time;
     rc |= residual(f, f->rho, f->u, f->v, f->p);
     stage_a(f, U1, U, dt);
     derive_all(f, U1, su[0], sv[0], spp[0], scs[0]);
+    f->bc_time = t_copy;
     rc |= residual(f, U1[0], su[0], sv[0], spp[0]);
     stage_b(f, U2, U, 3.0 / 4.0, U1, 1.0 / 4.0, (1.0 / 4.0) * dt);
     derive_all(f, U2, su[1], sv[1], spp[1], scs[1]);
@@ -1315,6 +1577,9 @@ int oracle_integrate(oracle_fluid* f, double dt, int32_t* error_code) {
     for (int k = 0; k < 4; ++k) memcpy(U0[k], U[k], nfield(d) * sizeof(double));
     /* U_prev starts as a copy of U (its primitives are U's) */
     for (int m = 0; m < ns; ++m) {
+      /* m = 1: U_prev is a fresh copy of U (allocate(source=U)) and carries U's solver clock,
+       * which rk_multistage never advances; later U_prev = U_curr restarts it at U%time */
+      f->bc_time = (m == 0) ? f->solver_time + dt : t_copy;
       if (m == 0) rc |= residual(f, f->rho, f->u, f->v, f->p);
       else rc |= residual(f, Uc[0], su[0], sv[0], spp[0]);
       stage_a(f, Uc, U0, dt * alpha[m]);
@@ -1395,7 +1660,10 @@ int oracle_config_check(const cato_config* c) {
   if (c->ni < c->n_ghost || c->nj < c->n_ghost) return CATO_ERR_CONFIG;
   int outlet = 0;
   for (int s = 0; s < 4; ++s) {
-    if (c->bc[s] < CATO_BC_ZERO_GRADIENT || c->bc[s] > CATO_BC_OUTLET) return CATO_ERR_CONFIG;
+    if (c->bc[s] < CATO_BC_ZERO_GRADIENT || c->bc[s] > CATO_BC_PRESSURE_INPUT)
+      return CATO_ERR_CONFIG;
+    /* the pressure input only implements +x (pressure_input_bc.f90:404-409) */
+    if (c->bc[s] == CATO_BC_PRESSURE_INPUT && s != CATO_PLUS_X) return CATO_ERR_CONFIG;
     outlet |= c->bc[s] == CATO_BC_OUTLET;
   }
   if (outlet && !(c->bc_pressure > 0.0)) return CATO_ERR_CONFIG; /* outlet_bc.f90:54-59 */

@@ -61,6 +61,17 @@ int oracle_convergence(oracle_fluid* f, double out[4]);
 /* interior totals of rho, rho u, rho v, rho E times the cell volume */
 int oracle_conservation_sums(oracle_fluid* f, double out[4]);
 int oracle_set_rectilinear(oracle_fluid* f, const double* x_nodes, const double* y_nodes);
+int oracle_set_time(oracle_fluid* f, double time, int64_t iteration);
+/* powers of the pressure-input inlet: 0 = libm pow (as the reference), 1 = correctly rounded */
+int oracle_set_pow_mode(int mode);
+double oracle_pow(int mode, double x, double y);
+int oracle_set_bc_table(oracle_fluid* f, int32_t n, const double* t, const double* p,
+                        const double* rho);
+/* oracle_solve with a pressure-input table evaluated at `time` */
+int oracle_solve_pbc(const cato_config* cfg, int32_t n, const double* t, const double* pt,
+                     const double* rhot, double time, double* rho, double* u, double* v,
+                     double* p, double* d_rho_dt, double* d_rho_u_dt, double* d_rho_v_dt,
+                     double* d_rho_E_dt);
 
 #ifdef __cplusplus
 }

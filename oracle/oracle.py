@@ -51,6 +51,13 @@ def lib():
         L.oracle_solve.argtypes = [cfgp] + [_dp] * 8
         L.oracle_solve_rect.argtypes = [cfgp] + [_dp] * 10
         L.oracle_set_rectilinear.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.oracle_set_time.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int64]
+        L.oracle_set_pow_mode.argtypes = [ctypes.c_int]
+        L.oracle_pow.restype = ctypes.c_double
+        L.oracle_pow.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.oracle_set_bc_table.argtypes = [ctypes.c_void_p, ctypes.c_int32, _dp, _dp, _dp]
+        L.oracle_solve_pbc.argtypes = ([cfgp, ctypes.c_int32, _dp, _dp, _dp, ctypes.c_double]
+                                       + [_dp] * 8)
         L.oracle_create.restype = ctypes.c_void_p
         L.oracle_create.argtypes = [cfgp]
         L.oracle_destroy.argtypes = [ctypes.c_void_p]
@@ -132,11 +139,32 @@ def interpolate_edges(cfg: SchemeConfig, q):
     return ie, je
 
 
-def solve(cfg: SchemeConfig, rho, u, v, p, nodes=None):
+class pow_mode:
+    """Context: the pressure-input inlet's powers in the oracle, "libm" (the reference's pow)
+    or "cr" (correctly rounded, the arithmetic of the CUDA path)."""
+
+    def __init__(self, mode: str):
+        self.mode = {"libm": 0, "cr": 1}[mode]
+
+    def __enter__(self):
+        lib().oracle_set_pow_mode(self.mode)
+        return self
+
+    def __exit__(self, *exc):
+        lib().oracle_set_pow_mode(0)
+
+
+def solve(cfg: SchemeConfig, rho, u, v, p, nodes=None, bc_table=None, time=0.0):
     """flux_solver_t%solve: BCs written into the ghosts of rho/u/v/p; returns d/dt of U.
-    ``nodes = (x(1..ni+1), y(1..nj+1))`` selects a rectilinear grid."""
+    ``nodes = (x(1..ni+1), y(1..nj+1))`` selects a rectilinear grid; ``bc_table = (t, p, rho)``
+    a tabulated pressure-input target evaluated at ``time``."""
     out = [empty_field(cfg) for _ in range(4)]
-    if nodes is None:
+    if bc_table is not None:
+        t, pt, rt = (np.ascontiguousarray(a, dtype=np.float64) for a in bc_table)
+        rc = lib().oracle_solve_pbc(_cfg(cfg), len(t), t.ctypes.data_as(_dp),
+                                    pt.ctypes.data_as(_dp), rt.ctypes.data_as(_dp), float(time),
+                                    _ptr(rho), _ptr(u), _ptr(v), _ptr(p), *(_ptr(a) for a in out))
+    elif nodes is None:
         rc = lib().oracle_solve(_cfg(cfg), _ptr(rho), _ptr(u), _ptr(v), _ptr(p),
                                 *(_ptr(a) for a in out))
     else:
@@ -172,6 +200,16 @@ class OracleFluid:
                                           ys.ctypes.data_as(_dp))
         if rc:
             raise ValueError(f"oracle_set_rectilinear: {rc}")
+
+    def set_time(self, time: float, iteration: int) -> None:
+        lib().oracle_set_time(self._h, float(time), int(iteration))
+
+    def set_bc_table(self, time, pressure, density) -> None:
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (time, pressure, density)]
+        rc = lib().oracle_set_bc_table(self._h, len(arrs[0]),
+                                       *(a.ctypes.data_as(_dp) for a in arrs))
+        if rc:
+            raise ValueError(f"oracle_set_bc_table: {rc}")
 
     def set_primitive(self, rho, u, v, p) -> None:
         arrs = [np.asfortranarray(a, dtype=np.float64) for a in (rho, u, v, p)]

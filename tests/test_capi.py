@@ -4,6 +4,7 @@ struct matches the C layout.  No GPU compute is called."""
 import ctypes
 import os
 import re
+import subprocess
 
 import pytest
 
@@ -32,10 +33,22 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
 
 
-def test_struct_layout():
-    assert ctypes.sizeof(CatoConfig) == 136
-    assert CatoConfig.bc_pressure.offset == 128
-    assert CatoConfig.gamma.offset == 56
+def test_struct_layout(tmp_path):
+    """The ctypes mirror has the C struct's size and every field's offset (compiled with gcc)."""
+    names = [f[0] for f in CatoConfig._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stddef.h>\n#include <stdio.h>\n#include \"cato_gpu.h\"\n"
+                   "int main(void) {\n  printf(\"%zu\\n\", sizeof(cato_config));\n"
+                   + "".join(f'  printf("%zu\\n", offsetof(cato_config, {n}));\n' for n in names)
+                   + "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    out = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    assert out[0] == ctypes.sizeof(CatoConfig)
+    for n, off in zip(names, out[1:]):
+        assert getattr(CatoConfig, n).offset == off, n
 
 
 def test_config_defaults_match_deck_defaults(oracle):

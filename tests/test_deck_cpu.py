@@ -4,6 +4,7 @@ import ctypes
 import glob
 import os
 
+import numpy as np
 import pytest
 
 from fvleg_2d_gb300 import _lib
@@ -105,3 +106,59 @@ def test_reference_integrated_decks_parse():
         sod = parse_deck(f.read())
     assert (sod.flux_solver, sod.limiter, sod.integration_strategy) == ("Roe", "MLP5", "ssp_rk2")
     assert sod.bc["+x"] == "zero_gradient" and sod.bc["+y"] == "periodic" and sod.cfl == 0.1
+
+
+PBC_DECK = """
+[reference_state]
+reference_length = 2.0
+reference_density = 0.5
+reference_velocity = 4.0
+[time]
+max_time = 0.05
+integration_strategy = 'ssp_rk2'
+[physics]
+polytropic_index = 1.4
+[scheme]
+flux_solver = 'AUSMPW+'
+[initial_conditions]
+read_from_file = false
+init_density = 1.0
+init_pressure = 1.0
+[grid]
+ni_nodes = 11
+nj_nodes = 6
+xmin = 0
+xmax = 1
+ymin = 0
+ymax = 0.5
+[boundary_conditions]
+plus_x = 'pressure_input'
+minus_x = 'symmetry'
+plus_y = 'symmetry'
+minus_y = 'symmetry'
+bc_density = 0.25
+bc_pressure_input_file = 'drive.dat'
+bc_pressure_scale_factor = 2.0
+"""
+
+
+def test_pressure_input_keys_and_table(tmp_path):
+    from fvleg_2d_gb300.deck import nondim_factors, read_bc_pressure_table
+
+    (tmp_path / "drive.dat").write_text("# time pressure density\n0.0 1.0d0 0.5\n"
+                                        "1e-1 3.0 0.75\n0.2, 2.0, 1.0\nend of table\n")
+    d = parse_deck(PBC_DECK)
+    assert d.bc["+x"] == "pressure_input" and not d.apply_constant_bc_pressure
+    t, p, rho = read_bc_pressure_table(d, str(tmp_path))
+    f = nondim_factors(d)
+    np.testing.assert_array_equal(t, np.array([0.0, 0.1, 0.2]) * (1.0 / (2.0 / 4.0)))
+    np.testing.assert_array_equal(p, (np.array([1.0, 3.0, 2.0]) * (1.0 / (0.5 * 16.0))) * 2.0)
+    np.testing.assert_array_equal(rho, (np.array([0.5, 0.75, 1.0]) * (1.0 / 0.5)) * 2.0)
+    cfg = d.scheme()
+    assert cfg.bc_density == 0.25 * f["density_to_dim"]
+    const = parse_deck(PBC_DECK.replace("bc_pressure_input_file = 'drive.dat'",
+                                        "apply_constant_bc_pressure = true\n"
+                                        "constant_bc_pressure_value = 3.0"))
+    assert const.scheme().constant_bc_pressure == 3.0 * f["press_to_nondim"]
+    with pytest.raises(DeckError):
+        parse_deck(PBC_DECK.replace("bc_pressure_input_file = 'drive.dat'", ""))
