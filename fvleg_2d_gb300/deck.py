@@ -331,12 +331,54 @@ def read_bc_pressure_table(deck: Deck, base_dir: str = "."):
             (a[:, 2] * f["density_to_nondim"]) * scale)
 
 
-def run_deck(deck: Deck, precision: str = "fp64", prims=None, grid=None, base_dir: str = "."):
+def main_loop(deck: Deck, fluid, step, results_dir: str | None = None) -> int:
+    """The time loop of ``main.f90:95-198`` (no restart, no start-up period) around a fluid:
+    ``step(dt)`` advances one step (``dt`` None: the CFL step) and returns its error code.  The
+    loop keeps its own clock: it snaps to the next output time when a step passes it, writes a
+    contour the iteration after (``write_contour`` of :mod:`.contour`, when ``results_dir`` is
+    given), and stops on that clock.  The first step uses ``initial_delta_t`` when it is set,
+    every step when ``use_constant_delta_t``.  Returns the iterations taken."""
+    from .contour import write_contour
+    from .fluid import CatoError
+
+    f = nondim_factors(deck)
+    interval = deck.contour_interval_dt * f["t_to_nondim"]
+    max_time = deck.max_time * f["t_to_nondim"]
+    eps = float(np.finfo(np.float64).eps)
+    time, iteration = 0.0, 0
+    next_output = 0.0 + interval
+    if results_dir is not None:
+        write_contour(fluid, results_dir, deck, iteration=iteration)
+    while time < max_time and iteration < deck.max_iterations:
+        fixed = deck.use_constant_delta_t or (iteration == 0 and deck.initial_delta_t > 0.0)
+        ec = step(deck.initial_delta_t * f["t_to_nondim"] if fixed else None)
+        delta_t = fluid.last_dt
+        new_time = fluid.time
+        if ec:
+            if results_dir is not None:
+                write_contour(fluid, results_dir, deck, iteration=iteration)
+            raise CatoError(ec, f"time integration failed at iteration {iteration}")
+        if abs(time - next_output) < eps:
+            next_output = next_output + interval
+            if results_dir is not None:
+                write_contour(fluid, results_dir, deck, iteration=iteration)
+        if new_time > next_output:
+            delta_t = abs(next_output - time)
+            new_time = time + delta_t
+        time = new_time
+        iteration = iteration + 1
+    return iteration
+
+
+def run_deck(deck: Deck, precision: str = "fp64", prims=None, grid=None, base_dir: str = ".",
+             results_dir: str | None = None):
     """The main.f90 time loop for a deck: returns (fluid, steps).  A deck that reads its
     initial state from a file loads it (grid included) from ``initial_condition_file`` relative
     to ``base_dir``; alternatively pass that state as ``prims`` (rho, u, v, p, halo-padded) and
     a uniform grid as ``grid=(ni, nj, dx, dy)``.  ``max_time`` is scaled by ``t_to_nondim``
-    as in ``main.f90:98``."""
+    as in ``main.f90:98``.  With ``results_dir`` (contour output) or a deck-given dt the loop
+    runs on the host (:func:`main_loop`); otherwise on the device (``cato_gpu_run``, the same
+    loop while no output time falls inside it)."""
     from .fluid import Fluid
 
     ic = None
@@ -352,5 +394,7 @@ def run_deck(deck: Deck, precision: str = "fp64", prims=None, grid=None, base_di
     if "pressure_input" in deck.bc.values() and not deck.apply_constant_bc_pressure:
         fluid.set_bc_table(*read_bc_pressure_table(deck, base_dir))
     fluid.initialize(*prims)
-    steps = fluid.run(deck.max_time * t_to_nondim(deck), deck.max_iterations)
-    return fluid, steps
+    if results_dir is None and not deck.use_constant_delta_t and not deck.initial_delta_t > 0.0:
+        steps = fluid.run(deck.max_time * t_to_nondim(deck), deck.max_iterations)
+        return fluid, steps
+    return fluid, main_loop(deck, fluid, lambda dt: fluid.integrate(dt)[1], results_dir)

@@ -124,6 +124,13 @@ class _Handle:
         _check(self.L.cato_gpu_get_time(self.h, None, ctypes.byref(it), None), self.h)
         return it.value
 
+    @property
+    def last_dt(self) -> float:
+        """dt of the last step taken (0 before the first)."""
+        dt = ctypes.c_double()
+        _check(self.L.cato_gpu_get_time(self.h, None, None, ctypes.byref(dt)), self.h)
+        return dt.value
+
 
 class Fluid(_Handle):
     """fluid_t on the GPU.  ``Fluid(cfg).initialize(rho, u, v, p)`` replaces
