@@ -54,6 +54,8 @@ def load(build_if_missing: bool = False):
         "cato_gpu_upload_primitive": (ctypes.c_int, [H, _dp, _dp, _dp, _dp, i64]),
         "cato_gpu_set_rectilinear": (ctypes.c_int, [H, _dp, _dp]),
         "cato_gpu_set_bc_table": (ctypes.c_int, [H, ctypes.c_int32, _dp, _dp, _dp]),
+        "cato_gpu_set_energy_source": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_int32,
+                                                      _dp, _dp, _dp]),
         "cato_gpu_get_timestep": (ctypes.c_int, [H, _dp]),
         "cato_gpu_integrate": (ctypes.c_int, [H, ctypes.c_double, _dp,
                                               ctypes.POINTER(ctypes.c_int32)]),

@@ -170,3 +170,54 @@ class SchemeConfig:
         """Shape of one halo-padded field, Fortran order (i, j)."""
         g = self.ghost_layers()
         return (self.ni + 2 * g, self.nj + 2 * g)
+
+
+SOURCE_GEOMETRY_IDS = {"uniform": 0, "constant_xy": 1, "1d_gaussian": 2, "decay": 3}
+
+
+class CatoEnergySource(ctypes.Structure):
+    """Mirror of ``struct cato_energy_source`` in ``include/cato_gpu.h``."""
+
+    _fields_ = [
+        ("geometry", ctypes.c_int32),
+        ("gaussian_order", ctypes.c_int32),
+        ("constant_value", ctypes.c_double),
+        ("multiplier", ctypes.c_double),
+        ("xlo", ctypes.c_double),
+        ("xhi", ctypes.c_double),
+        ("ylo", ctypes.c_double),
+        ("yhi", ctypes.c_double),
+        ("fwhm_x", ctypes.c_double),
+        ("fwhm_y", ctypes.c_double),
+    ]
+
+
+@dataclass
+class EnergySource:
+    """An energy source term ([source_terms], ``source_t`` of ``mod_source.f90``), in the
+    reference's non-dimensional units.  ``table = (time, value, critical_density)`` replaces
+    the constant value (scaled as read_input_file scales it)."""
+
+    geometry: str = "uniform"
+    constant_value: float = 0.0
+    multiplier: float = 1.0
+    xlo: float = 0.0
+    xhi: float = 0.0
+    ylo: float = 0.0
+    yhi: float = 0.0
+    fwhm_x: float = 0.0
+    fwhm_y: float = 0.0
+    gaussian_order: int = 1
+    table: tuple | None = None
+
+    def to_c(self) -> CatoEnergySource:
+        if self.geometry not in SOURCE_GEOMETRY_IDS:
+            raise ValueError(f"Unsupported geometry type {self.geometry!r}, must be one of "
+                             f"{sorted(SOURCE_GEOMETRY_IDS)}")
+        c = CatoEnergySource()
+        c.geometry = SOURCE_GEOMETRY_IDS[self.geometry]
+        c.gaussian_order = int(self.gaussian_order)
+        c.constant_value, c.multiplier = self.constant_value, self.multiplier
+        c.xlo, c.xhi, c.ylo, c.yhi = self.xlo, self.xhi, self.ylo, self.yhi
+        c.fwhm_x, c.fwhm_y = self.fwhm_x, self.fwhm_y
+        return c

@@ -65,6 +65,10 @@ __device__ __forceinline__ void batch_stage_args(InstDesc* d, const BatchStageAr
   A.bc_p = d->bc_p;
   A.cfl = d->cfl;
   A.G = d->G;
+  // single-handle features the batch does not carry (configurations are rejected at add)
+  A.pbc_edge = nullptr;
+  A.pbc_ng = 0;
+  A.src_q = nullptr;
   const bool raw = (B.stage == 0) && d->raw_pending;
   if constexpr (Prec<R>::kind != 1) {
     double* const* prev = (B.stage == 0) ? d->U[0] : d->S[(B.stage - 1) & 1];

@@ -23,6 +23,7 @@
 #include "cato_kernels.cuh"
 #include "cato_launch.cuh"
 #include "cato_pbc.cuh"
+#include "cato_source.cuh"
 
 using namespace cato;
 
@@ -69,6 +70,18 @@ struct cato_handle {
   double* pbc = nullptr;
   double* pbc_tab = nullptr;
   int pbc_n = 0, pbc_cap = 0;
+  // rectilinear grid nodes x(1..ni+1), y(1..nj+1) (while rect_on)
+  double* nodes[2] = {};
+  bool rect_on = false;
+  // energy source term: configuration, table (time, value, critical density), field, slots
+  bool src_on = false;
+  cato_energy_source src{};
+  double* src_tab = nullptr;
+  int src_n = 0;
+  double src_tmax = 0.0;
+  double* src_field = nullptr;
+  int* src_dep = nullptr;
+  int src_parity = 0;
   Plan plan;
   FluxConsts<double> K64{};
   FluxConsts<float> K32{};
@@ -248,10 +261,63 @@ static int enqueue_pbc(cato_handle* h, StageArgs& A, bool rk_first) {
   return CATO_OK;
 }
 
+static int grid_for(long long n) {
+  long long b = (n + 255) / 256;
+  if (b > 152LL * 32) b = 152LL * 32;
+  return (int)(b < 1 ? 1 : b);
+}
+
+// The energy source field of the step (source_t%integrate at the step start, once per step as
+// in every integrator, e.g. ssp_rk_3_3 mod_fluid.f90:770): the deposition column (only the
+// geometries that use it) and q_dot_h.
+static int enqueue_source(cato_handle* h) {
+  if (!h->src_on) return CATO_OK;
+  SourceArgs S{};
+  S.geometry = h->src.geometry;
+  S.order = h->src.gaussian_order;
+  S.n = h->src_n;
+  S.t = h->src_tab;
+  S.q = h->src_tab ? h->src_tab + h->src_n : nullptr;
+  S.rho_crit = h->src_tab ? h->src_tab + 2 * h->src_n : nullptr;
+  S.t_max = h->src_tmax;
+  S.constant_value = h->src.constant_value;
+  S.multiplier = h->src.multiplier;
+  S.xlo = h->src.xlo;
+  S.xhi = h->src.xhi;
+  S.ylo = h->src.ylo;
+  S.yhi = h->src.yhi;
+  S.fwhm_x = h->src.fwhm_x;
+  S.xn = h->rect_on ? h->nodes[0] : nullptr;
+  S.yn = h->rect_on ? h->nodes[1] : nullptr;
+  S.dx = h->cfg.dx;
+  S.dy = h->cfg.dy;
+  S.ni = h->ni;
+  S.nj = h->nj;
+  S.pitch = h->pitch;
+  S.rho = h->cfg.precision == CATO_MIXED ? h->U[h->cur][0] : h->U[0][0];
+  S.field = h->src_field;
+  S.i_dep = h->src_dep;
+  S.parity = h->src_parity;
+  S.ctl = h->ctl;
+  const int blocks = grid_for((long long)h->ni * h->nj);
+  if (S.geometry == SRC_GAUSSIAN_1D || S.geometry == SRC_DECAY) {
+    source_deposit_kernel<<<blocks, 256, 0, h->stream>>>(S);
+    CK(cudaGetLastError());
+  }
+  source_field_kernel<<<blocks, 256, 0, h->stream>>>(S);
+  CK(cudaGetLastError());
+  h->src_parity = 1 - h->src_parity;
+  return CATO_OK;
+}
+
 // Enqueue one full time step (step control + every stage) on the handle's stream.
 static int enqueue_step(cato_handle* h) {
   step_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctl);
   CK(cudaGetLastError());
+  {
+    const int rcs = enqueue_source(h);
+    if (rcs) return rcs;
+  }
   if (h->event_hook) CK(cudaEventRecord(h->event_hook[1], h->stream));
   const int ns = (int)h->stages.size();
   const bool fp64 = h->cfg.precision != CATO_MIXED;  // FP64 stage-buffer layout
@@ -290,6 +356,7 @@ static int enqueue_step(cato_handle* h) {
       A.ufo = A.last ? h->Uf[1 - h->cur] : nullptr;
       if (st.kind == 0) A.b = 0.0;  // rk(m,n): U_curr = U_0 + c L(U_prev)
     }
+    A.src_q = h->src_on ? h->src_field : nullptr;
     const int rcb = enqueue_pbc(h, A, k == 0 && h->cfg.rk >= CATO_RK_1_3);
     if (rcb) return rcb;
     CK(launch(h, A));
@@ -357,11 +424,6 @@ static void zero_host_field(cato_handle* h, double* a, int64_t ld) {
   for (size_t j = 0; j < rows; ++j) std::memset(a + j * ld, 0, sizeof(double) * (h->ni + 2 * h->ng));
 }
 
-static int grid_for(long long n) {
-  long long b = (n + 255) / 256;
-  if (b > 152LL * 32) b = 152LL * 32;
-  return (int)(b < 1 ? 1 : b);
-}
 
 extern "C" {
 
@@ -512,6 +574,10 @@ int cato_gpu_destroy(cato_handle* h) {
   cudaFree(h->red);
   cudaFree(h->pbc);
   cudaFree(h->pbc_tab);
+  for (int k = 0; k < 2; ++k) cudaFree(h->nodes[k]);
+  cudaFree(h->src_tab);
+  cudaFree(h->src_field);
+  cudaFree(h->src_dep);
   for (int k = 0; k < 6; ++k) cudaFree(h->rect[k]);
   for (int k = 0; k < 2; ++k) cudaFree(h->rectf[k]);
   if (h->ctl_host) cudaFreeHost(h->ctl_host);
@@ -894,8 +960,11 @@ int cato_host_free(void* p) { return cudaFreeHost(p) == cudaSuccess ? CATO_OK : 
 
 int cato_gpu_launches_per_step(const cato_handle* h, int32_t* n) {
   if (!h || !n) return CATO_ERR_ARG;
-  // step control + per stage: the stage kernel (+ the two pressure-input boundary kernels)
-  *n = 1 + (int32_t)h->stages.size() * (has_pbc(h) ? 3 : 1);
+  // step control (+ the source field kernels) + per stage: the stage kernel (+ the two
+  // pressure-input boundary kernels)
+  const int src = !h->src_on ? 0 : (h->src.geometry == CATO_SRC_GAUSSIAN_1D ||
+                                    h->src.geometry == CATO_SRC_DECAY ? 2 : 1);
+  *n = 1 + src + (int32_t)h->stages.size() * (has_pbc(h) ? 3 : 1);
   return CATO_OK;
 }
 
@@ -928,6 +997,53 @@ int cato_gpu_profile_step(cato_handle* h, float* kernel_ms, int32_t capacity, in
   rc = pull_ctl(h);
   if (rc) return rc;
   if (h->ctl_host->iter > c.iter) h->stepped = true;
+  return CATO_OK;
+}
+
+int cato_gpu_set_energy_source(cato_handle* h, const cato_energy_source* src, int32_t n,
+                               const double* time, const double* value,
+                               const double* critical_density) {
+  if (!h) return CATO_ERR_ARG;
+  CK(cudaStreamSynchronize(h->stream));
+  if (!src) {
+    h->src_on = false;
+    return CATO_OK;
+  }
+  if (src->geometry < CATO_SRC_UNIFORM || src->geometry > CATO_SRC_DECAY)
+    return fail(h, CATO_ERR_CONFIG, "unsupported source geometry");
+  if (src->geometry == CATO_SRC_GAUSSIAN_1D) {
+    // new_source (mod_source.f90:111-119) and get_source_field (:386-388)
+    if (src->gaussian_order < 1) return fail(h, CATO_ERR_CONFIG, "gaussian order < 1");
+    if (!(src->fwhm_x > 0.0 && !(src->fwhm_y > 0.0)))
+      return fail(h, CATO_ERR_CONFIG, "a 1d_gaussian source must be constant in y");
+  }
+  if (n == 1 || n < 0) return fail(h, CATO_ERR_ARG, "a table needs at least two points");
+  if (n > 0) {
+    if (!time || !value || !critical_density) return fail(h, CATO_ERR_ARG, "null table");
+    for (int k = 0; k < n; ++k) {
+      if (!std::isfinite(time[k]) || !std::isfinite(value[k]) ||
+          !std::isfinite(critical_density[k]))
+        return fail(h, CATO_ERR_ARG, "non-finite table entry");
+      if (k > 0 && !(time[k] > time[k - 1]))
+        return fail(h, CATO_ERR_ARG, "table times must be strictly increasing");
+    }
+    cudaFree(h->src_tab);
+    h->src_tab = nullptr;
+    CK(cudaMalloc(&h->src_tab, 3 * (size_t)n * sizeof(double)));
+    const double* s3[3] = {time, value, critical_density};
+    for (int k = 0; k < 3; ++k)
+      CK(cudaMemcpy(h->src_tab + (size_t)k * n, s3[k], n * sizeof(double),
+                    cudaMemcpyHostToDevice));
+    h->src_tmax = time[0];
+    for (int k = 1; k < n; ++k) h->src_tmax = std::max(h->src_tmax, time[k]);
+  }
+  if (!h->src_field) CK(cudaMalloc(&h->src_field, h->field_elems * sizeof(double)));
+  if (!h->src_dep) CK(cudaMalloc(&h->src_dep, 2 * sizeof(int)));
+  CK(cudaMemset(h->src_dep, 0xff, 2 * sizeof(int)));  // -1: no column found yet
+  h->src_parity = 0;
+  h->src = *src;
+  h->src_n = n;
+  h->src_on = true;
   return CATO_OK;
 }
 
@@ -987,6 +1103,7 @@ int cato_gpu_set_rectilinear(cato_handle* h, const double* x_nodes, const double
   h->uploaded = false;  // the stored CFL dt and state were for the previous geometry
   h->stepped = false;
   if (!x_nodes) {  // back to the uniform dx x dy grid of the configuration
+    h->rect_on = false;
     h->G.dxc = h->G.lxc = h->G.rdxc = h->G.dyc = h->G.lyc = h->G.rdyc = nullptr;
     h->G.rdxf = h->G.rdyf = nullptr;
     return CATO_OK;
@@ -1002,23 +1119,17 @@ int cato_gpu_set_rectilinear(cato_handle* h, const double* x_nodes, const double
       if (!h->rect[3 * a + k]) CK(cudaMalloc(&h->rect[3 * a + k], (n[a] + 1) * sizeof(double)));
     if (!h->rectf[a]) CK(cudaMalloc(&h->rectf[a], (n[a] + 1) * sizeof(float)));
   }
-  double* tmp = nullptr;
-  CK(cudaMalloc(&tmp, (std::max(h->ni, h->nj) + 1) * sizeof(double)));
   for (int a = 0; a < 2; ++a) {
-    cudaError_t e = cudaMemcpyAsync(tmp, nodes[a], (n[a] + 1) * sizeof(double),
-                                    cudaMemcpyHostToDevice, h->stream);
-    if (e == cudaSuccess) {
-      rect_metrics_kernel<<<grid_for(n[a]), 256, 0, h->stream>>>(
-          tmp, n[a], h->rect[3 * a], h->rect[3 * a + 1], h->rect[3 * a + 2], h->rectf[a]);
-      e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    if (e != cudaSuccess) {
-      cudaFree(tmp);
-      return cuda_fail(h, e, "cato_gpu_set_rectilinear");
-    }
+    // the nodes stay on the device (cell centroids of the energy source term)
+    if (!h->nodes[a]) CK(cudaMalloc(&h->nodes[a], (n[a] + 1) * sizeof(double)));
+    CK(cudaMemcpyAsync(h->nodes[a], nodes[a], (n[a] + 1) * sizeof(double),
+                       cudaMemcpyHostToDevice, h->stream));
+    rect_metrics_kernel<<<grid_for(n[a]), 256, 0, h->stream>>>(
+        h->nodes[a], n[a], h->rect[3 * a], h->rect[3 * a + 1], h->rect[3 * a + 2], h->rectf[a]);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
   }
-  cudaFree(tmp);
+  h->rect_on = true;
   h->G.dxc = h->rect[0]; h->G.lxc = h->rect[1]; h->G.rdxc = h->rect[2]; h->G.rdxf = h->rectf[0];
   h->G.dyc = h->rect[3]; h->G.lyc = h->rect[4]; h->G.rdyc = h->rect[5]; h->G.rdyf = h->rectf[1];
   return CATO_OK;

@@ -19,6 +19,7 @@ struct StepCtl {
   int status;         // ST_* bits of the current state
   double t_create;    // time the state was created at (upload / set_time): the flux solver of
                       // the persistent fluid keeps it under rk(m,n) (pressure-input table time)
+  double t_step;      // time at the start of the current step (energy source term time)
 };
 
 __device__ __forceinline__ double decode_dt(unsigned long long b) {

@@ -15,6 +15,7 @@ static __global__ void step_begin_kernel(StepCtl* c) {
   if (!act) return;
   double dt = c->fixed_dt > 0.0 ? c->fixed_dt : decode_dt(c->dt_min);
   c->dt = dt;
+  c->t_step = c->time;
   c->time = c->time + dt;
   c->iter = c->iter + 1;
   c->dt_min = ~0ULL;

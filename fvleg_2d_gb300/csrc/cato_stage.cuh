@@ -61,6 +61,9 @@ struct StageArgs {
   // -pbc_ng .. nj+pbc_ng-1, written for this stage by pbc_edge_kernel
   const double* pbc_edge;
   int pbc_ng;
+  // energy source term: q_dot_h per interior cell (pitch layout), added to the energy residual
+  // (time_derivative, mod_fluid.f90:503); null without a source
+  const double* src_q;
   Geom G;
 };
 
@@ -425,6 +428,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
             L = divergence_fp64(Fi, Fim, Fj, Fjm, cg);
           else  // double-float flux differences, the result carried to FP64
             L = from_df(-((Fi - Fim) * dx_inv + (Fj - Fjm) * dy_inv));
+          if (k == 3 && A.src_q) L = L + A.src_q[cidx];
           double r;
           if (A.kind == 2) {
             r = L;
@@ -451,6 +455,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
           float Fj = sfj[((j & 1) * 4 + k) * T + t];
           float Fjm = sfj[(((j - 1) & 1) * 4 + k) * T + t];
           float L = -((Fi - Fim) * idx_f + (Fj - Fjm) * idy_f);
+          if (k == 3 && A.src_q) L = L + d2f_int(A.src_q[cidx]);
           dn[k] = bf * f4get(dkc, k) + L * ccf;
         }
         if (A.last) {

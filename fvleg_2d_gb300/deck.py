@@ -105,6 +105,24 @@ class Deck:
     constant_bc_pressure_value: float = 0.0
     bc_pressure_input_file: str = ""
     bc_pressure_scale_factor: float = 1.0
+    # [source_terms] (mod_input.f90:394-427)
+    enable_source_terms: bool = False
+    source_geometry: str = ""
+    apply_constant_source: bool = False
+    source_file: str = ""
+    source_term_type: str = ""
+    constant_source_value: float = 0.0
+    source_scale_factor: float = 1.0
+    energy_deposition_critical_density: float = 0.1
+    source_xlo: float = 0.0
+    source_xhi: float = 0.0
+    source_ylo: float = 0.0
+    source_yhi: float = 0.0
+    source_center_x: float = 0.0
+    source_center_y: float = 0.0
+    source_gaussian_fwhm_x: float = 0.0
+    source_gaussian_fwhm_y: float = 0.0
+    source_gaussian_order: int = 1
     # [io]
     contour_interval_dt: float = 0.1
     contour_format: str = "xdmf"
@@ -252,6 +270,26 @@ def parse_deck(text: str) -> Deck:
         d.outflow_ambient_pressure = get("boundary_conditions", "outflow_ambient_pressure", _real,
                                          required=True)
         d.constant_bc_pressure_value = d.outflow_ambient_pressure
+    d.enable_source_terms = get("source_terms", "enable_source_terms", _logical, False)
+    if d.enable_source_terms:
+        d.source_geometry = get("source_terms", "geometry", required=True)
+        d.apply_constant_source = get("source_terms", "apply_constant_source", _logical, False)
+        d.source_file = get("source_terms", "source_file", required=True)
+        d.source_term_type = get("source_terms", "source_term_type", required=True)
+        d.constant_source_value = get("source_terms", "constant_source_value", _real, 0.0)
+        d.source_scale_factor = get("source_terms", "source_scale_factor", _real, 1.0)
+        d.energy_deposition_critical_density = get(
+            "source_terms", "energy_deposition_critical_density", _real, 0.1)
+        if d.source_geometry == "constant_xy":
+            for k in ("xlo", "xhi", "ylo", "yhi"):
+                setattr(d, "source_" + k, get("source_terms", k, _real, required=True))
+        elif d.source_geometry in ("1d_gaussian", "2d_gaussian"):
+            d.source_center_x = get("source_terms", "center_x", _real, 0.0)
+            d.source_center_y = get("source_terms", "center_y", _real, 0.0)
+            d.source_gaussian_fwhm_x = get("source_terms", "gaussian_fwhm_x", _real, 0.0)
+            d.source_gaussian_fwhm_y = get("source_terms", "gaussian_fwhm_y", _real, 0.0)
+            d.source_gaussian_order = get("source_terms", "gaussian_order",
+                                          lambda v: int(_real(v)), 1)
     d.contour_format = get("io", "format", default=get("io", "contour_format", default="xdmf"))
     d.contour_interval_dt = get("io", "contour_interval_dt", _real, 0.1)
     return d
@@ -279,14 +317,16 @@ def nondim_factors(deck: Deck) -> dict:
     """The scale factors of ``set_refrence_quantities`` (``non_dimensional.f90:95-135``), all 1
     without non-dimensionalization."""
     names = ("len_to_nondim", "t_to_nondim", "density_to_nondim", "density_to_dim",
-             "vel_to_nondim", "press_to_nondim")
+             "vel_to_nondim", "press_to_nondim", "pow_to_nondim")
     if not deck.non_dimensionalize:
         return dict.fromkeys(names, 1.0)
     L, R, V = deck.reference_length, deck.reference_density, deck.reference_velocity
     t_ref = L / V
     press_ref = R * (V * V)
+    pow_ref = R * (V * V) / t_ref
     return {"len_to_nondim": 1.0 / L, "t_to_nondim": 1.0 / t_ref, "density_to_nondim": 1.0 / R,
-            "density_to_dim": R, "vel_to_nondim": 1.0 / V, "press_to_nondim": 1.0 / press_ref}
+            "density_to_dim": R, "vel_to_nondim": 1.0 / V, "press_to_nondim": 1.0 / press_ref,
+            "pow_to_nondim": 1.0 / pow_ref}
 
 
 def t_to_nondim(deck: Deck) -> float:
@@ -301,11 +341,48 @@ def read_bc_pressure_table(deck: Deck, base_dir: str = "."):
     time [s], pressure [barye], density [g/cc] (list-directed, reading stops at the first row
     that does not parse); scaled to time x t_to_nondim, pressure x press_to_nondim x
     bc_pressure_scale_factor and density x density_to_nondim x bc_pressure_scale_factor."""
-    path = deck.bc_pressure_input_file
-    if not os.path.isabs(path):
-        path = os.path.join(base_dir, path)
+    a = _read_table3(deck.bc_pressure_input_file, base_dir, "Pressure input file")
+    f = nondim_factors(deck)
+    scale = deck.bc_pressure_scale_factor
+    return (a[:, 0] * f["t_to_nondim"], (a[:, 1] * f["press_to_nondim"]) * scale,
+            (a[:, 2] * f["density_to_nondim"]) * scale)
+
+
+def energy_source(deck: Deck, base_dir: str = "."):
+    """The deck's energy source term as an EnergySource (new_source, mod_source.f90:63-125:
+    positions x len_to_nondim; read_input_file :127-258: time x t_to_nondim, value x
+    pow_to_nondim, critical density x density_to_nondim; the constant value is used as given);
+    None when source terms are off."""
+    from .config import EnergySource, SOURCE_GEOMETRY_IDS
+
+    if not deck.enable_source_terms:
+        return None
+    if deck.source_term_type != "energy":
+        raise DeckError(f"source_term_type {deck.source_term_type!r} is not supported ('energy')")
+    if deck.source_geometry not in SOURCE_GEOMETRY_IDS:
+        raise DeckError("Unsupported geometry type, must be one of ['uniform', 'constant_xy', "
+                        "'1d_gaussian']")
+    f = nondim_factors(deck)
+    L = f["len_to_nondim"]
+    table = None
+    if not deck.apply_constant_source:
+        a = _read_table3(deck.source_file, base_dir, "source input file")
+        table = (a[:, 0] * f["t_to_nondim"], a[:, 1] * f["pow_to_nondim"],
+                 a[:, 2] * f["density_to_nondim"])
+    return EnergySource(
+        geometry=deck.source_geometry, constant_value=deck.constant_source_value,
+        multiplier=deck.source_scale_factor, xlo=deck.source_xlo * L, xhi=deck.source_xhi * L,
+        ylo=deck.source_ylo * L, yhi=deck.source_yhi * L,
+        fwhm_x=deck.source_gaussian_fwhm_x * L, fwhm_y=deck.source_gaussian_fwhm_y * L,
+        gaussian_order=deck.source_gaussian_order, table=table)
+
+
+def _read_table3(name: str, base_dir: str, what: str) -> np.ndarray:
+    """Rows of three reals after an optional '#' header line, list-directed: reading stops at
+    the first row that does not parse (read_pressure_input / read_input_file)."""
+    path = name if os.path.isabs(name) else os.path.join(base_dir, name)
     if not os.path.exists(path):
-        raise DeckError(f"Pressure input file '{path}' not found")
+        raise DeckError(f"{what} '{path}' not found")
     rows = []
     with open(path) as fh:
         lines = fh.read().splitlines()
@@ -323,12 +400,8 @@ def read_bc_pressure_table(deck: Deck, base_dir: str = "."):
             break
         rows.append(row)
     if len(rows) < 2:
-        raise DeckError(f"{path}: the pressure input table needs at least two rows")
-    a = np.array(rows, dtype=np.float64)
-    f = nondim_factors(deck)
-    scale = deck.bc_pressure_scale_factor
-    return (a[:, 0] * f["t_to_nondim"], (a[:, 1] * f["press_to_nondim"]) * scale,
-            (a[:, 2] * f["density_to_nondim"]) * scale)
+        raise DeckError(f"{path}: the table needs at least two rows")
+    return np.array(rows, dtype=np.float64)
 
 
 def main_loop(deck: Deck, fluid, step, results_dir: str | None = None) -> int:
@@ -393,6 +466,16 @@ def run_deck(deck: Deck, precision: str = "fp64", prims=None, grid=None, base_di
         ic.apply_grid(fluid)
     if "pressure_input" in deck.bc.values() and not deck.apply_constant_bc_pressure:
         fluid.set_bc_table(*read_bc_pressure_table(deck, base_dir))
+    src = energy_source(deck, base_dir)
+    if src is not None:
+        # the source's cell centroids need the node coordinates of the grid
+        if ic is not None:
+            if ic.uniform is not None:
+                fluid.set_rectilinear(ic.x_nodes, ic.y_nodes)
+        elif grid is None and not deck.read_from_file:
+            fluid.set_rectilinear(deck.xmin + np.arange(cfg.ni + 1) * cfg.dx,
+                                  deck.ymin + np.arange(cfg.nj + 1) * cfg.dy)
+        fluid.set_energy_source(src)
     fluid.initialize(*prims)
     if results_dir is None and not deck.use_constant_delta_t and not deck.initial_delta_t > 0.0:
         steps = fluid.run(deck.max_time * t_to_nondim(deck), deck.max_iterations)

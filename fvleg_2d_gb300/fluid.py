@@ -107,6 +107,28 @@ class _Handle:
         self.bc_table = tuple(arrs)
         return self
 
+    def set_energy_source(self, source=None):
+        """The energy source term (an EnergySource; None turns it off).  Its field is
+        recomputed at every step start and added to the energy equation at every stage."""
+        if source is None:
+            _check(self.L.cato_gpu_set_energy_source(self.h, None, 0, None, None, None), self.h,
+                   "set_energy_source")
+            self.source = None
+            return self
+        c = source.to_c()
+        if source.table is None:
+            arrs, n = [None] * 3, 0
+        else:
+            arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in source.table]
+            n = arrs[0].shape[0]
+            if any(a.shape != (n,) for a in arrs):
+                raise ValueError("the source table needs three 1-D arrays of one length")
+        _check(self.L.cato_gpu_set_energy_source(
+            self.h, ctypes.byref(c), n, *(None if a is None else _lib.ptr(a) for a in arrs)),
+            self.h, "set_energy_source")
+        self.source = source
+        return self
+
     def set_time(self, time: float, iteration: int) -> None:
         """fluid_t%set_time (mod_fluid.f90:400-409); also the time at which a FluxSolver
         evaluates a tabulated pressure-input target."""

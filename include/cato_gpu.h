@@ -163,6 +163,35 @@ int cato_gpu_upload_primitive(cato_handle* h, const double* rho, const double* u
  * returns to the uniform grid.  The state must be uploaded (again) afterwards. */
 int cato_gpu_set_rectilinear(cato_handle* h, const double* x_nodes, const double* y_nodes);
 
+/* Energy source term ([source_terms], source_t of src/lib/source_terms/mod_source.f90:63-425):
+ * q_dot_h added to the energy equation's right-hand side at every stage (time_derivative,
+ * mod_fluid.f90:503), recomputed once per step from the step-start time and density
+ * (source_t%integrate, :296-312). */
+enum cato_source_geometry {
+  CATO_SRC_UNIFORM = 0,     /* 'uniform' */
+  CATO_SRC_CONSTANT_XY = 1, /* 'constant_xy' (the reference tests centroid_x > ylo) */
+  CATO_SRC_GAUSSIAN_1D = 2, /* '1d_gaussian', constant in y, centred on the deposition column */
+  CATO_SRC_DECAY = 3        /* 'decay' */
+};
+
+typedef struct cato_energy_source {
+  int32_t geometry;        /* enum cato_source_geometry */
+  int32_t gaussian_order;  /* source_gaussian_order (1d_gaussian) */
+  double constant_value;   /* constant_source_value (apply_constant_source; used unscaled) */
+  double multiplier;       /* source_scale_factor */
+  double xlo, xhi, ylo, yhi;  /* constant_xy box, x len_to_nondim */
+  double fwhm_x, fwhm_y;      /* 1d_gaussian widths, x len_to_nondim */
+} cato_energy_source;
+
+/* Turn the energy source on (src != NULL) or off.  n = 0: the constant value; n >= 2: the
+ * table of read_input_file (mod_source.f90:127-258), already scaled: time x t_to_nondim,
+ * value x pow_to_nondim, critical density x density_to_nondim (strictly increasing times).
+ * Cell centroids come from the rectilinear nodes (cato_gpu_set_rectilinear), else from a
+ * uniform grid with its first node at 0. */
+int cato_gpu_set_energy_source(cato_handle* h, const cato_energy_source* src, int32_t n,
+                               const double* time, const double* value,
+                               const double* critical_density);
+
 /* Target of a CATO_BC_PRESSURE_INPUT side as a table in time: n >= 2 points (time strictly
  * increasing), pressure and density already scaled as read_pressure_input does
  * (pressure_input_bc.f90:92-181: time x t_to_nondim, pressure x press_to_nondim x

@@ -306,6 +306,27 @@ static double pow_cr(double x, double y) {
 
 double oracle_pow(int mode, double x, double y) { return mode ? pow_cr(x, y) : pow(x, y); }
 
+static double exp_cr(double x) {
+  if (!isfinite(x) || x > 709.0 || x < -745.0) return exp(x);
+  if (x == 0.0) return 1.0;
+  ddo_t a = {x, 0.0};
+  ddo_t e = ddo_exp(a);
+  return e.hi + e.lo;
+}
+
+static double bc_exp(double x) { return g_pow_mode ? exp_cr(x) : exp(x); }
+
+/* x**n for a variable integer n (gfortran calls libgcc's __powidf2: square and multiply) */
+static double powi(double x, int m) {
+  unsigned n = m < 0 ? -(unsigned)m : (unsigned)m;
+  double y = (n % 2) ? x : 1.0;
+  while (n >>= 1) {
+    x = x * x;
+    if (n % 2) y = y * x;
+  }
+  return m < 0 ? 1.0 / y : y;
+}
+
 static double bc_pow(double x, double y) { return g_pow_mode ? pow_cr(x, y) : pow(x, y); }
 
 /* subsonic_inlet, inlet_outlet.f90:60-165, for the +x normal (1, 0), flow angle 0 */
@@ -1235,6 +1256,15 @@ struct oracle_fluid {
    * assign_fluid mod_fluid.f90:706) */
   double* pbc_tab;
   int pbc_n;
+  /* energy source term (mod_source.f90): configuration, table (time, value, critical
+   * density), the grid nodes for the centroids, and q_dot_h of the current step */
+  int src_on;
+  cato_energy_source src;
+  double* src_tab;
+  int src_n;
+  double* xn;
+  double* yn;
+  double* srcq;
   double solver_time;
   double bc_time;    /* boundary time of the residual being evaluated */
   /* conserved (U) and derived (u, v, p, cs) of the current state */
@@ -1248,6 +1278,8 @@ struct oracle_fluid {
   double conv[4];   /* calculate_convergence of the last step */
   int conv_valid;
 };
+
+static void source_field(oracle_fluid* f);
 
 static double* falloc(dims_t d) { return (double*)calloc(nfield(d), sizeof(double)); }
 
@@ -1274,6 +1306,10 @@ void oracle_destroy(oracle_fluid* f) {
   for (int k = 0; k < 4; ++k) { free(f->sp[k]); free(f->L[k]); }
   free(f->cells);
   free(f->pbc_tab);
+  free(f->src_tab);
+  free(f->xn);
+  free(f->yn);
+  free(f->srcq);
   free(f);
 }
 
@@ -1417,8 +1453,15 @@ static int residual(oracle_fluid* f, const double* pr, const double* pu, const d
   memcpy(f->sp[3], pp, n);
   pbc_ctx_t pc = {f->pbc_n, f->pbc_tab, f->pbc_tab ? f->pbc_tab + f->pbc_n : NULL,
                   f->pbc_tab ? f->pbc_tab + 2 * f->pbc_n : NULL, f->bc_time};
-  return solve_geo(&f->c, f->cells, &pc, f->sp[0], f->sp[1], f->sp[2], f->sp[3], f->L[0],
-                   f->L[1], f->L[2], f->L[3]);
+  int rc = solve_geo(&f->c, f->cells, &pc, f->sp[0], f->sp[1], f->sp[2], f->sp[3], f->L[0],
+                     f->L[1], f->L[2], f->L[3]);
+  /* time_derivative (mod_fluid.f90:503): the source joins the energy equation */
+  const dims_t d = f->d;
+  if (f->src_on)
+    for (int j = 1; j <= f->d.nj; ++j)
+      for (int i = 1; i <= f->d.ni; ++i)
+        AT(f->L[3], i, j) = AT(f->L[3], i, j) + f->srcq[(size_t)(j - 1) * f->d.ni + (i - 1)];
+  return rc;
 }
 
 /* out = A + L*c with the field '+' flush (fluid operators mod_fluid.f90:609-669) */
@@ -1504,7 +1547,113 @@ int oracle_set_rectilinear(oracle_fluid* f, const double* x_nodes, const double*
   }
   free(f->cells);
   f->cells = cells;
+  free(f->xn);
+  free(f->yn);
+  f->xn = f->yn = NULL;
+  if (x_nodes) {
+    f->xn = (double*)malloc(sizeof(double) * (f->d.ni + 1));
+    f->yn = (double*)malloc(sizeof(double) * (f->d.nj + 1));
+    memcpy(f->xn, x_nodes, sizeof(double) * (f->d.ni + 1));
+    memcpy(f->yn, y_nodes, sizeof(double) * (f->d.nj + 1));
+  }
   return CATO_OK;
+}
+
+/* energy source term: src NULL turns it off; n = 0 constant value, else the scaled table */
+int oracle_set_energy_source(oracle_fluid* f, const cato_energy_source* src, int32_t n,
+                             const double* t, const double* v, const double* crit) {
+  free(f->src_tab);
+  f->src_tab = NULL;
+  f->src_on = 0;
+  if (!src) return 0;
+  if (n == 1 || n < 0) return CATO_ERR_ARG;
+  for (int k = 1; k < n; ++k)
+    if (!(t[k] > t[k - 1])) return CATO_ERR_ARG;
+  if (n > 0) {
+    f->src_tab = (double*)malloc(sizeof(double) * 3 * (size_t)n);
+    memcpy(f->src_tab, t, sizeof(double) * n);
+    memcpy(f->src_tab + n, v, sizeof(double) * n);
+    memcpy(f->src_tab + 2 * n, crit, sizeof(double) * n);
+  }
+  if (!f->srcq) f->srcq = (double*)calloc((size_t)f->d.ni * f->d.nj, sizeof(double));
+  f->src = *src;
+  f->src_n = n;
+  f->src_on = 1;
+  return 0;
+}
+
+/* The source field of a step starting now (f->time, f->rho): ni x nj values, i fastest. */
+int oracle_source_field(oracle_fluid* f, double* out) {
+  if (!f->src_on) return CATO_ERR_STATE;
+  source_field(f);
+  memcpy(out, f->srcq, sizeof(double) * (size_t)f->d.ni * f->d.nj);
+  return 0;
+}
+
+/* quad_cell_t centroid (quad_cell.f90:145) of column i / row j (1-based) */
+static double cen_x(const oracle_fluid* f, int i) {
+  double x1 = f->xn ? f->xn[i - 1] : (double)(i - 1) * f->c.dx;
+  double x2 = f->xn ? f->xn[i] : (double)i * f->c.dx;
+  return (x2 + x1) / 2.0;
+}
+static double cen_y(const oracle_fluid* f, int j) {
+  double y2 = f->yn ? f->yn[j - 1] : (double)(j - 1) * f->c.dy;
+  double y3 = f->yn ? f->yn[j] : (double)j * f->c.dy;
+  return (y3 + y2) / 2.0;
+}
+
+/* source_t%integrate (mod_source.f90:296-312) at the step start: find_deposition_location
+ * (:314-353) and get_source_field (:355-425) into f->srcq */
+static void source_field(oracle_fluid* f) {
+  const dims_t d = f->d;
+  const cato_energy_source* s = &f->src;
+  const int n = f->src_n;
+  const double t = f->time;
+  /* the critical-density interpolator is only initialised from a table; uninitialised it
+   * returns zero */
+  double crit = n > 0 ? interp_1d(n, f->src_tab, f->src_tab + 2 * n, t) : 0.0;
+  double x_center = 0.0;
+  for (int i = d.ni; i >= 1; --i) {
+    int any = 0;
+    for (int j = 1; j <= d.nj; ++j) any |= AT(f->rho, i, j) > crit;
+    if (any) {
+      x_center = cen_x(f, i);
+      break;
+    }
+  }
+  double p_input;
+  if (n == 0) {
+    p_input = s->constant_value;
+  } else {
+    double tmax = f->src_tab[0];
+    for (int k = 1; k < n; ++k) tmax = dmax(tmax, f->src_tab[k]);
+    p_input = t <= tmax ? interp_1d(n, f->src_tab, f->src_tab + n, t) : 0.0;
+  }
+  p_input = p_input * s->multiplier;
+  const double x0 = x_center;
+  for (int j = 1; j <= d.nj; ++j)
+    for (int i = 1; i <= d.ni; ++i) {
+      double q = 0.0;
+      if (fabs(p_input) > 0.0) {
+        double x = cen_x(f, i), y = cen_y(f, j);
+        switch (s->geometry) {
+          case CATO_SRC_UNIFORM: q = p_input; break;
+          case CATO_SRC_CONSTANT_XY:
+            if (x < s->xhi && x > s->xlo && y < s->yhi && x > s->ylo) q = p_input;
+            break;
+          case CATO_SRC_GAUSSIAN_1D:
+            if (fabs(x - x0) < s->fwhm_x * 5) {
+              double a = ((x - x0) * (x - x0)) / (2 * (s->fwhm_x * s->fwhm_x));
+              q = p_input * bc_exp(-powi(a, s->gaussian_order));
+            }
+            break;
+          default: /* decay */
+            if (x < x0) q = p_input * bc_exp(-bc_pow(x / x0, 1.5)) / bc_exp(-1.0);
+            else q = p_input * bc_exp(-1e4 * (((x - x0) / x0) * ((x - x0) / x0)));
+        }
+      }
+      f->srcq[(size_t)(j - 1) * d.ni + (i - 1)] = q;
+    }
 }
 
 /* stage primitives (u, v, p, cs reused from the scratch solver arrays' neighbours) */
@@ -1526,6 +1675,7 @@ int oracle_integrate(oracle_fluid* f, double dt, int32_t* error_code) {
   /* boundary times: U%t advances the persistent fluid's solver clock; the stage copies U_1, U_2
    * (assigned from expressions led by U) restart theirs at U%time before adding dt */
   const double t_copy = f->time + dt;
+  if (f->src_on) source_field(f); /* once per step, before the stages */
   if (f->c.rk == CATO_RK_SSP2) {
     double* U1[4] = {f->st[0][0], f->st[0][1], f->st[0][2], f->st[0][3]};
     double* U2[4] = {f->st[1][0], f->st[1][1], f->st[1][2], f->st[1][3]};

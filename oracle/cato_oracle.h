@@ -64,6 +64,9 @@ int oracle_set_rectilinear(oracle_fluid* f, const double* x_nodes, const double*
 int oracle_set_time(oracle_fluid* f, double time, int64_t iteration);
 /* powers of the pressure-input inlet: 0 = libm pow (as the reference), 1 = correctly rounded */
 int oracle_set_pow_mode(int mode);
+int oracle_set_energy_source(oracle_fluid* f, const cato_energy_source* src, int32_t n,
+                             const double* t, const double* v, const double* crit);
+int oracle_source_field(oracle_fluid* f, double* out);
 double oracle_pow(int mode, double x, double y);
 int oracle_set_bc_table(oracle_fluid* f, int32_t n, const double* t, const double* p,
                         const double* rho);

@@ -53,6 +53,9 @@ def lib():
         L.oracle_set_rectilinear.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.oracle_set_time.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int64]
         L.oracle_set_pow_mode.argtypes = [ctypes.c_int]
+        L.oracle_set_energy_source.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                               _dp, _dp, _dp]
+        L.oracle_source_field.argtypes = [ctypes.c_void_p, _dp]
         L.oracle_pow.restype = ctypes.c_double
         L.oracle_pow.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double]
         L.oracle_set_bc_table.argtypes = [ctypes.c_void_p, ctypes.c_int32, _dp, _dp, _dp]
@@ -204,12 +207,36 @@ class OracleFluid:
     def set_time(self, time: float, iteration: int) -> None:
         lib().oracle_set_time(self._h, float(time), int(iteration))
 
+    def set_energy_source(self, source=None) -> None:
+        """An EnergySource (fvleg_2d_gb300.config) or None."""
+        if source is None:
+            lib().oracle_set_energy_source(self._h, None, 0, None, None, None)
+            return
+        self._src_c = source.to_c()
+        if source.table is None:
+            self._src_tab, n, ptrs = None, 0, [None] * 3
+        else:
+            self._src_tab = [np.ascontiguousarray(a, dtype=np.float64) for a in source.table]
+            n = len(self._src_tab[0])
+            ptrs = [a.ctypes.data_as(_dp) for a in self._src_tab]
+        rc = lib().oracle_set_energy_source(self._h, ctypes.byref(self._src_c), n, *ptrs)
+        if rc:
+            raise ValueError(f"oracle_set_energy_source: {rc}")
+
     def set_bc_table(self, time, pressure, density) -> None:
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (time, pressure, density)]
         rc = lib().oracle_set_bc_table(self._h, len(arrs[0]),
                                        *(a.ctypes.data_as(_dp) for a in arrs))
         if rc:
             raise ValueError(f"oracle_set_bc_table: {rc}")
+
+    def source_field(self) -> np.ndarray:
+        """q_dot_h for a step starting now, (ni, nj)."""
+        out = np.zeros((self.cfg.ni, self.cfg.nj), order="F")
+        rc = lib().oracle_source_field(self._h, _ptr(out))
+        if rc:
+            raise RuntimeError(f"oracle_source_field: {rc}")
+        return out
 
     def set_primitive(self, rho, u, v, p) -> None:
         arrs = [np.asfortranarray(a, dtype=np.float64) for a in (rho, u, v, p)]
