@@ -119,11 +119,12 @@ __global__ void __launch_bounds__(256, batch_min_blocks<R>())
     batch_stage_args<R>(d, B, A);
     A.rows_per_cta = w.w;
     if constexpr (Prec<R>::kind == 0)
-      stage_tile<R, NG, FLUX, RECON>(A, d->K64, w.y, w.z, smem_raw);
+      stage_tile<R, NG, FLUX, RECON, true>(A, d->K64, w.y, w.z, smem_raw);
     else if constexpr (Prec<R>::kind == 1)
-      stage_tile<R, NG, FLUX, RECON>(A, d->K32, w.y, w.z, smem_raw);
+      // no rectilinear grid, source or pressure input in a batch: the lean FP32 kernel
+      stage_tile<R, NG, FLUX, RECON, false>(A, d->K32, w.y, w.z, smem_raw);
     else
-      stage_tile<R, NG, FLUX, RECON>(A, d->Kdf, w.y, w.z, smem_raw);
+      stage_tile<R, NG, FLUX, RECON, true>(A, d->Kdf, w.y, w.z, smem_raw);
   }
 }
 

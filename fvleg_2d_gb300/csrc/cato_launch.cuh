@@ -11,21 +11,38 @@
 namespace cato {
 
 
-template <typename R, int NG, int FLUX, int RECON>
-cudaError_t launch_stage_one(dim3 grid, int threads, cudaStream_t stream, const StageArgs& A,
+template <typename R, int NG, int FLUX, int RECON, bool EXT>
+cudaError_t launch_stage_ext(dim3 grid, int threads, cudaStream_t stream, const StageArgs& A,
                              const FluxConsts<R>& K) {
   static std::atomic<bool> attr_done{false};
   const size_t smem = stage_smem_bytes<R>(threads, NG);
   if (!attr_done.load(std::memory_order_acquire)) {
-    cudaError_t e = cudaFuncSetAttribute(stage_kernel<R, NG, FLUX, RECON>,
+    cudaError_t e = cudaFuncSetAttribute(stage_kernel<R, NG, FLUX, RECON, EXT>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)stage_smem_bytes<R>(256, 3));
     if (e != cudaSuccess) return e;
     attr_done.store(true, std::memory_order_release);
   }
   if (grid.x == 0 || grid.y == 0) return cudaSuccess;  // attribute warm-up only
-  stage_kernel<R, NG, FLUX, RECON><<<grid, threads, smem, stream>>>(A, K);
+  stage_kernel<R, NG, FLUX, RECON, EXT><<<grid, threads, smem, stream>>>(A, K);
   return cudaGetLastError();
+}
+
+// The FP32 path has a lean variant without the rectilinear, source and pressure-input code
+// (it is issue-bound: those checks cost ~3 %); FP64 and double-float keep one kernel.
+template <typename R, int NG, int FLUX, int RECON>
+cudaError_t launch_stage_one(dim3 grid, int threads, cudaStream_t stream, const StageArgs& A,
+                             const FluxConsts<R>& K) {
+  if constexpr (Prec<R>::kind == 1) {
+    if (grid.x == 0 || grid.y == 0) {  // warm-up: both variants
+      cudaError_t e = launch_stage_ext<R, NG, FLUX, RECON, false>(grid, threads, stream, A, K);
+      if (e != cudaSuccess) return e;
+      return launch_stage_ext<R, NG, FLUX, RECON, true>(grid, threads, stream, A, K);
+    }
+    if (!stage_needs_ext(A))
+      return launch_stage_ext<R, NG, FLUX, RECON, false>(grid, threads, stream, A, K);
+  }
+  return launch_stage_ext<R, NG, FLUX, RECON, true>(grid, threads, stream, A, K);
 }
 
 // recon: 0 = TVD2 (minmod / superbee / van Leer), 3 = MLP3, 5 = MLP5

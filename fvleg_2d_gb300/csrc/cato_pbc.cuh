@@ -248,7 +248,7 @@ __device__ __forceinline__ double prim_p_double(const StageArgs& A, int sx, int 
   load_src<R>(A, sx, row, s);
   R v[4];
   const R g = R(A.gamma), g1 = R(A.gamma - 1.0);
-  src_to_prim<R>(A, s, false, 0, g, g1, v);
+  src_to_prim<R>(A, s, false, 0, row, g, g1, v);
 #pragma unroll
   for (int k = 0; k < 4; ++k) q[k] = to_double(v[k]);
   return q[3];

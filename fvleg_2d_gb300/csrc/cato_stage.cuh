@@ -207,18 +207,15 @@ template <typename R> struct RowSrc;
 template <> struct RowSrc<double> {
   double c[4];  // conserved (or raw primitives) as loaded
   bool flipy;
-  int row;      // the (possibly ghost) row this sample stands for
 };
 template <> struct RowSrc<float> {
   float4 c;     // FP32 copy of U^n (or the raw primitives)
   float4 d;     // delta_k
   bool flipy;
-  int row;
 };
 template <> struct RowSrc<df> {
   double c[4];  // conserved state of the stage (or the raw primitives)
   bool flipy;
-  int row;
 };
 
 template <typename R>
@@ -226,7 +223,6 @@ __device__ __forceinline__ void load_src(const StageArgs& A, int sx, int row, Ro
   bool fy;
   const int sy = map_index(row, A.nj, A.bc[SIDE_MY], A.bc[SIDE_PY], fy);
   s.flipy = fy;
-  s.row = row;
   const size_t idx = (size_t)sy * A.pitch + sx;
   if constexpr (Prec<R>::kind != 1) {
     const double* const* src = A.Pin[0] ? A.Pin : A.Uk;
@@ -248,12 +244,13 @@ template <> __device__ __forceinline__ double from_double<double>(double x) { re
 template <> __device__ __forceinline__ float from_double<float>(double x) { return d2f_int(x); }
 template <> __device__ __forceinline__ df from_double<df>(double x) { return to_df(x); }
 
-// xmode: 0 interior / mapped ghost, 1 +x outlet ghost column, 2 +x pressure-input ghost column
+// xmode: 0 interior / mapped ghost, 1 +x outlet ghost column, 2 +x pressure-input ghost column;
+// row: the (possibly ghost) row of the sample
 template <typename R>
 __device__ __forceinline__ void src_to_prim(const StageArgs& A, const RowSrc<R>& s, bool flipx,
-                                            int xmode, R g, R g1, R out[4]) {
+                                            int xmode, int row, R g, R g1, R out[4]) {
   if (xmode == 2) {  // lowest-priority BC: the row's edge state replaces the mapped value
-    const double* e = A.pbc_edge + 3 * (size_t)(s.row + A.pbc_ng);
+    const double* e = A.pbc_edge + 3 * (size_t)(row + A.pbc_ng);
     out[0] = from_double<R>(e[0]);
     out[1] = from_double<R>(e[1]);
     out[2] = R(0);
@@ -303,7 +300,9 @@ __device__ __forceinline__ float f4get(const float4& v, int k) {
 // the kernel
 // ---------------------------------------------------------------------------------------------
 // One tile: columns [bx*W, bx*W + W) x rows [by*rows_per_cta, ...) of one instance.
-template <typename R, int NG, int FLUX, int RECON>
+// EXT = false compiles out the rectilinear metrics, the energy source and the pressure-input
+// ghost columns (a uniform grid without them); the issue-bound FP32 path uses it whenever it can.
+template <typename R, int NG, int FLUX, int RECON, bool EXT = true>
 __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<R>& K, int bx,
                                            int by, unsigned char* smem_raw) {
   constexpr int RING = 2 * NG;
@@ -321,8 +320,9 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
   const int sx = map_index(min(gx, A.ni + NG - 1), A.ni, A.bc[SIDE_MX], A.bc[SIDE_PX], flipx);
   // +x outlet / pressure-input ghost columns get the boundary state (lowest-priority BCs)
   const int xmode = gx < A.ni ? 0
-                    : (A.bc[SIDE_PX] == BC_OUTLET ? 1
-                                                  : (A.bc[SIDE_PX] == BC_PRESSURE_INPUT ? 2 : 0));
+                    : (A.bc[SIDE_PX] == BC_OUTLET
+                           ? 1
+                           : (EXT && A.bc[SIDE_PX] == BC_PRESSURE_INPUT ? 2 : 0));
   const bool in_i_edge = (t >= NG - 1) && (t <= NG + W - 1) && (gx <= A.ni - 1);
   const bool in_cell = (t >= NG) && (t <= NG + W - 1) && (gx < A.ni);
   const double dt = *A.dt;
@@ -337,14 +337,16 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
   }
   // FP32 reciprocal cell width of this thread's column (mixed path)
   [[maybe_unused]] const float idx_col =
-      A.G.rdxf ? A.G.rdxf[min(max(gx, 0), A.ni - 1)] : (float)(1.0 / A.G.dx);
+      (EXT && A.G.rdxf) ? A.G.rdxf[min(max(gx, 0), A.ni - 1)] : (float)(1.0 / A.G.dx);
+  // FP32 reciprocal row height of a uniform grid (one FP64 division per thread, not per row)
+  [[maybe_unused]] const float idy_uni = (float)(1.0 / A.G.dy);
 
   // prologue: rows y0-NG .. y0+NG-1
   for (int r = y0 - NG; r < y0 + NG; ++r) {
     RowSrc<R> s;
     load_src<R>(A, sx, r, s);
     R q[4];
-    src_to_prim<R>(A, s, flipx, xmode, g, g1, q);
+    src_to_prim<R>(A, s, flipx, xmode, r, g, g1, q);
     R* row = ring + slot_of<RING>(r) * 4 * T;
 #pragma unroll
     for (int k = 0; k < 4; ++k) row[k * T + t] = q[k];
@@ -389,7 +391,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
     if (j + 1 < y1) load_src<R>(A, sx, j + 1 + NG, nxt);
     {
       R q[4];
-      src_to_prim<R>(A, pre, flipx, xmode, g, g1, q);
+      src_to_prim<R>(A, pre, flipx, xmode, j + NG, g, g1, q);
       R* row = ring + slot_of<RING>(j + NG) * 4 * T;
 #pragma unroll
       for (int k = 0; k < 4; ++k) row[k * T + t] = q[k];
@@ -447,7 +449,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
       } else {
         const float ccf = (float)cc, bf = (float)A.b;
         const float idx_f = idx_col;
-        const float idy_f = A.G.rdyf ? A.G.rdyf[j] : (float)(1.0 / A.G.dy);
+        const float idy_f = (EXT && A.G.rdyf) ? A.G.rdyf[j] : idy_uni;
         float dn[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -455,7 +457,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
           float Fj = sfj[((j & 1) * 4 + k) * T + t];
           float Fjm = sfj[(((j - 1) & 1) * 4 + k) * T + t];
           float L = -((Fi - Fim) * idx_f + (Fj - Fjm) * idy_f);
-          if (k == 3 && A.src_q) L = L + d2f_int(A.src_q[cidx]);
+          if (EXT && k == 3 && A.src_q) L = L + d2f_int(A.src_q[cidx]);
           dn[k] = bf * f4get(dkc, k) + L * ccf;
         }
         if (A.last) {
@@ -496,8 +498,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
           prim_from_cons((float)A.gamma, (float)(A.gamma - 1.0), uf.x, uf.y, uf.z, uf.w, u, v,
                          p, cs);
           float d = (float)A.cfl / ((fabsf(u) + cs) * idx_col +
-                                    (fabsf(v) + cs) * (A.G.rdyf ? A.G.rdyf[j]
-                                                                : (float)(1.0 / A.G.dy)));
+                                    (fabsf(v) + cs) * ((EXT && A.G.rdyf) ? A.G.rdyf[j] : idy_uni));
           double dd = f2d_int(d);
           if (__double_as_longlong(dd) < __double_as_longlong(dt_loc) && d > 0.0f) dt_loc = dd;
           if (isnan(uf.x) || isnan(u) || isnan(v) || isnan(p)) st_loc |= ST_NAN;
@@ -550,12 +551,17 @@ template <typename R> constexpr int batch_min_blocks() {
                             : (Prec<R>::kind == 1 ? CATO_F32_BATCH_MIN_BLOCKS : CATO_F64_MIN_BLOCKS);
 }
 
-template <typename R, int NG, int FLUX, int RECON>
+template <typename R, int NG, int FLUX, int RECON, bool EXT>
 __global__ void __launch_bounds__(256, min_blocks<R>())
     stage_kernel(const StageArgs A, const FluxConsts<R> K) {
   if (A.active && *A.active == 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_tile<R, NG, FLUX, RECON>(A, K, blockIdx.x, blockIdx.y, smem_raw);
+  stage_tile<R, NG, FLUX, RECON, EXT>(A, K, blockIdx.x, blockIdx.y, smem_raw);
+}
+
+// whether a stage needs the EXT kernel (rectilinear grid, energy source, pressure input)
+inline bool stage_needs_ext(const StageArgs& A) {
+  return A.G.dxc != nullptr || A.src_q != nullptr || A.bc[SIDE_PX] == BC_PRESSURE_INPUT;
 }
 
 // dynamic shared memory of one CTA
