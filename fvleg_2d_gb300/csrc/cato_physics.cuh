@@ -117,6 +117,24 @@ __device__ __forceinline__ bool abs_lt(float x, float c) { return fabsf(x) < c; 
 __device__ __forceinline__ bool abs_lt(df x, df c) { return df_abs(x) < c; }
 
 // ---------------------------------------------------------------------------------------------
+// abs_lt(x / cs, 1e-13) with x / cs rounded, as the Mach filter of calculate_derived_quantities
+// (mod_fluid.f90:579-588; x below tiny counts as a zero Mach number).  The quotient is only
+// formed when the exponents leave the answer open: for normal x and cs with biased exponents
+// Ex, Ec, |x / cs| lies in (2^(Ex-Ec-1), 2^(Ex-Ec+1)), and 1e-13 lies in [2^-44, 2^-43), so
+// Ex - Ec >= -42 puts the rounded quotient at or above 2^-43 (not below 1e-13) and Ex - Ec <= -46
+// puts it at or below 2^-45 (below).  The division runs on the FP64 pipe, the test on the
+// integer pipe.
+__device__ __forceinline__ bool mach_below_1e13(double x, double cs) {
+  if (abs_lt(x, Num<double>::tiny)) return true;
+  const int ex = (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffULL);
+  const int ec = (int)(((unsigned long long)__double_as_longlong(cs) >> 52) & 0x7ffULL);
+  if (ex >= 1 && ex <= 2046 && ec >= 1 && ec <= 2046) {
+    if (ex - ec >= -42) return false;
+    if (ex - ec <= -46) return true;
+  }
+  return abs_lt(x / cs, 1e-13);
+}
+
 // FP64 <-> FP32 conversion on the integer pipe (GB300's F2F shares the narrow FP64 pipe).
 // d2f: round-to-nearest-even, values below FLT_MIN flush to signed zero, NaN stays NaN.
 // ---------------------------------------------------------------------------------------------
@@ -175,10 +193,9 @@ __device__ __forceinline__ void prim_from_cons(double g, double g1, double r, do
   p = (r * g1) * dd;
   double pr = abs_lt(p, TINY) ? 0.0 : p / r;
   cs = ::sqrt(pr * g);
-  double mu = abs_lt(u, TINY) ? 0.0 : u / cs;
-  double mv = abs_lt(v, TINY) ? 0.0 : v / cs;
-  if (abs_lt(mv, 1e-13)) v = 0.0;
-  if (abs_lt(mu, 1e-13)) u = 0.0;
+  // mach_u = u / cs, mach_v = v / cs, then |mach| < 1e-13 zeroes the velocity
+  if (mach_below_1e13(u, cs)) u = 0.0;  // each test reads only its own component and cs
+  if (mach_below_1e13(v, cs)) v = 0.0;
 }
 
 // FP32 (mixed path): same quantities with one reciprocal of rho; Mach filter as |u| < 1e-13 cs.
