@@ -239,6 +239,22 @@ __device__ __forceinline__ R tvd_phi(int lim, R r) {
   return Num<R>::div(r + rabs(r), R(1) + rabs(r));
 }
 
+// phi(num / den).  Every limiter gives +0 for r < 0, and FP64 knows r < 0 without dividing when
+// num and den are finite, non-zero and of opposite signs (the quotient is then negative, -inf or
+// -0); the sign test runs on the integer pipe.
+template <typename R>
+__device__ __forceinline__ R tvd_phi_of(int lim, R num, R den) {
+  if constexpr (std::is_same<R, double>::value) {
+    const long long bn = __double_as_longlong(num), bd = __double_as_longlong(den);
+    const unsigned long long an = (unsigned long long)bn << 1, ad = (unsigned long long)bd << 1;
+    // non-zero (an, ad != 0), finite (exponent != 0x7ff: shifted < 0xffe0...), signs differ
+    if (an != 0ULL && ad != 0ULL && an < 0xffe0000000000000ULL && ad < 0xffe0000000000000ULL &&
+        ((bn ^ bd) < 0))
+      return R(0);
+  }
+  return tvd_phi(lim, Num<R>::div(num, den));
+}
+
 template <typename R>
 __device__ __forceinline__ void recon_tvd2(int lim, R qm1, R q0, R qp1, R qp2, R& L, R& Rr) {
   const R EPS = Num<R>::eps;
@@ -248,11 +264,9 @@ __device__ __forceinline__ void recon_tvd2(int lim, R qm1, R q0, R qp1, R qp2, R
     if (abs_lt(d0, EPS)) d0 = R(0);
     if (abs_lt(dp, EPS)) dp = R(0);
   }
-  R rL = Num<R>::div(d0, dm + R(1e-16));
-  R rR = Num<R>::div(d0, dp + R(1e-16));
-  R phi = tvd_phi(lim, rL);
+  R phi = tvd_phi_of(lim, d0, dm + R(1e-16));
   L = q0 + R(0.5) * phi * dm;
-  phi = tvd_phi(lim, rR);
+  phi = tvd_phi_of(lim, d0, dp + R(1e-16));
   Rr = qp1 - R(0.5) * phi * dp;
 }
 
