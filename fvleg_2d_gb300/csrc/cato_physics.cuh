@@ -117,6 +117,34 @@ __device__ __forceinline__ bool abs_lt(float x, float c) { return fabsf(x) < c; 
 __device__ __forceinline__ bool abs_lt(df x, df c) { return df_abs(x) < c; }
 
 // ---------------------------------------------------------------------------------------------
+// Several IEEE quotients with one denominator b (Markstein, IBM J. Res. Dev. 34(1), 1990): with
+// y = RN(1/b), q0 = RN(a y) and the exact remainder r = a - b q0 (one FMA), RN(q0 + r y) is
+// RN(a / b).  One division for the reciprocal, then three FP64 operations per quotient instead
+// of a division each.  Used where |a| and |b| lie in [2^-500, 2^500] (no intermediate overflow
+// or underflow, a != 0); elsewhere the plain division.
+__device__ __forceinline__ bool exp_mid(double x) {
+  const unsigned e = (unsigned)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffULL);
+  return e - 523u <= 1000u;
+}
+struct DivBy {
+  double b, y;
+  bool ok;
+};
+__device__ __forceinline__ DivBy div_by_make(double b) {
+  DivBy d;
+  d.b = b;
+  d.ok = exp_mid(b);
+  d.y = d.ok ? 1.0 / b : 0.0;
+  return d;
+}
+__device__ __forceinline__ double div_by(const DivBy& d, double a) {
+  if (d.ok && exp_mid(a)) {
+    const double q0 = a * d.y;
+    return __fma_rn(__fma_rn(-d.b, q0, a), d.y, q0);
+  }
+  return a / d.b;
+}
+
 // abs_lt(x / cs, 1e-13) with x / cs rounded, as the Mach filter of calculate_derived_quantities
 // (mod_fluid.f90:579-588; x below tiny counts as a zero Mach number).  The quotient is only
 // formed when the exponents leave the answer open: for normal x and cs with biased exponents
@@ -182,16 +210,17 @@ __device__ __forceinline__ void prim_from_cons(double g, double g1, double r, do
                                                double rv, double rE, double& u, double& v,
                                                double& p, double& cs) {
   const double EPS = Num<double>::eps, TINY = Num<double>::tiny;
-  u = abs_lt(ru, TINY) ? 0.0 : ru / r;
-  v = abs_lt(rv, TINY) ? 0.0 : rv / r;
-  double e = abs_lt(rE, TINY) ? 0.0 : rE / r;
+  const DivBy by_r = div_by_make(r);  // four quotients by rho
+  u = abs_lt(ru, TINY) ? 0.0 : div_by(by_r, ru);
+  v = abs_lt(rv, TINY) ? 0.0 : div_by(by_r, rv);
+  double e = abs_lt(rE, TINY) ? 0.0 : div_by(by_r, rE);
   double s = u * u + v * v;
   if (abs_lt(s, EPS)) s = 0.0;
   double h = s * 0.5;
   double dd = e - h;
   if (abs_lt(dd, EPS)) dd = 0.0;
   p = (r * g1) * dd;
-  double pr = abs_lt(p, TINY) ? 0.0 : p / r;
+  double pr = abs_lt(p, TINY) ? 0.0 : div_by(by_r, p);
   cs = ::sqrt(pr * g);
   // mach_u = u / cs, mach_v = v / cs, then |mach| < 1e-13 zeroes the velocity
   if (mach_below_1e13(u, cs)) u = 0.0;  // each test reads only its own component and cs
@@ -997,8 +1026,9 @@ inline Geom uniform_geom(double dx, double dy) {
   return G;
 }
 
+// by_vol: the cell volume as a shared denominator (used when inv_vol is 0)
 __device__ __forceinline__ double divergence_fp64(double Fi, double Fim, double Fj, double Fjm,
-                                                  const Geom& G) {
+                                                  const Geom& G, const DivBy& by_vol) {
   const double REL_TOL = 1e-14;
   const double NEAR0 = 5.0 * Num<double>::tiny;  // near_zero, flux_solver.f90:461-474
   double mi = rmax(rmax(rabs(Fi), rabs(Fim)), 1.0);
@@ -1013,7 +1043,7 @@ __device__ __forceinline__ double divergence_fp64(double Fi, double Fim, double 
   if (rabs(b) < mj * REL_TOL) b = 0.0;
   double s = a + b;
   if (abs_lt(s, NEAR0)) s = 0.0;
-  return G.inv_vol != 0.0 ? (-s) * G.inv_vol : (-s) / G.vol;
+  return G.inv_vol != 0.0 ? (-s) * G.inv_vol : div_by(by_vol, -s);
 }
 
 }  // namespace cato
