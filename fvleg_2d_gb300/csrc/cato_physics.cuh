@@ -490,6 +490,7 @@ __device__ __forceinline__ void recon_mlp<df, 5>(df qm2, df qm1, df q0, df qp1, 
 template <typename R> struct FluxConsts {
   R gamma, g_over_gm1, gm1, two_gm1_over_gp1, gamma_factor, hllc_gf, harten_delta;
   R ausm_beta, ausm_kp, ausm_ku, ausm_sigma;
+  R inv_gm1;  // RN(1 / (gamma - 1)): the shared reciprocal of the FP64 divisions by gamma - 1
   int low_mach_fix, harten;
 };
 
@@ -507,6 +508,7 @@ template <typename R> inline FluxConsts<R> convert_consts(const FluxConsts<doubl
   C.ausm_kp = R(K.ausm_kp);
   C.ausm_ku = R(K.ausm_ku);
   C.ausm_sigma = R(K.ausm_sigma);
+  C.inv_gm1 = R(K.inv_gm1);
   C.low_mach_fix = K.low_mach_fix;
   C.harten = K.harten;
   return C;
@@ -934,8 +936,15 @@ __device__ __forceinline__ void flux_hllc(const FluxConsts<R>& K, const Prim<R>&
   R qL = (p_star <= A.p) ? R(1) : Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, A.p) - R(1)));
   R qR = (p_star <= B.p) ? R(1) : Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, B.p) - R(1)));
   R SL = qnL - cL * qL, SR = qnR + cR * qR;
-    R EL = Num<R>::div(A.p, R(K.gm1)) + R(0.5) * A.r * (A.u * A.u + A.v * A.v);
-  R ER = Num<R>::div(B.p, R(K.gm1)) + R(0.5) * B.r * (B.u * B.u + B.v * B.v);
+  R EL, ER;
+  if constexpr (std::is_same<R, double>::value) {  // p / (gamma - 1), one shared reciprocal
+    const DivBy by_gm1{K.gm1, K.inv_gm1, exp_mid(K.gm1)};
+    EL = div_by(by_gm1, A.p) + 0.5 * A.r * (A.u * A.u + A.v * A.v);
+    ER = div_by(by_gm1, B.p) + 0.5 * B.r * (B.u * B.u + B.v * B.v);
+  } else {
+    EL = Num<R>::div(A.p, R(K.gm1)) + R(0.5) * A.r * (A.u * A.u + A.v * A.v);
+    ER = Num<R>::div(B.p, R(K.gm1)) + R(0.5) * B.r * (B.u * B.u + B.v * B.v);
+  }
   R S_star = Num<R>::div(B.p - A.p + A.r * qnL * (SL - qnL) - B.r * qnR * (SR - qnR),
                          A.r * (SL - qnL) - B.r * (SR - qnR));
   R Fn[4];
