@@ -808,13 +808,25 @@ __device__ __forceinline__ void flux_roe(const FluxConsts<R>& K, const Prim<R>& 
   const R g = R(K.gamma);
   const R nx = DIR == 0 ? R(1) : R(0), ny = DIR == 0 ? R(0) : R(1);
   R rl = rabs(A.r), ul = A.u, vl = A.v, pl = rabs(A.p);
-  const R gq = R(K.g_over_gm1);
-  R hl = gq * Num<R>::div(pl, rl) + R(0.5) * (ul * ul + vl * vl);
   R rr = rabs(B.r), ur = B.u, vr = B.v, pr = rabs(B.p);
-  R hr = gq * Num<R>::div(pr, rr) + R(0.5) * (ur * ur + vr * vr);
+  // FP64: the three quotients by rl share one reciprocal (DivBy)
+  R q_pl, q_rav, q_gpl;
+  const R gq = R(K.g_over_gm1);
   R rav = Num<R>::sqrt(rl * rr);
+  if constexpr (std::is_same<R, double>::value) {
+    const DivBy by_l = div_by_make(rl);
+    q_pl = div_by(by_l, pl);
+    q_rav = div_by(by_l, rav);
+    q_gpl = div_by(by_l, g * pl);
+  } else {
+    q_pl = Num<R>::div(pl, rl);
+    q_rav = Num<R>::div(rav, rl);
+    q_gpl = Num<R>::div(g * pl, rl);
+  }
+  R hl = gq * q_pl + R(0.5) * (ul * ul + vl * vl);
+  R hr = gq * Num<R>::div(pr, rr) + R(0.5) * (ur * ur + vr * vr);
   R gam1 = R(K.gm1);
-  R dd = Num<R>::div(rav, rl);
+  R dd = q_rav;
   R dd1 = Num<R>::div(R(1), R(1) + dd);
   R uav = (ul + dd * ur) * dd1;
   R vav = (vl + dd * vr) * dd1;
@@ -826,7 +838,7 @@ __device__ __forceinline__ void flux_roe(const FluxConsts<R>& K, const Prim<R>& 
   R du = (ur - ul) * nx + (vr - vl) * ny;
   R du_trans = -((ur - ul) * ny) + (vr - vl) * nx;
   R cs_R = Num<R>::sqrt(Num<R>::div(g * pr, rr));
-  R cs_L = Num<R>::sqrt(Num<R>::div(g * pl, rl));
+  R cs_L = Num<R>::sqrt(q_gpl);
   R h1 = rabs(rmin(uv - cav, (ul * nx + vl * ny) - cs_L));
   R h2 = rabs(uv);
   R h4 = rabs(rmax(uv + cav, (ur * nx + vr * ny) + cs_R));
