@@ -738,13 +738,23 @@ __device__ __forceinline__ void flux_slau(const FluxConsts<R>& K, const Prim<R>&
   R c_bar = R(0.5) * (c_plus + c_minus);
   R V_n_bar = Num<R>::div(rho_L * rabs(Vp) + rho_R * rabs(Vm), rho_L + rho_R);
   R vel2 = R(0.5) * (u_L * u_L + v_L * v_L + u_R * u_R + v_R * v_R);
-  R M_hat = rmin(R(1), Num<R>::div(Num<R>::sqrt(vel2), c_bar));
+  // the four Mach numbers: quotients by c_bar, one shared reciprocal in FP64 (DivBy)
+  R M_hat, M_bar, M_plus, M_minus;
+  if constexpr (std::is_same<R, double>::value) {
+    const DivBy by_c = div_by_make(c_bar);
+    M_hat = rmin(1.0, div_by(by_c, ::sqrt(vel2)));
+    M_bar = div_by(by_c, V_n_bar);
+    M_plus = div_by(by_c, Vp);
+    M_minus = div_by(by_c, Vm);
+  } else {
+    M_hat = rmin(R(1), Num<R>::div(Num<R>::sqrt(vel2), c_bar));
+    M_bar = Num<R>::div(V_n_bar, c_bar);
+    M_plus = Num<R>::div(Vp, c_bar);
+    M_minus = Num<R>::div(Vm, c_bar);
+  }
   R Chi = (R(1) - M_hat) * (R(1) - M_hat);
-  R M_bar = Num<R>::div(V_n_bar, c_bar);
   R p_bar = R(0.5) * (p_L + p_R);
   R rho_bar = R(0.5) * (rho_L + rho_R);
-  R M_plus = Num<R>::div(Vp, c_bar);
-  R M_minus = Num<R>::div(Vm, c_bar);
   R B_plus, B_minus;
   if (rabs(M_plus) < R(1)) B_plus = R(0.25) * (R(2) - M_plus) * ((M_plus + R(1)) * (M_plus + R(1)));
   else B_plus = R(0.5) * (R(1) + fsign1(M_plus));
