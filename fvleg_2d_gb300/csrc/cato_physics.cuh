@@ -327,6 +327,16 @@ __device__ __forceinline__ void recon_tvd2<float>(int lim, float qm1, float q0, 
   Rr = qp1 - 0.5f * tvd_slope_f32(lim, d0, dp);
 }
 
+// num / den is certainly <= 0 and not NaN: num = +-0 over a finite non-zero den, or finite
+// non-zero operands of opposite signs (integer pipe)
+__device__ __forceinline__ bool ratio_nonpos(double num, double den) {
+  const long long bn = __double_as_longlong(num), bd = __double_as_longlong(den);
+  const unsigned long long an = (unsigned long long)bn << 1, ad = (unsigned long long)bd << 1;
+  if (ad == 0ULL || ad >= 0xffe0000000000000ULL) return false;  // den zero, inf or NaN
+  if (an == 0ULL) return true;
+  return an < 0xffe0000000000000ULL && ((bn ^ bd) < 0);
+}
+
 template <typename R, int ORDER>
 __device__ __forceinline__ void recon_mlp(R qm2, R qm1, R q0, R qp1, R qp2, R qp3, R t0p, R t0m,
                                           R t1p, R t1m, R& L, R& Rr) {
@@ -338,38 +348,59 @@ __device__ __forceinline__ void recon_mlp(R qm2, R qm1, R q0, R qp1, R qp2, R qp
     if (abs_lt(d0, EPS)) d0 = R(0);
     if (abs_lt(dp, EPS)) dp = R(0);
   }
-  R rR_p1 = Num<R>::div(d0, dp + S);
-  R rL = Num<R>::div(d0, dm + S);
-  R bL, bR;
-  if (ORDER == 5) {
-    R dm3 = qm1 - qm2, dp5 = qp3 - qp2;
-    if constexpr (!kFP32<R>) {
-      if (abs_lt(dm3, EPS)) dm3 = R(0);
-      if (abs_lt(dp5, EPS)) dp5 = R(0);
-    }
-    R rL_m1 = Num<R>::div(dm, dm3 + S);
-    R rL_p1 = Num<R>::div(dp, d0 + S);
-    R rR_p2 = Num<R>::div(dp, dp5 + S);
-    R rR = Num<R>::div(dm, d0 + S);
-    bL = Num<R>::div((((Num<R>::div(R(-2), rL_m1 + S)) + R(11)) + R(24) * rL) - R(3) * rL * rL_p1,
-                     R(30));
-    bR = Num<R>::div((((Num<R>::div(R(-2), rR_p2 + S)) + R(11)) + R(24) * rR_p1) -
-                         R(3) * rR_p1 * rR,
-                     R(30));
-  } else {
-    bL = Num<R>::div(R(1) + R(2) * rL, R(3));
-    bR = Num<R>::div(R(1) + R(2) * rR_p1, R(3));
+  // FP64: a side whose ratio is <= 0 has a limited slope of +0 whatever beta and alpha are
+  // (alpha is clamped to [1, 2], so min(alpha r, alpha, beta) <= 0 and max(0, .) = +0); its
+  // beta and alpha, which take most of the divisions, are skipped
+  bool zL = false, zR = false;
+  if constexpr (std::is_same<R, double>::value) {
+    zL = ratio_nonpos(d0, dm + S);
+    zR = ratio_nonpos(d0, dp + S);
   }
-  R tt = Num<R>::div(rabs(t0p - t0m), rabs(qp1 - qm1) + S);
-  R tt1 = Num<R>::div(rabs(t1p - t1m), rabs(qp2 - q0) + S);
-  R aLt = Num<R>::div(R(2) * rmax(R(1), rL) * (R(1) + rmax(R(0), Num<R>::div(tt1, rR_p1 + S))),
-                      R(1) + tt);
-  R aRt = Num<R>::div(R(2) * rmax(R(1), rR_p1) * (R(1) + rmax(R(0), Num<R>::div(tt, rL + S))),
-                      R(1) + tt1);
-  R aL = rmax(R(1), rmin(R(2), aLt));
-  R aR = rmax(R(1), rmin(R(2), aRt));
-  L = q0 + R(0.5) * rmax(R(0), rmin(rmin(aL * rL, aL), bL)) * dm;
-  Rr = qp1 - R(0.5) * rmax(R(0), rmin(rmin(aR * rR_p1, aR), bR)) * dp;
+  R phiL = R(0), phiR = R(0);
+  if (!zL || !zR) {
+    R rR_p1 = Num<R>::div(d0, dp + S);
+    R rL = Num<R>::div(d0, dm + S);
+    R bL = R(0), bR = R(0);
+    if (ORDER == 5) {
+      R dm3 = qm1 - qm2, dp5 = qp3 - qp2;
+      if constexpr (!kFP32<R>) {
+        if (abs_lt(dm3, EPS)) dm3 = R(0);
+        if (abs_lt(dp5, EPS)) dp5 = R(0);
+      }
+      if (!zL) {
+        R rL_m1 = Num<R>::div(dm, dm3 + S);
+        R rL_p1 = Num<R>::div(dp, d0 + S);
+        bL = Num<R>::div(
+            (((Num<R>::div(R(-2), rL_m1 + S)) + R(11)) + R(24) * rL) - R(3) * rL * rL_p1, R(30));
+      }
+      if (!zR) {
+        R rR_p2 = Num<R>::div(dp, dp5 + S);
+        R rR = Num<R>::div(dm, d0 + S);
+        bR = Num<R>::div((((Num<R>::div(R(-2), rR_p2 + S)) + R(11)) + R(24) * rR_p1) -
+                             R(3) * rR_p1 * rR,
+                         R(30));
+      }
+    } else {
+      if (!zL) bL = Num<R>::div(R(1) + R(2) * rL, R(3));
+      if (!zR) bR = Num<R>::div(R(1) + R(2) * rR_p1, R(3));
+    }
+    R tt = Num<R>::div(rabs(t0p - t0m), rabs(qp1 - qm1) + S);
+    R tt1 = Num<R>::div(rabs(t1p - t1m), rabs(qp2 - q0) + S);
+    if (!zL) {
+      R aLt = Num<R>::div(R(2) * rmax(R(1), rL) * (R(1) + rmax(R(0), Num<R>::div(tt1, rR_p1 + S))),
+                          R(1) + tt);
+      R aL = rmax(R(1), rmin(R(2), aLt));
+      phiL = rmax(R(0), rmin(rmin(aL * rL, aL), bL));
+    }
+    if (!zR) {
+      R aRt = Num<R>::div(R(2) * rmax(R(1), rR_p1) * (R(1) + rmax(R(0), Num<R>::div(tt, rL + S))),
+                          R(1) + tt1);
+      R aR = rmax(R(1), rmin(R(2), aRt));
+      phiR = rmax(R(0), rmin(rmin(aR * rR_p1, aR), bR));
+    }
+  }
+  L = q0 + R(0.5) * phiL * dm;
+  Rr = qp1 - R(0.5) * phiR * dp;
 }
 
 // ---------------------------------------------------------------------------------------------
