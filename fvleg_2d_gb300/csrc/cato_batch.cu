@@ -383,7 +383,6 @@ int cato_batch_add(cato_batch* b, const cato_config* cfg, const double* rho, con
   d.K64.gamma = g;
   d.K64.g_over_gm1 = g / (g - 1.0);
   d.K64.gm1 = g - 1.0;
-  d.K64.inv_gm1 = 1.0 / d.K64.gm1;
   d.K64.two_gm1_over_gp1 = 2.0 * ((g - 1.0) / (g + 1.0));
   d.K64.gamma_factor = ((2.0 * (g - 1.0)) / (g + 1.0));
   d.K64.hllc_gf = (g + 1.0) / (2.0 * g);

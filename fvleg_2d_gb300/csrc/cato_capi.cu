@@ -155,7 +155,6 @@ static void fill_consts(cato_handle* h) {
   K.gamma = g;
   K.g_over_gm1 = g / (g - 1.0);
   K.gm1 = g - 1.0;
-  K.inv_gm1 = 1.0 / K.gm1;
   K.two_gm1_over_gp1 = 2.0 * ((g - 1.0) / (g + 1.0));
   K.gamma_factor = ((2.0 * (g - 1.0)) / (g + 1.0));
   K.hllc_gf = (g + 1.0) / (2.0 * g);
@@ -425,6 +424,54 @@ static void zero_host_field(cato_handle* h, double* a, int64_t ld) {
   for (size_t j = 0; j < rows; ++j) std::memset(a + j * ld, 0, sizeof(double) * (h->ni + 2 * h->ng));
 }
 
+
+// cato_gpu_check_divsqrt: seeded operands through the integer-pipe division and square root of
+// the FP64 path and through the hardware instructions.  Families (by the top bits of the first
+// hash): random bit patterns (all classes, incl. zeros, subnormals, inf, NaN), a of a narrow
+// exponent range over b in [1, 2), b with few significand bits, a close to b.  c[0]/c[2] count
+// the cases the integer routines took, c[1]/c[3] their mismatches.
+static __device__ __forceinline__ unsigned long long check_mix(unsigned long long z) {
+  z += 0x9e3779b97f4a7c15ULL;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+static __global__ void divsqrt_check_kernel(long long n, unsigned long long seed,
+                                            unsigned long long* c) {
+  unsigned long long nd = 0, bd = 0, ns = 0, bs = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long h1 = check_mix(seed + 2 * (unsigned long long)i);
+    const unsigned long long h2 = check_mix(seed + 2 * (unsigned long long)i + 1);
+    unsigned long long ua = h1, ub = h2;
+    const int fam = (int)(h1 >> 62);
+    if (fam == 1) {
+      ua = (ua & ~(0x7ffULL << 52)) | ((unsigned long long)(990 + (h2 & 63)) << 52);
+      ub = (ub & ~(0x7ffULL << 52)) | (1023ULL << 52);
+    } else if (fam == 2) {
+      ub &= ~0xfffffffffff00ULL;
+    } else if (fam == 3) {
+      ua = (ub & 0xfffffffffffff000ULL) | (h1 & 0xfffULL);
+    }
+    const double a = __longlong_as_double((long long)ua), b = __longlong_as_double((long long)ub);
+    bool ok;
+    const uint64_t q = intdiv::div_bits(ua, ub, ok);
+    if (ok) {
+      ++nd;
+      bd += q != (uint64_t)__double_as_longlong(a / b);
+    }
+    const unsigned long long us = ua & 0x7fffffffffffffffULL;
+    const uint64_t r = intdiv::sqrt_bits(us, ok);
+    if (ok) {
+      ++ns;
+      bs += r != (uint64_t)__double_as_longlong(sqrt(__longlong_as_double((long long)us)));
+    }
+  }
+  atomicAdd(c + 0, nd);
+  atomicAdd(c + 1, bd);
+  atomicAdd(c + 2, ns);
+  atomicAdd(c + 3, bs);
+}
 
 extern "C" {
 
@@ -949,6 +996,28 @@ int cato_gpu_get_plan(const cato_handle* h, int32_t* threads, int32_t* rows_per_
 
 int cato_gpu_select_device(int32_t device) {
   return cudaSetDevice(device) == cudaSuccess ? CATO_OK : CATO_ERR_CUDA;
+}
+
+int cato_gpu_check_divsqrt(int64_t n, uint64_t seed, uint64_t tested[2], uint64_t mismatches[2]) {
+  if (n < 0 || !tested || !mismatches) return CATO_ERR_ARG;
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, 4 * sizeof(unsigned long long)) != cudaSuccess) return CATO_ERR_OOM;
+  cudaError_t e = cudaMemset(d, 0, 4 * sizeof(unsigned long long));
+  if (e == cudaSuccess && n > 0) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    divsqrt_check_kernel<<<(unsigned)(sms > 0 ? 8 * sms : 1024), 256>>>(n, seed, d);
+    e = cudaGetLastError();
+  }
+  unsigned long long h[4] = {0, 0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  tested[0] = h[0];
+  mismatches[0] = h[1];
+  tested[1] = h[2];
+  mismatches[1] = h[3];
+  return e == cudaSuccess ? CATO_OK : CATO_ERR_CUDA;
 }
 
 int cato_host_alloc(uint64_t bytes, void** out) {

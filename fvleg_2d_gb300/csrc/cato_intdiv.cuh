@@ -1,0 +1,184 @@
+// cato_intdiv.cuh -- IEEE-754 binary64 division and square root, rounded to nearest even, on the
+// integer pipe.
+//
+// GB300 runs FP64 arithmetic at 1/64 of the FP32 rate, and a division or square root costs
+// several FP64 instructions there.  The integer and FP32 pipes have room to spare.  These
+// routines get the exact IEEE result from integer arithmetic on the significands:
+//   1. an FP32 seed, y0 = RN32(1 / b) (division) or RN32(1 / RN32(sqrt(a))) (square root), of
+//      the operand's significand truncated to 24 bits;
+//   2. one Newton-Raphson step of third order in 64-bit fixed point, y1 = y0 (1 + e + e^2) for
+//      1/b with e = 1 - b y0, and y1 = y0 (1 + e/2 + 3e^2/8) for 1/sqrt(a) with e = 1 - a y0^2
+//      (J.-M. Muller et al., Handbook of Floating-Point Arithmetic, 2nd ed., 2018, sections 4.7
+//      and 11.3: Newton-Raphson iterations for the reciprocal and the reciprocal square root);
+//   3. the quotient a y1 (or the root a y1) from the high half of a 64 x 64-bit product, within
+//      three units of 2^-61 of the exact value, then the nearest significand M1;
+//   4. the exact rounding decision: the signs of the integer remainders
+//      2^k A - (2 M1 +- 1) B (division) or 2^k A - (2 M1 +- 1)^2 (square root), computed
+//      modulo 2^64 because their magnitudes are below 2^63, decide between M1 - 1, M1 and
+//      M1 + 1, with ties to even.
+// Operands that are zero, subnormal, infinite or NaN, negative square-root operands and quotients
+// outside the normal range take the hardware instruction instead (the caller's fallback).
+// The same source compiles for the host, where the FP32 seeds are the IEEE float operations
+// 1.0f / x and sqrtf(x) (correctly rounded, like __frcp_rn and __fsqrt_rn on the device); a host
+// test compares the routines bit for bit with the hardware division and square root.
+#pragma once
+
+#include <stdint.h>
+#include <string.h>
+
+#ifdef __CUDACC__
+#define CATO_HD __host__ __device__ __forceinline__
+#else
+#define CATO_HD static inline
+#endif
+
+namespace cato {
+namespace intdiv {
+
+CATO_HD uint64_t bits_of(double x) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t u;
+  memcpy(&u, &x, sizeof u);
+  return u;
+#endif
+}
+CATO_HD double double_of(uint64_t u) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)u);
+#else
+  double x;
+  memcpy(&x, &u, sizeof x);
+  return x;
+#endif
+}
+CATO_HD uint32_t fbits_of(float x) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(x);
+#else
+  uint32_t u;
+  memcpy(&u, &x, sizeof u);
+  return u;
+#endif
+}
+CATO_HD float float_of(uint32_t u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float x;
+  memcpy(&x, &u, sizeof x);
+  return x;
+#endif
+}
+CATO_HD uint64_t umulhi(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+// RN32(1 / x) and RN32(sqrt(x)) for x in [1, 4)
+CATO_HD float recip32(float x) {
+#ifdef __CUDA_ARCH__
+  return __frcp_rn(x);
+#else
+  return 1.0f / x;
+#endif
+}
+CATO_HD float sqrt32(float x) {
+#ifdef __CUDA_ARCH__
+  return __fsqrt_rn(x);
+#else
+  return __builtin_sqrtf(x);
+#endif
+}
+
+constexpr uint64_t kFrac = 0x000fffffffffffffULL;
+constexpr uint64_t kHid = 0x0010000000000000ULL;
+
+// y * 2^30 as an integer for y = RN32(...) in (0.5, 1] (24 significant bits: exact)
+CATO_HD uint32_t fixed30(float y) {
+  const uint32_t yb = fbits_of(y);
+  return ((yb & 0x7fffffu) | 0x800000u) << ((yb >> 23) - 120u);
+}
+
+// y0 (1 + t) * 2^62 for y0 = Y0 / 2^30 and t = T / 2^82 (floor of the correction term)
+CATO_HD uint64_t refine62(uint32_t Y0, int64_t T) {
+  const int64_t Th = T >> 32;                 // floor(T / 2^32)
+  const uint64_t Tl = (uint32_t)T;
+  const int64_t yt32 = (int64_t)Y0 * Th + (int64_t)(((uint64_t)Y0 * Tl) >> 32);  // floor(Y0 T / 2^32)
+  return ((uint64_t)Y0 << 32) + (uint64_t)(yt32 >> 18);
+}
+
+// RN(a / b) as bits for normal a, b; ok = false when an operand is not normal or the quotient
+// is not normal (the bits are then meaningless).
+//
+// With A, B the 53-bit significands (a = A 2^(ea-1075), b = B 2^(eb-1075)):
+//   y0 = RN32(1 / fb), fb = b' = B / 2^52 truncated to 24 bits: |y0 - 1/b'| < 1.25 2^-23,
+//   E = 2^82 (1 - b' y0) = -(B Y0) mod 2^64, |E| < 1.25 2^60;
+//   T = E + Eh^2 / 2^18 (Eh = floor(E / 2^32)) = 2^82 (e + e^2) within 2^-69;
+//   Y1 = 2^62 y0 (1 + T / 2^82): |Y1 - 2^62 / b'| < 1.13;
+//   H = floor(A 2^11 Y1 / 2^64): |H - 2^61 A / B| < 2.13;
+//   s = 9 (quotient >= 1) or 8, M1 = round(H / 2^s), Z = 2^(62-s) A - (2 M1 + 1) B, |Z| < 2^54.
+CATO_HD uint64_t div_bits(uint64_t ua, uint64_t ub, bool& ok) {
+  const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
+  const uint64_t A = (ua & kFrac) | kHid, B = (ub & kFrac) | kHid;
+  const float fb = float_of(0x3f800000u | (uint32_t)((ub & kFrac) >> 29));
+  const uint32_t Y0 = fixed30(recip32(fb));
+  const int64_t E = (int64_t)(0ULL - B * (uint64_t)Y0);
+  const int32_t Eh = (int32_t)(E >> 32);
+  const int64_t T = E + (((int64_t)Eh * Eh) >> 18);
+  const uint64_t Y1 = refine62(Y0, T);
+  const uint64_t H = umulhi(A << 11, Y1);
+  const uint32_t s = (H >> 61) ? 9u : 8u;
+  const uint64_t M1 = (H + (1ULL << (s - 1))) >> s;
+  const int64_t Z = (int64_t)((A << (62 - s)) - (2 * M1 + 1) * B);
+  uint64_t M = M1;
+  if (Z > 0 || (Z == 0 && (M1 & 1))) {
+    M = M1 + 1;
+  } else {
+    const int64_t W = Z + (int64_t)(2 * B);  // 2^(62-s) A - (2 M1 - 1) B
+    if (W < 0 || (W == 0 && (M1 & 1))) M = M1 - 1;
+  }
+  const int32_t Ef = (int32_t)ea - (int32_t)eb + 1014 + (int32_t)s;
+  ok = (ea - 1u < 2046u) && (eb - 1u < 2046u) && (Ef >= 1) && (Ef <= 2045);
+  const uint64_t sign = (ua ^ ub) & 0x8000000000000000ULL;
+  // M in [2^52, 2^53]: M = 2^53 carries into the exponent field
+  return sign | (((uint64_t)(uint32_t)Ef << 52) + (M - kHid));
+}
+
+// RN(sqrt(a)) as bits for normal a > 0; ok = false otherwise.
+//
+// a = A2 2^(2m) with A2 = A or 2A in [2^52, 2^54), a'' = A2 / 2^52 in [1, 4):
+//   y0 = RN32(1 / RN32(sqrt(fa))), fa = a'' truncated to 24 bits: |y0 sqrt(a'') - 1| < 1.5 2^-23;
+//   E = 2^82 (1 - a'' y0^2) = -floor(A2 Y0^2 / 2^30) mod 2^64;
+//   T = E / 2 + 3 Eh^2 / 2^21 = 2^82 (e/2 + 3e^2/8);  Y1 = 2^62 y0 (1 + T / 2^82);
+//   H = floor(A2 2^10 Y1 / 2^64): |H - 2^60 sqrt(a'')| < 2.1;
+//   M1 = round(H / 2^8), Z = 2^54 A2 - (2 M1 + 1)^2 (never 0), |Z| < 2^56.
+CATO_HD uint64_t sqrt_bits(uint64_t ua, bool& ok) {
+  const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu;
+  const uint32_t odd = (ea & 1u) ^ 1u;  // the unbiased exponent ea - 1075 is odd
+  const uint64_t A2 = ((ua & kFrac) | kHid) << odd;
+  const float fa = float_of(((127u + odd) << 23) | (uint32_t)((ua & kFrac) >> 29));
+  const uint32_t Y0 = fixed30(recip32(sqrt32(fa)));
+  const uint64_t S = (uint64_t)Y0 * Y0;  // Y0^2 <= 2^60
+  const uint64_t plo = A2 * S, phi = umulhi(A2, S);
+  const int64_t E = (int64_t)(0ULL - ((plo >> 30) | (phi << 34)));
+  const int32_t Eh = (int32_t)(E >> 32);
+  const int64_t T = (E >> 1) + ((3 * ((int64_t)Eh * Eh)) >> 21);
+  const uint64_t Y1 = refine62(Y0, T);
+  const uint64_t H = umulhi(A2 << 10, Y1);
+  const uint64_t M1 = (H + 128u) >> 8;
+  const uint64_t N = 2 * M1 + 1;
+  const int64_t Z = (int64_t)((A2 << 54) - N * N);
+  uint64_t M = M1;
+  if (Z > 0) M = M1 + 1;
+  else if (Z + (int64_t)(8 * M1) < 0) M = M1 - 1;  // 2^54 A2 - (2 M1 - 1)^2 < 0
+  ok = (ea - 1u < 2046u) && !(ua >> 63);
+  const uint32_t Ef = 512u + ((ea - odd) >> 1);  // 1049 + (ea - 1075 - odd) / 2
+  return (((uint64_t)Ef << 52) + (M - kHid));
+}
+
+}  // namespace intdiv
+}  // namespace cato

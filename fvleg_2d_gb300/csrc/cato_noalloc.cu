@@ -140,7 +140,6 @@ extern "C" int cato_gpu_solve_noalloc(const cato_config* cfg, double* rho, doubl
   K.gamma = g;
   K.g_over_gm1 = g / (g - 1.0);
   K.gm1 = g - 1.0;
-  K.inv_gm1 = 1.0 / K.gm1;
   K.two_gm1_over_gp1 = 2.0 * ((g - 1.0) / (g + 1.0));
   K.gamma_factor = ((2.0 * (g - 1.0)) / (g + 1.0));
   K.hllc_gf = (g + 1.0) / (2.0 * g);

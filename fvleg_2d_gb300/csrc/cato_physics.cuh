@@ -18,8 +18,27 @@
 #include <cuda_runtime.h>
 
 #include "cato_df.cuh"
+#include "cato_intdiv.cuh"
 
 namespace cato {
+
+// IEEE binary64 a / b and sqrt(a), rounded to nearest, for the FP64 path: the integer-pipe
+// routines of cato_intdiv.cuh, and the hardware instruction for the operands they leave out
+// (zero, subnormal, infinite or NaN operands, quotients outside the normal range).  The hardware
+// forms are kept out of line so that the compiler branches to them instead of evaluating them
+// alongside.
+static __device__ __noinline__ double div_hw(double a, double b) { return a / b; }
+static __device__ __noinline__ double sqrt_hw(double a) { return ::sqrt(a); }
+__device__ __forceinline__ double div_rn(double a, double b) {
+  bool ok;
+  const uint64_t q = intdiv::div_bits(intdiv::bits_of(a), intdiv::bits_of(b), ok);
+  return ok ? intdiv::double_of(q) : div_hw(a, b);
+}
+__device__ __forceinline__ double sqrt_rn(double a) {
+  bool ok;
+  const uint64_t r = intdiv::sqrt_bits(intdiv::bits_of(a), ok);
+  return ok ? intdiv::double_of(r) : sqrt_hw(a);
+}
 
 enum { FLUX_AUSMPW = 0, FLUX_SLAU = 1, FLUX_SLAU2 = 2, FLUX_SD_SLAU = 3, FLUX_SD_SLAU2 = 4,
        FLUX_ROE = 5, FLUX_AUSM_UP = 6, FLUX_HLLC = 7, FLUX_M_AUSMPW = 8 };
@@ -41,18 +60,20 @@ template <> constexpr bool kFP32<float> = true;
 template <> struct Num<double> {
   static constexpr double eps = 2.220446049250313080847263336181640625e-16;  // epsilon(1.0_rk)
   static constexpr double tiny = 2.2250738585072013830902327173324040642e-308; // tiny(1.0_rk)
-  // IEEE a / b.  Two exact cases are decided on the integer pipe (GB300's FP64 pipe is its
-  // narrowest and a division costs ~10 of its instructions): a signed zero over a finite
-  // non-zero b is the zero with the sign of the product, and a / 1 is a.
+  // IEEE a / b on the integer pipe (div_rn).  A signed zero over a finite non-zero b (flat
+  // data) is the zero with the sign of the product, decided before the general routine.
   static __device__ __forceinline__ double div(double a, double b) {
     const unsigned long long ua = (unsigned long long)__double_as_longlong(a);
     const unsigned long long ub = (unsigned long long)__double_as_longlong(b);
     if ((ua << 1) == 0ULL && (ub << 1) != 0ULL && ((ub >> 52) & 0x7ffULL) != 0x7ffULL)
       return __longlong_as_double((long long)((ua ^ ub) & 0x8000000000000000ULL));
-    if (ub == 0x3ff0000000000000ULL) return a;
-    return a / b;
+    return div_rn(a, b);
   }
-  static __device__ __forceinline__ double sqrt(double a) { return ::sqrt(a); }
+  // sqrt(+-0) = +-0 (a zero velocity), else sqrt_rn
+  static __device__ __forceinline__ double sqrt(double a) {
+    if (((unsigned long long)__double_as_longlong(a) << 1) == 0ULL) return a;
+    return sqrt_rn(a);
+  }
 };
 
 template <> struct Num<float> {
@@ -116,35 +137,6 @@ __device__ __forceinline__ bool abs_lt(double x, double c) {
 __device__ __forceinline__ bool abs_lt(float x, float c) { return fabsf(x) < c; }
 __device__ __forceinline__ bool abs_lt(df x, df c) { return df_abs(x) < c; }
 
-// ---------------------------------------------------------------------------------------------
-// Several IEEE quotients with one denominator b (Markstein, IBM J. Res. Dev. 34(1), 1990): with
-// y = RN(1/b), q0 = RN(a y) and the exact remainder r = a - b q0 (one FMA), RN(q0 + r y) is
-// RN(a / b).  One division for the reciprocal, then three FP64 operations per quotient instead
-// of a division each.  Used where |a| and |b| lie in [2^-500, 2^500] (no intermediate overflow
-// or underflow, a != 0); elsewhere the plain division.
-__device__ __forceinline__ bool exp_mid(double x) {
-  const unsigned e = (unsigned)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffULL);
-  return e - 523u <= 1000u;
-}
-struct DivBy {
-  double b, y;
-  bool ok;
-};
-__device__ __forceinline__ DivBy div_by_make(double b) {
-  DivBy d;
-  d.b = b;
-  d.ok = exp_mid(b);
-  d.y = d.ok ? 1.0 / b : 0.0;
-  return d;
-}
-__device__ __forceinline__ double div_by(const DivBy& d, double a) {
-  if (d.ok && exp_mid(a)) {
-    const double q0 = a * d.y;
-    return __fma_rn(__fma_rn(-d.b, q0, a), d.y, q0);
-  }
-  return a / d.b;
-}
-
 // abs_lt(x / cs, 1e-13) with x / cs rounded, as the Mach filter of calculate_derived_quantities
 // (mod_fluid.f90:579-588; x below tiny counts as a zero Mach number).  The quotient is only
 // formed when the exponents leave the answer open: for normal x and cs with biased exponents
@@ -160,7 +152,7 @@ __device__ __forceinline__ bool mach_below_1e13(double x, double cs) {
     if (ex - ec >= -42) return false;
     if (ex - ec <= -46) return true;
   }
-  return abs_lt(x / cs, 1e-13);
+  return abs_lt(div_rn(x, cs), 1e-13);
 }
 
 // FP64 <-> FP32 conversion on the integer pipe (GB300's F2F shares the narrow FP64 pipe).
@@ -210,18 +202,17 @@ __device__ __forceinline__ void prim_from_cons(double g, double g1, double r, do
                                                double rv, double rE, double& u, double& v,
                                                double& p, double& cs) {
   const double EPS = Num<double>::eps, TINY = Num<double>::tiny;
-  const DivBy by_r = div_by_make(r);  // four quotients by rho
-  u = abs_lt(ru, TINY) ? 0.0 : div_by(by_r, ru);
-  v = abs_lt(rv, TINY) ? 0.0 : div_by(by_r, rv);
-  double e = abs_lt(rE, TINY) ? 0.0 : div_by(by_r, rE);
+  u = abs_lt(ru, TINY) ? 0.0 : div_rn(ru, r);
+  v = abs_lt(rv, TINY) ? 0.0 : div_rn(rv, r);
+  double e = abs_lt(rE, TINY) ? 0.0 : div_rn(rE, r);
   double s = u * u + v * v;
   if (abs_lt(s, EPS)) s = 0.0;
   double h = s * 0.5;
   double dd = e - h;
   if (abs_lt(dd, EPS)) dd = 0.0;
   p = (r * g1) * dd;
-  double pr = abs_lt(p, TINY) ? 0.0 : div_by(by_r, p);
-  cs = ::sqrt(pr * g);
+  double pr = abs_lt(p, TINY) ? 0.0 : div_rn(p, r);
+  cs = Num<double>::sqrt(pr * g);
   // mach_u = u / cs, mach_v = v / cs, then |mach| < 1e-13 zeroes the velocity
   if (mach_below_1e13(u, cs)) u = 0.0;  // each test reads only its own component and cs
   if (mach_below_1e13(v, cs)) v = 0.0;
@@ -521,7 +512,6 @@ __device__ __forceinline__ void recon_mlp<df, 5>(df qm2, df qm1, df q0, df qp1, 
 template <typename R> struct FluxConsts {
   R gamma, g_over_gm1, gm1, two_gm1_over_gp1, gamma_factor, hllc_gf, harten_delta;
   R ausm_beta, ausm_kp, ausm_ku, ausm_sigma;
-  R inv_gm1;  // RN(1 / (gamma - 1)): the shared reciprocal of the FP64 divisions by gamma - 1
   int low_mach_fix, harten;
 };
 
@@ -539,7 +529,6 @@ template <typename R> inline FluxConsts<R> convert_consts(const FluxConsts<doubl
   C.ausm_kp = R(K.ausm_kp);
   C.ausm_ku = R(K.ausm_ku);
   C.ausm_sigma = R(K.ausm_sigma);
-  C.inv_gm1 = R(K.inv_gm1);
   C.low_mach_fix = K.low_mach_fix;
   C.harten = K.harten;
   return C;
@@ -769,20 +758,10 @@ __device__ __forceinline__ void flux_slau(const FluxConsts<R>& K, const Prim<R>&
   R c_bar = R(0.5) * (c_plus + c_minus);
   R V_n_bar = Num<R>::div(rho_L * rabs(Vp) + rho_R * rabs(Vm), rho_L + rho_R);
   R vel2 = R(0.5) * (u_L * u_L + v_L * v_L + u_R * u_R + v_R * v_R);
-  // the four Mach numbers: quotients by c_bar, one shared reciprocal in FP64 (DivBy)
-  R M_hat, M_bar, M_plus, M_minus;
-  if constexpr (std::is_same<R, double>::value) {
-    const DivBy by_c = div_by_make(c_bar);
-    M_hat = rmin(1.0, div_by(by_c, ::sqrt(vel2)));
-    M_bar = div_by(by_c, V_n_bar);
-    M_plus = div_by(by_c, Vp);
-    M_minus = div_by(by_c, Vm);
-  } else {
-    M_hat = rmin(R(1), Num<R>::div(Num<R>::sqrt(vel2), c_bar));
-    M_bar = Num<R>::div(V_n_bar, c_bar);
-    M_plus = Num<R>::div(Vp, c_bar);
-    M_minus = Num<R>::div(Vm, c_bar);
-  }
+  R M_hat = rmin(R(1), Num<R>::div(Num<R>::sqrt(vel2), c_bar));
+  R M_bar = Num<R>::div(V_n_bar, c_bar);
+  R M_plus = Num<R>::div(Vp, c_bar);
+  R M_minus = Num<R>::div(Vm, c_bar);
   R Chi = (R(1) - M_hat) * (R(1) - M_hat);
   R p_bar = R(0.5) * (p_L + p_R);
   R rho_bar = R(0.5) * (rho_L + rho_R);
@@ -850,20 +829,9 @@ __device__ __forceinline__ void flux_roe(const FluxConsts<R>& K, const Prim<R>& 
   const R nx = DIR == 0 ? R(1) : R(0), ny = DIR == 0 ? R(0) : R(1);
   R rl = rabs(A.r), ul = A.u, vl = A.v, pl = rabs(A.p);
   R rr = rabs(B.r), ur = B.u, vr = B.v, pr = rabs(B.p);
-  // FP64: the three quotients by rl share one reciprocal (DivBy)
-  R q_pl, q_rav, q_gpl;
   const R gq = R(K.g_over_gm1);
   R rav = Num<R>::sqrt(rl * rr);
-  if constexpr (std::is_same<R, double>::value) {
-    const DivBy by_l = div_by_make(rl);
-    q_pl = div_by(by_l, pl);
-    q_rav = div_by(by_l, rav);
-    q_gpl = div_by(by_l, g * pl);
-  } else {
-    q_pl = Num<R>::div(pl, rl);
-    q_rav = Num<R>::div(rav, rl);
-    q_gpl = Num<R>::div(g * pl, rl);
-  }
+  R q_pl = Num<R>::div(pl, rl), q_rav = Num<R>::div(rav, rl), q_gpl = Num<R>::div(g * pl, rl);
   R hl = gq * q_pl + R(0.5) * (ul * ul + vl * vl);
   R hr = gq * Num<R>::div(pr, rr) + R(0.5) * (ur * ur + vr * vr);
   R gam1 = R(K.gm1);
@@ -990,14 +958,8 @@ __device__ __forceinline__ void flux_hllc(const FluxConsts<R>& K, const Prim<R>&
   R qR = (p_star <= B.p) ? R(1) : Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, B.p) - R(1)));
   R SL = qnL - cL * qL, SR = qnR + cR * qR;
   R EL, ER;
-  if constexpr (std::is_same<R, double>::value) {  // p / (gamma - 1), one shared reciprocal
-    const DivBy by_gm1{K.gm1, K.inv_gm1, exp_mid(K.gm1)};
-    EL = div_by(by_gm1, A.p) + 0.5 * A.r * (A.u * A.u + A.v * A.v);
-    ER = div_by(by_gm1, B.p) + 0.5 * B.r * (B.u * B.u + B.v * B.v);
-  } else {
-    EL = Num<R>::div(A.p, R(K.gm1)) + R(0.5) * A.r * (A.u * A.u + A.v * A.v);
-    ER = Num<R>::div(B.p, R(K.gm1)) + R(0.5) * B.r * (B.u * B.u + B.v * B.v);
-  }
+  EL = Num<R>::div(A.p, R(K.gm1)) + R(0.5) * A.r * (A.u * A.u + A.v * A.v);
+  ER = Num<R>::div(B.p, R(K.gm1)) + R(0.5) * B.r * (B.u * B.u + B.v * B.v);
   R S_star = Num<R>::div(B.p - A.p + A.r * qnL * (SL - qnL) - B.r * qnR * (SR - qnR),
                          A.r * (SL - qnL) - B.r * (SR - qnR));
   R Fn[4];
@@ -1088,24 +1050,24 @@ inline Geom uniform_geom(double dx, double dy) {
   return G;
 }
 
-// by_vol: the cell volume as a shared denominator (used when inv_vol is 0)
 __device__ __forceinline__ double divergence_fp64(double Fi, double Fim, double Fj, double Fjm,
-                                                  const Geom& G, const DivBy& by_vol) {
+                                                  const Geom& G) {
   const double REL_TOL = 1e-14;
   const double NEAR0 = 5.0 * Num<double>::tiny;  // near_zero, flux_solver.f90:461-474
   double mi = rmax(rmax(rabs(Fi), rabs(Fim)), 1.0);
   double mj = rmax(rmax(rabs(Fj), rabs(Fjm)), 1.0);
   // x / 1.0 is exact: skip the division when the scale is 1
   double a, b;
+  using N = Num<double>;
   if (mi == 1.0) a = ((Fi * G.l2) + (-(Fim * G.l4))) * mi;
-  else a = ((Fi / mi * G.l2) + (-(Fim / mi * G.l4))) * mi;
+  else a = ((N::div(Fi, mi) * G.l2) + (-(N::div(Fim, mi) * G.l4))) * mi;
   if (mj == 1.0) b = ((Fj * G.l3) + (-(Fjm * G.l1))) * mj;
-  else b = ((Fj / mj * G.l3) + (-(Fjm / mj * G.l1))) * mj;
+  else b = ((N::div(Fj, mj) * G.l3) + (-(N::div(Fjm, mj) * G.l1))) * mj;
   if (rabs(a) < mi * REL_TOL) a = 0.0;
   if (rabs(b) < mj * REL_TOL) b = 0.0;
   double s = a + b;
   if (abs_lt(s, NEAR0)) s = 0.0;
-  return G.inv_vol != 0.0 ? (-s) * G.inv_vol : div_by(by_vol, -s);
+  return G.inv_vol != 0.0 ? (-s) * G.inv_vol : N::div(-s, G.vol);
 }
 
 }  // namespace cato

@@ -420,11 +420,6 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
         if (A.G.rdyc) dy_inv = to_df(A.G.rdyc[j]);
       }
       if constexpr (Prec<R>::kind != 1) {
-        // the four divisions by the cell volume share one reciprocal (non-power-of-two volumes)
-        [[maybe_unused]] DivBy by_vol{};
-        if constexpr (Prec<R>::kind == 0) {
-          if (cg.inv_vol == 0.0) by_vol = div_by_make(cg.vol);
-        }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const R Fi = sfi[k * T + t], Fim = sfi[k * T + t - 1];
@@ -432,7 +427,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
           const R Fjm = sfj[(((j - 1) & 1) * 4 + k) * T + t];
           double L;
           if constexpr (Prec<R>::kind == 0)
-            L = divergence_fp64(Fi, Fim, Fj, Fjm, cg, by_vol);
+            L = divergence_fp64(Fi, Fim, Fj, Fjm, cg);
           else  // double-float flux differences, the result carried to FP64
             L = from_df(-((Fi - Fim) * dx_inv + (Fj - Fjm) * dy_inv));
           if (k == 3 && A.src_q) L = L + A.src_q[cidx];
@@ -480,7 +475,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
         if constexpr (Prec<R>::kind == 0) {
           double u, v, p, cs;
           prim_from_cons(A.gamma, A.gamma - 1.0, un[0], un[1], un[2], un[3], u, v, p, cs);
-          double d = A.cfl / (((fabs(u) + cs) / cg.dx) + ((fabs(v) + cs) / cg.dy));
+          double d = div_rn(A.cfl, div_rn(fabs(u) + cs, cg.dx) + div_rn(fabs(v) + cs, cg.dy));
           if (d < dt_loc) dt_loc = d;
           if (isnan(un[0]) || isnan(u) || isnan(v) || isnan(p)) st_loc |= ST_NAN;
           if (un[0] < 0.0) st_loc |= ST_NEG_DENSITY;

@@ -289,6 +289,15 @@ int cato_gpu_get_plan(const cato_handle* h, int32_t* threads, int32_t* rows_per_
 /* Select the CUDA device used by handles created afterwards on this host thread. */
 int cato_gpu_select_device(int32_t device);
 
+/* Device self-check of the FP64 path's IEEE division and square root, which run on the integer
+ * pipe (GB300's FP64 pipe is 1/64 of the FP32 rate): n seeded operand pairs (random bit patterns,
+ * narrow exponent ranges, divisors with few significand bits, quotients near 1) go through the
+ * integer routines and the hardware instructions on the current device.  tested[0] / tested[1]:
+ * the divisions / square roots the integer routines took (the rest fall back to the hardware),
+ * mismatches[0] / mismatches[1]: how many of those differ in any bit.  No counterpart in the
+ * reference. */
+int cato_gpu_check_divsqrt(int64_t n, uint64_t seed, uint64_t tested[2], uint64_t mismatches[2]);
+
 /* cato_gpu_solve for callers that cannot allocate device memory: no handle, no cudaMalloc or
  * cudaFree.  It has no counterpart in the reference; it serves callers whose device memory is
  * owned by another allocator (a framework pool, a fixed HBM budget) and callers in
