@@ -16,6 +16,7 @@
 //      2^k A - (2 M1 +- 1) B (division) or 2^k A - (2 M1 +- 1)^2 (square root), computed
 //      modulo 2^64 because their magnitudes are below 2^63, decide between M1 - 1, M1 and
 //      M1 + 1, with ties to even.
+// Exact scalings by 2^-1, 2^-2, 2^-3 and 2 (scale_down, scale_up1) are exponent steps here.
 // Operands that are zero, subnormal, infinite or NaN, negative square-root operands and quotients
 // outside the normal range take the hardware instruction instead (the caller's fallback).
 // The same source compiles for the host, where the FP32 seeds are the IEEE float operations
@@ -178,6 +179,26 @@ CATO_HD uint64_t sqrt_bits(uint64_t ua, bool& ok) {
   ok = (ea - 1u < 2046u) && !(ua >> 63);
   const uint32_t Ef = 512u + ((ea - odd) >> 1);  // 1049 + (ea - 1075 - odd) / 2
   return (((uint64_t)Ef << 52) + (M - kHid));
+}
+
+// x * 2^-K (K = 1, 2, 3) and x * 2, equal to the IEEE products: an exponent step when the
+// result is normal; below the normal range the significand is shifted with round-to-nearest-even;
+// 2x overflows to infinity; infinities and NaN pass through.
+template <int K> CATO_HD double scale_down(double x) {
+  const uint64_t u = bits_of(x), a = u & 0x7fffffffffffffffULL;
+  const uint32_t e = (uint32_t)(a >> 52);
+  if (e > (uint32_t)K) return e == 0x7ffu ? x : double_of(u - ((uint64_t)K << 52));
+  const uint64_t n = e == 0u ? a : (((a & kFrac) | kHid) << (e - 1u));  // |x| = n 2^-1074
+  const uint64_t q = n >> K, rem = n & ((1ULL << K) - 1ULL), h = 1ULL << (K - 1);
+  const uint64_t r = q + ((rem > h || (rem == h && (q & 1ULL))) ? 1ULL : 0ULL);
+  return double_of((u & 0x8000000000000000ULL) | r);
+}
+CATO_HD double scale_up1(double x) {
+  const uint64_t u = bits_of(x), a = u & 0x7fffffffffffffffULL, s = u & 0x8000000000000000ULL;
+  const uint32_t e = (uint32_t)(a >> 52);
+  if (e == 0u) return double_of(s | (a << 1));  // zero or subnormal: exact
+  if (e >= 0x7feu) return e == 0x7ffu ? x : double_of(s | 0x7ff0000000000000ULL);
+  return double_of(u + (1ULL << 52));
 }
 
 }  // namespace intdiv

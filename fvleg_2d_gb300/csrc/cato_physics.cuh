@@ -128,6 +128,35 @@ template <> __device__ __forceinline__ df fsign1<df>(df x) {
   return signbit(x.hi) ? df(-1.0f) : df(1.0f);
 }
 
+// R(0.5) * x, R(0.25) * x, R(0.125) * x, R(2) * x
+template <typename R> __device__ __forceinline__ R half(R x) { return R(0.5) * x; }
+template <typename R> __device__ __forceinline__ R quarter(R x) { return R(0.25) * x; }
+template <typename R> __device__ __forceinline__ R eighth(R x) { return R(0.125) * x; }
+template <typename R> __device__ __forceinline__ R twice(R x) { return R(2) * x; }
+// FP64: exact scalings on the integer pipe (intdiv::scale_down / scale_up1)
+template <> __device__ __forceinline__ double half<double>(double x) {
+  return intdiv::scale_down<1>(x);
+}
+template <> __device__ __forceinline__ double quarter<double>(double x) {
+  return intdiv::scale_down<2>(x);
+}
+template <> __device__ __forceinline__ double eighth<double>(double x) {
+  return intdiv::scale_down<3>(x);
+}
+template <> __device__ __forceinline__ double twice<double>(double x) { return intdiv::scale_up1(x); }
+
+// a + b * R(0): the reference's products with the zero component of an axis-aligned unit normal.
+// FP64 on the integer pipe: b * 0 is the zero with the sign of b when b is finite (NaN
+// otherwise), and a + (+-0) is a unless a is a zero, where -0 results only from -0 + -0.
+template <typename R> __device__ __forceinline__ R add_mul0(R a, R b) { return a + b * R(0); }
+template <> __device__ __forceinline__ double add_mul0<double>(double a, double b) {
+  const unsigned long long ua = (unsigned long long)__double_as_longlong(a);
+  const unsigned long long ub = (unsigned long long)__double_as_longlong(b);
+  if ((ub << 1) >= 0xffe0000000000000ULL) return a + b * 0.0;  // b infinite or NaN
+  if ((ua << 1) != 0ULL) return a;
+  return ((ua & ub) >> 63) ? -0.0 : 0.0;
+}
+
 // |x| < c for c > 0 without an FP compare: bit patterns of non-negative IEEE values order like
 // unsigned integers and NaN compares false, as the reference's ABS(x) < c does.
 __device__ __forceinline__ bool abs_lt(double x, double c) {
@@ -207,7 +236,7 @@ __device__ __forceinline__ void prim_from_cons(double g, double g1, double r, do
   double e = abs_lt(rE, TINY) ? 0.0 : div_rn(rE, r);
   double s = u * u + v * v;
   if (abs_lt(s, EPS)) s = 0.0;
-  double h = s * 0.5;
+  double h = half(s);
   double dd = e - h;
   if (abs_lt(dd, EPS)) dd = 0.0;
   p = (r * g1) * dd;
@@ -252,7 +281,7 @@ __device__ __forceinline__ void prim_from_cons(df g, df g1, df r, df ru, df rv, 
 template <typename R>
 __device__ __forceinline__ R tvd_phi(int lim, R r) {
   if (lim == LIM_MINMOD) return rmax(R(0), rmin(r, R(1)));
-  if (lim == LIM_SUPERBEE) return rmax(rmax(R(0), rmin(R(2) * r, R(1))), rmin(r, R(2)));
+  if (lim == LIM_SUPERBEE) return rmax(rmax(R(0), rmin(twice(r), R(1))), rmin(r, R(2)));
   // "vanleer" (muscl_tvd2.fypp:199-200); for r <= 0 the numerator r + |r| is +0 and so is
   // the quotient (1 + |r| >= 1): skip the division
   if (nonpos(r)) return R(0);
@@ -275,6 +304,41 @@ __device__ __forceinline__ R tvd_phi_of(int lim, R num, R den) {
   return tvd_phi(lim, Num<R>::div(num, den));
 }
 
+// q + (0.5 phi) d, or q - (0.5 phi) d (minus).  FP64: 0.5 phi is an exponent step, and phi = +0
+// (flat data, or a limiter at zero) gives the product +-0 with the sign of d (d finite), so the
+// sum is q itself unless q is a signed zero, where IEEE gives -0 only for -0 + -0.
+template <typename R>
+__device__ __forceinline__ R slope_step(R q, R phi, R d, bool minus) {
+  return minus ? q - R(0.5) * phi * d : q + R(0.5) * phi * d;
+}
+template <>
+__device__ __forceinline__ double slope_step<double>(double q, double phi, double d, bool minus) {
+  const unsigned long long bq = (unsigned long long)__double_as_longlong(q);
+  const unsigned long long bd = (unsigned long long)__double_as_longlong(d);
+  if (__double_as_longlong(phi) == 0LL && ((bd << 1) < 0xffe0000000000000ULL)) {
+    if ((bq << 1) != 0ULL) return q;
+    const bool zneg = ((bd >> 63) != 0ULL) != minus;  // the sign of the zero added to q
+    return ((bq >> 63) && zneg) ? -0.0 : 0.0;
+  }
+  const double t = half(phi) * d;
+  return minus ? q - t : q + t;
+}
+
+// phi(d0 / (dq + 1e-16)).  FP64: d0 = +-0 over a finite dq gives r = +-0 (the denominator is
+// finite and non-zero: |dq| is 0 or at least epsilon after the flush) and phi(+-0) = +0 for
+// every limiter, without the regularising addition.
+template <typename R>
+__device__ __forceinline__ R tvd_phi_edge(int lim, R d0, R dq) {
+  return tvd_phi_of(lim, d0, dq + R(1e-16));
+}
+template <>
+__device__ __forceinline__ double tvd_phi_edge<double>(int lim, double d0, double dq) {
+  const unsigned long long b0 = (unsigned long long)__double_as_longlong(d0);
+  const unsigned long long bq = (unsigned long long)__double_as_longlong(dq);
+  if ((b0 << 1) == 0ULL && (bq << 1) < 0xffe0000000000000ULL) return 0.0;
+  return tvd_phi_of(lim, d0, dq + 1e-16);
+}
+
 template <typename R>
 __device__ __forceinline__ void recon_tvd2(int lim, R qm1, R q0, R qp1, R qp2, R& L, R& Rr) {
   const R EPS = Num<R>::eps;
@@ -284,10 +348,8 @@ __device__ __forceinline__ void recon_tvd2(int lim, R qm1, R q0, R qp1, R qp2, R
     if (abs_lt(d0, EPS)) d0 = R(0);
     if (abs_lt(dp, EPS)) dp = R(0);
   }
-  R phi = tvd_phi_of(lim, d0, dm + R(1e-16));
-  L = q0 + R(0.5) * phi * dm;
-  phi = tvd_phi_of(lim, d0, dp + R(1e-16));
-  Rr = qp1 - R(0.5) * phi * dp;
+  L = slope_step(q0, tvd_phi_edge(lim, d0, dm), dm, false);
+  Rr = slope_step(qp1, tvd_phi_edge(lim, d0, dp), dp, true);
 }
 
 // FP32 (mixed path): the limited slope phi(r) * dq without the ratio.  For r = d0/dq > 0,
@@ -372,26 +434,26 @@ __device__ __forceinline__ void recon_mlp(R qm2, R qm1, R q0, R qp1, R qp2, R qp
                          R(30));
       }
     } else {
-      if (!zL) bL = Num<R>::div(R(1) + R(2) * rL, R(3));
-      if (!zR) bR = Num<R>::div(R(1) + R(2) * rR_p1, R(3));
+      if (!zL) bL = Num<R>::div(R(1) + twice(rL), R(3));
+      if (!zR) bR = Num<R>::div(R(1) + twice(rR_p1), R(3));
     }
     R tt = Num<R>::div(rabs(t0p - t0m), rabs(qp1 - qm1) + S);
     R tt1 = Num<R>::div(rabs(t1p - t1m), rabs(qp2 - q0) + S);
     if (!zL) {
-      R aLt = Num<R>::div(R(2) * rmax(R(1), rL) * (R(1) + rmax(R(0), Num<R>::div(tt1, rR_p1 + S))),
+      R aLt = Num<R>::div(twice(rmax(R(1), rL)) * (R(1) + rmax(R(0), Num<R>::div(tt1, rR_p1 + S))),
                           R(1) + tt);
       R aL = rmax(R(1), rmin(R(2), aLt));
       phiL = rmax(R(0), rmin(rmin(aL * rL, aL), bL));
     }
     if (!zR) {
-      R aRt = Num<R>::div(R(2) * rmax(R(1), rR_p1) * (R(1) + rmax(R(0), Num<R>::div(tt, rL + S))),
+      R aRt = Num<R>::div(twice(rmax(R(1), rR_p1)) * (R(1) + rmax(R(0), Num<R>::div(tt, rL + S))),
                           R(1) + tt1);
       R aR = rmax(R(1), rmin(R(2), aRt));
       phiR = rmax(R(0), rmin(rmin(aR * rR_p1, aR), bR));
     }
   }
-  L = q0 + R(0.5) * phiL * dm;
-  Rr = qp1 - R(0.5) * phiR * dp;
+  L = slope_step(q0, phiL, dm, false);
+  Rr = slope_step(qp1, phiR, dp, true);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -538,22 +600,22 @@ template <typename R> struct Prim { R r, u, v, p; };
 
 // AUSMPW+ split functions, ausmpw_plus_solver.fypp:486-530 (alpha = 1/8)
 template <typename R> __device__ __forceinline__ R aw_p_plus(R M) {
-  if (rabs(M) > R(1)) return R(0.5) * (R(1) + fsign1(M));
-  return R(0.25) * ((M + R(1)) * (M + R(1))) * (R(2) - M) +
-         R(0.125) * M * ((M * M - R(1)) * (M * M - R(1)));
+  if (rabs(M) > R(1)) return half(R(1) + fsign1(M));
+  return quarter((M + R(1)) * (M + R(1))) * (R(2) - M) +
+         eighth(M) * ((M * M - R(1)) * (M * M - R(1)));
 }
 template <typename R> __device__ __forceinline__ R aw_p_minus(R M) {
-  if (rabs(M) > R(1)) return R(0.5) * (R(1) - fsign1(M));
-  return R(0.25) * ((M - R(1)) * (M - R(1))) * (R(2) + M) -
-         R(0.125) * M * ((M * M - R(1)) * (M * M - R(1)));
+  if (rabs(M) > R(1)) return half(R(1) - fsign1(M));
+  return quarter((M - R(1)) * (M - R(1))) * (R(2) + M) -
+         eighth(M) * ((M * M - R(1)) * (M * M - R(1)));
 }
 template <typename R> __device__ __forceinline__ R aw_m_plus(R M) {
-  if (rabs(M) > R(1)) return R(0.5) * (M + rabs(M));
-  return R(0.25) * ((M + R(1)) * (M + R(1)));
+  if (rabs(M) > R(1)) return half(M + rabs(M));
+  return quarter((M + R(1)) * (M + R(1)));
 }
 template <typename R> __device__ __forceinline__ R aw_m_minus(R M) {
-  if (rabs(M) > R(1)) return R(0.5) * (M - rabs(M));
-  return -(R(0.25) * ((M - R(1)) * (M - R(1))));
+  if (rabs(M) > R(1)) return half(M - rabs(M));
+  return -quarter((M - R(1)) * (M - R(1)));
 }
 
 // AUSMPW+, ausmpw_plus_solver.fypp:336-459.  pc[4] = p1_L, p1_R, p2_L, p2_R (:430-442).
@@ -571,19 +633,19 @@ __device__ __forceinline__ void flux_ausmpw(const FluxConsts<R>& K, const Prim<R
   R M_RHS = Num<R>::div(Num<R>::sqrt(u_RHS * u_RHS + v_RHS * v_RHS), cs_R);
   if (K.low_mach_fix && (rabs(M_LHS) < R(0.1) || rabs(M_RHS) < R(0.1))) {  // LOW_MACH
     R f_M = rmin(R(1), rmax(M_LHS, M_RHS));
-    R uLf = R(0.5) * (u_LHS + u_RHS) + f_M * R(0.5) * (u_LHS - u_RHS);
-    R uRf = R(0.5) * (u_LHS + u_RHS) - f_M * R(0.5) * (u_LHS - u_RHS);
-    R vLf = R(0.5) * (v_LHS + v_RHS) + f_M * R(0.5) * (v_LHS - v_RHS);
-    R vRf = R(0.5) * (v_LHS + v_RHS) - f_M * R(0.5) * (v_LHS - v_RHS);
+    R uLf = half(u_LHS + u_RHS) + half(f_M) * (u_LHS - u_RHS);
+    R uRf = half(u_LHS + u_RHS) - half(f_M) * (u_LHS - u_RHS);
+    R vLf = half(v_LHS + v_RHS) + half(f_M) * (v_LHS - v_RHS);
+    R vRf = half(v_LHS + v_RHS) - half(f_M) * (v_LHS - v_RHS);
     u_LHS = uLf; u_RHS = uRf; v_LHS = vLf; v_RHS = vRf;
   }
   const R gg = R(K.g_over_gm1);
-  R H_L = gg * Num<R>::div(p_L, rho_L) + R(0.5) * (u_LHS * u_LHS + v_LHS * v_LHS);
-  R H_R = gg * Num<R>::div(p_R, rho_R) + R(0.5) * (u_RHS * u_RHS + v_RHS * v_RHS);
-  R H_normal = rmin(H_L - R(0.5) * (V_L * V_L), H_R - R(0.5) * (V_R * V_R));
+  R H_L = gg * Num<R>::div(p_L, rho_L) + half(u_LHS * u_LHS + v_LHS * v_LHS);
+  R H_R = gg * Num<R>::div(p_R, rho_R) + half(u_RHS * u_RHS + v_RHS * v_RHS);
+  R H_normal = rmin(H_L - half(V_L * V_L), H_R - half(V_R * V_R));
   R c_s = Num<R>::sqrt(R(K.two_gm1_over_gp1) * H_normal);
   R c_half;
-  if (R(0.5) * (U_L + U_R) < R(0)) c_half = Num<R>::div(c_s * c_s, rmax(rabs(U_R), c_s));
+  if (half(U_L + U_R) < R(0)) c_half = Num<R>::div(c_s * c_s, rmax(rabs(U_R), c_s));
   else c_half = Num<R>::div(c_s * c_s, rmax(rabs(U_L), c_s));
   R M_L = Num<R>::div(U_L, c_half);
   R M_R = Num<R>::div(U_R, c_half);
@@ -634,25 +696,25 @@ __device__ __forceinline__ void flux_ausmpw(const FluxConsts<R>& K, const Prim<R
 // U_L/U_R/V_L/V_R are taken before the low-Mach fix, as in the reference.
 template <typename R>
 __device__ __forceinline__ R mausm_p_plus(R M) {
-  if (rabs(M) > R(1)) return R(0.5) * (R(1) + fsign1(M));
-  return R(0.25) * ((M + R(1)) * (M + R(1))) * (R(2) - M);
+  if (rabs(M) > R(1)) return half(R(1) + fsign1(M));
+  return quarter((M + R(1)) * (M + R(1))) * (R(2) - M);
 }
 template <typename R>
 __device__ __forceinline__ R mausm_p_minus(R M) {
-  if (rabs(M) > R(1)) return R(0.5) * (R(1) - fsign1(M));
-  return R(0.25) * ((M - R(1)) * (M - R(1))) * (R(2) + M);
+  if (rabs(M) > R(1)) return half(R(1) - fsign1(M));
+  return quarter((M - R(1)) * (M - R(1))) * (R(2) + M);
 }
 template <typename R>
 __device__ __forceinline__ R mausm_phi_L(R pL, R pR, R pLsb, R a) {
   if (rabs(pR - pL) < R(1) || rabs(pLsb - pL) < Num<R>::eps) return pL;
   return pL + Num<R>::div(rmax(R(0), (pR - pL) * (pLsb - pL)), (pR - pL) * rabs(pLsb - pL)) *
-                  rmin(rmin(a, R(0.5) * rabs(pR - pL)), rabs(pLsb - pL));
+                  rmin(rmin(a, half(rabs(pR - pL))), rabs(pLsb - pL));
 }
 template <typename R>
 __device__ __forceinline__ R mausm_phi_R(R pL, R pR, R pRsb, R a) {
   if (rabs(pL - pR) < Num<R>::eps || rabs(pRsb - pR) < R(1)) return pR;
   return pR + Num<R>::div(rmax(R(0), (pL - pR) * (pRsb - pR)), (pL - pR) * rabs(pRsb - pR)) *
-                  rmin(rmin(a, R(0.5) * rabs(pL - pR)), rabs(pRsb - pR));
+                  rmin(rmin(a, half(rabs(pL - pR))), rabs(pRsb - pR));
 }
 
 template <typename R, int DIR>
@@ -672,19 +734,19 @@ __device__ __forceinline__ void flux_mausmpw(const FluxConsts<R>& K, const Prim<
   R M_RHS = Num<R>::div(Num<R>::sqrt(u_RHS * u_RHS + v_RHS * v_RHS), cs_R);
   if (K.low_mach_fix && (rabs(M_LHS) < R(0.1) || rabs(M_RHS) < R(0.1))) {  // LOW_MACH
     R f_M = rmin(R(1), rmax(M_LHS, M_RHS));
-    R uLf = R(0.5) * (u_LHS + u_RHS) + f_M * R(0.5) * (u_LHS - u_RHS);
-    R uRf = R(0.5) * (u_LHS + u_RHS) - f_M * R(0.5) * (u_LHS - u_RHS);
-    R vLf = R(0.5) * (v_LHS + v_RHS) + f_M * R(0.5) * (v_LHS - v_RHS);
-    R vRf = R(0.5) * (v_LHS + v_RHS) - f_M * R(0.5) * (v_LHS - v_RHS);
+    R uLf = half(u_LHS + u_RHS) + half(f_M) * (u_LHS - u_RHS);
+    R uRf = half(u_LHS + u_RHS) - half(f_M) * (u_LHS - u_RHS);
+    R vLf = half(v_LHS + v_RHS) + half(f_M) * (v_LHS - v_RHS);
+    R vRf = half(v_LHS + v_RHS) - half(f_M) * (v_LHS - v_RHS);
     u_LHS = uLf; u_RHS = uRf; v_LHS = vLf; v_RHS = vRf;
   }
   const R gg = R(K.g_over_gm1);
-  R H_L = gg * Num<R>::div(p_L, rho_L) + R(0.5) * (u_LHS * u_LHS + v_LHS * v_LHS);
-  R H_R = gg * Num<R>::div(p_R, rho_R) + R(0.5) * (u_RHS * u_RHS + v_RHS * v_RHS);
-  R H_normal = rmin(H_L - R(0.5) * (V_L * V_L), H_R - R(0.5) * (V_R * V_R));
+  R H_L = gg * Num<R>::div(p_L, rho_L) + half(u_LHS * u_LHS + v_LHS * v_LHS);
+  R H_R = gg * Num<R>::div(p_R, rho_R) + half(u_RHS * u_RHS + v_RHS * v_RHS);
+  R H_normal = rmin(H_L - half(V_L * V_L), H_R - half(V_R * V_R));
   R c_s = Num<R>::sqrt(R(K.two_gm1_over_gp1) * H_normal);
   R c_half;
-  if (R(0.5) * (U_L + U_R) < R(0)) c_half = Num<R>::div(c_s * c_s, rmax(rabs(U_R), c_s));
+  if (half(U_L + U_R) < R(0)) c_half = Num<R>::div(c_s * c_s, rmax(rabs(U_R), c_s));
   else c_half = Num<R>::div(c_s * c_s, rmax(rabs(U_L), c_s));
   R M_L = Num<R>::div(U_L, c_half);
   R M_R = Num<R>::div(U_R, c_half);
@@ -724,8 +786,8 @@ __device__ __forceinline__ void flux_mausmpw(const FluxConsts<R>& K, const Prim<
   R uLh = mausm_phi_L(u_LHS, u_RHS, As.u, a), uRh = mausm_phi_R(u_LHS, u_RHS, Bs.u, a);
   R vLh = mausm_phi_L(v_LHS, v_RHS, As.v, a), vRh = mausm_phi_R(v_LHS, v_RHS, Bs.v, a);
   R pLh = mausm_phi_L(p_L, p_R, As.p, a), pRh = mausm_phi_R(p_L, p_R, Bs.p, a);
-  R H_Lh = gg * Num<R>::div(pLh, rLh) + R(0.5) * (uLh * uLh + vLh * vLh);
-  R H_Rh = gg * Num<R>::div(pRh, rRh) + R(0.5) * (uRh * uRh + vRh * vRh);
+  R H_Lh = gg * Num<R>::div(pLh, rLh) + half(uLh * uLh + vLh * vLh);
+  R H_Rh = gg * Num<R>::div(pRh, rRh) + half(uRh * uRh + vRh * vRh);
   R mL = Mb_L * c_half * rLh;
   R mR = Mb_R * c_half * rRh;
   if (rabs(mL + mR) < EPSF) { mL = R(0); mR = R(0); }
@@ -751,26 +813,26 @@ __device__ __forceinline__ void flux_slau(const FluxConsts<R>& K, const Prim<R>&
   R rho_L = A.r, u_L = A.u, v_L = A.v, p_L = A.p;
   R rho_R = B.r, u_R = B.u, v_R = B.v, p_R = B.p;
   // V_n = u*n_x + v*n_y with an exact unit normal
-  R Vp = DIR == 0 ? u_L + v_L * R(0) : u_L * R(0) + v_L;
-  R Vm = DIR == 0 ? u_R + v_R * R(0) : u_R * R(0) + v_R;
+  R Vp = DIR == 0 ? add_mul0(u_L, v_L) : add_mul0(v_L, u_L);
+  R Vm = DIR == 0 ? add_mul0(u_R, v_R) : add_mul0(v_R, u_R);
   R c_plus = Num<R>::sqrt(Num<R>::div(g * p_L, rho_L));
   R c_minus = Num<R>::sqrt(Num<R>::div(g * p_R, rho_R));
-  R c_bar = R(0.5) * (c_plus + c_minus);
+  R c_bar = half(c_plus + c_minus);
   R V_n_bar = Num<R>::div(rho_L * rabs(Vp) + rho_R * rabs(Vm), rho_L + rho_R);
-  R vel2 = R(0.5) * (u_L * u_L + v_L * v_L + u_R * u_R + v_R * v_R);
+  R vel2 = half(u_L * u_L + v_L * v_L + u_R * u_R + v_R * v_R);
   R M_hat = rmin(R(1), Num<R>::div(Num<R>::sqrt(vel2), c_bar));
   R M_bar = Num<R>::div(V_n_bar, c_bar);
   R M_plus = Num<R>::div(Vp, c_bar);
   R M_minus = Num<R>::div(Vm, c_bar);
   R Chi = (R(1) - M_hat) * (R(1) - M_hat);
-  R p_bar = R(0.5) * (p_L + p_R);
-  R rho_bar = R(0.5) * (rho_L + rho_R);
+  R p_bar = half(p_L + p_R);
+  R rho_bar = half(rho_L + rho_R);
   R B_plus, B_minus;
-  if (rabs(M_plus) < R(1)) B_plus = R(0.25) * (R(2) - M_plus) * ((M_plus + R(1)) * (M_plus + R(1)));
-  else B_plus = R(0.5) * (R(1) + fsign1(M_plus));
+  if (rabs(M_plus) < R(1)) B_plus = quarter(R(2) - M_plus) * ((M_plus + R(1)) * (M_plus + R(1)));
+  else B_plus = half(R(1) + fsign1(M_plus));
   if (rabs(M_minus) < R(1))
-    B_minus = R(0.25) * (R(2) + M_minus) * ((M_minus - R(1)) * (M_minus - R(1)));
-  else B_minus = R(0.5) * (R(1) + fsign1(-M_minus));
+    B_minus = quarter(R(2) + M_minus) * ((M_minus - R(1)) * (M_minus - R(1)));
+  else B_minus = half(R(1) + fsign1(-M_minus));
   R delta_p = p_R - p_L;
   if (abs_lt(delta_p, EPS) || rabs(delta_p) < THRESHOLD * p_bar) delta_p = R(0);
   R delta_rho = rho_R - rho_L;
@@ -796,25 +858,25 @@ __device__ __forceinline__ void flux_slau(const FluxConsts<R>& K, const Prim<R>&
   }
   R p_tilde;
   if (VARIANT == FLUX_SLAU || VARIANT == FLUX_SD_SLAU)
-    p_tilde = (p_bar + R(0.5) * delta_B * pLmR) + (R(1) - Chi) * (B_plus + B_minus - R(1)) * p_bar;
+    p_tilde = (p_bar + half(delta_B) * pLmR) + (R(1) - Chi) * (B_plus + B_minus - R(1)) * p_bar;
   else
-    p_tilde = p_bar + (R(0.5) * delta_B * pLmR) +
+    p_tilde = p_bar + (half(delta_B) * pLmR) +
               Num<R>::sqrt(vel2) * (B_plus + B_minus - R(1)) * rho_bar * c_bar;
   R gg = -(rmax(rmin(M_plus, R(0)), R(-1)) * rmin(rmax(M_minus, R(0)), R(1)));
   R diss = (VARIANT == FLUX_SLAU || VARIANT == FLUX_SLAU2) ? Chi : theta;
-  R mf = R(0.5) * ((rho_L * Vp) + (rho_R * Vm) - rabs(V_n_bar) * delta_rho) * (R(1) - gg) -
-         (Num<R>::div(diss, R(2) * c_bar) * delta_p);
-  R mL = R(0.5) * (mf + rabs(mf));
-  R mR = R(0.5) * (mf - rabs(mf));
+  R mf = half((rho_L * Vp) + (rho_R * Vm) - rabs(V_n_bar) * delta_rho) * (R(1) - gg) -
+         (Num<R>::div(diss, twice(c_bar)) * delta_p);
+  R mL = half(mf + rabs(mf));
+  R mR = half(mf - rabs(mf));
   const R gq = R(K.g_over_gm1);
-  R H_L = gq * Num<R>::div(p_L, rho_L) + R(0.5) * (u_L * u_L + v_L * v_L);
-  R H_R = gq * Num<R>::div(p_R, rho_R) + R(0.5) * (u_R * u_R + v_R * v_R);
+  R H_L = gq * Num<R>::div(p_L, rho_L) + half(u_L * u_L + v_L * v_L);
+  R H_R = gq * Num<R>::div(p_R, rho_R) + half(u_R * u_R + v_R * v_R);
   F[0] = mL + mR;
   if (DIR == 0) {
     F[1] = (mL * u_L) + (mR * u_R) + p_tilde;
-    F[2] = (mL * v_L) + (mR * v_R) + p_tilde * R(0);
+    F[2] = add_mul0((mL * v_L) + (mR * v_R), p_tilde);
   } else {
-    F[1] = (mL * u_L) + (mR * u_R) + p_tilde * R(0);
+    F[1] = add_mul0((mL * u_L) + (mR * u_R), p_tilde);
     F[2] = (mL * v_L) + (mR * v_R) + p_tilde;
   }
   F[3] = (mL * H_L) + (mR * H_R);
@@ -826,70 +888,80 @@ template <typename R, int DIR>
 __device__ __forceinline__ void flux_roe(const FluxConsts<R>& K, const Prim<R>& A, const Prim<R>& B,
                                          const R fa[5], const R fb[5], R F[4]) {
   const R g = R(K.gamma);
-  const R nx = DIR == 0 ? R(1) : R(0), ny = DIR == 0 ? R(0) : R(1);
   R rl = rabs(A.r), ul = A.u, vl = A.v, pl = rabs(A.p);
   R rr = rabs(B.r), ur = B.u, vr = B.v, pr = rabs(B.p);
   const R gq = R(K.g_over_gm1);
   R rav = Num<R>::sqrt(rl * rr);
   R q_pl = Num<R>::div(pl, rl), q_rav = Num<R>::div(rav, rl), q_gpl = Num<R>::div(g * pl, rl);
-  R hl = gq * q_pl + R(0.5) * (ul * ul + vl * vl);
-  R hr = gq * Num<R>::div(pr, rr) + R(0.5) * (ur * ur + vr * vr);
+  R hl = gq * q_pl + half(ul * ul + vl * vl);
+  R hr = gq * Num<R>::div(pr, rr) + half(ur * ur + vr * vr);
   R gam1 = R(K.gm1);
   R dd = q_rav;
   R dd1 = Num<R>::div(R(1), R(1) + dd);
   R uav = (ul + dd * ur) * dd1;
   R vav = (vl + dd * vr) * dd1;
   R hav = (hl + dd * hr) * dd1;
-  R q2a = R(0.5) * (uav * uav + vav * vav);
+  R q2a = half(uav * uav + vav * vav);
   R c2a = gam1 * (hav - q2a);
   R cav = Num<R>::sqrt(c2a);
-  R uv = uav * nx + vav * ny;
-  R du = (ur - ul) * nx + (vr - vl) * ny;
-  R du_trans = -((ur - ul) * ny) + (vr - vl) * nx;
+  // x n_x + y n_y with the unit normal's exact 1 and 0 (a product with 1 is the operand)
+  auto dotn = [](R x, R y) { return DIR == 0 ? add_mul0(x, y) : add_mul0(y, x); };
+  R uv = dotn(uav, vav);
+  R du = dotn(ur - ul, vr - vl);
+  R du_trans = DIR == 0 ? add_mul0(vr - vl, -(ur - ul)) : add_mul0(-(ur - ul), vr - vl);
   R cs_R = Num<R>::sqrt(Num<R>::div(g * pr, rr));
   R cs_L = Num<R>::sqrt(q_gpl);
-  R h1 = rabs(rmin(uv - cav, (ul * nx + vl * ny) - cs_L));
+  R h1 = rabs(rmin(uv - cav, dotn(ul, vl) - cs_L));
   R h2 = rabs(uv);
-  R h4 = rabs(rmax(uv + cav, (ur * nx + vr * ny) + cs_R));
+  R h4 = rabs(rmax(uv + cav, dotn(ur, vr) + cs_R));
   R e1 = h1, e2 = h2, e4 = h4;
   if (K.harten) {
     R delta = R(K.harten_delta) * cav;
-    e1 = (h1 > delta) ? h1 : Num<R>::div(R(0.5) * (h1 * h1 + delta * delta), delta);
-    e2 = (h2 > delta) ? h2 : Num<R>::div(R(0.5) * (h2 * h2 + delta * delta), delta);
-    e4 = (h4 > delta) ? h4 : Num<R>::div(R(0.5) * (h4 * h4 + delta * delta), delta);
+    e1 = (h1 > delta) ? h1 : Num<R>::div(half(h1 * h1 + delta * delta), delta);
+    e2 = (h2 > delta) ? h2 : Num<R>::div(half(h2 * h2 + delta * delta), delta);
+    e4 = (h4 > delta) ? h4 : Num<R>::div(half(h4 * h4 + delta * delta), delta);
   }
   h1 = rav * cav * du;
-  h2 = Num<R>::div(e1 * (pr - pl - h1), R(2) * c2a);
+  h2 = Num<R>::div(e1 * (pr - pl - h1), twice(c2a));
   R h3 = e2 * (rr - rl - Num<R>::div(pr - pl, c2a));
   h4 = e2 * rav;
-  R h5 = Num<R>::div(e4 * (pr - pl + h1), R(2) * c2a);
+  R h5 = Num<R>::div(e4 * (pr - pl + h1), twice(c2a));
   R psi = Num<R>::div(rabs(cs_R - cs_L), rmax(cs_R, cs_L));
-  R FR0 = rr * uv, FR1 = rr * ur * uv + nx * pr, FR2 = rr * vr * uv + ny * pr, FR3 = rr * hr * uv;
-  R FL0 = rl * uv, FL1 = rl * ul * uv + nx * pl, FL2 = rl * vl * uv + ny * pl, FL3 = rl * hl * uv;
+  // the normal-direction terms carry the exact 1, the tangential ones the exact 0
+  auto on = [](bool axis, R a, R b) { return axis ? a + b : add_mul0(a, b); };
+  R FR0 = rr * uv, FR1 = on(DIR == 0, rr * ur * uv, pr), FR2 = on(DIR == 1, rr * vr * uv, pr);
+  R FR3 = rr * hr * uv;
+  R FL0 = rl * uv, FL1 = on(DIR == 0, rl * ul * uv, pl), FL2 = on(DIR == 1, rl * vl * uv, pl);
+  R FL3 = rl * hl * uv;
   R m0 = (h2 + h3 + h5);
-  R m1 = (h2 * (uav - cav * nx) + h3 * uav + h4 * (ur - ul - du * nx) + h5 * (uav + cav * nx));
-  R m2 = (h2 * (vav - cav * ny) + h3 * vav + h4 * (vr - vl - du * ny) + h5 * (vav + cav * ny));
+  R m1 = (h2 * on(DIR == 0, uav, -cav) + h3 * uav + h4 * on(DIR == 0, ur - ul, -du) +
+          h5 * on(DIR == 0, uav, cav));
+  R m2 = (h2 * on(DIR == 1, vav, -cav) + h3 * vav + h4 * on(DIR == 1, vr - vl, -du) +
+          h5 * on(DIR == 1, vav, cav));
   R m3 = (h2 * (hav - cav * uv) + h3 * q2a + h4 * (uav * (ur - ul) + vav * (vr - vl) - uv * du) +
           h5 * (hav + cav * uv));
-  F[0] = R(0.5) * (FR0 + FL0 - m0);
-  F[1] = R(0.5) * (FR1 + FL1 - m1);
-  F[2] = R(0.5) * (FR2 + FL2 - m2);
-  F[3] = R(0.5) * (FR3 + FL3 - m3);
+  F[0] = half(FR0 + FL0 - m0);
+  F[1] = half(FR1 + FL1 - m1);
+  F[2] = half(FR2 + FL2 - m2);
+  F[3] = half(FR3 + FL3 - m3);
   R fmax = R(0);
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     R ratio = Num<R>::div(rabs(fb[k] - fa[k]), rmin(fb[k], fa[k]) + R(1e-16));
     fmax = rmax(fmax, (ratio < R(1)) ? R(0) : R(1));
   }
-  F[1] = F[1] - R(0.5) * fmax * rav * cav * (-(du_trans * ny) + psi * du * nx);
-  F[2] = F[2] - R(0.5) * fmax * rav * cav * (du_trans * nx + psi * du * ny);
+  // -(du_trans n_y) + psi du n_x and du_trans n_x + psi du n_y
+  const R c1 = DIR == 0 ? add_mul0(psi * du, -du_trans) : add_mul0(-du_trans, psi * du);
+  const R c2 = DIR == 0 ? add_mul0(du_trans, psi * du) : add_mul0(psi * du, du_trans);
+  F[1] = F[1] - half(fmax) * rav * cav * c1;
+  F[2] = F[2] - half(fmax) * rav * cav * c2;
 }
 
 // AUSM+-up (basic), ausm_plus_solver.f90:499-643 + upwinding of the commented driver :313-325.
-template <typename R> __device__ __forceinline__ R up_m1p(R M) { return R(0.5) * (M + rabs(M)); }
-template <typename R> __device__ __forceinline__ R up_m1m(R M) { return R(0.5) * (M - rabs(M)); }
-template <typename R> __device__ __forceinline__ R up_m2p(R M) { return R(0.25) * ((M + R(1)) * (M + R(1))); }
-template <typename R> __device__ __forceinline__ R up_m2m(R M) { return -(R(0.25) * ((M - R(1)) * (M - R(1)))); }
+template <typename R> __device__ __forceinline__ R up_m1p(R M) { return half(M + rabs(M)); }
+template <typename R> __device__ __forceinline__ R up_m1m(R M) { return half(M - rabs(M)); }
+template <typename R> __device__ __forceinline__ R up_m2p(R M) { return quarter((M + R(1)) * (M + R(1))); }
+template <typename R> __device__ __forceinline__ R up_m2m(R M) { return -quarter((M - R(1)) * (M - R(1))); }
 
 template <typename R, int DIR>
 __device__ __forceinline__ void flux_ausm_up(const FluxConsts<R>& K, const Prim<R>& A,
@@ -897,11 +969,11 @@ __device__ __forceinline__ void flux_ausm_up(const FluxConsts<R>& K, const Prim<
   const R EPS = Num<R>::eps;
   const R alpha = R(3.0 / 16.0);
   const R gamma_factor = R(K.gamma_factor);
-  R vel_L = DIR == 0 ? A.u + A.v * R(0) : A.u * R(0) + A.v;
-  R vel_R = DIR == 0 ? B.u + B.v * R(0) : B.u * R(0) + B.v;
+  R vel_L = DIR == 0 ? add_mul0(A.u, A.v) : add_mul0(A.v, A.u);
+  R vel_R = DIR == 0 ? add_mul0(B.u, B.v) : add_mul0(B.v, B.u);
   const R gq = R(K.g_over_gm1);
-  R H_L = Num<R>::div(A.p, A.r) * gq + R(0.5) * (A.u * A.u + A.v * A.v);
-  R H_R = Num<R>::div(B.p, B.r) * gq + R(0.5) * (B.u * B.u + B.v * B.v);
+  R H_L = Num<R>::div(A.p, A.r) * gq + half(A.u * A.u + A.v * A.v);
+  R H_R = Num<R>::div(B.p, B.r) * gq + half(B.u * B.u + B.v * B.v);
   R a_crit_L = Num<R>::sqrt(gamma_factor * rabs(H_L));
   R a_crit_R = Num<R>::sqrt(gamma_factor * rabs(H_R));
   R a_circ_L = Num<R>::div(a_crit_L * a_crit_L, rmax(a_crit_L, vel_L));
@@ -909,11 +981,11 @@ __device__ __forceinline__ void flux_ausm_up(const FluxConsts<R>& K, const Prim<
   R a_half = rmin(a_circ_L, a_circ_R);
   R M_L = Num<R>::div(vel_L, a_half);
   R M_R = Num<R>::div(vel_R, a_half);
-  R M_bar_sq = R(0.5) * (M_L + M_R);  // as written at ausm_plus_solver.f90:585
+  R M_bar_sq = half(M_L + M_R);  // as written at ausm_plus_solver.f90:585
   const R beta = R(K.ausm_beta);
   R M_plus = (rabs(M_L) >= R(1)) ? up_m1p(M_L) : up_m2p(M_L) * (R(1) - R(16) * beta * up_m2m(M_L));
   R M_minus = (rabs(M_R) >= R(1)) ? up_m1m(M_R) : up_m2m(M_R) * (R(1) + R(16) * beta * up_m2p(M_R));
-  R rho_half = R(0.5) * (B.r + A.r);
+  R rho_half = half(B.r + A.r);
   R M_p;
   if (abs_lt(B.p - A.p, EPS)) M_p = R(0);
   else
@@ -950,16 +1022,16 @@ __device__ __forceinline__ void flux_hllc(const FluxConsts<R>& K, const Prim<R>&
   R qnL = DIR == 0 ? A.u : A.v, qtL = DIR == 0 ? A.v : A.u;
   R qnR = DIR == 0 ? B.u : B.v, qtR = DIR == 0 ? B.v : B.u;
   R cL = Num<R>::sqrt(Num<R>::div(g * A.p, A.r)), cR = Num<R>::sqrt(Num<R>::div(g * B.p, B.r));
-  R rho_bar = R(0.5) * (A.r + B.r), c_bar = R(0.5) * (cL + cR);
-  R p_pvrs = R(0.5) * (A.p + B.p) - R(0.5) * (qnR - qnL) * rho_bar * c_bar;
+  R rho_bar = half(A.r + B.r), c_bar = half(cL + cR);
+  R p_pvrs = half(A.p + B.p) - half(qnR - qnL) * rho_bar * c_bar;
   R p_star = rmax(R(0), p_pvrs);
   const R gf = R(K.hllc_gf);
   R qL = (p_star <= A.p) ? R(1) : Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, A.p) - R(1)));
   R qR = (p_star <= B.p) ? R(1) : Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, B.p) - R(1)));
   R SL = qnL - cL * qL, SR = qnR + cR * qR;
   R EL, ER;
-  EL = Num<R>::div(A.p, R(K.gm1)) + R(0.5) * A.r * (A.u * A.u + A.v * A.v);
-  ER = Num<R>::div(B.p, R(K.gm1)) + R(0.5) * B.r * (B.u * B.u + B.v * B.v);
+  EL = Num<R>::div(A.p, R(K.gm1)) + half(A.r) * (A.u * A.u + A.v * A.v);
+  ER = Num<R>::div(B.p, R(K.gm1)) + half(B.r) * (B.u * B.u + B.v * B.v);
   R S_star = Num<R>::div(B.p - A.p + A.r * qnL * (SL - qnL) - B.r * qnR * (SR - qnR),
                          A.r * (SL - qnL) - B.r * (SR - qnR));
   R Fn[4];

@@ -7,7 +7,7 @@
 // mismatch.  Families: random normal operands over the full exponent range and over a narrow
 // one; significands near powers of two, near each other and with few bits set; quotients and
 // roots next to rounding midpoints; every FP32 seed (all 2^23 truncated significands) with the
-// largest truncation error.
+// largest truncation error; the exact power-of-two scalings.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -103,6 +103,27 @@ int main(int argc, char** argv) {
     check_sqrt(s * s);
   }
   report("sqrt");
+  fail |= bad != 0;
+
+  reset();  // the exact scalings against the products, over all exponent classes
+  for (long i = 0; i < 4 * n; ++i) {
+    const uint64_t u = rng();
+    const uint64_t cls = rng() % 4;
+    double x = double_of(u);
+    if (cls == 1) x = double_of((u & 0x800fffffffffffffULL) | ((rng() % 5) << 52));      // tiny
+    if (cls == 2) x = double_of((u & 0x800fffffffffffffULL) | ((0x7fcULL + rng() % 4) << 52));
+    if (x != x) continue;
+    ++tested;
+    const bool ok = bits_of(scale_down<1>(x)) == bits_of(x * 0.5) &&
+                    bits_of(scale_down<2>(x)) == bits_of(x * 0.25) &&
+                    bits_of(scale_down<3>(x)) == bits_of(x * 0.125) &&
+                    bits_of(scale_up1(x)) == bits_of(x * 2.0);
+    if (!ok) {
+      if (bad < 5) printf("scale mismatch %a\n", x);
+      ++bad;
+    }
+  }
+  report("scale");
   fail |= bad != 0;
 
   reset();  // every seed: b (a) = 1.t followed by 29 one bits (largest truncation), and zeros

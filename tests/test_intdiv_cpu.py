@@ -24,7 +24,7 @@ def checker(tmp_path_factory):
 def test_division_and_sqrt_bit_exact(checker):
     r = subprocess.run([checker, "1000000"], capture_output=True, text=True, timeout=600)
     lines = {ln.split()[0]: ln.split() for ln in r.stdout.splitlines() if " tested " in ln}
-    assert set(lines) == {"div_random", "div_structured", "sqrt", "seeds"}, r.stdout
+    assert set(lines) == {"div_random", "div_structured", "sqrt", "scale", "seeds"}, r.stdout
     for fam, f in lines.items():
         tested, fallback, bad = int(f[2]), int(f[4]), int(f[6])
         assert bad == 0, r.stdout
