@@ -79,7 +79,8 @@ def load(build_if_missing: bool = False):
         "cato_gpu_select_device": (ctypes.c_int, [ctypes.c_int32]),
         "cato_gpu_check_divsqrt": (ctypes.c_int, [ctypes.c_int64, ctypes.c_uint64,
                                                   ctypes.POINTER(ctypes.c_uint64),
-                                                  ctypes.POINTER(ctypes.c_uint64)]),
+                                                  ctypes.POINTER(ctypes.c_uint64),
+                                                  ctypes.POINTER(ctypes.c_int32)]),
         "cato_gpu_set_plan": (ctypes.c_int, [H, ctypes.c_int32, ctypes.c_int32]),
         "cato_gpu_get_plan": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int32),
                                              ctypes.POINTER(ctypes.c_int32)]),

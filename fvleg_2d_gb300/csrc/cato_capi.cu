@@ -473,6 +473,31 @@ static __global__ void divsqrt_check_kernel(long long n, unsigned long long seed
   atomicAdd(c + 3, bs);
 }
 
+// The FP32 seeds of the integer routines over every input they take: the 2^23 truncated divisor
+// significands fb in [1, 2) and the 2^24 square-root operands fa in [1, 4).  u[0] / u[1]: the
+// largest distance, in units in the last place, of the hardware reciprocal / reciprocal square
+// root approximation from the correctly rounded FP32 value (for 1/sqrt: RN32 of the FP64 value
+// 1 / sqrt(fa), the host test's reference).
+static __global__ void seed_ulps_kernel(unsigned* u) {
+  const unsigned n = (1u << 23) + (1u << 24);
+  unsigned m0 = 0, m1 = 0;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (i < (1u << 23)) {
+      const float fb = __uint_as_float(0x3f800000u | i);
+      const int d = (int)__float_as_uint(intdiv::recip_seed(fb)) - (int)__float_as_uint(__frcp_rn(fb));
+      m0 = max(m0, (unsigned)abs(d));
+    } else {
+      const unsigned j = i - (1u << 23);
+      const float fa = __uint_as_float(((127u + (j >> 23)) << 23) | (j & 0x7fffffu));
+      const float ref = __double2float_rn(1.0 / sqrt((double)fa));
+      const int d = (int)__float_as_uint(intdiv::rsqrt_seed(fa)) - (int)__float_as_uint(ref);
+      m1 = max(m1, (unsigned)abs(d));
+    }
+  }
+  atomicMax(u + 0, m0);
+  atomicMax(u + 1, m1);
+}
+
 extern "C" {
 
 const char* cato_gpu_version(void) { return "cato-gb300 0.1 (sm_103a)"; }
@@ -998,25 +1023,36 @@ int cato_gpu_select_device(int32_t device) {
   return cudaSetDevice(device) == cudaSuccess ? CATO_OK : CATO_ERR_CUDA;
 }
 
-int cato_gpu_check_divsqrt(int64_t n, uint64_t seed, uint64_t tested[2], uint64_t mismatches[2]) {
-  if (n < 0 || !tested || !mismatches) return CATO_ERR_ARG;
+int cato_gpu_check_divsqrt(int64_t n, uint64_t seed, uint64_t tested[2], uint64_t mismatches[2],
+                           int32_t seed_ulps[2]) {
+  if (n < 0 || !tested || !mismatches || !seed_ulps) return CATO_ERR_ARG;
   unsigned long long* d = nullptr;
-  if (cudaMalloc(&d, 4 * sizeof(unsigned long long)) != cudaSuccess) return CATO_ERR_OOM;
-  cudaError_t e = cudaMemset(d, 0, 4 * sizeof(unsigned long long));
+  if (cudaMalloc(&d, 5 * sizeof(unsigned long long)) != cudaSuccess) return CATO_ERR_OOM;
+  unsigned* du = reinterpret_cast<unsigned*>(d + 4);
+  cudaError_t e = cudaMemset(d, 0, 5 * sizeof(unsigned long long));
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned grid = (unsigned)(sms > 0 ? 8 * sms : 1024);
   if (e == cudaSuccess && n > 0) {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    divsqrt_check_kernel<<<(unsigned)(sms > 0 ? 8 * sms : 1024), 256>>>(n, seed, d);
+    divsqrt_check_kernel<<<grid, 256>>>(n, seed, d);
     e = cudaGetLastError();
   }
-  unsigned long long h[4] = {0, 0, 0, 0};
+  if (e == cudaSuccess) {
+    seed_ulps_kernel<<<grid, 256>>>(du);
+    e = cudaGetLastError();
+  }
+  unsigned long long h[5] = {0, 0, 0, 0, 0};
   if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
   cudaFree(d);
   tested[0] = h[0];
   mismatches[0] = h[1];
   tested[1] = h[2];
   mismatches[1] = h[3];
+  unsigned hu[2];
+  memcpy(hu, &h[4], sizeof hu);
+  seed_ulps[0] = (int32_t)hu[0];
+  seed_ulps[1] = (int32_t)hu[1];
   return e == cudaSuccess ? CATO_OK : CATO_ERR_CUDA;
 }
 

@@ -4,8 +4,9 @@
 // GB300 runs FP64 arithmetic at 1/64 of the FP32 rate, and a division or square root costs
 // several FP64 instructions there.  The integer and FP32 pipes have room to spare.  These
 // routines get the exact IEEE result from integer arithmetic on the significands:
-//   1. an FP32 seed, y0 = RN32(1 / b) (division) or RN32(1 / RN32(sqrt(a))) (square root), of
-//      the operand's significand truncated to 24 bits;
+//   1. an FP32 seed y0 ~ 1 / b (division) or 1 / sqrt(a) (square root) of the operand's
+//      significand truncated to 24 bits, from the hardware approximation (any seed within 2^-21
+//      relative will do);
 //   2. one Newton-Raphson step of third order in 64-bit fixed point, y1 = y0 (1 + e + e^2) for
 //      1/b with e = 1 - b y0, and y1 = y0 (1 + e/2 + 3e^2/8) for 1/sqrt(a) with e = 1 - a y0^2
 //      (J.-M. Muller et al., Handbook of Floating-Point Arithmetic, 2nd ed., 2018, sections 4.7
@@ -19,9 +20,9 @@
 // Exact scalings by 2^-1, 2^-2, 2^-3 and 2 (scale_down, scale_up1) are exponent steps here.
 // Operands that are zero, subnormal, infinite or NaN, negative square-root operands and quotients
 // outside the normal range take the hardware instruction instead (the caller's fallback).
-// The same source compiles for the host, where the FP32 seeds are the IEEE float operations
-// 1.0f / x and sqrtf(x) (correctly rounded, like __frcp_rn and __fsqrt_rn on the device); a host
-// test compares the routines bit for bit with the hardware division and square root.
+// The same source compiles for the host, with correctly rounded seeds that a test hook moves by a
+// few ulps; a host test compares the routines bit for bit with the hardware division and square
+// root.
 #pragma once
 
 #include <stdint.h>
@@ -72,77 +73,106 @@ CATO_HD float float_of(uint32_t u) {
   return x;
 #endif
 }
-CATO_HD uint64_t umulhi(uint64_t a, uint64_t b) {
+CATO_HD uint32_t umulhi32(uint32_t a, uint32_t b) {
 #ifdef __CUDA_ARCH__
-  return __umul64hi(a, b);
+  return __umulhi(a, b);
 #else
-  return (uint64_t)(((unsigned __int128)a * b) >> 64);
+  return (uint32_t)(((uint64_t)a * b) >> 32);
 #endif
 }
-// RN32(1 / x) and RN32(sqrt(x)) for x in [1, 4)
-CATO_HD float recip32(float x) {
-#ifdef __CUDA_ARCH__
-  return __frcp_rn(x);
+// floor(x y / 2^64) - d with 0 <= d < 3: the high half of a 64 x 64-bit product from three
+// 32 x 32-bit products (the low x low product dropped, the cross products truncated)
+CATO_HD uint64_t mulhi3(uint64_t x, uint64_t y) {
+  const uint32_t xh = (uint32_t)(x >> 32), xl = (uint32_t)x, yh = (uint32_t)(y >> 32);
+  const uint32_t yl = (uint32_t)y;
+  return (uint64_t)xh * yh + (uint64_t)umulhi32(xh, yl) + (uint64_t)umulhi32(xl, yh);
+}
+// FP32 seeds y0 ~ 1/x and y0 ~ 1/sqrt(x) for x in [1, 4): on the device the single-instruction
+// approximations (rcp.approx.ftz.f32, rsqrt.approx.ftz.f32).  The routines below are exact for
+// any seed within 2^-21 relative of the true value (the error analysis keeps every fixed-point
+// quantity inside 64 bits and the quotient within 4 units of its last bit); cato_gpu_check_divsqrt
+// measures the hardware seeds' error over every input they get.  On the host the seeds are the
+// correctly rounded values, moved by CATO_SEED_OFFSET units in the last place (a test hook that
+// exercises seeds up to a few ulps off).
+#if !defined(__CUDA_ARCH__) && defined(CATO_INTDIV_SEED_HOOK)
+extern int seed_offset_ulps;
+#define CATO_SEED_OFFSET seed_offset_ulps
 #else
-  return 1.0f / x;
+#define CATO_SEED_OFFSET 0
+#endif
+CATO_HD float recip_seed(float x) {
+#ifdef __CUDA_ARCH__
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  return float_of(fbits_of(1.0f / x) + (uint32_t)CATO_SEED_OFFSET);
 #endif
 }
-CATO_HD float sqrt32(float x) {
+CATO_HD float rsqrt_seed(float x) {
 #ifdef __CUDA_ARCH__
-  return __fsqrt_rn(x);
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
 #else
-  return __builtin_sqrtf(x);
+  return float_of(fbits_of((float)(1.0 / __builtin_sqrt((double)x))) + (uint32_t)CATO_SEED_OFFSET);
 #endif
 }
 
 constexpr uint64_t kFrac = 0x000fffffffffffffULL;
 constexpr uint64_t kHid = 0x0010000000000000ULL;
 
-// y * 2^30 as an integer for y = RN32(...) in (0.5, 1] (24 significant bits: exact)
+// y * 2^30 as an integer for an FP32 seed y near [0.5, 1] (24 significant bits: exact)
 CATO_HD uint32_t fixed30(float y) {
   const uint32_t yb = fbits_of(y);
   return ((yb & 0x7fffffu) | 0x800000u) << ((yb >> 23) - 120u);
 }
 
-// y0 (1 + t) * 2^62 for y0 = Y0 / 2^30 and t = T / 2^82 (floor of the correction term)
+// y0 (1 + t) * 2^62 for y0 = Y0 / 2^30 and t = T / 2^80 (floor of the correction term)
 CATO_HD uint64_t refine62(uint32_t Y0, int64_t T) {
   const int64_t Th = T >> 32;                 // floor(T / 2^32)
   const uint64_t Tl = (uint32_t)T;
   const int64_t yt32 = (int64_t)Y0 * Th + (int64_t)(((uint64_t)Y0 * Tl) >> 32);  // floor(Y0 T / 2^32)
-  return ((uint64_t)Y0 << 32) + (uint64_t)(yt32 >> 18);
+  return ((uint64_t)Y0 << 32) + (uint64_t)(yt32 >> 16);
 }
 
 // RN(a / b) as bits for normal a, b; ok = false when an operand is not normal or the quotient
 // is not normal (the bits are then meaningless).
 //
 // With A, B the 53-bit significands (a = A 2^(ea-1075), b = B 2^(eb-1075)):
-//   y0 = RN32(1 / fb), fb = b' = B / 2^52 truncated to 24 bits: |y0 - 1/b'| < 1.25 2^-23,
-//   E = 2^82 (1 - b' y0) = -(B Y0) mod 2^64, |E| < 1.25 2^60;
-//   T = E + Eh^2 / 2^18 (Eh = floor(E / 2^32)) = 2^82 (e + e^2) within 2^-69;
-//   Y1 = 2^62 y0 (1 + T / 2^82): |Y1 - 2^62 / b'| < 1.13;
-//   H = floor(A 2^11 Y1 / 2^64): |H - 2^61 A / B| < 2.13;
-//   s = 9 (quotient >= 1) or 8, M1 = round(H / 2^s), Z = 2^(62-s) A - (2 M1 + 1) B, |Z| < 2^54.
+//   y0 ~ 1 / fb, fb = b' = B / 2^52 truncated to 24 bits, |1 - fb y0| <= 2^-21, so that
+//   e = 1 - b' y0 has |e| < 1.25 2^-21 (the bounds below hold up to |e| = 2^-19);
+//   E = 2^80 e = -(B Y0 / 4) mod 2^64 (Y0 is a multiple of 4), |E| < 2^61;
+//   T = E + Eh^2 / 2^16 (Eh = floor(E / 2^32)) = 2^80 (e + e^2) within 2^-66;
+//   Y1 = 2^62 y0 (1 + T / 2^80): |Y1 - 2^62 / b'| < 2 (the omitted e^3 term: 2^-57 at most);
+//   H ~ A 2^11 Y1 / 2^64 (mulhi3): |H - 2^61 A / B| < 43;
+//   n = 1 when H < 2^61 (quotient below 1), and with the quotient's significand in [1, 2) as
+//   Hn = 2^n H, An = 2^n A: M1 = round(Hn / 2^9) is within 0.17 + 1/2 of X = 2^53 An / B, so
+//   RN(X) is M1 - 1, M1 or M1 + 1, decided by the signs of Z = 2^53 An - (2 M1 + 1) B and
+//   Z + 2 B (|Z| < 2^55).  Where n is taken wrongly (|H - 2^61| < 43), X lies within 0.17 of
+//   2^52 or 2^53 and either choice rounds to the same value.
 CATO_HD uint64_t div_bits(uint64_t ua, uint64_t ub, bool& ok) {
   const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
   const uint64_t A = (ua & kFrac) | kHid, B = (ub & kFrac) | kHid;
   const float fb = float_of(0x3f800000u | (uint32_t)((ub & kFrac) >> 29));
-  const uint32_t Y0 = fixed30(recip32(fb));
-  const int64_t E = (int64_t)(0ULL - B * (uint64_t)Y0);
+  const uint32_t Y0 = fixed30(recip_seed(fb));
+  const int64_t E = (int64_t)(0ULL - B * (uint64_t)(Y0 >> 2));
   const int32_t Eh = (int32_t)(E >> 32);
-  const int64_t T = E + (((int64_t)Eh * Eh) >> 18);
+  const int64_t T = E + (((int64_t)Eh * Eh) >> 16);
   const uint64_t Y1 = refine62(Y0, T);
-  const uint64_t H = umulhi(A << 11, Y1);
-  const uint32_t s = (H >> 61) ? 9u : 8u;
-  const uint64_t M1 = (H + (1ULL << (s - 1))) >> s;
-  const int64_t Z = (int64_t)((A << (62 - s)) - (2 * M1 + 1) * B);
+  const uint64_t H = mulhi3(A << 11, Y1);
+  const uint32_t n = (uint32_t)(H >> 61) ^ 1u;
+  const uint64_t Hn = H << n, An = A << n;
+  const uint64_t M1 = (Hn + 256u) >> 9;
+  const int64_t Z = (int64_t)((An << 53) - (2 * M1 + 1) * B);
   uint64_t M = M1;
   if (Z > 0 || (Z == 0 && (M1 & 1))) {
     M = M1 + 1;
   } else {
-    const int64_t W = Z + (int64_t)(2 * B);  // 2^(62-s) A - (2 M1 - 1) B
+    const int64_t W = Z + (int64_t)(2 * B);  // 2^53 An - (2 M1 - 1) B
     if (W < 0 || (W == 0 && (M1 & 1))) M = M1 - 1;
   }
-  const int32_t Ef = (int32_t)ea - (int32_t)eb + 1014 + (int32_t)s;
+  const int32_t Ef = (int32_t)ea - (int32_t)eb + 1023 - (int32_t)n;
   ok = (ea - 1u < 2046u) && (eb - 1u < 2046u) && (Ef >= 1) && (Ef <= 2045);
   const uint64_t sign = (ua ^ ub) & 0x8000000000000000ULL;
   // M in [2^52, 2^53]: M = 2^53 carries into the exponent field
@@ -152,24 +182,31 @@ CATO_HD uint64_t div_bits(uint64_t ua, uint64_t ub, bool& ok) {
 // RN(sqrt(a)) as bits for normal a > 0; ok = false otherwise.
 //
 // a = A2 2^(2m) with A2 = A or 2A in [2^52, 2^54), a'' = A2 / 2^52 in [1, 4):
-//   y0 = RN32(1 / RN32(sqrt(fa))), fa = a'' truncated to 24 bits: |y0 sqrt(a'') - 1| < 1.5 2^-23;
-//   E = 2^82 (1 - a'' y0^2) = -floor(A2 Y0^2 / 2^30) mod 2^64;
-//   T = E / 2 + 3 Eh^2 / 2^21 = 2^82 (e/2 + 3e^2/8);  Y1 = 2^62 y0 (1 + T / 2^82);
-//   H = floor(A2 2^10 Y1 / 2^64): |H - 2^60 sqrt(a'')| < 2.1;
+//   y0 ~ 1 / sqrt(fa), fa = a'' truncated to 24 bits, |1 - fa y0^2| <= 2^-21, so that
+//   e = 1 - a'' y0^2 has |e| < 1.5 2^-21 (the bounds below hold up to |e| = 2^-19);
+//   E = 2^80 e = -floor(A2 Y0^2 / 2^32) mod 2^64 (within 2 units), |E| < 2^61;
+//   T = E / 2 + 3 floor(Eh^2 / 2^19) = 2^80 (e/2 + 3e^2/8);  Y1 = 2^62 y0 (1 + T / 2^80), within
+//   6 units (the omitted 5e^3/16 term: 2^-58.7 at most);
+//   H ~ A2 2^10 Y1 / 2^64 (mulhi3): |H - 2^60 sqrt(a'')| < 29, inside the 128 the rounding
+//   allows;
 //   M1 = round(H / 2^8), Z = 2^54 A2 - (2 M1 + 1)^2 (never 0), |Z| < 2^56.
 CATO_HD uint64_t sqrt_bits(uint64_t ua, bool& ok) {
   const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu;
   const uint32_t odd = (ea & 1u) ^ 1u;  // the unbiased exponent ea - 1075 is odd
   const uint64_t A2 = ((ua & kFrac) | kHid) << odd;
   const float fa = float_of(((127u + odd) << 23) | (uint32_t)((ua & kFrac) >> 29));
-  const uint32_t Y0 = fixed30(recip32(sqrt32(fa)));
+  const uint32_t Y0 = fixed30(rsqrt_seed(fa));
   const uint64_t S = (uint64_t)Y0 * Y0;  // Y0^2 <= 2^60
-  const uint64_t plo = A2 * S, phi = umulhi(A2, S);
-  const int64_t E = (int64_t)(0ULL - ((plo >> 30) | (phi << 34)));
+  // floor(A2 S / 2^32) mod 2^64 from 32-bit halves (the carry out of the lowest product dropped)
+  const uint32_t ah = (uint32_t)(A2 >> 32), al = (uint32_t)A2;
+  const uint32_t sh = (uint32_t)(S >> 32), sl = (uint32_t)S;
+  const uint64_t P = ((uint64_t)(ah * sh) << 32) + (uint64_t)ah * sl + (uint64_t)al * sh +
+                     umulhi32(al, sl);
+  const int64_t E = (int64_t)(0ULL - P);
   const int32_t Eh = (int32_t)(E >> 32);
-  const int64_t T = (E >> 1) + ((3 * ((int64_t)Eh * Eh)) >> 21);
+  const int64_t T = (E >> 1) + 3 * (((int64_t)Eh * Eh) >> 19);
   const uint64_t Y1 = refine62(Y0, T);
-  const uint64_t H = umulhi(A2 << 10, Y1);
+  const uint64_t H = mulhi3(A2 << 10, Y1);
   const uint64_t M1 = (H + 128u) >> 8;
   const uint64_t N = 2 * M1 + 1;
   const int64_t Z = (int64_t)((A2 << 54) - N * N);

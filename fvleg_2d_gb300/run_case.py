@@ -40,10 +40,19 @@ def main(argv=None) -> int:
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--plan", default="", help="threads,rows_per_cta (default: the handle's)")
+    ap.add_argument("--flux", default="", help="edge flux instead of the workload's (e.g. Roe)")
+    ap.add_argument("--limiter", default="", help="limiter instead of the workload's (e.g. MLP5)")
     ap.add_argument("--t-start", type=float, default=0.0,
                     help="first advance the flow to this time with the mixed path")
     a = ap.parse_args(argv)
     cfg, prims = make(a.workload, a.n, a.precision, a.seed)
+    if a.flux or a.limiter:
+        old_g = cfg.ghost_layers()
+        cfg = dataclasses.replace(cfg, flux_solver=a.flux or cfg.flux_solver,
+                                  limiter=a.limiter or cfg.limiter)
+        if cfg.ghost_layers() != old_g:  # re-pad the halo-padded primitives
+            d = cfg.ghost_layers() - old_g
+            prims = [np.pad(q, d, mode="edge") if d > 0 else q[-d:d, -d:d] for q in prims]
     if a.t_start > 0:
         g = Fluid(dataclasses.replace(cfg, precision="mixed")).initialize(*prims)
         g.run(a.t_start)
@@ -55,7 +64,8 @@ def main(argv=None) -> int:
         f.set_plan(*(int(x) for x in a.plan.split(",")))
     ms, kern = f.run_timed(a.steps, per_kernel=True)
     cells = cfg.ni * cfg.nj
-    print(json.dumps({"workload": a.workload, "ni": cfg.ni, "nj": cfg.nj,
+    print(json.dumps({"workload": a.workload, "flux": cfg.flux_solver, "limiter": cfg.limiter,
+                      "ni": cfg.ni, "nj": cfg.nj,
                       "precision": a.precision, "steps": a.steps, "ms": ms,
                       "kernel_ms": kern, "cell_updates_per_s": cells * a.steps / (ms / 1e3)}))
     return 0

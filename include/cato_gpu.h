@@ -294,9 +294,13 @@ int cato_gpu_select_device(int32_t device);
  * narrow exponent ranges, divisors with few significand bits, quotients near 1) go through the
  * integer routines and the hardware instructions on the current device.  tested[0] / tested[1]:
  * the divisions / square roots the integer routines took (the rest fall back to the hardware),
- * mismatches[0] / mismatches[1]: how many of those differ in any bit.  No counterpart in the
- * reference. */
-int cato_gpu_check_divsqrt(int64_t n, uint64_t seed, uint64_t tested[2], uint64_t mismatches[2]);
+ * mismatches[0] / mismatches[1]: how many of those differ in any bit.  seed_ulps[0] / [1]: the
+ * largest distance, in FP32 units in the last place and over every input, of the hardware
+ * reciprocal / reciprocal-square-root approximations that seed the routines from the correctly
+ * rounded values (the routines are verified on the host for seeds up to 8 ulps off).  No
+ * counterpart in the reference. */
+int cato_gpu_check_divsqrt(int64_t n, uint64_t seed, uint64_t tested[2], uint64_t mismatches[2],
+                           int32_t seed_ulps[2]);
 
 /* cato_gpu_solve for callers that cannot allocate device memory: no handle, no cudaMalloc or
  * cudaFree.  It has no counterpart in the reference; it serves callers whose device memory is

@@ -2,7 +2,11 @@
 // source as the device code, with the FP32 seeds computed by the host's IEEE float division and
 // square root, compared bit for bit with the host's hardware a / b and sqrt(a).
 //
-// usage: intdiv_check <random cases per family>
+// The device seeds are hardware approximations, so every family runs with the host seeds moved by
+// up to 8 units in the last place either way (cato_gpu_check_divsqrt measures the hardware seeds
+// against the same correctly rounded values over all their inputs).
+//
+// usage: intdiv_check <random cases per family and seed offset>
 // Prints one line per family ("<family> tested <n> fallback <n> bad <n>") and exits 1 on any
 // mismatch.  Families: random normal operands over the full exponent range and over a narrow
 // one; significands near powers of two, near each other and with few bits set; quotients and
@@ -13,7 +17,14 @@
 #include <cstdlib>
 #include <random>
 
+#define CATO_INTDIV_SEED_HOOK
 #include "../fvleg_2d_gb300/csrc/cato_intdiv.cuh"
+
+namespace cato {
+namespace intdiv {
+int seed_offset_ulps = 0;  // ulps added to the host seeds (the device uses approximations)
+}  // namespace intdiv
+}  // namespace cato
 
 using namespace cato::intdiv;
 
@@ -57,14 +68,20 @@ static double random_double(int emin, int emax, bool sign = true) {
 int main(int argc, char** argv) {
   const long n = argc > 1 ? atol(argv[1]) : 1000000;
   int fail = 0;
+  static const int kOffsets[] = {0, -8, -4, -2, -1, 1, 2, 4, 8};
 
   reset();
-  for (long i = 0; i < n; ++i) check_div(random_double(1, 2046), random_double(1, 2046));
-  for (long i = 0; i < n; ++i) check_div(random_double(960, 1090), random_double(960, 1090));
+  for (const int off : kOffsets) {
+    seed_offset_ulps = off;
+    for (long i = 0; i < n; ++i) check_div(random_double(1, 2046), random_double(1, 2046));
+    for (long i = 0; i < n; ++i) check_div(random_double(960, 1090), random_double(960, 1090));
+  }
   report("div_random");
   fail |= bad != 0;
 
   reset();
+  for (const int off : kOffsets) {
+  seed_offset_ulps = off;
   for (long i = 0; i < n; ++i) {
     uint64_t ma = rng() & kFrac, mb = rng() & kFrac;
     switch (rng() % 6) {
@@ -88,10 +105,13 @@ int main(int argc, char** argv) {
     check_div(std::nextafter(a, 1e300), b);
     check_div(q * b, b);
   }
+  }
   report("div_structured");
   fail |= bad != 0;
 
   reset();
+  for (const int off : kOffsets) {
+  seed_offset_ulps = off;
   for (long i = 0; i < n; ++i) check_sqrt(random_double(1, 2046, false));
   for (long i = 0; i < n; ++i) {  // next to a rounding midpoint of the root, and exact squares
     const double s = random_double(1000, 1046, false);
@@ -101,6 +121,7 @@ int main(int argc, char** argv) {
     check_sqrt(std::nextafter(a, 0.0));
     check_sqrt(std::nextafter(a, 1e300));
     check_sqrt(s * s);
+  }
   }
   report("sqrt");
   fail |= bad != 0;
@@ -127,6 +148,8 @@ int main(int argc, char** argv) {
   fail |= bad != 0;
 
   reset();  // every seed: b (a) = 1.t followed by 29 one bits (largest truncation), and zeros
+  for (const int off : {-8, 0, 8}) {
+  seed_offset_ulps = off;
   for (uint64_t t = 0; t < (1ULL << 23); ++t) {
     for (const uint64_t low : {0ULL, (1ULL << 29) - 1}) {
       const uint64_t m = (t << 29) | low;
@@ -138,6 +161,8 @@ int main(int argc, char** argv) {
       check_sqrt(double_of((1024ULL << 52) | m));
     }
   }
+  }
+  seed_offset_ulps = 0;
   report("seeds");
   fail |= bad != 0;
   return fail;
