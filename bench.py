@@ -238,6 +238,7 @@ def bench_precision(args, precision, dist, world, peak_gbs):
     cfg, prims = quadrant_state(args)
     cfg = dataclasses.replace(cfg, precision=precision)
     f = Fluid(cfg).initialize(*prims)
+    tuned_steps, _ = f.tune(2)  # plan and kernel variant, on real steps before the warm-up
     f.run_timed(args.warmup)
     barrier(dist)
     with ClockSampler(env_int("LOCAL_RANK", 0)) as clk:
@@ -268,6 +269,8 @@ def bench_precision(args, precision, dist, world, peak_gbs):
             "algorithmic_bytes_per_launch": stage_bytes / n_stage_launches,
         },
         "clocks": clk.summary(),
+        "plan": {"threads": f.get_plan()[0], "rows_per_cta": f.get_plan()[1],
+                 "kernel_variant": f.get_kernel_variant(), "tuning_steps": tuned_steps},
     }
     if precision == "fp64":
         # The FP64 kernel is bound by GB300's FP64 pipe (2 FP64 thread-instructions per SM and
@@ -311,6 +314,7 @@ def bench_e2e(args, cfg, prims):
     f = Fluid(cfg)
     # warm-up on the same handle (allocations, module load)
     f.initialize(*(p.array for p in pinned[:4]))
+    f.tune(2)  # the same autotuning as the device-timed leg, outside the timed region
     for _ in range(min(args.warmup, 2)):
         f.integrate()
     L, h, ld = f.L, f.h, f.ld
@@ -339,7 +343,8 @@ def bench_e2e(args, cfg, prims):
 def bench_kh(args, peak_gbs):
     """Roofline stress: Kelvin-Helmholtz shear layer on 8192^2 (Roe with Harten's entropy fix,
     superbee, SSP-RK3, CFL 0.4, periodic x, symmetry y).  The mixed path runs the full 200-step
-    window; the FP64 path a bounded window of it (it is FP64-ALU bound, ~0.5 s per step)."""
+    window; the FP64 path a bounded window of it (~0.35 s per step).  Each handle is autotuned on
+a few real steps first."""
     from fvleg_2d_gb300 import ic
     from fvleg_2d_gb300.fluid import Fluid
 
@@ -350,6 +355,7 @@ def bench_kh(args, peak_gbs):
             continue
         cfg, prims = ic.kelvin_helmholtz(args.kh_n, roe_entropy_fix="harten", precision=precision)
         f = Fluid(cfg).initialize(*prims)
+        f.tune(1 if precision == "fp64" else 2)
         f.run_timed(3)
         with ClockSampler(env_int("LOCAL_RANK", 0)) as clk:
             total_ms, kernel_ms = f.run_timed(steps, per_kernel=True)
@@ -359,6 +365,8 @@ def bench_kh(args, peak_gbs):
         out[precision] = {
             "value": cells * steps / (total_ms / 1e3), "unit": "cell-updates/s",
             "steps": steps, "ms_per_step": total_ms / steps,
+            "plan": {"threads": f.get_plan()[0], "rows_per_cta": f.get_plan()[1],
+                     "kernel_variant": f.get_kernel_variant()},
             "stage_ms_per_step": [m / steps for m in kernel_ms[1:]],
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
                          "frac": achieved / peak_gbs,
@@ -398,12 +406,15 @@ def bench_rectilinear(args, uniform_values):
     for precision in ("fp64", "mixed", "mixed_df"):
         cfg = dataclasses.replace(cfg0, precision=precision)
         f = Fluid(cfg).set_rectilinear(xs, ys).initialize(*prims)
+        f.tune(2)
         f.run_timed(args.warmup)
         with ClockSampler(env_int("LOCAL_RANK", 0)) as clk:
             total_ms, _ = f.run_timed(args.steps, per_kernel=False)
         value = cfg.ni * cfg.nj * args.steps / (total_ms / 1e3)
         out[precision] = {"value": value, "unit": "cell-updates/s",
                           "ms_per_step": total_ms / args.steps,
+                          "plan": {"threads": f.get_plan()[0], "rows_per_cta": f.get_plan()[1],
+                                   "kernel_variant": f.get_kernel_variant()},
                           "vs_uniform_grid": value / uniform_values[precision],
                           "clocks": clk.summary()}
         f.close()
@@ -597,7 +608,7 @@ def main() -> int:
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": workload_config(args, world),
+        "config": dict(workload_config(args, world), plan=fp64["plan"]),
         "hbm_gbs": fp64["roofline"]["achieved"],
         "roofline": dict(fp64["roofline"], peak_source=f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                          if peak_kind == "measured" else "fallback 6.8 TB/s"),
@@ -611,7 +622,7 @@ def main() -> int:
             "ms_per_step": mixed["ms_per_step"], "speedup_vs_fp64": mixed["value"] / fp64["value"],
             "roofline": mixed["roofline"], "stage_ms_per_step": mixed["stage_ms_per_step"],
             "gpu_launches": mixed["launches_per_step"] * args.steps, "clocks": mixed["clocks"],
-            "e2e": e2e_mixed,
+            "plan": mixed["plan"], "e2e": e2e_mixed,
         },
         "mixed_df": {
             "value": mixed_df["value"], "unit": "cell-updates/s",
@@ -620,7 +631,7 @@ def main() -> int:
             "speedup_vs_fp64": mixed_df["value"] / fp64["value"],
             "roofline": mixed_df["roofline"], "stage_ms_per_step": mixed_df["stage_ms_per_step"],
             "gpu_launches": mixed_df["launches_per_step"] * args.steps,
-            "clocks": mixed_df["clocks"], "e2e": e2e_df,
+            "clocks": mixed_df["clocks"], "plan": mixed_df["plan"], "e2e": e2e_df,
         },
         "rectilinear": rect,
         "kelvin_helmholtz": kh,

@@ -77,6 +77,11 @@ def load(build_if_missing: bool = False):
         "cato_gpu_run_timed": (ctypes.c_int, [H, i64, ctypes.POINTER(ctypes.c_float),
                                               ctypes.POINTER(ctypes.c_float), ctypes.c_int32]),
         "cato_gpu_select_device": (ctypes.c_int, [ctypes.c_int32]),
+        "cato_gpu_set_kernel_variant": (ctypes.c_int, [H, ctypes.c_int32]),
+        "cato_gpu_get_kernel_variant": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int32)]),
+        "cato_gpu_tune": (ctypes.c_int, [H, ctypes.c_int32,
+                                         ctypes.POINTER(ctypes.c_int32),
+                                         ctypes.POINTER(ctypes.c_float)]),
         "cato_gpu_check_divsqrt": (ctypes.c_int, [ctypes.c_int64, ctypes.c_uint64,
                                                   ctypes.POINTER(ctypes.c_uint64),
                                                   ctypes.POINTER(ctypes.c_uint64),

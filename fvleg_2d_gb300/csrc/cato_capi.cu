@@ -32,6 +32,7 @@ namespace {
 struct Plan {
   int threads = 128;       // CTA width incl. halo
   int rows_per_cta = 64;   // rows marched per CTA
+  int variant = 0;         // FP64 stage kernel register budget (launch_stage_one)
 };
 
 struct Stage {
@@ -210,7 +211,8 @@ static cudaError_t launch(cato_handle* h, const StageArgs& A) {
   dim3 grid((h->ni + W - 1) / W, (h->nj + A.rows_per_cta - 1) / A.rows_per_cta);
   const int recon = recon_of(h->cfg.limiter);
   if (h->cfg.precision == CATO_FP64)
-    return launch_stage<double>(h->cfg.flux, recon, grid, T, h->stream, A, h->K64);
+    return launch_stage<double>(h->cfg.flux, recon, grid, T, h->stream, A, h->K64,
+                                h->plan.variant);
   if (h->cfg.precision == CATO_MIXED_DF)
     return launch_stage<df>(h->cfg.flux, recon, grid, T, h->stream, A, h->Kdf);
   return launch_stage<float>(h->cfg.flux, recon, grid, T, h->stream, A, h->K32);
@@ -1009,6 +1011,65 @@ int cato_gpu_set_plan(cato_handle* h, int32_t threads, int32_t rows_per_cta) {
     return fail(h, CATO_ERR_ARG, "invalid plan");
   h->plan.threads = threads;
   h->plan.rows_per_cta = rows_per_cta;
+  return CATO_OK;
+}
+
+int cato_gpu_set_kernel_variant(cato_handle* h, int32_t variant) {
+  if (!h) return CATO_ERR_ARG;
+  if (variant < 0 || variant > 1) return fail(h, CATO_ERR_ARG, "invalid kernel variant");
+  h->plan.variant = variant;
+  return CATO_OK;
+}
+
+int cato_gpu_get_kernel_variant(const cato_handle* h, int32_t* variant) {
+  if (!h || !variant) return CATO_ERR_ARG;
+  *variant = h->plan.variant;
+  return CATO_OK;
+}
+
+int cato_gpu_tune(cato_handle* h, int32_t steps, int32_t* steps_taken, float* best_ms) {
+  if (!h || steps < 1) return CATO_ERR_ARG;
+  if (steps_taken) *steps_taken = 0;
+  if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  // candidates: the default plan, 256-wide strips, half the rows per CTA; each with both FP64
+  // register budgets
+  const Plan p0 = h->plan;
+  std::vector<Plan> cands;
+  const int wide = 256, half_rows = std::max(8, p0.rows_per_cta / 2);
+  const int nvar = h->cfg.precision == CATO_FP64 ? 2 : 1;
+  for (int v = 0; v < nvar; ++v) {
+    Plan a = p0, b = p0, c = p0;
+    a.variant = b.variant = c.variant = v;
+    b.threads = wide;
+    c.rows_per_cta = half_rows;
+    for (const Plan& q : {a, b, c}) {
+      bool dup = false;
+      for (const Plan& x : cands)
+        dup |= x.threads == q.threads && x.rows_per_cta == q.rows_per_cta && x.variant == q.variant;
+      if (!dup && q.threads - 2 * h->ng <= h->ni + 2 * h->ng) cands.push_back(q);
+    }
+  }
+  Plan best = p0;
+  float best_t = INFINITY;
+  int taken = 0;
+  for (const Plan& q : cands) {
+    h->plan = q;
+    float ms = 0.0f;
+    const int rc = cato_gpu_run_timed(h, steps, &ms, nullptr, 0);
+    taken += steps;
+    if (rc) {
+      h->plan = best_t < INFINITY ? best : p0;
+      if (steps_taken) *steps_taken = taken;
+      return rc;
+    }
+    if (ms < best_t) {
+      best_t = ms;
+      best = q;
+    }
+  }
+  h->plan = best;
+  if (steps_taken) *steps_taken = taken;
+  if (best_ms) *best_ms = best_t / (float)steps;
   return CATO_OK;
 }
 

@@ -11,30 +11,32 @@
 namespace cato {
 
 
-template <typename R, int NG, int FLUX, int RECON, bool EXT>
+template <typename R, int NG, int FLUX, int RECON, bool EXT, int MB = min_blocks<R>()>
 cudaError_t launch_stage_ext(dim3 grid, int threads, cudaStream_t stream, const StageArgs& A,
                              const FluxConsts<R>& K) {
   static std::atomic<bool> attr_done{false};
   const size_t smem = stage_smem_bytes<R>(threads, NG);
   if (!attr_done.load(std::memory_order_acquire)) {
-    cudaError_t e = cudaFuncSetAttribute(stage_kernel<R, NG, FLUX, RECON, EXT>,
+    cudaError_t e = cudaFuncSetAttribute(stage_kernel<R, NG, FLUX, RECON, EXT, MB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)stage_smem_bytes<R>(256, 3));
     if (e != cudaSuccess) return e;
     attr_done.store(true, std::memory_order_release);
   }
   if (grid.x == 0 || grid.y == 0) return cudaSuccess;  // attribute warm-up only
-  stage_kernel<R, NG, FLUX, RECON, EXT><<<grid, threads, smem, stream>>>(A, K);
+  stage_kernel<R, NG, FLUX, RECON, EXT, MB><<<grid, threads, smem, stream>>>(A, K);
   return cudaGetLastError();
 }
 
 // The FP32 path has a lean variant without the rectilinear, source and pressure-input code
-// (it is issue-bound: those checks cost ~3 %); FP64 and double-float keep one kernel.
+// (it is issue-bound: those checks cost ~3 %); double-float keeps one kernel.  The FP64 path
+// has one kernel per register budget (variant 0: the compiler's choice, 1: at most 128).
 template <typename R, int NG, int FLUX, int RECON>
 cudaError_t launch_stage_one(dim3 grid, int threads, cudaStream_t stream, const StageArgs& A,
-                             const FluxConsts<R>& K) {
+                             const FluxConsts<R>& K, int variant) {
+  const bool warm = grid.x == 0 || grid.y == 0;  // attribute warm-up of every variant
   if constexpr (Prec<R>::kind == 1) {
-    if (grid.x == 0 || grid.y == 0) {  // warm-up: both variants
+    if (warm) {
       cudaError_t e = launch_stage_ext<R, NG, FLUX, RECON, false>(grid, threads, stream, A, K);
       if (e != cudaSuccess) return e;
       return launch_stage_ext<R, NG, FLUX, RECON, true>(grid, threads, stream, A, K);
@@ -42,17 +44,27 @@ cudaError_t launch_stage_one(dim3 grid, int threads, cudaStream_t stream, const 
     if (!stage_needs_ext(A))
       return launch_stage_ext<R, NG, FLUX, RECON, false>(grid, threads, stream, A, K);
   }
+  if constexpr (Prec<R>::kind == 0) {
+    if (warm) {
+      cudaError_t e = launch_stage_ext<R, NG, FLUX, RECON, true, CATO_F64_MIN_BLOCKS_ALT>(
+          grid, threads, stream, A, K);
+      if (e != cudaSuccess) return e;
+    } else if (variant == 1) {
+      return launch_stage_ext<R, NG, FLUX, RECON, true, CATO_F64_MIN_BLOCKS_ALT>(grid, threads,
+                                                                                stream, A, K);
+    }
+  }
   return launch_stage_ext<R, NG, FLUX, RECON, true>(grid, threads, stream, A, K);
 }
 
 // recon: 0 = TVD2 (minmod / superbee / van Leer), 3 = MLP3, 5 = MLP5
 template <typename R, int FLUX>
 inline cudaError_t launch_stage_flux(int recon, dim3 grid, int threads, cudaStream_t stream,
-                                     const StageArgs& A, const FluxConsts<R>& K) {
+                                     const StageArgs& A, const FluxConsts<R>& K, int variant) {
   switch (recon) {
-    case 0: return launch_stage_one<R, 2, FLUX, 0>(grid, threads, stream, A, K);
-    case 3: return launch_stage_one<R, 2, FLUX, 3>(grid, threads, stream, A, K);
-    case 5: return launch_stage_one<R, 3, FLUX, 5>(grid, threads, stream, A, K);
+    case 0: return launch_stage_one<R, 2, FLUX, 0>(grid, threads, stream, A, K, variant);
+    case 3: return launch_stage_one<R, 2, FLUX, 3>(grid, threads, stream, A, K, variant);
+    case 5: return launch_stage_one<R, 3, FLUX, 5>(grid, threads, stream, A, K, variant);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -102,7 +114,7 @@ inline cudaError_t launch_batch_flux(int recon, int threads, cudaStream_t stream
 #define CATO_DECLARE_ONE(R, F, NG, RC)                                                         \
   extern template cudaError_t launch_stage_one<R, NG, F, RC>(dim3, int, cudaStream_t,          \
                                                              const StageArgs&,                 \
-                                                             const FluxConsts<R>&);            \
+                                                             const FluxConsts<R>&, int);       \
   extern template cudaError_t launch_batch_one<R, NG, F, RC>(int, cudaStream_t,               \
                                                              const BatchStageArgs&);
 #define CATO_DECLARE_STAGE(R, F) \
@@ -118,19 +130,20 @@ CATO_DECLARE_PREC(df)
 #undef CATO_DECLARE_STAGE
 #undef CATO_DECLARE_ONE
 
+// variant: the FP64 kernel's register budget (0 or 1, see launch_stage_one); ignored otherwise
 template <typename R>
 inline cudaError_t launch_stage(int flux, int recon, dim3 grid, int threads, cudaStream_t s,
-                                const StageArgs& A, const FluxConsts<R>& K) {
+                                const StageArgs& A, const FluxConsts<R>& K, int variant = 0) {
   switch (flux) {
-    case 0: return launch_stage_flux<R, 0>(recon, grid, threads, s, A, K);
-    case 1: return launch_stage_flux<R, 1>(recon, grid, threads, s, A, K);
-    case 2: return launch_stage_flux<R, 2>(recon, grid, threads, s, A, K);
-    case 3: return launch_stage_flux<R, 3>(recon, grid, threads, s, A, K);
-    case 4: return launch_stage_flux<R, 4>(recon, grid, threads, s, A, K);
-    case 5: return launch_stage_flux<R, 5>(recon, grid, threads, s, A, K);
-    case 6: return launch_stage_flux<R, 6>(recon, grid, threads, s, A, K);
-    case 7: return launch_stage_flux<R, 7>(recon, grid, threads, s, A, K);
-    case 8: return launch_stage_flux<R, 8>(recon, grid, threads, s, A, K);
+    case 0: return launch_stage_flux<R, 0>(recon, grid, threads, s, A, K, variant);
+    case 1: return launch_stage_flux<R, 1>(recon, grid, threads, s, A, K, variant);
+    case 2: return launch_stage_flux<R, 2>(recon, grid, threads, s, A, K, variant);
+    case 3: return launch_stage_flux<R, 3>(recon, grid, threads, s, A, K, variant);
+    case 4: return launch_stage_flux<R, 4>(recon, grid, threads, s, A, K, variant);
+    case 5: return launch_stage_flux<R, 5>(recon, grid, threads, s, A, K, variant);
+    case 6: return launch_stage_flux<R, 6>(recon, grid, threads, s, A, K, variant);
+    case 7: return launch_stage_flux<R, 7>(recon, grid, threads, s, A, K, variant);
+    case 8: return launch_stage_flux<R, 8>(recon, grid, threads, s, A, K, variant);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -538,9 +538,15 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
 #ifndef CATO_F32_BATCH_MIN_BLOCKS
 #define CATO_F32_BATCH_MIN_BLOCKS 3
 #endif
-// and for the FP64 kernels
+// and for the FP64 kernels, which come in two register budgets (kernel variants 0 and 1): the
+// compiler's choice, and at most 128 registers (two 256-thread CTAs per SM).  Which is faster
+// depends on the flux, the reconstruction and the flow (cato_gpu_tune measures it); both give
+// bit-identical results.
 #ifndef CATO_F64_MIN_BLOCKS
 #define CATO_F64_MIN_BLOCKS 1
+#endif
+#ifndef CATO_F64_MIN_BLOCKS_ALT
+#define CATO_F64_MIN_BLOCKS_ALT 2
 #endif
 template <typename R> constexpr int min_blocks() {
   return Prec<R>::kind == 2 ? CATO_DF_MIN_BLOCKS
@@ -551,8 +557,8 @@ template <typename R> constexpr int batch_min_blocks() {
                             : (Prec<R>::kind == 1 ? CATO_F32_BATCH_MIN_BLOCKS : CATO_F64_MIN_BLOCKS);
 }
 
-template <typename R, int NG, int FLUX, int RECON, bool EXT>
-__global__ void __launch_bounds__(256, min_blocks<R>())
+template <typename R, int NG, int FLUX, int RECON, bool EXT, int MB>
+__global__ void __launch_bounds__(256, MB)
     stage_kernel(const StageArgs A, const FluxConsts<R> K) {
   if (A.active && *A.active == 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -18,7 +18,7 @@
 
 #define CATO_INST_STAGE(NG, RC)                                                               \
   template cudaError_t launch_stage_one<CATO_REAL, NG, CATO_FLUX, RC>(                        \
-      dim3, int, cudaStream_t, const StageArgs&, const FluxConsts<CATO_REAL>&);
+      dim3, int, cudaStream_t, const StageArgs&, const FluxConsts<CATO_REAL>&, int);
 #define CATO_INST_BATCH(NG, RC)                                                               \
   template cudaError_t launch_batch_one<CATO_REAL, NG, CATO_FLUX, RC>(int, cudaStream_t,      \
                                                                       const BatchStageArgs&);

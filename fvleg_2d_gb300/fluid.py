@@ -210,6 +210,24 @@ class Fluid(_Handle):
         _check(self.L.cato_gpu_get_plan(self.h, ctypes.byref(t), ctypes.byref(r)), self.h)
         return t.value, r.value
 
+    def set_kernel_variant(self, variant: int) -> None:
+        """FP64 stage kernel register budget: 0 (compiler's choice) or 1 (<= 128 registers)."""
+        _check(self.L.cato_gpu_set_kernel_variant(self.h, int(variant)), self.h, "variant")
+
+    def get_kernel_variant(self) -> int:
+        v = ctypes.c_int32()
+        _check(self.L.cato_gpu_get_kernel_variant(self.h, ctypes.byref(v)), self.h)
+        return v.value
+
+    def tune(self, steps: int = 2) -> tuple[int, float]:
+        """Autotune plan and kernel variant on the live state (cato_gpu_tune).  The candidates
+        run real CFL steps, bit-identical whichever runs them.  Returns (steps taken, the
+        fastest candidate's ms per step); raises CatoError on a fluid error."""
+        n, ms = ctypes.c_int32(), ctypes.c_float()
+        rc = self.L.cato_gpu_tune(self.h, int(steps), ctypes.byref(n), ctypes.byref(ms))
+        _check(rc, self.h, f"tune (after {n.value} steps)")
+        return n.value, ms.value
+
     def launches_per_step(self) -> int:
         n = ctypes.c_int32()
         _check(self.L.cato_gpu_launches_per_step(self.h, ctypes.byref(n)), self.h)
