@@ -119,6 +119,26 @@ template <> __device__ __forceinline__ bool nonpos<double>(double x) {
   const long long b = __double_as_longlong(x);
   return (b < 0 || (b << 1) == 0) && !d_isnan(x);
 }
+// a <= b, x >= 0, x > 0, x < 0 (IEEE: false with a NaN operand); FP64 on the integer pipe
+template <typename R> __device__ __forceinline__ bool le(R a, R b) { return a <= b; }
+template <typename R> __device__ __forceinline__ bool ge0(R x) { return x >= R(0); }
+template <typename R> __device__ __forceinline__ bool gt0(R x) { return x > R(0); }
+template <typename R> __device__ __forceinline__ bool lt0(R x) { return x < R(0); }
+template <> __device__ __forceinline__ bool le<double>(double a, double b) {
+  return d_key(a) <= d_key(b) && !d_isnan(a) && !d_isnan(b);
+}
+template <> __device__ __forceinline__ bool ge0<double>(double x) {
+  const long long b = __double_as_longlong(x);
+  return (b >= 0 || (b << 1) == 0) && !d_isnan(x);
+}
+template <> __device__ __forceinline__ bool gt0<double>(double x) {
+  const long long b = __double_as_longlong(x);
+  return b > 0 && !d_isnan(x);
+}
+template <> __device__ __forceinline__ bool lt0<double>(double x) {
+  const long long b = __double_as_longlong(x);
+  return b < 0 && (b << 1) != 0 && !d_isnan(x);
+}
 template <> __device__ __forceinline__ float rmin<float>(float a, float b) { return fminf(a, b); }
 template <typename R> __device__ __forceinline__ R rabs(R a) { return fabs(a); }
 template <> __device__ __forceinline__ df rabs<df>(df a) { return df_abs(a); }
@@ -285,7 +305,7 @@ __device__ __forceinline__ R tvd_phi(int lim, R r) {
   // "vanleer" (muscl_tvd2.fypp:199-200); for r <= 0 the numerator r + |r| is +0 and so is
   // the quotient (1 + |r| >= 1): skip the division
   if (nonpos(r)) return R(0);
-  return Num<R>::div(r + rabs(r), R(1) + rabs(r));
+  return Num<R>::div(twice(r), R(1) + r);  // r > 0: r + |r| = 2r exactly, |r| = r
 }
 
 // phi(num / den).  Every limiter gives +0 for r < 0, and FP64 knows r < 0 without dividing when
@@ -1026,8 +1046,8 @@ __device__ __forceinline__ void flux_hllc(const FluxConsts<R>& K, const Prim<R>&
   R p_pvrs = half(A.p + B.p) - half(qnR - qnL) * rho_bar * c_bar;
   R p_star = rmax(R(0), p_pvrs);
   const R gf = R(K.hllc_gf);
-  R qL = (p_star <= A.p) ? R(1) : Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, A.p) - R(1)));
-  R qR = (p_star <= B.p) ? R(1) : Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, B.p) - R(1)));
+  R qL = le(p_star, A.p) ? R(1) : Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, A.p) - R(1)));
+  R qR = le(p_star, B.p) ? R(1) : Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, B.p) - R(1)));
   R SL = qnL - cL * qL, SR = qnR + cR * qR;
   R EL, ER;
   EL = Num<R>::div(A.p, R(K.gm1)) + half(A.r) * (A.u * A.u + A.v * A.v);
@@ -1035,8 +1055,8 @@ __device__ __forceinline__ void flux_hllc(const FluxConsts<R>& K, const Prim<R>&
   R S_star = Num<R>::div(B.p - A.p + A.r * qnL * (SL - qnL) - B.r * qnR * (SR - qnR),
                          A.r * (SL - qnL) - B.r * (SR - qnR));
   R Fn[4];
-  if (SL >= R(0) || !(SR > R(0) || S_star >= R(0))) {
-    const bool useL = SL >= R(0);
+  if (ge0(SL) || !(gt0(SR) || ge0(S_star))) {
+    const bool useL = ge0(SL);
     const Prim<R>& S = useL ? A : B;
     R qn = useL ? qnL : qnR, qt = useL ? qtL : qtR, E = useL ? EL : ER;
     Fn[0] = S.r * qn;
@@ -1044,7 +1064,7 @@ __device__ __forceinline__ void flux_hllc(const FluxConsts<R>& K, const Prim<R>&
     Fn[2] = S.r * qn * qt;
     Fn[3] = qn * (E + S.p);
   } else {
-    const bool useL = S_star >= R(0);
+    const bool useL = ge0(S_star);
     const Prim<R>& S = useL ? A : B;
     R qn = useL ? qnL : qnR, qt = useL ? qtL : qtR, E = useL ? EL : ER, SK = useL ? SL : SR;
     R f = Num<R>::div(S.r * (SK - qn), SK - S_star);
@@ -1130,13 +1150,23 @@ __device__ __forceinline__ double divergence_fp64(double Fi, double Fim, double 
   double mj = rmax(rmax(rabs(Fj), rabs(Fjm)), 1.0);
   // x / 1.0 is exact: skip the division when the scale is 1
   double a, b;
+  // (the scale is 1 or above; compares on the integer pipe, mi * REL_TOL = REL_TOL for mi = 1)
   using N = Num<double>;
-  if (mi == 1.0) a = ((Fi * G.l2) + (-(Fim * G.l4))) * mi;
-  else a = ((N::div(Fi, mi) * G.l2) + (-(N::div(Fim, mi) * G.l4))) * mi;
-  if (mj == 1.0) b = ((Fj * G.l3) + (-(Fjm * G.l1))) * mj;
-  else b = ((N::div(Fj, mj) * G.l3) + (-(N::div(Fjm, mj) * G.l1))) * mj;
-  if (rabs(a) < mi * REL_TOL) a = 0.0;
-  if (rabs(b) < mj * REL_TOL) b = 0.0;
+  const long long ONE = 0x3ff0000000000000LL;
+  if (__double_as_longlong(mi) == ONE) {
+    a = ((Fi * G.l2) + (-(Fim * G.l4))) * mi;
+    if (abs_lt(a, REL_TOL)) a = 0.0;
+  } else {
+    a = ((N::div(Fi, mi) * G.l2) + (-(N::div(Fim, mi) * G.l4))) * mi;
+    if (abs_lt(a, mi * REL_TOL)) a = 0.0;
+  }
+  if (__double_as_longlong(mj) == ONE) {
+    b = ((Fj * G.l3) + (-(Fjm * G.l1))) * mj;
+    if (abs_lt(b, REL_TOL)) b = 0.0;
+  } else {
+    b = ((N::div(Fj, mj) * G.l3) + (-(N::div(Fjm, mj) * G.l1))) * mj;
+    if (abs_lt(b, mj * REL_TOL)) b = 0.0;
+  }
   double s = a + b;
   if (abs_lt(s, NEAR0)) s = 0.0;
   return G.inv_vol != 0.0 ? (-s) * G.inv_vol : N::div(-s, G.vol);

@@ -476,10 +476,10 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
           double u, v, p, cs;
           prim_from_cons(A.gamma, A.gamma - 1.0, un[0], un[1], un[2], un[3], u, v, p, cs);
           double d = div_rn(A.cfl, div_rn(fabs(u) + cs, cg.dx) + div_rn(fabs(v) + cs, cg.dy));
-          if (d < dt_loc) dt_loc = d;
-          if (isnan(un[0]) || isnan(u) || isnan(v) || isnan(p)) st_loc |= ST_NAN;
-          if (un[0] < 0.0) st_loc |= ST_NEG_DENSITY;
-          if (p < 0.0) st_loc |= ST_NEG_PRESSURE;
+          if (d_less(d, dt_loc)) dt_loc = d;
+          if (d_isnan(un[0]) || d_isnan(u) || d_isnan(v) || d_isnan(p)) st_loc |= ST_NAN;
+          if (lt0(un[0])) st_loc |= ST_NEG_DENSITY;
+          if (lt0(p)) st_loc |= ST_NEG_PRESSURE;
         } else if constexpr (Prec<R>::kind == 2) {
           df u, v, p, cs;
           prim_from_cons(g, g1, to_df(un[0]), to_df(un[1]), to_df(un[2]), to_df(un[3]), u, v,

@@ -40,6 +40,10 @@ def main(argv=None) -> int:
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--plan", default="", help="threads,rows_per_cta (default: the handle's)")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="FP64 stage kernel register budget 0 or 1 (default: the handle's)")
+    ap.add_argument("--tune", action="store_true",
+                    help="autotune plan and variant on real steps before the timed ones")
     ap.add_argument("--flux", default="", help="edge flux instead of the workload's (e.g. Roe)")
     ap.add_argument("--limiter", default="", help="limiter instead of the workload's (e.g. MLP5)")
     ap.add_argument("--t-start", type=float, default=0.0,
@@ -62,12 +66,17 @@ def main(argv=None) -> int:
     f = Fluid(cfg).initialize(*prims)
     if a.plan:
         f.set_plan(*(int(x) for x in a.plan.split(",")))
+    if a.variant >= 0:
+        f.set_kernel_variant(a.variant)
+    tuned = f.tune(2)[0] if a.tune else 0
     ms, kern = f.run_timed(a.steps, per_kernel=True)
     cells = cfg.ni * cfg.nj
     print(json.dumps({"workload": a.workload, "flux": cfg.flux_solver, "limiter": cfg.limiter,
                       "ni": cfg.ni, "nj": cfg.nj,
                       "precision": a.precision, "steps": a.steps, "ms": ms,
-                      "kernel_ms": kern, "cell_updates_per_s": cells * a.steps / (ms / 1e3)}))
+                      "kernel_ms": kern, "cell_updates_per_s": cells * a.steps / (ms / 1e3),
+                      "plan": list(f.get_plan()), "variant": f.get_kernel_variant(),
+                      "tuning_steps": tuned}))
     return 0
 
 
