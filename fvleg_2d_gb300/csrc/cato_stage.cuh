@@ -552,9 +552,14 @@ template <typename R> constexpr int min_blocks() {
   return Prec<R>::kind == 2 ? CATO_DF_MIN_BLOCKS
                             : (Prec<R>::kind == 1 ? CATO_F32_MIN_BLOCKS : CATO_F64_MIN_BLOCKS);
 }
+// the persistent FP64 batch kernels (256-thread CTAs)
+#ifndef CATO_F64_BATCH_MIN_BLOCKS
+#define CATO_F64_BATCH_MIN_BLOCKS CATO_F64_MIN_BLOCKS
+#endif
 template <typename R> constexpr int batch_min_blocks() {
   return Prec<R>::kind == 2 ? CATO_DF_MIN_BLOCKS
-                            : (Prec<R>::kind == 1 ? CATO_F32_BATCH_MIN_BLOCKS : CATO_F64_MIN_BLOCKS);
+                            : (Prec<R>::kind == 1 ? CATO_F32_BATCH_MIN_BLOCKS
+                                                  : CATO_F64_BATCH_MIN_BLOCKS);
 }
 
 template <typename R, int NG, int FLUX, int RECON, bool EXT, int MB>
