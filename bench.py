@@ -220,6 +220,17 @@ def quadrant_state(args):
     from fvleg_2d_gb300.fluid import Fluid
 
     key = (args.n, args.t_start)
+    # optional on-disk copy (CATO_BENCH_STATE_CACHE=<dir>), so that a profiler run of the bench
+    # after a plain run does not spend its launch budget on the mixed-path advance
+    cache_dir = os.environ.get("CATO_BENCH_STATE_CACHE")
+    cache = (os.path.join(cache_dir, f"quadrant_{args.n}_{args.t_start}.npz")
+             if cache_dir and args.t_start > 0 else None)
+    if key not in _DEVELOPED and cache and os.path.exists(cache):
+        import numpy as np
+
+        cfg, _ = ic.riemann_quadrant(args.n)
+        with np.load(cache) as z:
+            _DEVELOPED[key] = (cfg, [np.asfortranarray(z[k]) for k in ("rho", "u", "v", "p")])
     if key not in _DEVELOPED:
         cfg, prims = ic.riemann_quadrant(args.n)
         if args.t_start > 0:
@@ -228,6 +239,11 @@ def quadrant_state(args):
             s = f.state(("rho", "u", "v", "p"))
             prims = [s["rho"], s["u"], s["v"], s["p"]]
             f.close()
+            if cache:
+                import numpy as np
+
+                os.makedirs(cache_dir, exist_ok=True)
+                np.savez(cache, **dict(zip(("rho", "u", "v", "p"), prims)))
         _DEVELOPED[key] = (cfg, prims)
     return _DEVELOPED[key]
 
