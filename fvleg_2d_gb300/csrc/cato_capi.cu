@@ -421,9 +421,20 @@ static int d2h_interior(cato_handle* h, double* dst, const double* src, int64_t 
   return CATO_OK;
 }
 
+// zero the ghost ring of a halo-padded host field (the interior is overwritten by the copy that
+// follows): the first and last ng columns in full, ng cells at both ends of every other column
 static void zero_host_field(cato_handle* h, double* a, int64_t ld) {
-  const size_t rows = (size_t)h->nj + 2 * h->ng;
-  for (size_t j = 0; j < rows; ++j) std::memset(a + j * ld, 0, sizeof(double) * (h->ni + 2 * h->ng));
+  const size_t ng = (size_t)h->ng, ni = (size_t)h->ni, nj = (size_t)h->nj;
+  const size_t len = ni + 2 * ng;
+  for (size_t j = 0; j < nj + 2 * ng; ++j) {
+    double* col = a + j * ld;
+    if (j < ng || j >= nj + ng) {
+      std::memset(col, 0, sizeof(double) * len);
+    } else {
+      std::memset(col, 0, sizeof(double) * ng);
+      std::memset(col + ng + ni, 0, sizeof(double) * ng);
+    }
+  }
 }
 
 
