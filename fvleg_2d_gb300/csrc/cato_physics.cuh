@@ -1049,19 +1049,23 @@ __device__ __forceinline__ void flux_hllc(const FluxConsts<R>& K, const Prim<R>&
   R p_pvrs = half(A.p + B.p) - half(qnR - qnL) * rho_bar * c_bar;
   R p_star = rmax(R(0), p_pvrs);
   const R gf = R(K.hllc_gf);
-  R qL = le(p_star, A.p) ? R(1) : Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, A.p) - R(1)));
-  R qR = le(p_star, B.p) ? R(1) : Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, B.p) - R(1)));
-  R SL = qnL - cL * qL, SR = qnR + cR * qR;
-  R EL, ER;
-  EL = Num<R>::div(A.p, R(K.gm1)) + half(A.r) * (A.u * A.u + A.v * A.v);
-  ER = Num<R>::div(B.p, R(K.gm1)) + half(B.r) * (B.u * B.u + B.v * B.v);
+  // SL = qnL - cL qL, SR = qnR + cR qR with q = 1 (then c q is c) unless p_star exceeds p
+  R SL, SR;
+  if (le(p_star, A.p)) SL = qnL - cL;
+  else SL = qnL - cL * Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, A.p) - R(1)));
+  if (le(p_star, B.p)) SR = qnR + cR;
+  else SR = qnR + cR * Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, B.p) - R(1)));
+  // the total energy of the side the flux is taken from (only that one is needed)
+  auto energy = [&](const Prim<R>& S) {
+    return Num<R>::div(S.p, R(K.gm1)) + half(S.r) * (S.u * S.u + S.v * S.v);
+  };
   R S_star = Num<R>::div(B.p - A.p + A.r * qnL * (SL - qnL) - B.r * qnR * (SR - qnR),
                          A.r * (SL - qnL) - B.r * (SR - qnR));
   R Fn[4];
   if (ge0(SL) || !(gt0(SR) || ge0(S_star))) {
     const bool useL = ge0(SL);
     const Prim<R>& S = useL ? A : B;
-    R qn = useL ? qnL : qnR, qt = useL ? qtL : qtR, E = useL ? EL : ER;
+    R qn = useL ? qnL : qnR, qt = useL ? qtL : qtR, E = energy(S);
     Fn[0] = S.r * qn;
     Fn[1] = S.r * qn * qn + S.p;
     Fn[2] = S.r * qn * qt;
@@ -1069,7 +1073,7 @@ __device__ __forceinline__ void flux_hllc(const FluxConsts<R>& K, const Prim<R>&
   } else {
     const bool useL = ge0(S_star);
     const Prim<R>& S = useL ? A : B;
-    R qn = useL ? qnL : qnR, qt = useL ? qtL : qtR, E = useL ? EL : ER, SK = useL ? SL : SR;
+    R qn = useL ? qnL : qnR, qt = useL ? qtL : qtR, E = energy(S), SK = useL ? SL : SR;
     R f = Num<R>::div(S.r * (SK - qn), SK - S_star);
     R Us0 = f, Us1 = f * S_star, Us2 = f * qt;
     R Us3 = f * (Num<R>::div(E, S.r) +
