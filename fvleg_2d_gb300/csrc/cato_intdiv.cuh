@@ -11,8 +11,9 @@
 //      1/b with e = 1 - b y0, and y1 = y0 (1 + e/2 + 3e^2/8) for 1/sqrt(a) with e = 1 - a y0^2
 //      (J.-M. Muller et al., Handbook of Floating-Point Arithmetic, 2nd ed., 2018, sections 4.7
 //      and 11.3: Newton-Raphson iterations for the reciprocal and the reciprocal square root);
-//   3. the quotient a y1 (or the root a y1) from the high half of a 64 x 64-bit product, within
-//      three units of 2^-61 of the exact value, then the nearest significand M1;
+//   3. the quotient a y1 (or the root a y1) from three 32 x 32-bit partial products of the
+//      64 x 64-bit product, within 43 units of 2^-61 (29 units of 2^-60 for the root) of the exact
+//      value, far inside the 128 units the next step allows, then the nearest significand M1;
 //   4. the exact rounding decision: the signs of the integer remainders
 //      2^k A - (2 M1 +- 1) B (division) or 2^k A - (2 M1 +- 1)^2 (square root), computed
 //      modulo 2^64 because their magnitudes are below 2^63, decide between M1 - 1, M1 and
