@@ -1042,18 +1042,20 @@ int cato_gpu_tune(cato_handle* h, int32_t steps, int32_t* steps_taken, float* be
   if (!h || steps < 1) return CATO_ERR_ARG;
   if (steps_taken) *steps_taken = 0;
   if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
-  // candidates: the default plan, 256-wide strips, half the rows per CTA; each with both FP64
-  // register budgets
+  // candidates: the default plan, 256-wide strips, half and a quarter of the rows per CTA; each
+  // with both FP64 register budgets
   const Plan p0 = h->plan;
   std::vector<Plan> cands;
   const int wide = 256, half_rows = std::max(8, p0.rows_per_cta / 2);
+  const int quarter_rows = std::max(8, p0.rows_per_cta / 4);
   const int nvar = h->cfg.precision == CATO_FP64 ? 2 : 1;
   for (int v = 0; v < nvar; ++v) {
-    Plan a = p0, b = p0, c = p0;
-    a.variant = b.variant = c.variant = v;
+    Plan a = p0, b = p0, c = p0, d = p0;
+    a.variant = b.variant = c.variant = d.variant = v;
     b.threads = wide;
     c.rows_per_cta = half_rows;
-    for (const Plan& q : {a, b, c}) {
+    d.rows_per_cta = quarter_rows;
+    for (const Plan& q : {a, b, c, d}) {
       bool dup = false;
       for (const Plan& x : cands)
         dup |= x.threads == q.threads && x.rows_per_cta == q.rows_per_cta && x.variant == q.variant;

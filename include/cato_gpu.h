@@ -294,7 +294,7 @@ int cato_gpu_set_kernel_variant(cato_handle* h, int32_t variant);
 int cato_gpu_get_kernel_variant(const cato_handle* h, int32_t* variant);
 
 /* Autotune the stage kernel on the live state: a few candidate plans (the current one, 256-wide
- * strips, half the rows per CTA), each with both FP64 register budgets, run `steps` CFL steps
+ * strips, half and a quarter of the rows per CTA), each with both FP64 register budgets, run `steps` CFL steps
  * each (timed with CUDA events), and the fastest stays set.  These are real steps of the run
  * (the solution advances by *steps_taken steps, bit-identical whichever candidate runs them);
  * *best_ms = the fastest candidate's time per step.  Returns the first fluid error, if any. */
