@@ -1,5 +1,5 @@
 // cato_batch.cu -- C-ABI of the batched engine: many independent grid instances of uneven
-// sizes advanced together (BASELINE configs 3 and 4).
+// sizes advanced together (the batched workload of 256 random-circle grids and the serving stream).
 //
 // * Every instance has its own state buffers (as a single-instance handle), its own CFL dt, time,
 //   iteration count and stop condition (t_end, max_steps), kept in a device descriptor.

@@ -1,4 +1,4 @@
-"""Continuous-batching serving loop over the batched engine (BASELINE config 4).
+"""Continuous-batching serving loop over the batched engine (a stream of solve requests).
 
 Solve requests arrive over time (Poisson arrivals in the benchmark).  The loop admits a
 request as soon as a slot and enough of the HBM budget are free, keeps every admitted state on
