@@ -10,7 +10,7 @@ system (``units.f90:94-143``); and for the ``xdmf`` format the XDMF description 
 ``write_xdmf`` (``:386-529``) that points at ``<name>.h5:/<dataset>``.
 
 The datasets are written to ``<name>.h5`` with h5py when it is installed.  Without an HDF5
-library (this build) they go to ``<name>.npz`` with the same names, shapes and attributes
+library they go to ``<name>.npz`` with the same names, shapes and attributes
 (``<dataset>.units``, ``<dataset>.description``), arrays stored transposed as an HDF5 file written
 from Fortran reads in C order.  Scaling follows the reference: a field is written as
 ``data * to_dim * unit_factor`` with ``to_dim = 1 / to_nondim`` of that field

@@ -6,8 +6,8 @@ keys and defaults (``mod_input.f90:34-155``).  Values may be quoted with single 
 use a Fortran ``d`` exponent.
 
 A deck whose initial conditions come from a file (``read_from_file = true``) takes its grid and
-state from that file in pycato's layout (:mod:`.icfile`; ``.npz`` stands in for HDF5, which has
-no library in this build): :func:`run_deck` loads it.  A deck with ``read_from_file = false`` is
+state from that file in pycato's layout (:mod:`.icfile`; ``.npz`` stands in for HDF5 when
+h5py is not installed): :func:`run_deck` loads it.  A deck with ``read_from_file = false`` is
 complete: its uniform initial state and grid come from the deck (``[initial_conditions] init_*``,
 ``[grid] ni_nodes ... ymax``).
 """

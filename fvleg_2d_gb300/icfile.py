@@ -17,7 +17,7 @@ primitives by ``density_to_nondim``, ``vel_to_nondim`` and ``press_to_nondim``
 (``mod_fluid.f90:347-350``; the factors of ``set_refrence_quantities``,
 ``src/lib/non_dimensional.f90:95-135``).
 
-No HDF5 library is part of this build.  ``.npz`` files with the same dataset names, shapes and
+Without an HDF5 library (h5py), ``.npz`` files with the same dataset names, shapes and
 transposition (and the units as ``<name>.units`` strings) stand in for the HDF5 file;
 :func:`write_ic` writes one, :func:`read_ic` reads either (``.h5`` through ``h5py`` when that is
 installed).
