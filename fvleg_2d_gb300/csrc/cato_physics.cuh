@@ -375,6 +375,18 @@ __device__ __forceinline__ void recon_tvd2(int lim, R qm1, R q0, R qp1, R qp2, R
   Rr = slope_step(qp1, tvd_phi_edge(lim, d0, dp), dp, true);
 }
 
+// FP64 TVD2 edge values out of line: one copy per kernel instead of one per variable and
+// direction keeps the stage kernel inside the instruction cache
+struct EdgePair {
+  double L, R;
+};
+static __device__ __noinline__ EdgePair recon_tvd2_f64(int lim, double qm1, double q0, double qp1,
+                                                      double qp2) {
+  EdgePair e;
+  recon_tvd2<double>(lim, qm1, q0, qp1, qp2, e.L, e.R);
+  return e;
+}
+
 // FP32 (mixed path): the limited slope phi(r) * dq without the ratio.  For r = d0/dq > 0,
 // minmod gives min(r, 1) dq = (|d0| < |dq| ? d0 : dq), superbee picks one of 2 d0, dq, d0, 2 dq,
 // and van Leer's 2r/(1+r) dq = 2 d0 dq / (dq + d0); r <= 0 gives 0.  Written with selects (no

@@ -131,7 +131,13 @@ __device__ __forceinline__ void edge_flux(const R* const rp[6], int T, int lim, 
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     if (RECON == 0) {
-      recon_tvd2<R>(lim, Q(k, -1, 0), Q(k, 0, 0), Q(k, 1, 0), Q(k, 2, 0), Lv[k], Rv[k]);
+      if constexpr (Prec<R>::kind == 0) {
+        const EdgePair e = recon_tvd2_f64(lim, Q(k, -1, 0), Q(k, 0, 0), Q(k, 1, 0), Q(k, 2, 0));
+        Lv[k] = e.L;
+        Rv[k] = e.R;
+      } else {
+        recon_tvd2<R>(lim, Q(k, -1, 0), Q(k, 0, 0), Q(k, 1, 0), Q(k, 2, 0), Lv[k], Rv[k]);
+      }
     } else {
       R qm2 = RECON == 5 ? Q(k, -2, 0) : R(0), qp3 = RECON == 5 ? Q(k, 3, 0) : R(0);
       recon_mlp<R, RECON>(qm2, Q(k, -1, 0), Q(k, 0, 0), Q(k, 1, 0), Q(k, 2, 0), qp3, Q(k, 0, 1),
