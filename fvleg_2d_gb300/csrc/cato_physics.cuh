@@ -491,6 +491,16 @@ __device__ __forceinline__ void recon_mlp(R qm2, R qm1, R q0, R qp1, R qp2, R qp
   Rr = slope_step(qp1, phiR, dp, true);
 }
 
+// FP64 MLP edge values out of line (one copy per kernel, as recon_tvd2_f64)
+template <int ORDER>
+static __device__ __noinline__ EdgePair recon_mlp_f64(double qm2, double qm1, double q0, double qp1,
+                                                     double qp2, double qp3, double t0p,
+                                                     double t0m, double t1p, double t1m) {
+  EdgePair e;
+  recon_mlp<double, ORDER>(qm2, qm1, q0, qp1, qp2, qp3, t0p, t0m, t1p, t1m, e.L, e.R);
+  return e;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Double-float reconstruction (mixed_df).  The limited slope phi(r) * dq is, for each branch of
 // the limiter, an algebraic combination of the slope differences themselves: with r = d0/dm,

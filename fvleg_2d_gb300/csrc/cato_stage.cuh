@@ -140,8 +140,16 @@ __device__ __forceinline__ void edge_flux(const R* const rp[6], int T, int lim, 
       }
     } else {
       R qm2 = RECON == 5 ? Q(k, -2, 0) : R(0), qp3 = RECON == 5 ? Q(k, 3, 0) : R(0);
-      recon_mlp<R, RECON>(qm2, Q(k, -1, 0), Q(k, 0, 0), Q(k, 1, 0), Q(k, 2, 0), qp3, Q(k, 0, 1),
-                          Q(k, 0, -1), Q(k, 1, 1), Q(k, 1, -1), Lv[k], Rv[k]);
+      if constexpr (Prec<R>::kind == 0) {
+        const EdgePair e = recon_mlp_f64<RECON>(qm2, Q(k, -1, 0), Q(k, 0, 0), Q(k, 1, 0),
+                                                Q(k, 2, 0), qp3, Q(k, 0, 1), Q(k, 0, -1),
+                                                Q(k, 1, 1), Q(k, 1, -1));
+        Lv[k] = e.L;
+        Rv[k] = e.R;
+      } else {
+        recon_mlp<R, RECON>(qm2, Q(k, -1, 0), Q(k, 0, 0), Q(k, 1, 0), Q(k, 2, 0), qp3,
+                            Q(k, 0, 1), Q(k, 0, -1), Q(k, 1, 1), Q(k, 1, -1), Lv[k], Rv[k]);
+      }
     }
   }
   Prim<R> A = {Lv[0], Lv[1], Lv[2], Lv[3]}, B = {Rv[0], Rv[1], Rv[2], Rv[3]};
