@@ -301,8 +301,7 @@ def bench_precision(args, precision, dist, world, peak_gbs):
             peak = 2 * sms * mhz / 1e3
             res["roofline"]["fp64_pipe"] = {
                 "achieved": got, "peak": peak, "unit": "G FP64 thread-instructions/s",
-                "frac": got / peak, "instructions_per_cell_stage": ipc,
-                "source": "profiles/stage_kernel_fp64_quadrant2048_developed.md"}
+                "frac": got / peak, "instructions_per_cell_stage": ipc}
     f.close()
     return res, cfg, prims
 

@@ -20,6 +20,7 @@
 #include "../../include/cato_gpu.h"
 #include "cato_kernels.cuh"
 #include "cato_launch.cuh"
+#include "cato_setup.cuh"
 
 using namespace cato;
 
@@ -379,20 +380,7 @@ int cato_batch_add(cato_batch* b, const cato_config* cfg, const double* rho, con
   d.bc_p = cfg->bc_pressure;
   d.cfl = cfg->cfl;
   // the same constants and uniform geometry as a single-instance handle
-  const double g = cfg->gamma;
-  d.K64.gamma = g;
-  d.K64.g_over_gm1 = g / (g - 1.0);
-  d.K64.gm1 = g - 1.0;
-  d.K64.two_gm1_over_gp1 = 2.0 * ((g - 1.0) / (g + 1.0));
-  d.K64.gamma_factor = ((2.0 * (g - 1.0)) / (g + 1.0));
-  d.K64.hllc_gf = (g + 1.0) / (2.0 * g);
-  d.K64.harten_delta = cfg->harten_delta;
-  d.K64.ausm_beta = cfg->ausm_beta;
-  d.K64.ausm_kp = cfg->ausm_kp;
-  d.K64.ausm_ku = cfg->ausm_ku;
-  d.K64.ausm_sigma = cfg->ausm_sigma;
-  d.K64.low_mach_fix = cfg->apply_low_mach_fix ? 1 : 0;
-  d.K64.harten = cfg->roe_entropy_fix == CATO_ROE_HARTEN ? 1 : 0;
+  d.K64 = flux_consts_of(*cfg);
   d.K32 = convert_consts<float>(d.K64);
   d.Kdf = convert_consts<df>(d.K64);
   d.G = uniform_geom(cfg->dx, cfg->dy);

@@ -23,6 +23,7 @@
 #include "cato_kernels.cuh"
 #include "cato_launch.cuh"
 #include "cato_pbc.cuh"
+#include "cato_setup.cuh"
 #include "cato_source.cuh"
 
 using namespace cato;
@@ -111,9 +112,7 @@ static int cuda_fail(cato_handle* h, cudaError_t e, const char* where) {
     if (_e != cudaSuccess) return cuda_fail(h, _e, #call); \
   } while (0)
 
-static int recon_of(int limiter) {
-  return limiter == CATO_LIM_MLP3 ? 3 : (limiter == CATO_LIM_MLP5 ? 5 : 0);
-}
+static int recon_of(int limiter) { return recon_of_limiter(limiter); }
 
 // rk(m,n) stage weights, mod_fluid.f90:926-945
 static const double* rk_alpha(int rk, int* ns) {
@@ -150,38 +149,18 @@ static std::vector<Stage> build_stages(int rk) {
 }
 
 static void fill_consts(cato_handle* h) {
-  const cato_config& c = h->cfg;
-  const double g = c.gamma;
-  FluxConsts<double> K{};
-  K.gamma = g;
-  K.g_over_gm1 = g / (g - 1.0);
-  K.gm1 = g - 1.0;
-  K.two_gm1_over_gp1 = 2.0 * ((g - 1.0) / (g + 1.0));
-  K.gamma_factor = ((2.0 * (g - 1.0)) / (g + 1.0));
-  K.hllc_gf = (g + 1.0) / (2.0 * g);
-  K.harten_delta = c.harten_delta;
-  K.ausm_beta = c.ausm_beta;
-  K.ausm_kp = c.ausm_kp;
-  K.ausm_ku = c.ausm_ku;
-  K.ausm_sigma = c.ausm_sigma;
-  K.low_mach_fix = c.apply_low_mach_fix ? 1 : 0;
-  K.harten = c.roe_entropy_fix == CATO_ROE_HARTEN ? 1 : 0;
+  const FluxConsts<double> K = flux_consts_of(h->cfg);
   h->K64 = K;
   h->K32 = convert_consts<float>(K);
   h->Kdf = convert_consts<df>(K);
-  const Geom G = uniform_geom(c.dx, c.dy);
-  h->G = G;
+  h->G = uniform_geom(h->cfg.dx, h->cfg.dy);
 }
 
 static void default_plan(cato_handle* h) {
-  // Wide strips for large grids; narrow strips and short marches for small grids so that the
-  // launch fills the 152 SMs.
-  const long long cells = (long long)h->ni * h->nj;
+  const LaunchShape d = default_shape(h->ni, h->nj, h->ng);
   Plan p;
-  if (cells < 200000) { p.threads = 64; p.rows_per_cta = 8; }
-  else if (cells < 4000000) { p.threads = 128; p.rows_per_cta = 32; }
-  else { p.threads = 128; p.rows_per_cta = 64; }
-  if (p.threads - 2 * h->ng > h->ni + 2 * h->ng) p.threads = 64;
+  p.threads = d.threads;
+  p.rows_per_cta = d.rows_per_cta;
   h->plan = p;
 }
 

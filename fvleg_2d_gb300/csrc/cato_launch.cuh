@@ -10,18 +10,33 @@
 
 namespace cato {
 
+// A kernel's function attributes (here its dynamic shared-memory limit) belong to the GPU that
+// is current when they are set, so the "already set" flags are kept per device.
+constexpr int kMaxDevices = 64;
+struct PerDevice {
+  std::atomic<bool> done[kMaxDevices] = {};
+  std::atomic<int> sms[kMaxDevices] = {};
+};
+// the current device, or -1 when it cannot be read or lies beyond kMaxDevices
+inline int launch_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return -1;
+  return dev;
+}
 
 template <typename R, int NG, int FLUX, int RECON, bool EXT, int MB = min_blocks<R>()>
 cudaError_t launch_stage_ext(dim3 grid, int threads, cudaStream_t stream, const StageArgs& A,
                              const FluxConsts<R>& K) {
-  static std::atomic<bool> attr_done{false};
+  static PerDevice attr;
   const size_t smem = stage_smem_bytes<R>(threads, NG);
-  if (!attr_done.load(std::memory_order_acquire)) {
+  const int dev = launch_device();
+  if (dev < 0) return cudaErrorInvalidDevice;
+  if (!attr.done[dev].load(std::memory_order_acquire)) {
     cudaError_t e = cudaFuncSetAttribute(stage_kernel<R, NG, FLUX, RECON, EXT, MB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)stage_smem_bytes<R>(256, 3));
     if (e != cudaSuccess) return e;
-    attr_done.store(true, std::memory_order_release);
+    attr.done[dev].store(true, std::memory_order_release);
   }
   if (grid.x == 0 || grid.y == 0) return cudaSuccess;  // attribute warm-up only
   stage_kernel<R, NG, FLUX, RECON, EXT, MB><<<grid, threads, smem, stream>>>(A, K);
@@ -72,26 +87,26 @@ inline cudaError_t launch_stage_flux(int recon, dim3 grid, int threads, cudaStre
 // Persistent batch launch: as many CTAs as can be resident, each looping over work items.
 template <typename R, int NG, int FLUX, int RECON>
 cudaError_t launch_batch_one(int threads, cudaStream_t stream, const BatchStageArgs& B) {
-  static std::atomic<bool> attr_done{false};
-  static std::atomic<int> sms{0};
+  static PerDevice attr;
   const size_t smem = stage_smem_bytes<R>(threads, NG);
-  if (!attr_done.load(std::memory_order_acquire)) {
+  const int dev = launch_device();
+  if (dev < 0) return cudaErrorInvalidDevice;
+  if (!attr.done[dev].load(std::memory_order_acquire)) {
     cudaError_t e = cudaFuncSetAttribute(batch_stage_kernel<R, NG, FLUX, RECON>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)stage_smem_bytes<R>(256, 3));
     if (e != cudaSuccess) return e;
-    int dev = 0, n = 0;
-    cudaGetDevice(&dev);
+    int n = 0;
     cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    sms.store(n > 0 ? n : 1);
-    attr_done.store(true, std::memory_order_release);
+    attr.sms[dev].store(n > 0 ? n : 1);
+    attr.done[dev].store(true, std::memory_order_release);
   }
   if (B.n_items <= 0) return cudaSuccess;
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
       &per_sm, batch_stage_kernel<R, NG, FLUX, RECON>, threads, smem);
   if (e != cudaSuccess) return e;
-  long long grid = (long long)(per_sm > 0 ? per_sm : 1) * sms.load();
+  long long grid = (long long)(per_sm > 0 ? per_sm : 1) * attr.sms[dev].load();
   if (grid > B.n_items) grid = B.n_items;
   batch_stage_kernel<R, NG, FLUX, RECON><<<(unsigned)grid, threads, smem, stream>>>(B);
   return cudaGetLastError();

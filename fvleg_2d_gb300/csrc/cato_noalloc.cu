@@ -16,22 +16,25 @@
 //   CATO_ERR_CAPACITY before any GPU work.
 // * The first call on a device looks up the array's device address (cudaGetSymbolAddress, with
 //   that device current) and caches it per device; make that first call before any CUDA stream
-//   capture.
+//   capture.  The cached address belongs to the device's primary context: after
+//   cudaDeviceReset on that device the entry point must not be called again in this process.
 // * Every call in the process shares the one array, which keeps the last call's contents.  Calls
 //   that overlapped on the GPU would race on it, so each call holds a per-device lock, works on
-//   the legacy default stream and synchronizes it before returning.
+//   the calling thread's per-thread default stream (cudaStreamPerThread, which does not wait for
+//   or block the process's other streams) and synchronizes it before returning.
 #include <cstring>
 #include <mutex>
 
 #include "../../include/cato_gpu.h"
+#include "cato_kernels.cuh"
 #include "cato_launch.cuh"
+#include "cato_setup.cuh"
 
 using namespace cato;
 
 namespace {
 
 constexpr size_t kScratchDoubles = size_t(4) << 20;  // 4 Mi doubles = 32 MiB per device
-constexpr int kMaxDevices = 64;
 constexpr size_t kAlign = 32;                         // doubles (256 B)
 
 }  // namespace
@@ -45,31 +48,6 @@ std::mutex g_dev_mutex[kMaxDevices];
 double* g_scratch_dev[kMaxDevices] = {};
 
 size_t round_up(size_t n) { return (n + kAlign - 1) / kAlign * kAlign; }
-
-// the BC-filled halo-padded primitives written back to the caller (flux_solver.f90:138-185)
-__global__ void noalloc_fill_ghosts(int ni, int nj, int pitch, int ng, int4 bc, double gamma,
-                                    double bc_p,
-                                    const double* __restrict__ r_, const double* __restrict__ u_,
-                                    const double* __restrict__ v_, const double* __restrict__ p_,
-                                    double* ro, double* uo, double* vo, double* po, long long ld) {
-  const int W = ni + 2 * ng, H = nj + 2 * ng;
-  const int bcs[4] = {bc.x, bc.y, bc.z, bc.w};
-  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < (long long)W * H;
-       n += (long long)gridDim.x * blockDim.x) {
-    const int ii = (int)(n % W), jj = (int)(n / W);
-    bool fx, fy;
-    const int sx = map_index(ii - ng, ni, bcs[SIDE_MX], bcs[SIDE_PX], fx);
-    const int sy = map_index(jj - ng, nj, bcs[SIDE_MY], bcs[SIDE_PY], fy);
-    const size_t s = (size_t)sy * pitch + sx;
-    const size_t o = (size_t)jj * ld + ii;
-    double r = r_[s], u = fx ? -u_[s] : u_[s], v = fy ? -v_[s] : v_[s], p = p_[s];
-    if (bcs[SIDE_PX] == BC_OUTLET && ii - ng >= ni) outlet_ghost<double>(gamma, bc_p, r, u, v, p);
-    ro[o] = r;
-    uo[o] = u;
-    vo[o] = v;
-    po[o] = p;
-  }
-}
 
 }  // namespace
 
@@ -114,7 +92,7 @@ extern "C" int cato_gpu_solve_noalloc(const cato_config* cfg, double* rho, doubl
     gh[k] = base + 8 * field + k * halo;
   }
   double* ctl = base + 8 * field + 4 * halo;
-  const cudaStream_t s = 0;  // legacy default stream
+  const cudaStream_t s = cudaStreamPerThread;
   double* host_prim[4] = {rho, u, v, p};
   double* host_res[4] = {d_rho_dt, d_rho_u_dt, d_rho_v_dt, d_rho_E_dt};
 
@@ -134,23 +112,10 @@ extern "C" int cato_gpu_solve_noalloc(const cato_config* cfg, double* rho, doubl
                             host_prim[k] + (size_t)ng * ld + ng, (size_t)ld * sizeof(double),
                             (size_t)ni * sizeof(double), (size_t)nj, cudaMemcpyHostToDevice, s));
 
-  // flux constants and uniform geometry, the same quantities a handle derives from cfg
-  const double g = cfg->gamma;
-  FluxConsts<double> K{};
-  K.gamma = g;
-  K.g_over_gm1 = g / (g - 1.0);
-  K.gm1 = g - 1.0;
-  K.two_gm1_over_gp1 = 2.0 * ((g - 1.0) / (g + 1.0));
-  K.gamma_factor = ((2.0 * (g - 1.0)) / (g + 1.0));
-  K.hllc_gf = (g + 1.0) / (2.0 * g);
-  K.harten_delta = cfg->harten_delta;
-  K.ausm_beta = cfg->ausm_beta;
-  K.ausm_kp = cfg->ausm_kp;
-  K.ausm_ku = cfg->ausm_ku;
-  K.ausm_sigma = cfg->ausm_sigma;
-  K.low_mach_fix = cfg->apply_low_mach_fix ? 1 : 0;
-  K.harten = cfg->roe_entropy_fix == CATO_ROE_HARTEN ? 1 : 0;
+  // flux constants, uniform geometry and launch shape: those a handle derives from cfg
+  const FluxConsts<double> K = flux_consts_of(*cfg);
   const Geom G = uniform_geom(cfg->dx, cfg->dy);
+  const LaunchShape shape = default_shape(ni, nj, ng);
 
   StageArgs A;
   std::memset(&A, 0, sizeof(A));
@@ -159,9 +124,8 @@ extern "C" int cato_gpu_solve_noalloc(const cato_config* cfg, double* rho, doubl
   A.pitch = pitch;
   for (int k = 0; k < 4; ++k) A.bc[k] = cfg->bc[k];
   A.limiter = cfg->limiter;
-  const bool small = (long long)ni * nj < 200000;
-  const int threads = small ? 64 : 128;
-  A.rows_per_cta = small ? 8 : 32;
+  const int threads = shape.threads;
+  A.rows_per_cta = shape.rows_per_cta;
   A.kind = 2;
   A.dt = ctl;
   A.dt_min = reinterpret_cast<unsigned long long*>(ctl + 1);
@@ -176,7 +140,7 @@ extern "C" int cato_gpu_solve_noalloc(const cato_config* cfg, double* rho, doubl
     A.Uo[k] = res[k];
   }
   const int W = threads - 2 * ng;
-  const int recon = cfg->limiter == CATO_LIM_MLP3 ? 3 : (cfg->limiter == CATO_LIM_MLP5 ? 5 : 0);
+  const int recon = recon_of_limiter(cfg->limiter);
   NA_CK(launch_stage<double>(cfg->flux, recon, dim3((ni + W - 1) / W, (nj + A.rows_per_cta - 1) /
                                                                           A.rows_per_cta),
                              threads, s, A, K));
@@ -184,9 +148,11 @@ extern "C" int cato_gpu_solve_noalloc(const cato_config* cfg, double* rho, doubl
   const long long nh = hld * (nj + 2 * ng);
   int blocks = (int)((nh + 255) / 256);
   blocks = blocks > 4864 ? 4864 : blocks;
-  noalloc_fill_ghosts<<<blocks, 256, 0, s>>>(ni, nj, pitch, ng, bc, cfg->gamma, cfg->bc_pressure,
-                                             prim[0], prim[1], prim[2], prim[3], gh[0], gh[1],
-                                             gh[2], gh[3], hld);
+  // the BC-filled halo-padded primitives written back to the caller (flux_solver.f90:138-185);
+  // no pressure-input edge states (that boundary is refused above)
+  fill_ghosts_kernel<<<blocks, 256, 0, s>>>(ni, nj, pitch, ng, bc, cfg->gamma, cfg->bc_pressure,
+                                            nullptr, prim[0], prim[1], prim[2], prim[3], gh[0],
+                                            gh[1], gh[2], gh[3], hld);
   NA_CK(cudaGetLastError());
   for (int k = 0; k < 4; ++k)
     NA_CK(cudaMemcpy2DAsync(host_prim[k], (size_t)ld * sizeof(double), gh[k],

@@ -324,9 +324,12 @@ int cato_gpu_check_divsqrt(int64_t n, uint64_t seed, uint64_t tested[2], uint64_
  * memory is one fixed 32 MiB array per GPU: grids needing more than
  * 8*pitch*nj + 4*(ni+2ng)*(nj+2ng) + 32 doubles (pitch = ni rounded up to 32; 512 x 512 fits)
  * are refused with CATO_ERR_CAPACITY.  The first call on a device sets up the array's address
- * (cudaGetSymbolAddress) and should come before any stream capture.  Calls share the array and
- * would race if they overlapped on the GPU, so each call locks its device, runs on the legacy
- * default stream and synchronizes before returning. */
+ * (cudaGetSymbolAddress) and should come before any stream capture; that address belongs to the
+ * device's primary context, so the entry point must not be called on a device after
+ * cudaDeviceReset of it.  Calls share the array and would race if they overlapped on the GPU, so
+ * each call locks its device, runs on the calling thread's per-thread default stream
+ * (cudaStreamPerThread: it neither waits for nor blocks the process's other streams) and
+ * synchronizes it before returning. */
 int cato_gpu_solve_noalloc(const cato_config* cfg, double* rho, double* u, double* v, double* p,
                            double* d_rho_dt, double* d_rho_u_dt, double* d_rho_v_dt,
                            double* d_rho_E_dt, int64_t ld);

@@ -12,8 +12,8 @@ tests are read as text:
 * ``tests/unit/test_geometry/test_quad_cell.pf`` and ``mod_test_grid.f90`` -- cell metrics and
   the simple grid's node coordinates.
 
-Run from the repository root with the reference checked out at REFERENCE (default
-/root/reference):  ``python tests/golden/make_golden.py``.
+Run from the repository root with the environment variable REFERENCE naming the reference
+checkout:  ``REFERENCE=<checkout> python tests/golden/make_golden.py``.
 """
 from __future__ import annotations
 
@@ -22,7 +22,7 @@ import os
 import re
 import sys
 
-REF = os.environ.get("REFERENCE", "/root/reference")
+REF = os.environ.get("REFERENCE", "")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_unit_vectors.json")
 
 NUM = r"[-+]?\d+\.\d*(?:_rk)?"
@@ -172,6 +172,9 @@ def grid_nodes() -> dict:
 
 
 def main() -> int:
+    if not REF or not os.path.isdir(REF):
+        print("set REFERENCE to the reference checkout", file=sys.stderr)
+        return 2
     data = {
         "generated_by": "tests/golden/make_golden.py",
         "reference": "smillerc/fvleg_2d",

@@ -76,7 +76,9 @@ def test_invalid_decks(edit, msg):
         parse_deck(text).scheme()
 
 
-REF_DECKS = sorted(glob.glob("/root/reference/tests/integrated/*/input.ini"))
+# the reference checkout, when the environment variable REFERENCE names one
+_REF = os.environ.get("REFERENCE", "")
+REF_DECKS = sorted(glob.glob(os.path.join(_REF, "tests/integrated/*/input.ini"))) if _REF else []
 
 
 @pytest.mark.skipif(not REF_DECKS, reason="reference checkout not present")

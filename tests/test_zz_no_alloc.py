@@ -7,6 +7,7 @@ that keeps the previous call's contents.
 This file is collected last so that a run stopping at the first failure has run every other
 test; it also passes on its own in a fresh process."""
 import ctypes
+import gc
 
 import numpy as np
 import pytest
@@ -64,3 +65,45 @@ def test_noalloc_refuses_grids_beyond_its_capacity():
                        700, 700, 0)
     rc, _ = _noalloc(L, cfg, prims)
     assert rc == CATO_ERR_CAPACITY
+    # the refusal leaves the shared array usable: a grid that fits still gives the residual
+    cfg, prims = _case("AUSMPW+", "minmod", {s: "zero_gradient" for s in ("+x", "-x", "+y", "-y")},
+                       64, 40, 1)
+    ref = FluxSolver(cfg).solve(*[a.copy(order="F") for a in prims])
+    rc, got = _noalloc(L, cfg, [a.copy(order="F") for a in prims])
+    assert rc == 0, rc
+    for k in range(4):
+        np.testing.assert_array_equal(got[k], ref[k], err_msg=f"residual {k}")
+
+
+def _cudart():
+    for name in ("libcudart.so", "libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so"):
+        try:
+            return ctypes.CDLL(name)
+        except OSError:
+            continue
+    pytest.fail("libcudart not found: cannot read the device's free memory")
+
+
+def _free_bytes(rt):
+    free, total = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    assert rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    return free.value
+
+
+def test_noalloc_takes_no_device_memory():
+    """The device's free memory is the same before and after further calls of other sizes
+    (each scheme runs once first, so that its kernels are loaded before the measurement)."""
+    L = _lib.load(build_if_missing=True)
+    rt = _cudart()
+    zg = {s: "zero_gradient" for s in ("+x", "-x", "+y", "-y")}
+    cases = [_case("HLLC", "van_leer", zg, 96, 80, 3), _case("HLLC", "van_leer", zg, 512, 500, 4),
+             _case("HLLC", "van_leer", zg, 33, 17, 5)]
+    rc, _ = _noalloc(L, cases[0][0], [a.copy(order="F") for a in cases[0][1]])
+    assert rc == 0, rc
+    gc.collect()
+    before = _free_bytes(rt)
+    for _ in range(2):
+        for cfg, prims in cases:
+            rc, _ = _noalloc(L, cfg, [a.copy(order="F") for a in prims])
+            assert rc == 0, rc
+    assert _free_bytes(rt) == before
