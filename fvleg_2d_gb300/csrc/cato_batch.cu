@@ -508,9 +508,11 @@ int cato_batch_query(cato_batch* b, int32_t slot, int64_t* iteration, double* ti
     *running = (d.ctl.status == 0 && d.ctl.time < d.ctl.t_end && d.ctl.iter < d.ctl.max_iter);
   if (error_code) {
     const int bits = d.ctl.status;
-    *error_code = (bits & ST_NEG_DENSITY) ? CATO_NEG_DENSITY
-                  : (bits & ST_NEG_PRESSURE) ? CATO_NEG_PRESSURE
-                  : (bits & ST_NAN) ? CATO_NANS_FOUND : CATO_OK;
+    // the reference's order: NaN checks at every stage assignment, then negative density,
+    // then negative pressure (mod_fluid.f90:718-737)
+    *error_code = (bits & ST_NAN) ? CATO_NANS_FOUND
+                  : (bits & ST_NEG_DENSITY) ? CATO_NEG_DENSITY
+                  : (bits & ST_NEG_PRESSURE) ? CATO_NEG_PRESSURE : CATO_OK;
   }
   return CATO_OK;
 }

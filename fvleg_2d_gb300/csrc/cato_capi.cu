@@ -354,12 +354,25 @@ static int pull_ctl(cato_handle* h) {
   return CATO_OK;
 }
 
+// The reference's order of checks after a step: the pressure-input BC stops inside the boundary
+// condition, before the state is checked; every stage assignment runs check_for_nans on rho, u,
+// v, p (assign_fluid, mod_fluid.f90:718-721) before sanity_check looks for negative density,
+// then negative pressure (:726-737).
 static int status_code(int bits) {
-  // the reference stops inside the boundary condition, before the state is ever checked
   if (bits & ST_BC_INPUT) return CATO_ERR_BC_INPUT;
+  if (bits & ST_NAN) return CATO_NANS_FOUND;
   if (bits & ST_NEG_DENSITY) return CATO_NEG_DENSITY;
   if (bits & ST_NEG_PRESSURE) return CATO_NEG_PRESSURE;
-  if (bits & ST_NAN) return CATO_NANS_FOUND;
+  return CATO_OK;
+}
+
+// The checks of an uploaded state (initialize_from_hdf5, mod_fluid.f90:352-360): pressure below
+// tiny, then density below tiny.  A NaN (which minval skips) is not refused here: the state
+// keeps its status bit, and the first step reports NANS_FOUND as the reference's first stage
+// assignment does.
+static int upload_code(int bits) {
+  if (bits & ST_NEG_PRESSURE) return CATO_NEG_PRESSURE;
+  if (bits & ST_NEG_DENSITY) return CATO_NEG_DENSITY;
   return CATO_OK;
 }
 
@@ -689,7 +702,7 @@ int cato_gpu_upload_primitive(cato_handle* h, const double* rho, const double* u
   h->uploaded = true;
   h->raw_pending = true;
   h->stepped = false;
-  return status_code(h->ctl_host->status);
+  return upload_code(h->ctl_host->status);
 }
 
 int cato_gpu_get_timestep(cato_handle* h, double* dt) {

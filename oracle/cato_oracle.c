@@ -1379,6 +1379,14 @@ int oracle_set_primitive(oracle_fluid* f, const double* rho, const double* u, co
   f->solver_time = 0.0;
   f->iteration = 0;
   f->conv_valid = 0;
+  /* initialize_from_hdf5's checks of the loaded state (mod_fluid.f90:352-360): pressure below
+   * tiny, then density below tiny (comparisons with a NaN are false, as minval skips NaNs) */
+  for (int j = 1; j <= d.nj; ++j)
+    for (int i = 1; i <= d.ni; ++i)
+      if (AT(p, i, j) < TINY) return CATO_NEG_PRESSURE;
+  for (int j = 1; j <= d.nj; ++j)
+    for (int i = 1; i <= d.ni; ++i)
+      if (AT(rho, i, j) < TINY) return CATO_NEG_DENSITY;
   return 0;
 }
 
@@ -1740,14 +1748,22 @@ int oracle_integrate(oracle_fluid* f, double dt, int32_t* error_code) {
   }
   f->time = f->time + dt;
   derive_all(f, U, f->u, f->v, f->p, f->cs);
+  /* the reference's order of checks: check_for_nans on rho, u, v, p at the stage assignment
+   * (assign_fluid, mod_fluid.f90:718-721; field_2d.f90:825-844), then sanity_check's negative
+   * density, then negative pressure over the whole field (mod_fluid.f90:726-737;
+   * field_2d.f90:846-867); the first failing check stops (error.f90:6-9 codes) */
   int32_t ec = 0;
   for (int j = 1; j <= d.nj && !ec; ++j)
-    for (int i = 1; i <= d.ni; ++i) {
-      double r = AT(f->rho, i, j), pp = AT(f->p, i, j);
-      if (isnan(r) || isnan(AT(f->u, i, j)) || isnan(AT(f->v, i, j)) || isnan(pp)) { ec = CATO_NANS_FOUND; break; }
-      if (r < 0.0) { ec = CATO_NEG_DENSITY; break; }
-      if (pp < 0.0) { ec = CATO_NEG_PRESSURE; break; }
-    }
+    for (int i = 1; i <= d.ni && !ec; ++i)
+      if (isnan(AT(f->rho, i, j)) || isnan(AT(f->u, i, j)) || isnan(AT(f->v, i, j)) ||
+          isnan(AT(f->p, i, j)))
+        ec = CATO_NANS_FOUND;
+  for (int j = 1; j <= d.nj && !ec; ++j)
+    for (int i = 1; i <= d.ni && !ec; ++i)
+      if (AT(f->rho, i, j) < 0.0) ec = CATO_NEG_DENSITY;
+  for (int j = 1; j <= d.nj && !ec; ++j)
+    for (int i = 1; i <= d.ni && !ec; ++i)
+      if (AT(f->p, i, j) < 0.0) ec = CATO_NEG_PRESSURE;
   if (error_code) *error_code = ec;
   for (int s = 0; s < 4; ++s) { free(su[s]); free(sv[s]); free(spp[s]); free(scs[s]); }
   return rc;

@@ -64,6 +64,7 @@ def lib():
         L.oracle_create.restype = ctypes.c_void_p
         L.oracle_create.argtypes = [cfgp]
         L.oracle_destroy.argtypes = [ctypes.c_void_p]
+        L.oracle_set_primitive.restype = ctypes.c_int
         L.oracle_set_primitive.argtypes = [ctypes.c_void_p] + [_dp] * 4
         L.oracle_set_conserved.argtypes = [ctypes.c_void_p] + [_dp] * 4
         L.oracle_get_timestep.restype = ctypes.c_double
@@ -238,9 +239,11 @@ class OracleFluid:
             raise RuntimeError(f"oracle_source_field: {rc}")
         return out
 
-    def set_primitive(self, rho, u, v, p) -> None:
+    def set_primitive(self, rho, u, v, p) -> int:
+        """Load a primitive state; returns initialize_from_hdf5's verdict on it (0, or
+        NEG_PRESSURE / NEG_DENSITY for a pressure / density below tiny)."""
         arrs = [np.asfortranarray(a, dtype=np.float64) for a in (rho, u, v, p)]
-        lib().oracle_set_primitive(self._h, *(_ptr(a) for a in arrs))
+        return lib().oracle_set_primitive(self._h, *(_ptr(a) for a in arrs))
 
     def set_conserved(self, rho, rho_u, rho_v, rho_E) -> None:
         arrs = [np.asfortranarray(a, dtype=np.float64) for a in (rho, rho_u, rho_v, rho_E)]
