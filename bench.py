@@ -32,13 +32,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cell-updates/s & HBM GB/s, plain FP64 vs mixed/batched; p99 solve latency"
 HBM_FALLBACK_GBS = 6800.0
-# algorithmic HBM bytes per cell and stage kernel launch (state in, state out), SSP-RK3:
-#   FP64 : stage 1 reads U^n, writes U1 (64 B); stages 2, 3 read U^n + U^k, write 32 B (96 B)
-#   mixed: stage 1 reads the FP32 copy of U^n and writes delta1 (16+16); stage 2 reads it and
-#          delta1, writes delta2 (16+16+16); stage 3 reads it, delta2 and the FP64 U^n, writes the
-#          FP64 U^{n+1} and its FP32 copy (16+16+32+32+16)
-#   mixed_df: the FP64 layout
-BYTES_PER_CELL_STAGE = {"fp64": (64, 96, 96), "mixed": (32, 48, 112), "mixed_df": (64, 96, 96)}
+# algorithmic HBM bytes per cell and stage kernel launch (state in, state out), SSP-RK3, the same
+# FP64 state layout in every precision: stage 1 reads U^n and writes U1 (64 B); stages 2 and 3
+# read U^n and U^k and write 32 B (96 B)
+BYTES_PER_CELL_STAGE = {"fp64": (64, 96, 96), "mixed": (64, 96, 96), "mixed_df": (64, 96, 96)}
 
 
 def env_int(name, default):
@@ -633,7 +630,7 @@ def main() -> int:
         "clocks": fp64["clocks"],
         "stage_ms_per_step": fp64["stage_ms_per_step"],
         "mixed": {
-            "value": mixed["value"], "unit": "cell-updates/s", "dtype": "f32 flux / f64 state",
+            "value": mixed["value"], "unit": "cell-updates/s", "dtype": "f32 reconstruction/flux, f64 stage accumulation",
             "ms_per_step": mixed["ms_per_step"], "speedup_vs_fp64": mixed["value"] / fp64["value"],
             "roofline": mixed["roofline"], "stage_ms_per_step": mixed["stage_ms_per_step"],
             "gpu_launches": mixed["launches_per_step"] * args.steps, "clocks": mixed["clocks"],

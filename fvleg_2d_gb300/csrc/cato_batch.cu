@@ -46,15 +46,12 @@ __global__ void batch_step_begin(InstDesc* descs, int n, int* counters, int n_co
   c.dt_min = ~0ULL;
 }
 
-// after the last stage: the mixed path's new state is in the other buffer
+// after the last stage: the uploaded primitives have been consumed
 __global__ void batch_step_end(InstDesc* descs, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   InstDesc& d = descs[i];
-  if (d.in_use && d.ctl.active) {
-    if (d.prec == 1) d.cur = 1 - d.cur;  // the mixed path writes U^{n+1} to the other buffer
-    d.raw_pending = 0;
-  }
+  if (d.in_use && d.ctl.active) d.raw_pending = 0;
 }
 
 cudaError_t launch_batch_prec(int prec, int flux, int recon, int threads, cudaStream_t s,
@@ -146,13 +143,9 @@ static int bcheck(cudaError_t e) { return e == cudaSuccess ? CATO_OK : CATO_ERR_
   } while (0)
 
 static void free_instance(InstDesc& d) {
-  for (int s = 0; s < 2; ++s) {
-    for (int v = 0; v < 4; ++v) {
-      cudaFree(d.U[s][v]);
-      cudaFree(d.S[s][v]);
-    }
-    cudaFree(d.D[s]);
-    cudaFree(d.Uf[s]);
+  for (int v = 0; v < 4; ++v) {
+    cudaFree(d.U[v]);
+    for (int s = 0; s < 2; ++s) cudaFree(d.S[s][v]);
   }
   std::memset(&d, 0, sizeof(d));
 }
@@ -287,8 +280,8 @@ int cato_batch_instance_bytes(const cato_config* cfg, uint64_t* bytes) {
   if (!cfg || !bytes) return CATO_ERR_ARG;
   const size_t pitch = (size_t)(cfg->ni + 31) / 32 * 32;
   const size_t cells = pitch * (size_t)cfg->nj;
-  // FP64 and mixed_df: U + two stage buffers; mixed: two U + two FP32 copies + two increments
-  *bytes = cfg->precision != CATO_MIXED ? cells * 8 * 12 : cells * (8 * 8 + 16 * 4);
+  // every precision: U + two stage buffers of four FP64 fields
+  *bytes = cells * 8 * 12;
   return CATO_OK;
 }
 
@@ -387,19 +380,10 @@ int cato_batch_add(cato_batch* b, const cato_config* cfg, const double* rho, con
   const size_t cells = (size_t)d.pitch * d.nj, fb = cells * sizeof(double);
   bool ok = true;
   for (int k = 0; k < 4 && ok; ++k) {
-    ok = cudaMalloc(&d.U[0][k], fb) == cudaSuccess;
-    if (ok && d.prec != CATO_MIXED) {
-      ok = cudaMalloc(&d.S[0][k], fb) == cudaSuccess && cudaMalloc(&d.S[1][k], fb) == cudaSuccess;
-      d.prim_raw[k] = d.S[1][k];
-    } else if (ok) {
-      ok = cudaMalloc(&d.U[1][k], fb) == cudaSuccess;
-      d.prim_raw[k] = d.U[1][k];
-    }
+    ok = cudaMalloc(&d.U[k], fb) == cudaSuccess && cudaMalloc(&d.S[0][k], fb) == cudaSuccess &&
+         cudaMalloc(&d.S[1][k], fb) == cudaSuccess;
+    d.prim_raw[k] = d.S[1][k];  // S1 is first written by stage 2, after stage 1 read these
   }
-  if (ok && d.prec == CATO_MIXED)
-    for (int k = 0; k < 2 && ok; ++k)
-      ok = cudaMalloc(&d.D[k], cells * sizeof(float4)) == cudaSuccess &&
-           cudaMalloc(&d.Uf[k], cells * sizeof(float4)) == cudaSuccess;
   if (!ok) {
     (void)cudaGetLastError();
     free_instance(d);
@@ -424,14 +408,9 @@ int cato_batch_add(cato_batch* b, const cato_config* cfg, const double* rho, con
   upload_init_kernel<<<blocks, 256, 0, b->stream>>>(
       d.ni, d.nj, d.pitch, d.gamma, d.cfl, d.G.dx, d.G.dy, nullptr, nullptr, d.prim_raw[0],
       d.prim_raw[1],
-      d.prim_raw[2], d.prim_raw[3], d.U[0][0], d.U[0][1], d.U[0][2], d.U[0][3],
+      d.prim_raw[2], d.prim_raw[3], d.U[0], d.U[1], d.U[2], d.U[3],
       &b->d_descs[s].ctl);
   BK(cudaGetLastError());
-  if (d.prec == CATO_MIXED) {
-    pack_f32_kernel<<<blocks, 256, 0, b->stream>>>(d.ni, d.nj, d.pitch, d.U[0][0], d.U[0][1],
-                                                   d.U[0][2], d.U[0][3], d.Uf[0]);
-    BK(cudaGetLastError());
-  }
   BK(cudaStreamSynchronize(b->stream));
   uint64_t bytes = 0;
   cato_batch_instance_bytes(cfg, &bytes);
@@ -542,7 +521,7 @@ int cato_batch_download(cato_batch* b, int32_t slot, double* rho, double* rho_u,
   BK(cudaStreamSynchronize(b->stream));
   const InstDesc& d = b->h_pinned[slot];
   if (ld < d.ni + 2 * d.ng) return CATO_ERR_ARG;
-  double* const* U = d.prec != CATO_MIXED ? d.U[0] : d.U[d.cur];
+  double* const* U = d.U;
   double* out[4] = {rho, rho_u, rho_v, rho_E};
   for (int k = 0; k < 4; ++k) {
     if (!out[k]) continue;

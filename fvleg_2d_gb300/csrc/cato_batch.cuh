@@ -15,19 +15,16 @@ struct InstDesc {
   int ni, nj, pitch, ng;
   int bc[4];
   int limiter, rows_per_cta, flux, recon;
-  int cur;                 // mixed: which U buffer holds U^n
   int raw_pending;         // the first stage uses the uploaded primitives as is
-  int prec;                // 0 FP64, 1 mixed, 2 mixed_df (FP64 layout)
+  int prec;                // 0 FP64, 1 mixed, 2 mixed_df (one FP64 layout for all)
   int in_use;
   double gamma, cfl, bc_p;
   Geom G;
   FluxConsts<double> K64;
   FluxConsts<float> K32;
   FluxConsts<df> Kdf;
-  double* U[2][4];
-  double* S[2][4];
-  float4* D[2];
-  float4* Uf[2];
+  double* U[4];            // U^n
+  double* S[2][4];         // stage buffers
   double* prim_raw[4];
 };
 
@@ -70,34 +67,14 @@ __device__ __forceinline__ void batch_stage_args(InstDesc* d, const BatchStageAr
   A.pbc_ng = 0;
   A.src_q = nullptr;
   const bool raw = (B.stage == 0) && d->raw_pending;
-  if constexpr (Prec<R>::kind != 1) {
-    double* const* prev = (B.stage == 0) ? d->U[0] : d->S[(B.stage - 1) & 1];
-    double* const* out = B.last ? d->U[0] : d->S[B.stage & 1];
+  double* const* prev = (B.stage == 0) ? d->U : d->S[(B.stage - 1) & 1];
+  double* const* out = B.last ? d->U : d->S[B.stage & 1];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      A.Uk[v] = prev[v];
-      A.Ua[v] = d->U[0][v];
-      A.Uo[v] = out[v];
-      A.Pin[v] = raw ? d->prim_raw[v] : nullptr;
-    }
-    A.uf = nullptr;
-    A.dk = nullptr;
-    A.dout = nullptr;
-    A.ufo = nullptr;
-  } else {
-    const int cur = d->cur;
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      A.Uk[v] = nullptr;
-      A.Ua[v] = d->U[cur][v];
-      A.Uo[v] = B.last ? d->U[1 - cur][v] : nullptr;
-      A.Pin[v] = raw ? d->prim_raw[v] : nullptr;
-    }
-    A.uf = d->Uf[cur];
-    A.dk = (B.stage == 0) ? nullptr : d->D[(B.stage - 1) & 1];
-    A.dout = B.last ? nullptr : d->D[B.stage & 1];
-    A.ufo = B.last ? d->Uf[1 - cur] : nullptr;
-    if (B.kind == 0) A.b = 0.0;
+  for (int v = 0; v < 4; ++v) {
+    A.Uk[v] = prev[v];
+    A.Ua[v] = d->U[v];
+    A.Uo[v] = out[v];
+    A.Pin[v] = raw ? d->prim_raw[v] : nullptr;
   }
 }
 

@@ -1,14 +1,11 @@
 // cato_capi.cu -- the C-ABI of include/cato_gpu.h: handles, device state, step sequencing.
 //
 // Device layout of one instance (all interior-only, row-major with i fastest = the reference's
-// Fortran (i, j) order, row pitch rounded up to 32 elements so every row starts 256-B aligned):
-//   FP64 path : U^n (4 x f64) + two stage buffers S0, S1 (4 x f64 each).  The last stage writes
-//               U^{n+1} over U^n in place (U^n is only read point-wise there).
-//   mixed path: U^n double-buffered (2 x 4 x f64) with FP32 copies (2 x float4 per cell) and
-//               stage increments delta (2 x float4 per cell): U^k = U^n + delta_k,
-//               delta_{k+1} = b delta_k + c L(U^k), U^{n+1} = U^n + delta in FP64.
-//   mixed_df  : the FP64 layout; reconstruction, flux and divergence in double-float (pairs of
-//               FP32) and the stage combine in FP64.
+// Fortran (i, j) order, row pitch rounded up to 32 elements so every row starts 256-B aligned),
+// the same for every precision: U^n (4 x f64) + two stage buffers S0, S1 (4 x f64 each).  The
+// last stage writes U^{n+1} over U^n in place (U^n is only read point-wise there).  The stage
+// combine (the RK accumulation) is FP64 in every precision; reconstruction, flux and divergence
+// are FP64 (fp64), FP32 (mixed) or double-float pairs of FP32 (mixed_df).
 // The primitives of an upload are kept (in a buffer not needed before the first step) because
 // the first stage after an upload uses them as is, like the reference after initialize.
 #include <cmath>
@@ -51,17 +48,14 @@ struct cato_handle {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // device buffers
-  double* U[2][4] = {};    // FP64: U[0] = U^n ; mixed: U[cur], U[1-cur]
-  double* S[2][4] = {};    // FP64 stage buffers
-  float4* D[2] = {};       // mixed stage increments (rho, rho u, rho v, rho E per cell)
-  float4* Uf[2] = {};      // mixed: FP32 copies of U[0], U[1]
+  double* U[4] = {};       // U^n
+  double* S[2][4] = {};    // stage buffers
   double* prim_raw[4] = {};  // primitives of the last upload (alias of a free buffer)
   double* scratch[8] = {};   // solve / download / interpolation scratch (lazy)
   double* halo[4] = {};      // halo-padded scratch (lazy)
   size_t halo_elems = 0;
   StepCtl* ctl = nullptr;    // device
   StepCtl* ctl_host = nullptr;  // pinned mirror
-  int cur = 0;               // mixed: which U holds U^n
   bool uploaded = false;
   bool raw_pending = false;  // next stage 1 uses prim_raw
   bool stepped = false;      // a step ran since the last upload (its stage buffers are valid)
@@ -275,7 +269,7 @@ static int enqueue_source(cato_handle* h) {
   S.ni = h->ni;
   S.nj = h->nj;
   S.pitch = h->pitch;
-  S.rho = h->cfg.precision == CATO_MIXED ? h->U[h->cur][0] : h->U[0][0];
+  S.rho = h->U[0];
   S.field = h->src_field;
   S.i_dep = h->src_dep;
   S.parity = h->src_parity;
@@ -301,7 +295,6 @@ static int enqueue_step(cato_handle* h) {
   }
   if (h->event_hook) CK(cudaEventRecord(h->event_hook[1], h->stream));
   const int ns = (int)h->stages.size();
-  const bool fp64 = h->cfg.precision != CATO_MIXED;  // FP64 stage-buffer layout
   for (int k = 0; k < ns; ++k) {
     const Stage& st = h->stages[k];
     StageArgs A = base_args(h);
@@ -311,31 +304,15 @@ static int enqueue_step(cato_handle* h) {
     A.coef = st.coef;
     A.last = (k == ns - 1);
     const bool raw = (k == 0) && h->raw_pending;
-    if (fp64) {
-      double** Un = h->U[0];
-      // stencil operand: U^n for the first stage, else the previous stage's output
-      double** prev = (k == 0) ? Un : h->S[(k - 1) & 1];
-      double** out = A.last ? Un : h->S[k & 1];
-      for (int v = 0; v < 4; ++v) {
-        A.Uk[v] = prev[v];
-        A.Ua[v] = Un[v];
-        A.Uo[v] = out[v];
-        A.Pin[v] = raw ? h->prim_raw[v] : nullptr;
-      }
-    } else {
-      double** Un = h->U[h->cur];
-      double** Unext = h->U[1 - h->cur];
-      for (int v = 0; v < 4; ++v) {
-        A.Uk[v] = nullptr;
-        A.Ua[v] = Un[v];
-        A.Uo[v] = A.last ? Unext[v] : nullptr;
-        A.Pin[v] = raw ? h->prim_raw[v] : nullptr;
-      }
-      A.uf = h->Uf[h->cur];
-      A.dk = (k == 0) ? nullptr : h->D[(k - 1) & 1];
-      A.dout = A.last ? nullptr : h->D[k & 1];
-      A.ufo = A.last ? h->Uf[1 - h->cur] : nullptr;
-      if (st.kind == 0) A.b = 0.0;  // rk(m,n): U_curr = U_0 + c L(U_prev)
+    double** Un = h->U;
+    // stencil operand: U^n for the first stage, else the previous stage's output
+    double** prev = (k == 0) ? Un : h->S[(k - 1) & 1];
+    double** out = A.last ? Un : h->S[k & 1];
+    for (int v = 0; v < 4; ++v) {
+      A.Uk[v] = prev[v];
+      A.Ua[v] = Un[v];
+      A.Uo[v] = out[v];
+      A.Pin[v] = raw ? h->prim_raw[v] : nullptr;
     }
     A.src_q = h->src_on ? h->src_field : nullptr;
     const int rcb = enqueue_pbc(h, A, k == 0 && h->cfg.rk >= CATO_RK_1_3);
@@ -343,7 +320,6 @@ static int enqueue_step(cato_handle* h) {
     CK(launch(h, A));
     if (h->event_hook) CK(cudaEventRecord(h->event_hook[k + 2], h->stream));
   }
-  if (!fp64) h->cur = 1 - h->cur;
   h->raw_pending = false;
   return CATO_OK;
 }
@@ -590,28 +566,16 @@ int cato_gpu_create(const cato_config* cfg, cato_handle** out) {
   if (e != cudaSuccess) { delete h; return CATO_ERR_CUDA; }
   h->own_stream = true;
   const size_t fb = h->field_elems * sizeof(double);
-  const bool fp64 = cfg->precision != CATO_MIXED;  // FP64 stage-buffer layout
   auto dalloc = [&](void** p, size_t bytes) -> bool {
     cudaError_t ee = cudaMalloc(p, bytes);
     if (ee != cudaSuccess) { (void)cudaGetLastError(); return false; }
     return true;
   };
   for (int v = 0; v < 4; ++v) {
-    if (!dalloc((void**)&h->U[0][v], fb)) return cleanup(CATO_ERR_OOM);
-    if (fp64) {
-      if (!dalloc((void**)&h->S[0][v], fb)) return cleanup(CATO_ERR_OOM);
-      if (!dalloc((void**)&h->S[1][v], fb)) return cleanup(CATO_ERR_OOM);
-      h->prim_raw[v] = h->S[1][v];  // S1 is first written by stage 2, after stage 1 read these
-    } else {
-      if (!dalloc((void**)&h->U[1][v], fb)) return cleanup(CATO_ERR_OOM);
-      h->prim_raw[v] = h->U[1][v];  // U[1] is first written by the last stage of step 1
-    }
-  }
-  if (!fp64) {
-    for (int s2 = 0; s2 < 2; ++s2) {
-      if (!dalloc((void**)&h->D[s2], h->field_elems * sizeof(float4))) return cleanup(CATO_ERR_OOM);
-      if (!dalloc((void**)&h->Uf[s2], h->field_elems * sizeof(float4))) return cleanup(CATO_ERR_OOM);
-    }
+    if (!dalloc((void**)&h->U[v], fb)) return cleanup(CATO_ERR_OOM);
+    if (!dalloc((void**)&h->S[0][v], fb)) return cleanup(CATO_ERR_OOM);
+    if (!dalloc((void**)&h->S[1][v], fb)) return cleanup(CATO_ERR_OOM);
+    h->prim_raw[v] = h->S[1][v];  // S1 is first written by stage 2, after stage 1 read these
   }
   if (!dalloc((void**)&h->ctl, sizeof(StepCtl))) return cleanup(CATO_ERR_OOM);
   if (cudaMallocHost((void**)&h->ctl_host, sizeof(StepCtl)) != cudaSuccess) return cleanup(CATO_ERR_OOM);
@@ -638,13 +602,9 @@ int cato_gpu_create(const cato_config* cfg, cato_handle** out) {
 int cato_gpu_destroy(cato_handle* h) {
   if (!h) return CATO_ERR_ARG;
   if (h->stream) cudaStreamSynchronize(h->stream);
-  for (int s = 0; s < 2; ++s) {
-    for (int v = 0; v < 4; ++v) {
-      cudaFree(h->U[s][v]);
-      cudaFree(h->S[s][v]);
-    }
-    cudaFree(h->D[s]);
-    cudaFree(h->Uf[s]);
+  for (int v = 0; v < 4; ++v) {
+    cudaFree(h->U[v]);
+    for (int s = 0; s < 2; ++s) cudaFree(h->S[s][v]);
   }
   for (int k = 0; k < 8; ++k) cudaFree(h->scratch[k]);
   for (int k = 0; k < 4; ++k) cudaFree(h->halo[k]);
@@ -685,18 +645,12 @@ int cato_gpu_upload_primitive(cato_handle* h, const double* rho, const double* u
   c.max_iter = (1LL << 62);
   *h->ctl_host = c;
   CK(cudaMemcpyAsync(h->ctl, h->ctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice, h->stream));
-  h->cur = 0;
-  double** Un = h->U[0];
+  double** Un = h->U;
   upload_init_kernel<<<grid_for((long long)h->ni * h->nj), 256, 0, h->stream>>>(
       h->ni, h->nj, h->pitch, h->cfg.gamma, h->cfg.cfl, h->G.dx, h->G.dy, h->G.dxc, h->G.dyc,
       h->prim_raw[0],
       h->prim_raw[1], h->prim_raw[2], h->prim_raw[3], Un[0], Un[1], Un[2], Un[3], h->ctl);
   CK(cudaGetLastError());
-  if (h->cfg.precision == CATO_MIXED) {
-    pack_f32_kernel<<<grid_for((long long)h->ni * h->nj), 256, 0, h->stream>>>(
-        h->ni, h->nj, h->pitch, Un[0], Un[1], Un[2], Un[3], h->Uf[0]);
-    CK(cudaGetLastError());
-  }
   int rc = pull_ctl(h);
   if (rc) return rc;
   h->uploaded = true;
@@ -760,7 +714,6 @@ int cato_gpu_run(cato_handle* h, int64_t max_steps, double t_end, int64_t* steps
   const long long chunk = 32;
   while (issued < total) {
     const long long n = (total - issued) < chunk ? (total - issued) : chunk;
-    const int parity0 = h->cur;
     for (long long k = 0; k < n; ++k) {
       rc = enqueue_step(h);
       if (rc) return rc;
@@ -768,11 +721,6 @@ int cato_gpu_run(cato_handle* h, int64_t max_steps, double t_end, int64_t* steps
     issued += n;
     rc = pull_ctl(h);
     if (rc) return rc;
-    if (h->cfg.precision == CATO_MIXED) {
-      // steps past the stop condition were no-ops: U^n sits in the buffer of the last active one
-      const long long active = h->ctl_host->iter - (it0 + (issued - n));
-      h->cur = (int)((parity0 + active) & 1);
-    }
     if (!h->ctl_host->active || h->ctl_host->status) break;
   }
   if (h->ctl_host->iter > it0) h->stepped = true;
@@ -809,7 +757,7 @@ int cato_gpu_download(cato_handle* h, double* rho, double* rho_u, double* rho_v,
   if (!h) return CATO_ERR_ARG;
   if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
   if (ld < h->ni + 2 * h->ng) return fail(h, CATO_ERR_ARG, "leading dimension too small");
-  double** Un = h->U[h->cfg.precision != CATO_MIXED ? 0 : h->cur];
+  double** Un = h->U;
   double* cons_out[4] = {rho, rho_u, rho_v, rho_E};
   double* der_out[4] = {u, v, p, cs};
   int rc;
@@ -843,8 +791,6 @@ int cato_gpu_solve(cato_handle* h, double* rho, double* u, double* v, double* p,
   if (!rho || !u || !v || !p || !d_rho_dt || !d_rho_u_dt || !d_rho_v_dt || !d_rho_E_dt)
     return fail(h, CATO_ERR_ARG, "null field pointer");
   if (ld < h->ni + 2 * h->ng) return fail(h, CATO_ERR_ARG, "leading dimension too small");
-  if (h->cfg.precision != CATO_FP64)
-    return fail(h, CATO_ERR_CONFIG, "solve is the FP64 reference boundary");
   int rc;
   if ((rc = pbc_prepare(h))) return rc;
   if ((rc = ensure_scratch(h))) return rc;
@@ -979,7 +925,6 @@ int cato_gpu_run_timed(cato_handle* h, int64_t n_steps, float* total_ms, float* 
   std::vector<cudaEvent_t> ev(kernel_ms ? (size_t)n_steps * nk + 1 : 2);
   for (auto& e : ev) CK(cudaEventCreate(&e));
   CK(cudaEventRecord(ev[0], h->stream));
-  const int parity0 = h->cur;
   for (long long s = 0; s < n_steps; ++s) {
     if (kernel_ms) h->event_hook = ev.data() + s * nk;
     rc = enqueue_step(h);
@@ -1001,8 +946,6 @@ int cato_gpu_run_timed(cato_handle* h, int64_t n_steps, float* total_ms, float* 
   for (auto& e : ev) cudaEventDestroy(e);
   rc = pull_ctl(h);
   if (rc) return rc;
-  if (h->cfg.precision == CATO_MIXED)
-    h->cur = (int)((parity0 + (h->ctl_host->iter - it0)) & 1);
   if (h->ctl_host->iter > it0) h->stepped = true;
   return status_code(h->ctl_host->status);
 }
@@ -1324,10 +1267,8 @@ static int reduce(cato_handle* h, RedArgs R, double out[RED_Q]) {
   return CATO_OK;
 }
 
-// U^n of the handle: FP64 U[0]; mixed U[cur]
-static double* const* state_now(cato_handle* h) {
-  return h->cfg.precision != CATO_MIXED ? h->U[0] : h->U[h->cur];
-}
+// U^n of the handle
+static double* const* state_now(cato_handle* h) { return h->U; }
 
 int cato_gpu_conservation_sums(cato_handle* h, double totals[4]) {
   if (!h || !totals) return CATO_ERR_ARG;
@@ -1352,22 +1293,13 @@ int cato_gpu_convergence(cato_handle* h, double l2[4]) {
   const bool ssp = rk == CATO_RK_SSP2 || rk == CATO_RK_SSP3;
   RedArgs R{};
   R.mode = 1;
-  if (h->cfg.precision != CATO_MIXED) {
-    // SSP: the first stage's output U_1 is still in S0; rk(m,n) compares with U^n, which the
-    // last stage overwrote in place
-    if (!ssp)
-      return fail(h, CATO_ERR_STATE, "rk(m,n) steps update U^n in place: no U_0 to compare");
-    for (int k = 0; k < 4; ++k) {
-      R.A[k] = h->S[0][k];
-      R.B[k] = h->U[0][k];
-    }
-  } else {
-    // U^n is in U[1-cur] after the step; U_1 = U^n + delta_1 for SSP, U_0 = U^n for rk(m,n)
-    for (int k = 0; k < 4; ++k) {
-      R.A[k] = h->U[1 - h->cur][k];
-      R.B[k] = h->U[h->cur][k];
-    }
-    R.d1 = ssp ? h->D[0] : nullptr;
+  // SSP: the first stage's output U_1 is still in S0; rk(m,n) compares with U^n, which the
+  // last stage overwrote in place
+  if (!ssp)
+    return fail(h, CATO_ERR_STATE, "rk(m,n) steps update U^n in place: no U_0 to compare");
+  for (int k = 0; k < 4; ++k) {
+    R.A[k] = h->S[0][k];
+    R.B[k] = h->U[k];
   }
   double out[RED_Q];
   int rc = reduce(h, R, out);

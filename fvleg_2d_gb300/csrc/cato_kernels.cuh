@@ -69,18 +69,6 @@ static __global__ void upload_init_kernel(int ni, int nj, int pitch, double gamm
   }
 }
 
-// FP32 copy (one float4 per cell) of an FP64 conserved state, for the mixed path.
-static __global__ void pack_f32_kernel(int ni, int nj, int pitch, const double* __restrict__ a0,
-                                const double* __restrict__ a1, const double* __restrict__ a2,
-                                const double* __restrict__ a3, float4* out) {
-  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < (long long)ni * nj;
-       n += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(n % ni), j = (int)(n / ni);
-    const size_t idx = (size_t)j * pitch + i;
-    out[idx] = make_float4(d2f_int(a0[idx]), d2f_int(a1[idx]), d2f_int(a2[idx]), d2f_int(a3[idx]));
-  }
-}
-
 // fluid_t's derived quantities for download: u, v, p, cs of the conserved state (FP64,
 // calculate_derived_quantities), or of the raw primitives before the first step.
 static __global__ void derive_kernel(int ni, int nj, int pitch, double gamma, int raw,
@@ -189,10 +177,9 @@ constexpr int RED_Q = 8;         // quantities per reduction
 
 struct RedArgs {
   int ni, nj, pitch;
-  int mode;               // 0: sums of A; 1: sums of (B - A1)^2 and A1^2, A1 = A (+ d1)
+  int mode;               // 0: sums of A; 1: sums of (B - A)^2 and A^2
   const double* A[4];
   const double* B[4];
-  const float4* d1;       // mode 1, mixed path: first-stage increment (A1 = A + d1)
   const double* dxc;      // mode 0 on a rectilinear grid: the sums are of A * dx_i * dy_j
   const double* dyc;
   double* partials;       // RED_BLOCKS x RED_Q
@@ -221,16 +208,12 @@ static __global__ void __launch_bounds__(RED_THREADS) reduce_partials_kernel(Red
   for (int j = blockIdx.x; j < R.nj; j += gridDim.x) {
     for (int i = threadIdx.x; i < R.ni; i += blockDim.x) {
       const size_t idx = (size_t)j * R.pitch + i;
-      float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (R.mode == 1 && R.d1) d = R.d1[idx];
-      const float dd[4] = {d.x, d.y, d.z, d.w};
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         double a = R.A[k][idx];
         if (R.mode == 0) {
           acc[k] += R.dxc ? a * (R.dxc[i] * R.dyc[j] - 0.0 * 0.0) : a;
         } else {
-          if (R.d1) a = a + (double)dd[k];
           const double df = R.B[k][idx] - a;
           acc[k] += df * df;
           acc[4 + k] += a * a;

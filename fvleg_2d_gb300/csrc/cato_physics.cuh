@@ -257,7 +257,8 @@ __device__ __forceinline__ void prim_from_cons(double g, double g1, double r, do
   u = abs_lt(ru, TINY) ? 0.0 : div_rn(ru, r);
   v = abs_lt(rv, TINY) ? 0.0 : div_rn(rv, r);
   double e = abs_lt(rE, TINY) ? 0.0 : div_rn(rE, r);
-  double s = u * u + v * v;
+  // explicitly rounded: identical in translation units built with FMA contraction
+  double s = __dadd_rn(__dmul_rn(u, u), __dmul_rn(v, v));
   if (abs_lt(s, EPS)) s = 0.0;
   double h = half(s);
   double dd = e - h;
@@ -268,6 +269,26 @@ __device__ __forceinline__ void prim_from_cons(double g, double g1, double r, do
   // mach_u = u / cs, mach_v = v / cs, then |mach| < 1e-13 zeroes the velocity
   if (mach_below_1e13(u, cs)) u = 0.0;  // each test reads only its own component and cs
   if (mach_below_1e13(v, cs)) v = 0.0;
+}
+
+// The FP64 recovery out of line, for the double-float path's rare cells where its own
+// arithmetic cannot resolve the pressure (see near_vacuum)
+static __device__ __noinline__ void prim_from_cons_f64(double g, double r, double ru, double rv,
+                                                       double rE, double& u, double& v,
+                                                       double& p) {
+  double cs;
+  prim_from_cons(g, __dsub_rn(g, 1.0), r, ru, rv, rE, u, v, p, cs);
+}
+
+// Whether the double-float pressure p, recovered as (gamma - 1)(rho E - kinetic energy), is too
+// close to zero for its arithmetic: the difference loses all the digits a cancellation of
+// rho E against the kinetic energy takes, and the FP64 recovery flushes a specific internal
+// energy below epsilon to an exact zero pressure (field_2d_cpu_operators.f90 '-' flush).  Such
+// cells (near-vacuum expansions) take the FP64 recovery from the FP64 conserved state, so that
+// their pressure, its zero and its sign (the negative-pressure check) are the FP64 path's.
+// rel: where p loses its digits (double-float: below ~1e-4 of rho E, with margin).
+__device__ __forceinline__ bool near_vacuum(float p, float rE, float rel) {
+  return !(fabsf(p) >= rel * fabsf(rE));
 }
 
 // FP32 (mixed path): same quantities with one reciprocal of rho; Mach filter as |u| < 1e-13 cs.
@@ -505,26 +526,32 @@ static __device__ __noinline__ EdgePair recon_mlp_f64(double qm2, double qm1, do
 // Double-float reconstruction (mixed_df).  The limited slope phi(r) * dq is, for each branch of
 // the limiter, an algebraic combination of the slope differences themselves: with r = d0/dm,
 // r * dm = d0, (1 + 2r)/3 * dm = (dm + 2 d0)/3, and the MLP5 coefficient times dm is the
-// fifth-order combination (-2 dm3 + 11 dm + 24 d0 - 3 dp)/30.  So the branch is chosen in FP32
-// (only a near-tie can go the other way, where both branches agree to FP32 rounding) and the
-// chosen slope is evaluated in double-float from the double-float differences, without the
-// ratio divisions.  The reference's 1e-16 / 1e-30 regularisations only matter for differences
+// fifth-order combination (-2 dm3 + 11 dm + 24 d0 - 3 dp)/30.  So the slope candidates are formed
+// in double-float from the double-float differences without the ratio divisions, and every
+// choice between them is a comparison of those double-float candidates (exact for normalised
+// pairs), so a near-tie never picks a branch on FP32 rounding.  Only the MLP alpha, which needs
+// divisions, is estimated in FP32 first and formed in double-float when the estimate cannot
+// settle the choice.  The reference's 1e-16 / 1e-30 regularisations only matter for differences
 // at the epsilon flush threshold, where the slope term is itself ~1e-16.
 // ---------------------------------------------------------------------------------------------
 __device__ __forceinline__ df df_half(df a) { return df(a.hi * 0.5f, a.lo * 0.5f); }  // exact
 __device__ __forceinline__ df df_twice(df a) { return df(a.hi * 2.0f, a.lo * 2.0f); }  // exact
 __device__ __forceinline__ df df_scale(df a, float c) { return a * df(c); }
 
+// r = d0 / dq <= 0 from the signs of normalised pairs (exact): a zero, or opposite signs
+__device__ __forceinline__ bool df_ratio_nonpos(df D0, df Dq) {
+  return D0.hi == 0.0f || Dq.hi == 0.0f || ((D0.hi > 0.0f) != (Dq.hi > 0.0f));
+}
+
 // TVD2 slope phi(r) * dq for r = d0 / dq (dq = dm for the left state, dp for the right)
 __device__ __forceinline__ df tvd_slope_df(int lim, df D0, df Dq) {
-  const float d0 = D0.hi, dq = Dq.hi;
-  if (d0 == 0.0f || dq == 0.0f || ((d0 > 0.0f) != (dq > 0.0f))) return df(0.0f);  // r <= 0
-  const float a0 = fabsf(d0), aq = fabsf(dq);  // r = a0 / aq > 0
+  if (df_ratio_nonpos(D0, Dq)) return df(0.0f);  // r <= 0
+  const df a0 = df_abs(D0), aq = df_abs(Dq);    // r = a0 / aq > 0
   if (lim == LIM_MINMOD) return a0 < aq ? D0 : Dq;            // min(r, 1) * dq
   if (lim == LIM_SUPERBEE) {                                    // max(min(2r, 1), min(r, 2)) * dq
-    if (2.0f * a0 <= aq) return df_twice(D0);
+    if (df_twice(a0) <= aq) return df_twice(D0);
     if (a0 <= aq) return Dq;
-    if (a0 <= 2.0f * aq) return D0;
+    if (a0 <= df_twice(aq)) return D0;
     return df_twice(Dq);
   }
   // van Leer: 2r / (1 + r) * dq = 2 d0 dq / (dq + d0)
@@ -543,18 +570,53 @@ __device__ __forceinline__ void recon_tvd2<df>(int lim, df qm1, df q0, df qp1, d
   Rr = qp1 - df_half(tvd_slope_df(lim, D0, Dp));
 }
 
-// MLP slope: phi * dq with phi = max(0, min(alpha r, alpha, beta)); candidates
-// alpha * d0, alpha * dq and beta * dq (the latter given in double-float as bdq).
-__device__ __forceinline__ df mlp_slope_df(float r, float alpha, float beta, df D0, df Dq,
-                                           df bdq) {
-  const float c1 = alpha * r, c2 = alpha;
-  float m = fminf(c1, c2);
-  int pick = c1 <= c2 ? 1 : 2;
-  if (beta < m) { m = beta; pick = 3; }
-  if (!(m > 0.0f)) return df(0.0f);
-  if (pick == 1) return df_scale(D0, alpha);
-  if (pick == 2) return df_scale(Dq, alpha);
-  return bdq;
+// One side of the MLP limiter: the slope phi * dq, phi = max(0, min(alpha r, alpha, beta)),
+// for r = d0 / dq > 0 (the caller handles r <= 0).  min(alpha r, alpha) dq = alpha mq with
+// mq = (|d0| < |dq| ? d0 : dq) = min(r, 1) dq; beta dq is bdq.  dq is the own-side difference
+// (dm on the left), dother the opposite one.  alpha = clamp(alpha_t, 1, 2) with
+//   alpha_t = 2 max(1, r) (1 + max(0, tt_oth / r_oth)) / (1 + tt_own),
+//   tt = n / (d + S) (transverse difference over normal difference), r_oth = d0 / dother,
+// and because max(1, r) mq = d0 in both cases of mq, the unclamped candidate is the single
+// quotient
+//   alpha_t mq = 2 (d0 (d_oth + S) + x n_oth dother) (d_own + S) / ((d_oth + S) (d_own + S + n_own))
+// with x = 1 when tt_oth / r_oth > 0, else 0 (the regularisation S = 1e-30 inside the ratios
+// only matters for differences below the epsilon flush).  r32, at32, b32: FP32 estimates of r,
+// alpha_t and beta; bmag: the FP32 magnitude of beta's terms, which bounds the estimate's
+// absolute error.  The FP32 estimates only skip work: every slope returned is a double-float
+// candidate chosen by double-float comparisons, except that beta is taken without forming alpha
+// when it is below alpha min(r, 1) by a margin far above the estimates' errors.
+__device__ __forceinline__ df mlp_side_df(df D0, df Dq, df Dother, df n_own, df d_own, df n_oth,
+                                          df d_oth, df bdq, float r32, float at32, float b32,
+                                          float bmag) {
+  const df mq = df_abs(D0) < df_abs(Dq) ? D0 : Dq;
+  const bool pos = Dq.hi > 0.0f;
+  const float mr = fminf(r32, 1.0f);
+  const float a32 = fmaxf(1.0f, fminf(2.0f, at32));
+  df cand;
+  if (b32 < a32 * mr * (1.0f - 1e-4f) - 1e-6f * bmag - 1e-6f) {
+    cand = bdq;
+  } else {
+    df ca;
+    if (at32 >= 2.0f * (1.0f + 2e-4f)) {
+      ca = df_twice(mq);
+    } else if (at32 <= 1.0f - 2e-4f) {
+      ca = mq;
+    } else {
+      const df S = df(1e-30f);
+      const df ao = df_abs(d_own) + S, at = df_abs(d_oth) + S;
+      const bool x = n_oth.hi != 0.0f && ((D0.hi > 0.0f) == (Dother.hi > 0.0f)) &&
+                     Dother.hi != 0.0f;
+      const df num = x ? D0 * at + df_abs(n_oth) * Dother : D0 * at;
+      ca = df_div(df_twice(num * ao), at * (ao + df_abs(n_own)));
+      // clamp alpha to [1, 2]: the candidate between mq and 2 mq (oriented by the sign of dq)
+      const df m2 = df_twice(mq);
+      if (pos) ca = ca < mq ? mq : (m2 < ca ? m2 : ca);
+      else ca = mq < ca ? mq : (ca < m2 ? m2 : ca);
+    }
+    cand = pos ? (bdq < ca ? bdq : ca) : (ca < bdq ? bdq : ca);
+  }
+  // max(0, phi): the slope has the sign of dq, or is zero
+  return pos ? (cand.hi > 0.0f ? cand : df(0.0f)) : (cand.hi < 0.0f ? cand : df(0.0f));
 }
 
 template <int ORDER>
@@ -564,16 +626,18 @@ __device__ __forceinline__ void recon_mlp_df(df qm2, df qm1, df q0, df qp1, df q
   const df Dm = flushed(q0 - qm1), D0 = flushed(qp1 - q0), Dp = flushed(qp2 - qp1);
   const float dm = Dm.hi, d0 = D0.hi, dp = Dp.hi;
   const float rR_p1 = __fdividef(d0, dp + S), rL = __fdividef(d0, dm + S);
-  float bL, bR;
-  df bdL, bdR;  // beta * dm (left), beta * dp (right) in double-float
+  float bL, bR, mL, mR;  // FP32 beta estimates and the magnitudes of their terms
+  df bdL, bdR;           // beta * dm (left), beta * dp (right) in double-float
   if (ORDER == 5) {
     const df Dm3 = flushed(qm1 - qm2), Dp5 = flushed(qp3 - qp2);
     const float dm3 = Dm3.hi, dp5 = Dp5.hi;
     const float rL_m1 = __fdividef(dm, dm3 + S), rL_p1 = __fdividef(dp, d0 + S);
     const float rR_p2 = __fdividef(dp, dp5 + S), rR = __fdividef(dm, d0 + S);
-    bL = ((__fdividef(-2.0f, rL_m1 + S) + 11.0f) + 24.0f * rL - 3.0f * rL * rL_p1) * (1.0f / 30.0f);
-    bR = ((__fdividef(-2.0f, rR_p2 + S) + 11.0f) + 24.0f * rR_p1 - 3.0f * rR_p1 * rR) *
-         (1.0f / 30.0f);
+    const float uL = __fdividef(-2.0f, rL_m1 + S), uR = __fdividef(-2.0f, rR_p2 + S);
+    bL = ((uL + 11.0f) + 24.0f * rL - 3.0f * rL * rL_p1) * (1.0f / 30.0f);
+    bR = ((uR + 11.0f) + 24.0f * rR_p1 - 3.0f * rR_p1 * rR) * (1.0f / 30.0f);
+    mL = (fabsf(uL) + 11.0f + 24.0f * fabsf(rL) + 3.0f * fabsf(rL * rL_p1)) * (1.0f / 30.0f);
+    mR = (fabsf(uR) + 11.0f + 24.0f * fabsf(rR_p1) + 3.0f * fabsf(rR_p1 * rR)) * (1.0f / 30.0f);
     // beta_L dm = (-2 dm3 + 11 dm + 24 d0 - 3 rL rL_p1 dm)/30 with rL rL_p1 dm = dp (0 if d0 = 0)
     const df t3L = d0 == 0.0f ? df(0.0f) : Dp, t3R = d0 == 0.0f ? df(0.0f) : Dm;
     bdL = (df_scale(Dm3, -2.0f) + df_scale(Dm, 11.0f) + df_scale(D0, 24.0f) - df_scale(t3L, 3.0f)) *
@@ -584,18 +648,25 @@ __device__ __forceinline__ void recon_mlp_df(df qm2, df qm1, df q0, df qp1, df q
   } else {
     bL = (1.0f + 2.0f * rL) * (1.0f / 3.0f);
     bR = (1.0f + 2.0f * rR_p1) * (1.0f / 3.0f);
+    mL = (1.0f + 2.0f * fabsf(rL)) * (1.0f / 3.0f);
+    mR = (1.0f + 2.0f * fabsf(rR_p1)) * (1.0f / 3.0f);
     bdL = (Dm + df_twice(D0)) * df(1.0 / 3.0);
     bdR = (Dp + df_twice(D0)) * df(1.0 / 3.0);
   }
-  const float tt = __fdividef(fabsf((t0p - t0m).hi), fabsf((qp1 - qm1).hi) + S);
-  const float tt1 = __fdividef(fabsf((t1p - t1m).hi), fabsf((qp2 - q0).hi) + S);
+  // transverse ratios: numerators and denominators in double-float, FP32 estimates
+  const df n0 = t0p - t0m, e0 = qp1 - qm1, n1 = t1p - t1m, e1 = qp2 - q0;
+  const float tt = __fdividef(fabsf(n0.hi), fabsf(e0.hi) + S);
+  const float tt1 = __fdividef(fabsf(n1.hi), fabsf(e1.hi) + S);
   const float aLt = __fdividef(2.0f * fmaxf(1.0f, rL) * (1.0f + fmaxf(0.0f, __fdividef(tt1, rR_p1 + S))),
                                1.0f + tt);
   const float aRt = __fdividef(2.0f * fmaxf(1.0f, rR_p1) * (1.0f + fmaxf(0.0f, __fdividef(tt, rL + S))),
                                1.0f + tt1);
-  const float aL = fmaxf(1.0f, fminf(2.0f, aLt)), aR = fmaxf(1.0f, fminf(2.0f, aRt));
-  L = dm == 0.0f ? q0 : q0 + df_half(mlp_slope_df(rL, aL, bL, D0, Dm, bdL));
-  Rr = dp == 0.0f ? qp1 : qp1 - df_half(mlp_slope_df(rR_p1, aR, bR, D0, Dp, bdR));
+  L = df_ratio_nonpos(D0, Dm)
+          ? q0
+          : q0 + df_half(mlp_side_df(D0, Dm, Dp, n0, e0, n1, e1, bdL, rL, aLt, bL, mL));
+  Rr = df_ratio_nonpos(D0, Dp)
+           ? qp1
+           : qp1 - df_half(mlp_side_df(D0, Dp, Dm, n1, e1, n0, e0, bdR, rR_p1, aRt, bR, mR));
 }
 
 template <>

@@ -20,11 +20,12 @@
 
 namespace cato {
 
-// How a compute type keeps and reads the state.
-//   0 FP64    : structure-of-arrays FP64 state, stage buffers FP64 (bit-exact drop-in path)
-//   1 FP32    : stencil from an FP32 copy of U^n plus FP32 stage increments (mixed)
-//   2 df      : the FP64 layout (FP64 stage states, no FP32 rounding between stages) with the
-//               reconstruction, flux and divergence in double-float (mixed_df)
+// How a compute type computes a stage.  Every precision keeps the same structure-of-arrays FP64
+// state and FP64 stage buffers, and combines the stages (the RK accumulation) in FP64.
+//   0 FP64    : reconstruction, flux and divergence in FP64 (bit-exact drop-in path)
+//   1 FP32    : the stencil's conserved values rounded to FP32; reconstruction, flux and
+//               divergence in FP32 (mixed)
+//   2 df      : reconstruction, flux and divergence in double-float (mixed_df)
 template <typename R> struct Prec;
 template <> struct Prec<double> { static constexpr int kind = 0; };
 template <> struct Prec<float> { static constexpr int kind = 1; };
@@ -39,16 +40,11 @@ struct StageArgs {
                            // flushed) ; 2: out = L (flux_solver_t%solve output, FP64 path)
   int last;                // last stage of the step: emit the CFL dt and the state checks
   double a, b, coef;       // c = coef * dt (the reference's (0.5_rk*dt), ((1/4)*dt), dt*alpha ...)
-  // FP64 path (structure of arrays, one array per conserved variable)
+  // structure of arrays, one FP64 array per conserved variable
   const double* Uk[4];     // conserved state of this stage (stencil operand)
-  const double* Ua[4];     // U_a (point-wise operand; the step's U^n); mixed: U^n (last stage)
-  double* Uo[4];           // output conserved state; mixed: U^{n+1} (last stage)
+  const double* Ua[4];     // U_a (point-wise operand; the step's U^n)
+  double* Uo[4];           // output conserved state
   const double* Pin[4];    // when non-null: primitives to use as-is for this stage (after upload)
-  // mixed path (one float4 (rho, rho u, rho v, rho E) per cell): U^k = U^n + delta_k
-  const float4* uf;        // FP32 copy of U^n (stencil operand)
-  const float4* dk;        // delta_k (null for the first stage)
-  float4* dout;            // delta_{k+1} (not on the last stage)
-  float4* ufo;             // FP32 copy of U^{n+1} (last stage)
   // device scalars
   const double* dt;
   const int* active;
@@ -217,18 +213,8 @@ __device__ __forceinline__ void edge_flux(const R* const rp[6], int T, int lim, 
 // ---------------------------------------------------------------------------------------------
 // primitive row load
 // ---------------------------------------------------------------------------------------------
-template <typename R> struct RowSrc;
-template <> struct RowSrc<double> {
-  double c[4];  // conserved (or raw primitives) as loaded
-  bool flipy;
-};
-template <> struct RowSrc<float> {
-  float4 c;     // FP32 copy of U^n (or the raw primitives)
-  float4 d;     // delta_k
-  bool flipy;
-};
-template <> struct RowSrc<df> {
-  double c[4];  // conserved state of the stage (or the raw primitives)
+template <typename R> struct RowSrc {
+  double c[4];  // conserved state of the stage (or the raw primitives) as loaded
   bool flipy;
 };
 
@@ -238,19 +224,9 @@ __device__ __forceinline__ void load_src(const StageArgs& A, int sx, int row, Ro
   const int sy = map_index(row, A.nj, A.bc[SIDE_MY], A.bc[SIDE_PY], fy);
   s.flipy = fy;
   const size_t idx = (size_t)sy * A.pitch + sx;
-  if constexpr (Prec<R>::kind != 1) {
-    const double* const* src = A.Pin[0] ? A.Pin : A.Uk;
+  const double* const* src = A.Pin[0] ? A.Pin : A.Uk;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) s.c[k] = __ldg(src[k] + idx);
-  } else {
-    if (A.Pin[0]) {
-      s.c = make_float4(d2f_int(__ldg(A.Pin[0] + idx)), d2f_int(__ldg(A.Pin[1] + idx)),
-                        d2f_int(__ldg(A.Pin[2] + idx)), d2f_int(__ldg(A.Pin[3] + idx)));
-    } else {
-      s.c = __ldg(A.uf + idx);
-    }
-    s.d = A.dk ? __ldg(A.dk + idx) : make_float4(0.f, 0.f, 0.f, 0.f);
-  }
+  for (int k = 0; k < 4; ++k) s.c[k] = __ldg(src[k] + idx);
 }
 
 template <typename R> __device__ __forceinline__ R from_double(double x);
@@ -286,15 +262,21 @@ __device__ __forceinline__ void src_to_prim(const StageArgs& A, const RowSrc<R>&
     } else {
       R cs;
       r = to_df(s.c[0]);
-      prim_from_cons(g, g1, r, to_df(s.c[1]), to_df(s.c[2]), to_df(s.c[3]), u, v, p, cs, false);
+      const df rE = to_df(s.c[3]);
+      prim_from_cons(g, g1, r, to_df(s.c[1]), to_df(s.c[2]), rE, u, v, p, cs, false);
+      if (near_vacuum(p.hi, rE.hi, 1e-4f)) {
+        double u64, v64, p64;
+        prim_from_cons_f64(A.gamma, s.c[0], s.c[1], s.c[2], s.c[3], u64, v64, p64);
+        u = to_df(u64); v = to_df(v64); p = to_df(p64);
+      }
     }
   } else {
+    r = d2f_int(s.c[0]);
     if (A.Pin[0]) {
-      r = s.c.x; u = s.c.y; v = s.c.z; p = s.c.w;
+      u = d2f_int(s.c[1]); v = d2f_int(s.c[2]); p = d2f_int(s.c[3]);
     } else {
       R cs;
-      r = s.c.x + s.d.x;
-      prim_from_cons(g, g1, r, s.c.y + s.d.y, s.c.z + s.d.z, s.c.w + s.d.w, u, v, p, cs);
+      prim_from_cons(g, g1, r, d2f_int(s.c[1]), d2f_int(s.c[2]), d2f_int(s.c[3]), u, v, p, cs);
     }
   }
   u = flipx ? -u : u;
@@ -304,10 +286,6 @@ __device__ __forceinline__ void src_to_prim(const StageArgs& A, const RowSrc<R>&
   out[1] = u;
   out[2] = v;
   out[3] = p;
-}
-
-__device__ __forceinline__ float f4get(const float4& v, int k) {
-  return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -385,20 +363,11 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
     // operands of this row's cell update, issued early
     const size_t cidx = (size_t)j * A.pitch + (size_t)min(max(gx, 0), A.ni - 1);
     double ua[4], uk[4];
-    float4 dkc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (in_cell) {
-      if constexpr (Prec<R>::kind != 1) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          ua[k] = A.Ua[k] ? A.Ua[k][cidx] : 0.0;  // may alias Uo: plain load, read before write
-          uk[k] = (A.kind == 1) ? __ldg(A.Uk[k] + cidx) : 0.0;
-        }
-      } else {
-        if (A.dk) dkc = __ldg(A.dk + cidx);
-        if (A.last) {
-#pragma unroll
-          for (int k = 0; k < 4; ++k) ua[k] = __ldg(A.Ua[k] + cidx);
-        }
+      for (int k = 0; k < 4; ++k) {
+        ua[k] = A.Ua[k] ? A.Ua[k][cidx] : 0.0;  // may alias Uo: plain load, read before write
+        uk[k] = (A.kind == 1) ? __ldg(A.Uk[k] + cidx) : 0.0;
       }
     }
     RowSrc<R> nxt;
@@ -461,27 +430,23 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
           A.Uo[k][cidx] = r;
         }
       } else {
-        const float ccf = (float)cc, bf = (float)A.b;
+        // FP32 divergence; the stage combine (the RK accumulation) in FP64
         const float idx_f = idx_col;
         const float idy_f = (EXT && A.G.rdyf) ? A.G.rdyf[j] : idy_uni;
-        float dn[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           float Fi = sfi[k * T + t], Fim = sfi[k * T + t - 1];
           float Fj = sfj[((j & 1) * 4 + k) * T + t];
           float Fjm = sfj[(((j - 1) & 1) * 4 + k) * T + t];
-          float L = -((Fi - Fim) * idx_f + (Fj - Fjm) * idy_f);
-          if (EXT && k == 3 && A.src_q) L = L + d2f_int(A.src_q[cidx]);
-          dn[k] = bf * f4get(dkc, k) + L * ccf;
-        }
-        if (A.last) {
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            un[k] = ua[k] + f2d_int(dn[k]);
-            A.Uo[k][cidx] = un[k];
-          }
-        } else {
-          A.dout[cidx] = make_float4(dn[0], dn[1], dn[2], dn[3]);
+          float Lf = -((Fi - Fim) * idx_f + (Fj - Fjm) * idy_f);
+          if (EXT && k == 3 && A.src_q) Lf = Lf + d2f_int(A.src_q[cidx]);
+          const double L = f2d_int(Lf);
+          double r;
+          if (A.kind == 2) r = L;
+          else if (A.kind == 0) r = fma(L, cc, ua[k]);
+          else r = fma(L, cc, fma(uk[k], A.b, ua[k] * A.a));
+          un[k] = r;
+          A.Uo[k][cidx] = r;
         }
       }
       if (A.last) {
@@ -496,8 +461,14 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
           if (lt0(p)) st_loc |= ST_NEG_PRESSURE;
         } else if constexpr (Prec<R>::kind == 2) {
           df u, v, p, cs;
-          prim_from_cons(g, g1, to_df(un[0]), to_df(un[1]), to_df(un[2]), to_df(un[3]), u, v,
-                         p, cs, true);
+          const df rE = to_df(un[3]);
+          prim_from_cons(g, g1, to_df(un[0]), to_df(un[1]), to_df(un[2]), rE, u, v, p, cs, true);
+          if (near_vacuum(p.hi, rE.hi, 1e-4f)) {  // the FP64 recovery decides p and its sign
+            double u64, v64, p64;
+            prim_from_cons_f64(A.gamma, un[0], un[1], un[2], un[3], u64, v64, p64);
+            u = to_df(u64); v = to_df(v64); p = to_df(p64);
+            cs = df_sqrt(g * df_div(p, to_df(un[0])));
+          }
           const df d = df_div(cfl_df, (df_abs(u) + cs) * dx_inv + (df_abs(v) + cs) * dy_inv);
           const double dd = from_df(d);
           if (dd > 0.0 && dd < dt_loc) dt_loc = dd;
@@ -507,7 +478,6 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
         } else {
           const float4 uf = make_float4(d2f_int(un[0]), d2f_int(un[1]), d2f_int(un[2]),
                                         d2f_int(un[3]));
-          A.ufo[cidx] = uf;
           float u, v, p, cs;
           prim_from_cons((float)A.gamma, (float)(A.gamma - 1.0), uf.x, uf.y, uf.z, uf.w, u, v,
                          p, cs);

@@ -68,12 +68,12 @@ def test_periodic_box_conserves_mass_and_energy(cato_lib, precision):
 @pytest.mark.parametrize("precision", ["mixed", "mixed_df"])
 @pytest.mark.parametrize("rk", ["ssp_rk2", "ssp_rk3", "rk(2,4)"])
 def test_mixed_convergence_close_to_oracle(oracle, cato_lib, rk, precision):
-    if precision == "mixed_df" and rk.startswith("rk("):
-        pytest.skip("mixed_df keeps the FP64 layout: rk(m,n) overwrites U_0 (tested above)")
+    if rk.startswith("rk("):
+        pytest.skip("every precision keeps the FP64 layout: rk(m,n) overwrites U_0 (tested above)")
     cfg = _cfg(rk, precision=precision)
     f, o = _pair(oracle, cfg, 21, 3)
     # FP32 flux arithmetic: the stage change itself carries ~1e-6 relative error; double-float
-    # ~1e-12, plus the FP32 rounding of the intermediate stage increments
+    # ~1e-12
     rtol = {"mixed": 2e-4, "mixed_df": 1e-6}[precision]
     np.testing.assert_allclose(f.convergence(), o.convergence(), rtol=rtol, atol=1e-12)
 
