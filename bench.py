@@ -181,8 +181,12 @@ def run_reference(args, world, rank, dist):
         "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": dict(workload_config(args, world),
-                       window="steps from the initial state: the restatement does the same "
-                              "arithmetic for every cell whatever the data"),
+                       window="steps from the initial state, not the GPU arm's developed window "
+                              "at t = 0.15: reaching it takes ~1100 steps of the 4096^2 grid, "
+                              "hours of this CPU arm; the restatement has no data-dependent "
+                              "shortcuts, and the GPU arm's cpu_baseline times it on the "
+                              "developed state itself",
+                       same_window=False),
         "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": used,
                          "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
@@ -355,28 +359,37 @@ def bench_e2e(args, cfg, prims):
 def bench_kh(args, peak_gbs):
     """Roofline stress: Kelvin-Helmholtz shear layer on 8192^2 (Roe with Harten's entropy fix,
     superbee, SSP-RK3, CFL 0.4, periodic x, symmetry y).  The mixed path runs the full 200-step
-    window; the FP64 path a bounded window of it (~0.35 s per step).  Each handle is autotuned on
-a few real steps first."""
+    window from the initial state; the double-float and FP64 paths then time a window of steps
+    from the state the mixed run reached (the developed shear layer, uploaded as primitives).
+    Each handle is autotuned on a few real steps first."""
     from fvleg_2d_gb300 import ic
     from fvleg_2d_gb300.fluid import Fluid
 
     out = {}
+    developed = None
     for precision, steps in (("mixed", args.kh_steps), ("mixed_df", args.kh_df_steps),
                              ("fp64", args.kh_fp64_steps)):
         if steps <= 0:
             continue
         cfg, prims = ic.kelvin_helmholtz(args.kh_n, roe_entropy_fix="harten", precision=precision)
+        start = "initial state"
+        if precision != "mixed" and developed is not None:
+            prims, start = developed
         f = Fluid(cfg).initialize(*prims)
         f.tune(1 if precision == "fp64" else 2)
         f.run_timed(3)
         with ClockSampler(env_int("LOCAL_RANK", 0)) as clk:
             total_ms, kernel_ms = f.run_timed(steps, per_kernel=True)
+        if precision == "mixed":
+            s = f.state(("rho", "u", "v", "p"))
+            developed = ([s["rho"], s["u"], s["v"], s["p"]],
+                         f"developed state at t = {f.time:.4f} after the mixed window")
         cells = cfg.ni * cfg.nj
         per_stage = BYTES_PER_CELL_STAGE[precision]
         achieved = sum(per_stage) * cells * steps / (sum(kernel_ms[1:]) / 1e3) / 1e9
         out[precision] = {
             "value": cells * steps / (total_ms / 1e3), "unit": "cell-updates/s",
-            "steps": steps, "ms_per_step": total_ms / steps,
+            "steps": steps, "ms_per_step": total_ms / steps, "window_start": start,
             "plan": {"threads": f.get_plan()[0], "rows_per_cta": f.get_plan()[1],
                      "kernel_variant": f.get_kernel_variant()},
             "stage_ms_per_step": [m / steps for m in kernel_ms[1:]],
@@ -433,11 +446,66 @@ def bench_rectilinear(args, uniform_values):
     return out
 
 
+def error_stats(x):
+    """Median, p90, p99, max and the count above 1e-6 of a list of per-instance errors."""
+    import numpy as np
+
+    if not x:
+        return {"n": 0}
+    a = np.asarray(x, dtype=np.float64)
+    return {"n": int(a.size), "median": float(np.median(a)),
+            "p90": float(np.quantile(a, 0.90)), "p99": float(np.quantile(a, 0.99)),
+            "max": float(a.max()), "above_1e-6": int((a > 1e-6).sum())}
+
+
+def fp64_conditioning(insts, ref, rhos, codes, steps, worst=8):
+    """How far the FP64 run itself moves when its initial state is perturbed by 1e-13 (relative,
+    per cell), for the instances where the double-float path is furthest from FP64: an instance
+    whose flow amplifies a 1e-13 perturbation beyond 1e-6 cannot be held within 1e-6 of FP64 by
+    any arithmetic that is not bit-identical to it."""
+    import numpy as np
+
+    from fvleg_2d_gb300.batch import Batch
+
+    errs = []
+    for i in range(len(insts)):
+        if ref[0][i] or codes[i]:
+            continue
+        a = ref[1][i]
+        errs.append((float(np.abs(rhos[i] - a).sum() / np.abs(a).sum()), i))
+    pick = [i for e, i in sorted(errs, reverse=True)[:worst]]
+    if not pick:
+        return None
+    prng = np.random.default_rng(5)
+    b = Batch(len(pick), precision="fp64")
+    slots = []
+    for i in pick:
+        cfg, prims = insts[i]
+        p = [q.copy(order="F") for q in prims]
+        for q in p:
+            q *= 1.0 + 1e-13 * prng.standard_normal(q.shape)
+        slots.append(b.add(cfg, p, max_steps=steps))
+    b.step(steps)
+    rows = []
+    for i, s in zip(pick, slots):
+        g = insts[i][0].ghost_layers()
+        r = b.state(s)["rho"][g:-g, g:-g]
+        a = ref[1][i]
+        rows.append({"instance": i, "ni": insts[i][0].ni, "nj": insts[i][0].nj,
+                     "mixed_df_rel_l1": float(np.abs(rhos[i] - a).sum() / np.abs(a).sum()),
+                     "fp64_perturbed_1e-13_rel_l1": float(np.abs(r - a).sum() / np.abs(a).sum()),
+                     "perturbed_code": b.query(s)["error_code"]})
+    b.close()
+    return {"perturbation": "FP64 initial state x (1 + 1e-13 N(0,1)) per cell", "instances": rows}
+
+
 def bench_batched(args):
     """Config 3: 256 uneven grids (sides log-uniform [64,1024] rounded to 16, aspect U[1,4]),
     random circles, SLAU + MLP5, SSP-RK2, CFL 0.5, 500 steps each; one persistent launch per
-    stage, CUDA-graph chunks, autotuned tile plan.  Run in the two mixed precisions (FP32 flux,
-    double-float flux) with the relative L1 density error against FP64 on a sample of instances."""
+    stage, CUDA-graph chunks, autotuned tile plan.  Timed in FP64 (the plain path on the same
+    workload) and in the two mixed precisions; every instance's final density is compared with
+    its FP64 result (relative L1 and Linf over all instances that finish in both), and every
+    instance's error code with its FP64 code."""
     import numpy as np
 
     from fvleg_2d_gb300 import ic
@@ -447,23 +515,12 @@ def bench_batched(args):
     sides = ic.batch_sides(args.batch_n, rng)
     insts = [ic.random_circles(nx, ny, rng) for nx, ny in sides]
     cells = sum(c.ni * c.nj for c, _ in insts)
-    pick_rng = np.random.default_rng(args.batch_seed + 1)
-    ref_states = {}
-
-    def fp64_reference(idx):
-        todo = [i for i in idx if i not in ref_states]
-        if not todo:
-            return
-        ref = Batch(len(todo), precision="fp64")
-        slots = [ref.add(insts[i][0], insts[i][1], max_steps=args.batch_steps) for i in todo]
-        ref.step(args.batch_steps)
-        for i, s in zip(todo, slots):
-            q = ref.query(s)
-            ref_states[i] = (q["error_code"], ref.state(s)["rho"])
-        ref.close()
-
+    precisions = args.batch_precisions.split(",")
+    if "fp64" in precisions:  # the reference of the error statistics runs first
+        precisions = ["fp64"] + [p for p in precisions if p != "fp64"]
+    ref = None
     out = {}
-    for precision in args.batch_precisions.split(","):
+    for precision in precisions:
         pinsts = [(dataclasses.replace(c, precision=precision), p) for c, p in insts]
         # autotune the shared tile plan on a scratch batch of the same instances
         tune = Batch(len(pinsts), precision=precision)
@@ -472,8 +529,8 @@ def bench_batched(args):
         table = {}
         for threads, rows in [(64, 16), (128, 16), (128, 32), (256, 16), (256, 32)]:
             tune.set_plan(threads, rows)
-            tune.step(4)
-            table[f"{threads}x{rows}"] = tune.step(8) / 8
+            tune.step(2)
+            table[f"{threads}x{rows}"] = tune.step(4) / 4
         tune.close()
         best = min(table, key=table.get)
         threads, rows = (int(x) for x in best.split("x"))
@@ -483,61 +540,88 @@ def bench_batched(args):
         ms = b.step(args.batch_steps)
         n_run, _ = b.running()
         qs = [b.query(s) for s in slots]
-        failed = sum(1 for q in qs if q["error_code"])
+        codes = [q["error_code"] for q in qs]
         updates_done = sum(q["iteration"] * c.ni * c.nj for q, (c, _) in zip(qs, pinsts))
         value = updates_done / (ms / 1e3)
-        # algorithmic bytes per cell-update, SSP-RK2: FP32 mixed 32 + 112, FP64 layout 64 + 96
-        bytes_per_update = 144 if precision == "mixed" else 160
-        ok = [i for i, q in enumerate(qs) if q["error_code"] == 0]
-        k = min(args.batch_ref, len(ok))
-        pick = sorted(pick_rng.choice(ok, size=k, replace=False).tolist()) if k else []
-        fp64_reference(pick)
-        errs = []
-        for i in pick:
-            ec, a = ref_states[i]
-            if ec:
-                continue
+        rhos = []
+        for i, s in enumerate(slots):
             g = insts[i][0].ghost_layers()
-            a = a[g:-g, g:-g]
-            m = b.state(slots[i])["rho"][g:-g, g:-g]
-            errs.append(float(np.abs(m - a).sum() / np.abs(a).sum()))
+            rhos.append(b.state(s)["rho"][g:-g, g:-g].copy())
         b.close()
-        out[precision] = {
+        # algorithmic bytes per cell-update, SSP-RK2 on the FP64 state layout: 64 + 96
+        res = {
             "value": value, "unit": "cell-updates/s", "device_ms": ms, "still_running": n_run,
-            "ended_with_error": failed, "cell_updates": updates_done,
+            "ended_with_error": sum(1 for c in codes if c), "cell_updates": updates_done,
             "plan": {"threads": threads, "rows_per_cta": rows, "tuning_ms_per_step": table},
-            "roofline": {"bound": "hbm", "achieved": value * bytes_per_update / 1e9,
-                         "unit": "GB/s", "algorithmic_bytes_per_cell_update": bytes_per_update},
-            "rel_l1_density_error_vs_fp64": {"max": max(errs, default=None),
-                                             "mean": sum(errs) / len(errs) if errs else None,
-                                             "instances": len(errs)},
+            "roofline": {"bound": "hbm", "achieved": value * 160 / 1e9, "unit": "GB/s",
+                         "algorithmic_bytes_per_cell_update": 160},
         }
+        if precision == "fp64":
+            ref = (codes, rhos)
+        elif ref is not None:
+            l1, linf = [], []
+            for i in range(len(insts)):
+                if ref[0][i] or codes[i]:
+                    continue
+                a, m = ref[1][i], rhos[i]
+                l1.append(float(np.abs(m - a).sum() / np.abs(a).sum()))
+                linf.append(float(np.abs(m - a).max() / np.abs(a).max()))
+            diff = [(i, ref[0][i], codes[i]) for i in range(len(insts)) if ref[0][i] != codes[i]]
+            res["density_error_vs_fp64"] = {"rel_l1": error_stats(l1),
+                                            "rel_linf": error_stats(linf),
+                                            "instances_compared": len(l1)}
+            res["error_codes_vs_fp64"] = {"agree": len(insts) - len(diff),
+                                          "disagree_instance_fp64_this": [list(t) for t in diff]}
+            if "fp64" in out:
+                res["speedup_vs_fp64_batched"] = value / out["fp64"]["value"]
+            if precision == "mixed_df":
+                res["conditioning"] = fp64_conditioning(insts, ref, rhos, codes, args.batch_steps)
+        out[precision] = res
     out.update({
         "instances": len(insts), "cells": cells, "steps_each": args.batch_steps,
         "launches_per_step": 4,
         "scheme": "SLAU, MLP5 (3 ghost layers), SSP-RK2, CFL 0.5, zero-gradient BCs",
-        "precisions": {"mixed": "FP32 reconstruction/flux, FP64 state",
-                       "mixed_df": "double-float (FP32 pairs) reconstruction/flux, FP64 state"},
+        "precisions": {"fp64": "FP64 reconstruction/flux (the plain path), FP64 state",
+                       "mixed": "FP32 reconstruction/flux/divergence, FP64 stage accumulation",
+                       "mixed_df": "double-float (FP32 pairs) reconstruction/flux/divergence, "
+                                   "FP64 stage accumulation"},
     })
     return out
 
 
 def bench_serving(args):
-    """Config 4 stream through the continuous-batching server (mixed and FP64)."""
+    """Config 4: a Poisson stream of solve requests (square sides log-uniform in [128, 2048],
+    random-circle states, flux uniform over AUSM+-up, AUSMPW+, SLAU, HLLC and Roe, minmod,
+    SSP-RK2, CFL 0.5, t_end U[0.05, 0.3]) through the continuous-batching server with a 120 GB
+    HBM admission budget, at several arrival rates and in every precision.  Each stream is cut
+    after a wall-time cap: requests still queued or running then are censored.  A mean request
+    is ~1e9-1e10 cell-updates, so the offered load exceeds the GPU at every rate of the sweep and
+    the sustainable request rate is what completes within the cap."""
     from fvleg_2d_gb300.serve import Server, make_requests
 
     out = {}
+    rates = [float(x) for x in args.serve_rates.split(",")]
     for precision in ("mixed", "mixed_df", "fp64"):
-        reqs = make_requests(args.serve_n, rate=args.serve_rate, seed=args.serve_seed,
-                             side=(args.serve_min_side, args.serve_max_side), precision=precision)
-        srv = Server(precision=precision, budget_gb=120.0, capacity=1024, chunk_steps=16)
-        st = srv.serve(reqs, max_wall_s=args.serve_max_wall)
-        srv.close()
-        out[precision] = st.summary()
-    out["stream"] = {"requests": args.serve_n, "rate_per_s": args.serve_rate,
+        rows = []
+        for rate in rates:
+            reqs = make_requests(args.serve_n, rate=rate, seed=args.serve_seed,
+                                 side=(args.serve_min_side, args.serve_max_side),
+                                 precision=precision)
+            srv = Server(precision=precision, budget_gb=120.0, capacity=1024, chunk_steps=16)
+            st = srv.serve(reqs, max_wall_s=args.serve_max_wall)
+            srv.close()
+            row = st.summary()
+            row.update({"rate_per_s": rate,
+                        "arrived": sum(1 for r in reqs if r.arrival <= st.wall_s),
+                        "sustained_req_per_s": (row["completed"] / st.wall_s
+                                                if st.wall_s else None)})
+            rows.append(row)
+        out[precision] = rows
+    out["stream"] = {"requests": args.serve_n, "rates_per_s": rates,
                      "side": [args.serve_min_side, args.serve_max_side], "t_end": [0.05, 0.3],
                      "fluxes": "AUSM+-up, AUSMPW+, SLAU, HLLC, Roe (uniform)",
-                     "admission": "120 GB HBM budget"}
+                     "scheme": "minmod, SSP-RK2, CFL 0.5, zero-gradient BCs",
+                     "admission": "120 GB HBM budget", "wall_cap_s": args.serve_max_wall}
     return out
 
 
@@ -556,21 +640,20 @@ def main() -> int:
     ap.add_argument("--batch-n", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=500)
     ap.add_argument("--batch-seed", type=int, default=2024)
-    ap.add_argument("--batch-ref", type=int, default=8)
-    ap.add_argument("--batch-precisions", default="mixed,mixed_df")
+    ap.add_argument("--batch-precisions", default="fp64,mixed_df,mixed")
     ap.add_argument("--no-rectilinear", action="store_true")
     ap.add_argument("--no-kh", action="store_true")
     ap.add_argument("--kh-n", type=int, default=8192)
     ap.add_argument("--kh-steps", type=int, default=200)
-    ap.add_argument("--kh-fp64-steps", type=int, default=5)
+    ap.add_argument("--kh-fp64-steps", type=int, default=20)
     ap.add_argument("--kh-df-steps", type=int, default=20)
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--serve-n", type=int, default=100)
-    ap.add_argument("--serve-rate", type=float, default=100.0)
+    ap.add_argument("--serve-n", type=int, default=2000)
+    ap.add_argument("--serve-rates", default="10,100,500")
     ap.add_argument("--serve-seed", type=int, default=7)
-    ap.add_argument("--serve-min-side", type=int, default=64)
-    ap.add_argument("--serve-max-side", type=int, default=256)
-    ap.add_argument("--serve-max-wall", type=float, default=90.0)
+    ap.add_argument("--serve-min-side", type=int, default=128)
+    ap.add_argument("--serve-max-side", type=int, default=2048)
+    ap.add_argument("--serve-max-wall", type=float, default=10.0)
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":
