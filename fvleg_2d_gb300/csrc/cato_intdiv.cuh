@@ -219,6 +219,36 @@ CATO_HD uint64_t sqrt_bits(uint64_t ua, bool& ok) {
   return (((uint64_t)Ef << 52) + (M - kHid));
 }
 
+// RN(a * b) as bits for normal a, b with a normal product; ok = false otherwise (zero, subnormal,
+// infinite or NaN operands, products below the normal range or above the largest finite value;
+// the bits are then meaningless).
+//
+// With A, B the 53-bit significands, the exact product P = A B (106 bits) is in [2^104, 2^106);
+// t = 1 when P >= 2^105.  The rounded significand is M = floor(P / 2^(52+t)) plus one when the
+// dropped bits exceed half a unit, or equal it with M odd (ties to even).  The dropped bits are
+// left-aligned in a 64-bit word R, so that half a unit is 2^63.  M + 1 = 2^53 carries into the
+// exponent field, and a carry out of the largest exponent gives the infinity that IEEE rounding
+// to nearest gives.  Biased result exponent: ea + eb - 1023 + t.
+CATO_HD uint64_t mul_bits(uint64_t ua, uint64_t ub, bool& ok) {
+  const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
+  const uint64_t A = (ua & kFrac) | kHid, B = (ub & kFrac) | kHid;
+#ifdef __CUDA_ARCH__
+  const uint64_t hi = __umul64hi(A, B), lo = A * B;
+#else
+  const unsigned __int128 P = (unsigned __int128)A * B;
+  const uint64_t hi = (uint64_t)(P >> 64), lo = (uint64_t)P;
+#endif
+  const uint32_t t = (uint32_t)(hi >> 41);  // P >= 2^105
+  const uint64_t M = (hi << (12u - t)) | (lo >> (52u + t));
+  const uint64_t R = lo << (12u - t);
+  const uint64_t up = (R > 0x8000000000000000ULL || (R == 0x8000000000000000ULL && (M & 1u)))
+                          ? 1u : 0u;
+  const int32_t E = (int32_t)(ea + eb + t) - 1023;
+  ok = (ea - 1u < 2046u) && (eb - 1u < 2046u) && (E >= 1) && (E <= 2046);
+  const uint64_t sign = (ua ^ ub) & 0x8000000000000000ULL;
+  return sign | ((((uint64_t)(uint32_t)(E - 1)) << 52) + M + up);
+}
+
 // x * 2^-K (K = 1, 2, 3) and x * 2, equal to the IEEE products: an exponent step when the
 // result is normal; below the normal range the significand is shifted with round-to-nearest-even;
 // 2x overflows to infinity; infinities and NaN pass through.

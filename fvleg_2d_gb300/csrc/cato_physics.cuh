@@ -42,6 +42,19 @@ static __device__ __noinline__ double sqrt_rn(double a) {
   const uint64_t r = intdiv::sqrt_bits(intdiv::bits_of(a), ok);
   return ok ? intdiv::double_of(r) : sqrt_hw(a);
 }
+// IEEE binary64 a * b on the integer pipe (intdiv::mul_bits), bit-identical to the FP64
+// instruction: a zero operand times a finite one is the zero with the product's sign; operands
+// or products outside the normal range take the hardware instruction.  Out of line, as div_rn.
+static __device__ __noinline__ double mul_hw(double a, double b) { return a * b; }
+static __device__ __noinline__ double mul_rn(double a, double b) {
+  const uint64_t ua = intdiv::bits_of(a), ub = intdiv::bits_of(b);
+  const uint64_t za = ua << 1, zb = ub << 1;
+  if ((za == 0ULL || zb == 0ULL) && za < 0xffe0000000000000ULL && zb < 0xffe0000000000000ULL)
+    return intdiv::double_of((ua ^ ub) & 0x8000000000000000ULL);
+  bool ok;
+  const uint64_t r = intdiv::mul_bits(ua, ub, ok);
+  return ok ? intdiv::double_of(r) : mul_hw(a, b);
+}
 
 enum { FLUX_AUSMPW = 0, FLUX_SLAU = 1, FLUX_SLAU2 = 2, FLUX_SD_SLAU = 3, FLUX_SD_SLAU2 = 4,
        FLUX_ROE = 5, FLUX_AUSM_UP = 6, FLUX_HLLC = 7, FLUX_M_AUSMPW = 8 };
@@ -77,6 +90,8 @@ template <> struct Num<double> {
     if (((unsigned long long)__double_as_longlong(a) << 1) == 0ULL) return a;
     return sqrt_rn(a);
   }
+  // a * b on the integer pipe (mul_rn)
+  static __device__ __forceinline__ double mul(double a, double b) { return mul_rn(a, b); }
 };
 
 template <> struct Num<float> {
@@ -84,6 +99,7 @@ template <> struct Num<float> {
   static constexpr float tiny = FLT_MIN;
   static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
   static __device__ __forceinline__ float sqrt(float a) { return ::sqrtf(a); }
+  static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
 };
 
 template <> struct Num<df> {
@@ -91,6 +107,7 @@ template <> struct Num<df> {
   static constexpr df tiny = df(FLT_MIN, 0.0f);
   static __device__ __forceinline__ df div(df a, df b) { return df_div(a, b); }
   static __device__ __forceinline__ df sqrt(df a) { return df_sqrt(a); }
+  static __device__ __forceinline__ df mul(df a, df b) { return a * b; }
 };
 
 // FP64: the reference's MAX/MIN as compare-and-select (identical signed-zero behaviour to the
@@ -235,6 +252,20 @@ __device__ __forceinline__ double f2d_int(float f) {
   return __hiloint2double((int)hi, (int)lo);
 }
 
+// FP64 -> FP32 for the mixed path's stencil values: the exponent rebiased and the fraction
+// truncated to 23 bits (at most one FP32 unit in the last place towards zero from the rounded
+// value); magnitudes below FLT_MIN become a signed zero.  One funnel shift, an add, a select and
+// two logic operations, against ~14 integer operations for the rounded d2f_int.  Valid for
+// finite magnitudes below 2^128 (conserved states); NaN and infinity are not preserved, so the
+// state checks keep d2f_int.
+__device__ __forceinline__ float d2f_fast(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  // bits 31..23: the low 9 bits of the FP64 exponent, minus 384 = the FP32 exponent (mod 512)
+  const unsigned m = __funnelshift_l(lo, hi, 3) - (384u << 23);
+  const unsigned sign = hi & 0x80000000u;
+  return __uint_as_float((hi << 1) >= (897u << 21) ? (m | sign) : sign);
+}
+
 // FP64 <-> df: hi = the FP64 value rounded to FP32, lo = the (exact) remainder rounded to FP32;
 // one FP64 add, the conversions on the integer pipe.
 __device__ __forceinline__ df to_df(double d) {
@@ -257,15 +288,16 @@ __device__ __forceinline__ void prim_from_cons(double g, double g1, double r, do
   u = abs_lt(ru, TINY) ? 0.0 : div_rn(ru, r);
   v = abs_lt(rv, TINY) ? 0.0 : div_rn(rv, r);
   double e = abs_lt(rE, TINY) ? 0.0 : div_rn(rE, r);
-  // explicitly rounded: identical in translation units built with FMA contraction
-  double s = __dadd_rn(__dmul_rn(u, u), __dmul_rn(v, v));
+  // explicitly rounded (identical in translation units built with FMA contraction); the
+  // products on the integer pipe
+  double s = __dadd_rn(mul_rn(u, u), mul_rn(v, v));
   if (abs_lt(s, EPS)) s = 0.0;
   double h = half(s);
   double dd = e - h;
   if (abs_lt(dd, EPS)) dd = 0.0;
-  p = (r * g1) * dd;
+  p = mul_rn(mul_rn(r, g1), dd);
   double pr = abs_lt(p, TINY) ? 0.0 : div_rn(p, r);
-  cs = Num<double>::sqrt(pr * g);
+  cs = Num<double>::sqrt(mul_rn(pr, g));
   // mach_u = u / cs, mach_v = v / cs, then |mach| < 1e-13 zeroes the velocity
   if (mach_below_1e13(u, cs)) u = 0.0;  // each test reads only its own component and cs
   if (mach_below_1e13(v, cs)) v = 0.0;
@@ -364,7 +396,7 @@ __device__ __forceinline__ double slope_step<double>(double q, double phi, doubl
     const bool zneg = ((bd >> 63) != 0ULL) != minus;  // the sign of the zero added to q
     return ((bq >> 63) && zneg) ? -0.0 : 0.0;
   }
-  const double t = half(phi) * d;
+  const double t = mul_rn(half(phi), d);
   return minus ? q - t : q + t;
 }
 
@@ -1134,47 +1166,52 @@ __device__ __forceinline__ void flux_ausm_up(const FluxConsts<R>& K, const Prim<
 template <typename R, int DIR>
 __device__ __forceinline__ void flux_hllc(const FluxConsts<R>& K, const Prim<R>& A, const Prim<R>& B,
                                           R F[4]) {
+  // products through Num<R>::mul: on the FP64 path they run on the integer pipe (mul_rn), in the
+  // same left-to-right order as the expressions they spell out
+  auto m = [](R x, R y) { return Num<R>::mul(x, y); };
   const R g = R(K.gamma);
   R qnL = DIR == 0 ? A.u : A.v, qtL = DIR == 0 ? A.v : A.u;
   R qnR = DIR == 0 ? B.u : B.v, qtR = DIR == 0 ? B.v : B.u;
-  R cL = Num<R>::sqrt(Num<R>::div(g * A.p, A.r)), cR = Num<R>::sqrt(Num<R>::div(g * B.p, B.r));
+  R cL = Num<R>::sqrt(Num<R>::div(m(g, A.p), A.r)), cR = Num<R>::sqrt(Num<R>::div(m(g, B.p), B.r));
   R rho_bar = half(A.r + B.r), c_bar = half(cL + cR);
-  R p_pvrs = half(A.p + B.p) - half(qnR - qnL) * rho_bar * c_bar;
+  R p_pvrs = half(A.p + B.p) - m(m(half(qnR - qnL), rho_bar), c_bar);
   R p_star = rmax(R(0), p_pvrs);
   const R gf = R(K.hllc_gf);
   // SL = qnL - cL qL, SR = qnR + cR qR with q = 1 (then c q is c) unless p_star exceeds p
   R SL, SR;
   if (le(p_star, A.p)) SL = qnL - cL;
-  else SL = qnL - cL * Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, A.p) - R(1)));
+  else SL = qnL - m(cL, Num<R>::sqrt(R(1) + m(gf, Num<R>::div(p_star, A.p) - R(1))));
   if (le(p_star, B.p)) SR = qnR + cR;
-  else SR = qnR + cR * Num<R>::sqrt(R(1) + gf * (Num<R>::div(p_star, B.p) - R(1)));
+  else SR = qnR + m(cR, Num<R>::sqrt(R(1) + m(gf, Num<R>::div(p_star, B.p) - R(1))));
   // the total energy of the side the flux is taken from (only that one is needed)
   auto energy = [&](const Prim<R>& S) {
-    return Num<R>::div(S.p, R(K.gm1)) + half(S.r) * (S.u * S.u + S.v * S.v);
+    return Num<R>::div(S.p, R(K.gm1)) + m(half(S.r), m(S.u, S.u) + m(S.v, S.v));
   };
-  R S_star = Num<R>::div(B.p - A.p + A.r * qnL * (SL - qnL) - B.r * qnR * (SR - qnR),
-                         A.r * (SL - qnL) - B.r * (SR - qnR));
+  R S_star = Num<R>::div(B.p - A.p + m(m(A.r, qnL), SL - qnL) - m(m(B.r, qnR), SR - qnR),
+                         m(A.r, SL - qnL) - m(B.r, SR - qnR));
   R Fn[4];
   if (ge0(SL) || !(gt0(SR) || ge0(S_star))) {
     const bool useL = ge0(SL);
     const Prim<R>& S = useL ? A : B;
     R qn = useL ? qnL : qnR, qt = useL ? qtL : qtR, E = energy(S);
-    Fn[0] = S.r * qn;
-    Fn[1] = S.r * qn * qn + S.p;
-    Fn[2] = S.r * qn * qt;
-    Fn[3] = qn * (E + S.p);
+    const R rq = m(S.r, qn);
+    Fn[0] = rq;
+    Fn[1] = m(rq, qn) + S.p;
+    Fn[2] = m(rq, qt);
+    Fn[3] = m(qn, E + S.p);
   } else {
     const bool useL = ge0(S_star);
     const Prim<R>& S = useL ? A : B;
     R qn = useL ? qnL : qnR, qt = useL ? qtL : qtR, E = energy(S), SK = useL ? SL : SR;
-    R f = Num<R>::div(S.r * (SK - qn), SK - S_star);
-    R Us0 = f, Us1 = f * S_star, Us2 = f * qt;
-    R Us3 = f * (Num<R>::div(E, S.r) +
-                 (S_star - qn) * (S_star + Num<R>::div(S.p, S.r * (SK - qn))));
-    Fn[0] = S.r * qn + SK * (Us0 - S.r);
-    Fn[1] = (S.r * qn * qn + S.p) + SK * (Us1 - S.r * qn);
-    Fn[2] = S.r * qn * qt + SK * (Us2 - S.r * qt);
-    Fn[3] = qn * (E + S.p) + SK * (Us3 - E);
+    const R rk = m(S.r, SK - qn);
+    R f = Num<R>::div(rk, SK - S_star);
+    R Us0 = f, Us1 = m(f, S_star), Us2 = m(f, qt);
+    R Us3 = m(f, Num<R>::div(E, S.r) + m(S_star - qn, S_star + Num<R>::div(S.p, rk)));
+    const R rq = m(S.r, qn);
+    Fn[0] = rq + m(SK, Us0 - S.r);
+    Fn[1] = (m(rq, qn) + S.p) + m(SK, Us1 - rq);
+    Fn[2] = m(rq, qt) + m(SK, Us2 - m(S.r, qt));
+    Fn[3] = m(qn, E + S.p) + m(SK, Us3 - E);
   }
   F[0] = Fn[0];
   F[1] = DIR == 0 ? Fn[1] : Fn[2];
@@ -1185,10 +1222,15 @@ __device__ __forceinline__ void flux_hllc(const FluxConsts<R>& K, const Prim<R>&
 // ---------------------------------------------------------------------------------------------
 // flux_split_edges for one cell and one conserved variable, flux_solver.f90:252-425.
 // ---------------------------------------------------------------------------------------------
+constexpr int kNotPow2 = 1 << 20;
+
 struct Geom {
   double vol, l1, l2, l3, l4;  // volume, edge lengths (bottom, right, top, left)
   double dx, dy;               // min_dx / min_dy for the CFL step
   double inv_vol;              // 1/vol when vol is a power of two (x/vol == x*inv_vol exactly), else 0
+  // base-2 exponents of l1..l4 and inv_vol when they are powers of two, else kNotPow2: the
+  // products with them are exponent steps
+  int k1 = kNotPow2, k2 = kNotPow2, k3 = kNotPow2, k4 = kNotPow2, kinv = kNotPow2;
   // Rectilinear grids (null pointers on a uniform grid): per column i the cell width
   // x(i+1) - x(i), its edge length and reciprocal; per row j the same in y.  Every pycato grid
   // (uniform and layered, generate_initial_grids.py) is a tensor product of 1-D node arrays.
@@ -1218,6 +1260,7 @@ __device__ __forceinline__ Geom cell_geom(const Geom& G, int i, int j) {
   c.dx = dx;
   c.dy = dy;
   c.inv_vol = 0.0;
+  c.k1 = c.k2 = c.k3 = c.k4 = c.kinv = kNotPow2;
   return c;
 }
 
@@ -1239,7 +1282,30 @@ inline Geom uniform_geom(double dx, double dy) {
   int e = 0;
   const double m = std::frexp(G.vol, &e);
   G.inv_vol = (m == 0.5 && e > -1020 && e < 1020) ? 1.0 / G.vol : 0.0;
+  auto pow2_exp = [](double x) {
+    int ex = 0;
+    const double mx = std::frexp(x, &ex);
+    return (mx == 0.5 && ex > -1000 && ex < 1000) ? ex - 1 : kNotPow2;
+  };
+  G.k1 = pow2_exp(G.l1);
+  G.k2 = pow2_exp(G.l2);
+  G.k3 = pow2_exp(G.l3);
+  G.k4 = pow2_exp(G.l4);
+  G.kinv = G.inv_vol != 0.0 ? pow2_exp(G.inv_vol) : kNotPow2;
   return G;
+}
+
+// x * p for p = 2^k (k != kNotPow2): the exponent step when x and the product are normal, a
+// signed zero for a zero x (p > 0), otherwise the IEEE product; bit-identical to x * p
+__device__ __forceinline__ double mul_pow2(double x, double p, int k) {
+  const uint64_t u = intdiv::bits_of(x);
+  const int e = (int)((u >> 52) & 0x7ffu);
+  if (k != kNotPow2) {
+    if ((u << 1) == 0ULL) return x;
+    if (e >= 1 && e <= 2046 && e + k >= 1 && e + k <= 2046)
+      return intdiv::double_of(u + ((uint64_t)(int64_t)k << 52));
+  }
+  return Num<double>::mul(x, p);
 }
 
 __device__ __forceinline__ double divergence_fp64(double Fi, double Fim, double Fj, double Fjm,
@@ -1253,23 +1319,27 @@ __device__ __forceinline__ double divergence_fp64(double Fi, double Fim, double 
   // (the scale is 1 or above; compares on the integer pipe, mi * REL_TOL = REL_TOL for mi = 1)
   using N = Num<double>;
   const long long ONE = 0x3ff0000000000000LL;
+  // products with the edge lengths: exponent steps when those are powers of two, else on the
+  // integer pipe; x * 1.0 (the scale is 1) is x itself
   if (__double_as_longlong(mi) == ONE) {
-    a = ((Fi * G.l2) + (-(Fim * G.l4))) * mi;
+    a = mul_pow2(Fi, G.l2, G.k2) + (-mul_pow2(Fim, G.l4, G.k4));
     if (abs_lt(a, REL_TOL)) a = 0.0;
   } else {
-    a = ((N::div(Fi, mi) * G.l2) + (-(N::div(Fim, mi) * G.l4))) * mi;
-    if (abs_lt(a, mi * REL_TOL)) a = 0.0;
+    a = N::mul(mul_pow2(N::div(Fi, mi), G.l2, G.k2) + (-mul_pow2(N::div(Fim, mi), G.l4, G.k4)),
+               mi);
+    if (abs_lt(a, N::mul(mi, REL_TOL))) a = 0.0;
   }
   if (__double_as_longlong(mj) == ONE) {
-    b = ((Fj * G.l3) + (-(Fjm * G.l1))) * mj;
+    b = mul_pow2(Fj, G.l3, G.k3) + (-mul_pow2(Fjm, G.l1, G.k1));
     if (abs_lt(b, REL_TOL)) b = 0.0;
   } else {
-    b = ((N::div(Fj, mj) * G.l3) + (-(N::div(Fjm, mj) * G.l1))) * mj;
-    if (abs_lt(b, mj * REL_TOL)) b = 0.0;
+    b = N::mul(mul_pow2(N::div(Fj, mj), G.l3, G.k3) + (-mul_pow2(N::div(Fjm, mj), G.l1, G.k1)),
+               mj);
+    if (abs_lt(b, N::mul(mj, REL_TOL))) b = 0.0;
   }
   double s = a + b;
   if (abs_lt(s, NEAR0)) s = 0.0;
-  return G.inv_vol != 0.0 ? (-s) * G.inv_vol : N::div(-s, G.vol);
+  return G.inv_vol != 0.0 ? mul_pow2(-s, G.inv_vol, G.kinv) : N::div(-s, G.vol);
 }
 
 }  // namespace cato

@@ -271,12 +271,13 @@ __device__ __forceinline__ void src_to_prim(const StageArgs& A, const RowSrc<R>&
       }
     }
   } else {
-    r = d2f_int(s.c[0]);
+    r = d2f_fast(s.c[0]);
     if (A.Pin[0]) {
-      u = d2f_int(s.c[1]); v = d2f_int(s.c[2]); p = d2f_int(s.c[3]);
+      u = d2f_fast(s.c[1]); v = d2f_fast(s.c[2]); p = d2f_fast(s.c[3]);
     } else {
       R cs;
-      prim_from_cons(g, g1, r, d2f_int(s.c[1]), d2f_int(s.c[2]), d2f_int(s.c[3]), u, v, p, cs);
+      prim_from_cons(g, g1, r, d2f_fast(s.c[1]), d2f_fast(s.c[2]), d2f_fast(s.c[3]), u, v, p,
+                     cs);
     }
   }
   u = flipx ? -u : u;
@@ -319,6 +320,8 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
   const bool in_cell = (t >= NG) && (t <= NG + W - 1) && (gx < A.ni);
   const double dt = *A.dt;
   const double cc = A.coef * dt;
+  [[maybe_unused]] const float ccf = (float)cc;  // mixed: the stage increment c L in FP32
+  [[maybe_unused]] const float cfl_f = (float)A.cfl;
   const R* rp[6];
   // mixed_df constants of the update (unused by the other paths)
   [[maybe_unused]] df dx_inv, dy_inv, cfl_df;
@@ -418,19 +421,20 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
           if (A.kind == 2) {
             r = L;
           } else if (A.kind == 0) {
-            r = ua[k] + L * cc;
+            r = ua[k] + Num<double>::mul(L, cc);
             if (abs_lt(r, Num<double>::eps)) r = 0.0;
           } else {
-            double s = ua[k] * A.a + uk[k] * A.b;
+            double s = Num<double>::mul(ua[k], A.a) + Num<double>::mul(uk[k], A.b);
             if (abs_lt(s, Num<double>::eps)) s = 0.0;
-            r = s + L * cc;
+            r = s + Num<double>::mul(L, cc);
             if (abs_lt(r, Num<double>::eps)) r = 0.0;
           }
           un[k] = r;
           A.Uo[k][cidx] = r;
         }
       } else {
-        // FP32 divergence; the stage combine (the RK accumulation) in FP64
+        // FP32 divergence and stage increment c L; the stage combine (the RK accumulation)
+        // in FP64
         const float idx_f = idx_col;
         const float idy_f = (EXT && A.G.rdyf) ? A.G.rdyf[j] : idy_uni;
 #pragma unroll
@@ -440,11 +444,10 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
           float Fjm = sfj[(((j - 1) & 1) * 4 + k) * T + t];
           float Lf = -((Fi - Fim) * idx_f + (Fj - Fjm) * idy_f);
           if (EXT && k == 3 && A.src_q) Lf = Lf + d2f_int(A.src_q[cidx]);
-          const double L = f2d_int(Lf);
           double r;
-          if (A.kind == 2) r = L;
-          else if (A.kind == 0) r = fma(L, cc, ua[k]);
-          else r = fma(L, cc, fma(uk[k], A.b, ua[k] * A.a));
+          if (A.kind == 2) r = f2d_int(Lf);
+          else if (A.kind == 0) r = ua[k] + f2d_int(Lf * ccf);
+          else r = fma(uk[k], A.b, fma(ua[k], A.a, f2d_int(Lf * ccf)));
           un[k] = r;
           A.Uo[k][cidx] = r;
         }
@@ -476,17 +479,19 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
           if (un[0] < 0.0) st_loc |= ST_NEG_DENSITY;
           if (p.hi < 0.0f) st_loc |= ST_NEG_PRESSURE;
         } else {
-          const float4 uf = make_float4(d2f_int(un[0]), d2f_int(un[1]), d2f_int(un[2]),
-                                        d2f_int(un[3]));
+          const float4 uf = make_float4(d2f_fast(un[0]), d2f_fast(un[1]), d2f_fast(un[2]),
+                                        d2f_fast(un[3]));
           float u, v, p, cs;
-          prim_from_cons((float)A.gamma, (float)(A.gamma - 1.0), uf.x, uf.y, uf.z, uf.w, u, v,
-                         p, cs);
-          float d = (float)A.cfl / ((fabsf(u) + cs) * idx_col +
-                                    (fabsf(v) + cs) * ((EXT && A.G.rdyf) ? A.G.rdyf[j] : idy_uni));
+          prim_from_cons(g, g1, uf.x, uf.y, uf.z, uf.w, u, v, p, cs);
+          float d = cfl_f / ((fabsf(u) + cs) * idx_col +
+                             (fabsf(v) + cs) * ((EXT && A.G.rdyf) ? A.G.rdyf[j] : idy_uni));
           double dd = f2d_int(d);
           if (__double_as_longlong(dd) < __double_as_longlong(dt_loc) && d > 0.0f) dt_loc = dd;
-          if (isnan(uf.x) || isnan(u) || isnan(v) || isnan(p)) st_loc |= ST_NAN;
-          if (uf.x < 0.0f) st_loc |= ST_NEG_DENSITY;
+          // NaN and sign tests on the FP64 state itself (the fast conversion keeps neither)
+          if (d_isnan(un[0]) || d_isnan(un[1]) || d_isnan(un[2]) || d_isnan(un[3]) ||
+              isnan(u) || isnan(v) || isnan(p))
+            st_loc |= ST_NAN;
+          if (lt0(un[0])) st_loc |= ST_NEG_DENSITY;
           if (p < 0.0f) st_loc |= ST_NEG_PRESSURE;
         }
       }

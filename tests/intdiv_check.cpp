@@ -1,5 +1,5 @@
-// Host check of the integer-pipe binary64 division and square root (cato_intdiv.cuh): the same
-// source as the device code, with the FP32 seeds computed by the host's IEEE float division and
+// Host check of the integer-pipe binary64 division, square root and multiplication
+// (cato_intdiv.cuh): the same source as the device code, with the FP32 seeds computed by the host's IEEE float division and
 // square root, compared bit for bit with the host's hardware a / b and sqrt(a).
 //
 // The device seeds are hardware approximations, so every family runs with the host seeds moved by
@@ -11,7 +11,8 @@
 // mismatch.  Families: random normal operands over the full exponent range and over a narrow
 // one; significands near powers of two, near each other and with few bits set; quotients and
 // roots next to rounding midpoints; every FP32 seed (all 2^23 truncated significands) with the
-// largest truncation error; the exact power-of-two scalings.
+// largest truncation error; the exact power-of-two scalings; products over the full exponent
+// range and of significands with few bits set (exact products and ties).
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -54,6 +55,17 @@ static void check_sqrt(double a) {
   ++tested;
   if (r != bits_of(std::sqrt(a))) {
     if (bad < 5) printf("sqrt mismatch %a: %a, hardware %a\n", a, double_of(r), std::sqrt(a));
+    ++bad;
+  }
+}
+
+static void check_mul(double a, double b) {
+  bool ok;
+  const uint64_t r = mul_bits(bits_of(a), bits_of(b), ok);
+  if (!ok) { ++fallback; return; }
+  ++tested;
+  if (r != bits_of(a * b)) {
+    if (bad < 5) printf("mul mismatch %a * %a: %a, hardware %a\n", a, b, double_of(r), a * b);
     ++bad;
   }
 }
@@ -164,6 +176,29 @@ int main(int argc, char** argv) {
   }
   seed_offset_ulps = 0;
   report("seeds");
+  fail |= bad != 0;
+
+  reset();  // products: random operands, few significant bits (exact products, ties), overflow
+  for (long i = 0; i < 4 * n; ++i) {
+    check_mul(random_double(1, 2046), random_double(1, 2046));
+    check_mul(random_double(900, 1150), random_double(900, 1150));
+    uint64_t ma = rng() & kFrac, mb = rng() & kFrac;
+    switch (rng() % 5) {
+      case 0: mb = (1ULL << (rng() % 52)); break;                    // b = 1 + 2^-k
+      case 1: mb = (1ULL << (rng() % 52)) | (1ULL << (rng() % 52)); ma |= 1; break;
+      case 2: ma &= ~((1ULL << (rng() % 53)) - 1); mb &= ~((1ULL << (rng() % 53)) - 1); break;
+      case 3: ma = kFrac - (ma & 0xff); mb = kFrac - (mb & 0xff); break;  // near 2 x 2
+      default: ma &= 0xfff; break;
+    }
+    const uint64_t s2 = rng() & 0x8000000000000000ULL;
+    const double a = double_of(s2 | ((uint64_t)(1000 + rng() % 47) << 52) | ma);
+    const double b = double_of(((uint64_t)(1000 + rng() % 47) << 52) | mb);
+    check_mul(a, b);
+    // near the ends of the normal range: subnormal and overflowing products fall back
+    check_mul(random_double(1, 30), random_double(990, 1030));
+    check_mul(random_double(2020, 2046), random_double(1020, 1030));
+  }
+  report("mul");
   fail |= bad != 0;
   return fail;
 }
