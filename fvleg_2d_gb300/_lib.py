@@ -66,6 +66,8 @@ def load(build_if_missing: bool = False):
         "cato_gpu_download": (ctypes.c_int, [H] + [_dp] * 8 + [i64]),
         "cato_gpu_conservation_sums": (ctypes.c_int, [H, _dp]),
         "cato_gpu_convergence": (ctypes.c_int, [H, _dp]),
+        "cato_gpu_set_step_options": (ctypes.c_int, [H, ctypes.c_int32, ctypes.c_int32,
+                                                     ctypes.c_double]),
         "cato_gpu_solve": (ctypes.c_int, [H] + [_dp] * 8 + [i64]),
         "cato_gpu_interpolate_edges": (ctypes.c_int, [H, _dp, i64, _dp, _dp]),
         "cato_gpu_status": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int32)]),

@@ -59,6 +59,14 @@ struct cato_handle {
   bool uploaded = false;
   bool raw_pending = false;  // next stage 1 uses prim_raw
   bool stepped = false;      // a step ran since the last upload (its stage buffers are valid)
+  // step options (cato_gpu_set_step_options): keep U^n of each step (U_0 of the convergence
+  // norms of rk(m,n) steps), and subcycle SSP steps (retry with dt / 10)
+  bool keep_start = false;
+  bool subcycle = false;
+  double subcycle_tol = 1e-3;
+  double* bak[4] = {};       // U^n of the last step
+  double* bak_raw[4] = {};   // the uploaded primitives while a first step may be retried
+  bool bak_valid = false;
   double* rect[6] = {};      // rectilinear grid: dx, lx, 1/dx per column; dy, ly, 1/dy per row
   float* rectf[2] = {};      // FP32 1/dx per column, 1/dy per row
   double* red = nullptr;     // reduction partials + results (lazy)
@@ -605,6 +613,8 @@ int cato_gpu_destroy(cato_handle* h) {
   for (int v = 0; v < 4; ++v) {
     cudaFree(h->U[v]);
     for (int s = 0; s < 2; ++s) cudaFree(h->S[s][v]);
+    cudaFree(h->bak[v]);
+    cudaFree(h->bak_raw[v]);
   }
   for (int k = 0; k < 8; ++k) cudaFree(h->scratch[k]);
   for (int k = 0; k < 4; ++k) cudaFree(h->halo[k]);
@@ -654,6 +664,7 @@ int cato_gpu_upload_primitive(cato_handle* h, const double* rho, const double* u
   int rc = pull_ctl(h);
   if (rc) return rc;
   h->uploaded = true;
+  h->bak_valid = false;
   h->raw_pending = true;
   h->stepped = false;
   return upload_code(h->ctl_host->status);
@@ -665,6 +676,72 @@ int cato_gpu_get_timestep(cato_handle* h, double* dt) {
   int rc = pull_ctl(h);
   if (rc) return rc;
   *dt = host_decode(h->ctl_host->dt_min);
+  return CATO_OK;
+}
+
+// One step with the step options on: U^n (and, while the first step after an upload may be
+// retried, the uploaded primitives) is copied aside first; with subcycling, an SSP step whose
+// convergence norm exceeds the tolerance is undone and taken again with dt / 10
+// (subcycle_check, mod_fluid.f90:856-887, inside the stage loops of ssp_rk_2_2 and ssp_rk_3_3).
+static int step_kept(cato_handle* h, const StepCtl& c0) {
+  const size_t fb = h->field_elems * sizeof(double);
+  const int rk = h->cfg.rk;
+  const bool retry = h->subcycle && (rk == CATO_RK_SSP2 || rk == CATO_RK_SSP3);
+  const bool raw = h->raw_pending;
+  for (int k = 0; k < 4; ++k) {
+    if (!h->bak[k]) CK(cudaMalloc(&h->bak[k], fb));
+    CK(cudaMemcpyAsync(h->bak[k], h->U[k], fb, cudaMemcpyDeviceToDevice, h->stream));
+    if (retry && raw) {
+      if (!h->bak_raw[k]) CK(cudaMalloc(&h->bak_raw[k], fb));
+      CK(cudaMemcpyAsync(h->bak_raw[k], h->prim_raw[k], fb, cudaMemcpyDeviceToDevice,
+                         h->stream));
+    }
+  }
+  // the step's dt: the caller's, else the CFL dt of U^n (the step kernel's own choice)
+  double dt = c0.fixed_dt > 0.0 ? c0.fixed_dt : host_decode(c0.dt_min);
+  for (int attempt = 0;; ++attempt) {
+    StepCtl c = c0;
+    if (attempt > 0) c.fixed_dt = dt;
+    *h->ctl_host = c;
+    CK(cudaMemcpyAsync(h->ctl, h->ctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice, h->stream));
+    int rc = enqueue_step(h);
+    if (rc) return rc;
+    rc = pull_ctl(h);
+    if (rc) return rc;
+    h->bak_valid = true;
+    if (h->ctl_host->iter > c0.iter) h->stepped = true;
+    // 40 retries take dt below 1e-40 of the CFL dt: the norm is then as small as it gets
+    if (!retry || h->ctl_host->status || attempt >= 40) break;
+    double l2[4];
+    rc = cato_gpu_convergence(h, l2);
+    if (rc) return rc;
+    bool again = false;
+    for (int k = 0; k < 4; ++k) again |= l2[k] > h->subcycle_tol;  // NaN: no subcycle
+    if (!again) break;
+    for (int k = 0; k < 4; ++k) {
+      CK(cudaMemcpyAsync(h->U[k], h->bak[k], fb, cudaMemcpyDeviceToDevice, h->stream));
+      if (raw)
+        CK(cudaMemcpyAsync(h->prim_raw[k], h->bak_raw[k], fb, cudaMemcpyDeviceToDevice,
+                           h->stream));
+    }
+    h->raw_pending = raw;
+    dt = dt / 10.0;
+  }
+  return CATO_OK;
+}
+
+int cato_gpu_set_step_options(cato_handle* h, int32_t keep_step_start, int32_t allow_subcycle,
+                              double subcycle_tolerance) {
+  if (!h) return CATO_ERR_ARG;
+  if (allow_subcycle && !(subcycle_tolerance > 0.0))
+    return fail(h, CATO_ERR_ARG, "subcycle tolerance must be positive");
+  // the pressure-input boundary's clock advances with every residual evaluation in the
+  // reference, so a retried step would see other boundary times: not combined here
+  if (allow_subcycle && h->cfg.bc[CATO_PLUS_X] == CATO_BC_PRESSURE_INPUT)
+    return fail(h, CATO_ERR_CONFIG, "subcycling with the pressure-input boundary");
+  h->keep_start = keep_step_start != 0 || allow_subcycle != 0;
+  h->subcycle = allow_subcycle != 0;
+  h->subcycle_tol = subcycle_tolerance;
   return CATO_OK;
 }
 
@@ -681,14 +758,20 @@ int cato_gpu_integrate(cato_handle* h, double dt, double* dt_used, int32_t* erro
   c.max_iter = c.iter + 1;
   c.fixed_dt = dt > 0.0 ? dt : 0.0;
   *h->ctl_host = c;
-  CK(cudaMemcpyAsync(h->ctl, h->ctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice, h->stream));
-  if (c.status == 0) {
-    rc = enqueue_step(h);
+  if (c.status == 0 && h->keep_start) {
+    rc = step_kept(h, c);
     if (rc) return rc;
+  } else {
+    CK(cudaMemcpyAsync(h->ctl, h->ctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice,
+                       h->stream));
+    if (c.status == 0) {
+      rc = enqueue_step(h);
+      if (rc) return rc;
+    }
+    rc = pull_ctl(h);
+    if (rc) return rc;
+    if (h->ctl_host->iter > c.iter) h->stepped = true;
   }
-  rc = pull_ctl(h);
-  if (rc) return rc;
-  if (h->ctl_host->iter > c.iter) h->stepped = true;
   if (dt_used) *dt_used = h->ctl_host->dt;
   if (error_code) *error_code = status_code(h->ctl_host->status);
   return CATO_OK;
@@ -712,7 +795,18 @@ int cato_gpu_run(cato_handle* h, int64_t max_steps, double t_end, int64_t* steps
   const long long total = max_steps >= 0 ? max_steps : (1LL << 62);
   long long issued = 0;
   const long long chunk = 32;
-  while (issued < total) {
+  // with the step options on, each step is taken from the host (copies, subcycle decisions)
+  while (h->keep_start && issued < total) {
+    const StepCtl& now = *h->ctl_host;
+    if (now.status != 0 || !(now.time < t_end)) break;
+    StepCtl s = now;
+    s.max_iter = s.iter + 1;
+    s.fixed_dt = 0.0;
+    rc = step_kept(h, s);
+    if (rc) return rc;
+    ++issued;
+  }
+  while (!h->keep_start && issued < total) {
     const long long n = (total - issued) < chunk ? (total - issued) : chunk;
     for (long long k = 0; k < n; ++k) {
       rc = enqueue_step(h);
@@ -1293,12 +1387,13 @@ int cato_gpu_convergence(cato_handle* h, double l2[4]) {
   const bool ssp = rk == CATO_RK_SSP2 || rk == CATO_RK_SSP3;
   RedArgs R{};
   R.mode = 1;
-  // SSP: the first stage's output U_1 is still in S0; rk(m,n) compares with U^n, which the
-  // last stage overwrote in place
-  if (!ssp)
-    return fail(h, CATO_ERR_STATE, "rk(m,n) steps update U^n in place: no U_0 to compare");
+  // SSP: the first stage's output U_1 is still in S0.  rk(m,n) compares with U^n
+  // (mod_fluid.f90:970), which the last stage overwrote in place: only a kept copy has it
+  if (!ssp && !h->bak_valid)
+    return fail(h, CATO_ERR_STATE,
+                "rk(m,n) steps update U^n in place: keep the step start to compare with U_0");
   for (int k = 0; k < 4; ++k) {
-    R.A[k] = h->S[0][k];
+    R.A[k] = ssp ? h->S[0][k] : h->bak[k];
     R.B[k] = h->U[k];
   }
   double out[RED_Q];

@@ -67,6 +67,7 @@ class Deck:
     integration_strategy: str = ""
     max_iterations: int = 2**31 - 1
     allow_subcycle: bool = False
+    subcycle_error_tolerance: float = 1e-3
     # [physics]
     polytropic_index: float = 5.0 / 3.0
     # [scheme]
@@ -221,6 +222,7 @@ def parse_deck(text: str) -> Deck:
     d.integration_strategy = get("time", "integration_strategy", required=True)
     d.max_iterations = get("time", "max_iterations", lambda v: int(_real(v)), 2**31 - 1)
     d.allow_subcycle = get("time", "allow_subcycle", _logical, False)
+    d.subcycle_error_tolerance = get("time", "subcycle_error_tolerance", _real, 1e-3)
     d.polytropic_index = get("physics", "polytropic_index", _real, required=True)
     d.flux_solver = get("scheme", "flux_solver", required=True)
     if d.flux_solver == "AUSM+-up":
@@ -404,13 +406,73 @@ def _read_table3(name: str, base_dir: str, what: str) -> np.ndarray:
     return np.array(rows, dtype=np.float64)
 
 
+def fortran_es(x: float, w: int, d: int) -> str:
+    """Fortran ESw.d editing: one digit before the point, d after, a two-digit exponent with
+    its E (three digits without it beyond 99), right-justified in w characters."""
+    import math
+
+    if math.isnan(x):
+        return "NaN".rjust(w)
+    if math.isinf(x):
+        return ("-Infinity" if x < 0 else "Infinity").rjust(w)
+    mant, exp = f"{x:.{d}E}".split("E")
+    e = int(exp)
+    return (f"{mant}E{e:+03d}" if abs(e) < 100 else f"{mant}{e:+04d}").rjust(w)
+
+
+class RunHistory:
+    """The reference's per-run files: ``residual_hist.csv`` (fluid_t%initialize truncates it and
+    write_residual_history appends a line per step, mod_fluid.f90:244-246, 1207-1223),
+    ``timing.csv`` (timer_t%log_time, mod_timing.f90:57-94) and ``timing_summary.yaml``
+    (timer_t%output_stats, :104-127), written into ``directory``."""
+
+    def __init__(self, directory: str, t_to_dim: float):
+        import os
+        import time
+
+        os.makedirs(directory, exist_ok=True)
+        self.dir = directory
+        self.t_to_dim = t_to_dim
+        self.res = open(os.path.join(directory, "residual_hist.csv"), "w")
+        self.res.write("iteration,time,dt,rho,rho_u,rho_v,rho_E\n")
+        self.tim = open(os.path.join(directory, "timing.csv"), "w")
+        self.tim.write("iteration, elapsed_wall_time[sec], elapsed_cpu_time[sec], timestep[sec]\n")
+        self.wall0, self.cpu0 = time.perf_counter(), time.process_time()
+
+    def residual(self, iteration: int, time: float, dt: float, norms) -> None:
+        vals = [time * self.t_to_dim, dt * self.t_to_dim] + [float(x) for x in norms]
+        self.res.write(f"{iteration}," + "".join(fortran_es(v, 16, 6) + "," for v in vals) + "\n")
+        self.res.flush()
+
+    def timing(self, iteration: int, timestep: float) -> None:
+        import time
+
+        vals = [time.perf_counter() - self.wall0, time.process_time() - self.cpu0, timestep]
+        self.tim.write(f"{iteration}" + "".join(", " + fortran_es(v, 14, 4) for v in vals) + "\n")
+
+    def close(self) -> None:
+        import os
+        import time
+
+        wall, cpu = time.perf_counter() - self.wall0, time.process_time() - self.cpu0
+        with open(os.path.join(self.dir, "timing_summary.yaml"), "w") as f:
+            for label, v in (("wall time [s]", wall), ("wall time [m]", wall / 60.0),
+                             ("wall time [hr]", wall / 3600.0), ("CPU time [s]", cpu),
+                             ("CPU time [m]", cpu / 60.0), ("CPU time [hr]", cpu / 3600.0)):
+                f.write(f"Total elapsed {label}:{fortran_es(v, 10, 3)}\n")
+        self.res.close()
+        self.tim.close()
+
+
 def main_loop(deck: Deck, fluid, step, results_dir: str | None = None) -> int:
     """The time loop of ``main.f90:95-198`` (no restart, no start-up period) around a fluid:
     ``step(dt)`` advances one step (``dt`` None: the CFL step) and returns its error code.  The
     loop keeps its own clock: it snaps to the next output time when a step passes it, writes a
     contour the iteration after (``write_contour`` of :mod:`.contour`, when ``results_dir`` is
     given), and stops on that clock.  The first step uses ``initial_delta_t`` when it is set,
-    every step when ``use_constant_delta_t``.  Returns the iterations taken."""
+    every step when ``use_constant_delta_t``.  With ``results_dir`` it also writes the
+    residual history and the timing files there (:class:`RunHistory`).  Returns the iterations
+    taken."""
     from .contour import write_contour
     from .fluid import CatoError
 
@@ -420,16 +482,21 @@ def main_loop(deck: Deck, fluid, step, results_dir: str | None = None) -> int:
     eps = float(np.finfo(np.float64).eps)
     time, iteration = 0.0, 0
     next_output = 0.0 + interval
+    hist = None
     if results_dir is not None:
         write_contour(fluid, results_dir, deck, iteration=iteration)
+        hist = RunHistory(results_dir, 1.0 / f["t_to_nondim"])
     while time < max_time and iteration < deck.max_iterations:
         fixed = deck.use_constant_delta_t or (iteration == 0 and deck.initial_delta_t > 0.0)
         ec = step(deck.initial_delta_t * f["t_to_nondim"] if fixed else None)
         delta_t = fluid.last_dt
         new_time = fluid.time
+        if hist is not None:
+            hist.residual(fluid.iteration, new_time, delta_t, fluid.convergence())
         if ec:
             if results_dir is not None:
                 write_contour(fluid, results_dir, deck, iteration=iteration)
+                hist.close()
             raise CatoError(ec, f"time integration failed at iteration {iteration}")
         if abs(time - next_output) < eps:
             next_output = next_output + interval
@@ -440,6 +507,10 @@ def main_loop(deck: Deck, fluid, step, results_dir: str | None = None) -> int:
             new_time = time + delta_t
         time = new_time
         iteration = iteration + 1
+        if hist is not None:
+            hist.timing(iteration, delta_t)
+    if hist is not None:
+        hist.close()
     return iteration
 
 
@@ -476,6 +547,11 @@ def run_deck(deck: Deck, precision: str = "fp64", prims=None, grid=None, base_di
             fluid.set_rectilinear(deck.xmin + np.arange(cfg.ni + 1) * cfg.dx,
                                   deck.ymin + np.arange(cfg.nj + 1) * cfg.dy)
         fluid.set_energy_source(src)
+    if deck.allow_subcycle or results_dir is not None:
+        # subcycling, and U^n of every step for the residual history of rk(m,n) steps
+        fluid.set_step_options(keep_step_start=results_dir is not None,
+                               allow_subcycle=deck.allow_subcycle,
+                               subcycle_tolerance=deck.subcycle_error_tolerance)
     fluid.initialize(*prims)
     if results_dir is None and not deck.use_constant_delta_t and not deck.initial_delta_t > 0.0:
         steps = fluid.run(deck.max_time * t_to_nondim(deck), deck.max_iterations)

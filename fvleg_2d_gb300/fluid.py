@@ -256,6 +256,17 @@ class Fluid(_Handle):
                "conservation_sums")
         return out
 
+    def set_step_options(self, keep_step_start: bool = False, allow_subcycle: bool = False,
+                         subcycle_tolerance: float = 1e-3) -> None:
+        """[time] allow_subcycle / subcycle_error_tolerance (subcycle_check,
+        mod_fluid.f90:856-887: SSP steps repeat with dt / 10 while a convergence norm exceeds
+        the tolerance), and keeping U^n of every step so that :meth:`convergence` also covers
+        rk(m,n) steps (the residual history)."""
+        _check(self.L.cato_gpu_set_step_options(self.h, int(bool(keep_step_start)),
+                                                 int(bool(allow_subcycle)),
+                                                 float(subcycle_tolerance)),
+               self.h, "set_step_options")
+
     def convergence(self) -> np.ndarray:
         """calculate_convergence (mod_fluid.f90:1162-1205) of the last step:
         [rho, rho u, rho v, rho E] relative L2 change from the first to the last stage."""

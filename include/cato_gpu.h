@@ -300,6 +300,19 @@ int cato_gpu_get_kernel_variant(const cato_handle* h, int32_t* variant);
  * *best_ms = the fastest candidate's time per step.  Returns the first fluid error, if any. */
 int cato_gpu_tune(cato_handle* h, int32_t steps, int32_t* steps_taken, float* best_ms);
 
+/* Step options of the deck's [time] section.
+ * keep_step_start: each step first copies U^n aside (one extra state, 32 B per cell, and a
+ *   copy per step), so that cato_gpu_convergence also covers rk(m,n) steps, whose norms compare
+ *   the last stage with U_0 = U^n (mod_fluid.f90:970); the residual history needs them.
+ * allow_subcycle, subcycle_tolerance: subcycle_check (mod_fluid.f90:856-887): an SSP-RK2/3 step
+ *   whose L2 convergence norms (calculate_convergence) exceed the tolerance in any variable is
+ *   taken again from U^n with dt / 10, until they do not; the step's dt and the clock use the
+ *   last dt.  rk(m,n) steps are not subcycled, as in the reference.  Implies keep_step_start.
+ *   Not combined with the pressure-input boundary (CATO_ERR_CONFIG).
+ * Off by default; with either on, cato_gpu_run takes its steps from the host. */
+int cato_gpu_set_step_options(cato_handle* h, int32_t keep_step_start, int32_t allow_subcycle,
+                              double subcycle_tolerance);
+
 /* Select the CUDA device used by handles created afterwards on this host thread. */
 int cato_gpu_select_device(int32_t device);
 

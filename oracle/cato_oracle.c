@@ -1277,6 +1277,9 @@ struct oracle_fluid {
   int64_t iteration;
   double conv[4];   /* calculate_convergence of the last step */
   int conv_valid;
+  /* allow_subcycle / subcycle_tolerance (mod_fluid.f90:98-99, 856-887) */
+  int subcycle;
+  double subcycle_tol;
 };
 
 static void source_field(oracle_fluid* f);
@@ -1669,6 +1672,23 @@ typedef struct {
   double *u, *v, *p, *cs;
 } prims_t;
 
+/* subcycle_check (mod_fluid.f90:856-887): with allow_subcycle, any L2 convergence norm of the
+ * step above the tolerance repeats it with dt / 10 (a NaN norm does not) */
+static int subcycle_check(const oracle_fluid* f) {
+  if (!f->subcycle) return 0;
+  for (int k = 0; k < 4; ++k)
+    if (f->conv[k] > f->subcycle_tol) return 1;
+  return 0;
+}
+
+double oracle_dt(const oracle_fluid* f) { return f->dt; }
+
+int oracle_set_subcycle(oracle_fluid* f, int allow, double tolerance) {
+  f->subcycle = allow ? 1 : 0;
+  f->subcycle_tol = tolerance;
+  return 0;
+}
+
 /* fluid_t%integrate (mod_fluid.f90:411-450) for ssp_rk2 (:1081-1160), ssp_rk3 (:739-854) and
  * rk(m,n) (:889-1007); sanity check of the new state (:726-737) returns the reference codes. */
 int oracle_integrate(oracle_fluid* f, double dt, int32_t* error_code) {
@@ -1687,32 +1707,42 @@ int oracle_integrate(oracle_fluid* f, double dt, int32_t* error_code) {
   if (f->c.rk == CATO_RK_SSP2) {
     double* U1[4] = {f->st[0][0], f->st[0][1], f->st[0][2], f->st[0][3]};
     double* U2[4] = {f->st[1][0], f->st[1][1], f->st[1][2], f->st[1][3]};
-    f->solver_time = f->solver_time + dt;
-    f->bc_time = f->solver_time;
-    rc |= residual(f, f->rho, f->u, f->v, f->p);
-    stage_a(f, U1, U, dt);
-    derive_all(f, U1, su[0], sv[0], spp[0], scs[0]);
-    f->bc_time = t_copy;
-    rc |= residual(f, U1[0], su[0], sv[0], spp[0]);
-    stage_b(f, U2, U, 0.5, U1, 0.5, 0.5 * dt);
-    convergence(f, U1, U2);
+    /* the stages repeat with dt / 10 while subcycle_check asks for it (ssp_rk_2_2's loop,
+     * mod_fluid.f90:1108-1140); U itself changes only after the loop */
+    for (;;) {
+      f->solver_time = f->solver_time + dt;
+      f->bc_time = f->solver_time;
+      rc |= residual(f, f->rho, f->u, f->v, f->p);
+      stage_a(f, U1, U, dt);
+      derive_all(f, U1, su[0], sv[0], spp[0], scs[0]);
+      f->bc_time = f->time + dt;
+      rc |= residual(f, U1[0], su[0], sv[0], spp[0]);
+      stage_b(f, U2, U, 0.5, U1, 0.5, 0.5 * dt);
+      convergence(f, U1, U2);
+      if (!subcycle_check(f)) break;
+      dt = dt / 10.0;
+    }
     for (int k = 0; k < 4; ++k) memcpy(U[k], U2[k], nfield(d) * sizeof(double));
   } else if (f->c.rk == CATO_RK_SSP3) {
     double* U1[4] = {f->st[0][0], f->st[0][1], f->st[0][2], f->st[0][3]};
     double* U2[4] = {f->st[1][0], f->st[1][1], f->st[1][2], f->st[1][3]};
     double* U3[4] = {f->st[2][0], f->st[2][1], f->st[2][2], f->st[2][3]};
-    f->solver_time = f->solver_time + dt;
-    f->bc_time = f->solver_time;
-    rc |= residual(f, f->rho, f->u, f->v, f->p);
-    stage_a(f, U1, U, dt);
-    derive_all(f, U1, su[0], sv[0], spp[0], scs[0]);
-    f->bc_time = t_copy;
-    rc |= residual(f, U1[0], su[0], sv[0], spp[0]);
-    stage_b(f, U2, U, 3.0 / 4.0, U1, 1.0 / 4.0, (1.0 / 4.0) * dt);
-    derive_all(f, U2, su[1], sv[1], spp[1], scs[1]);
-    rc |= residual(f, U2[0], su[1], sv[1], spp[1]);
-    stage_b(f, U3, U, 1.0 / 3.0, U2, 2.0 / 3.0, (2.0 / 3.0) * dt);
-    convergence(f, U1, U3);
+    for (;;) {  /* ssp_rk_3_3's subcycle loop, mod_fluid.f90:762-829 */
+      f->solver_time = f->solver_time + dt;
+      f->bc_time = f->solver_time;
+      rc |= residual(f, f->rho, f->u, f->v, f->p);
+      stage_a(f, U1, U, dt);
+      derive_all(f, U1, su[0], sv[0], spp[0], scs[0]);
+      f->bc_time = f->time + dt;
+      rc |= residual(f, U1[0], su[0], sv[0], spp[0]);
+      stage_b(f, U2, U, 3.0 / 4.0, U1, 1.0 / 4.0, (1.0 / 4.0) * dt);
+      derive_all(f, U2, su[1], sv[1], spp[1], scs[1]);
+      rc |= residual(f, U2[0], su[1], sv[1], spp[1]);
+      stage_b(f, U3, U, 1.0 / 3.0, U2, 2.0 / 3.0, (2.0 / 3.0) * dt);
+      convergence(f, U1, U3);
+      if (!subcycle_check(f)) break;
+      dt = dt / 10.0;
+    }
     for (int k = 0; k < 4; ++k) memcpy(U[k], U3[k], nfield(d) * sizeof(double));
   } else {
     /* rk(m,n), mod_fluid.f90:926-966 */
@@ -1746,6 +1776,7 @@ int oracle_integrate(oracle_fluid* f, double dt, int32_t* error_code) {
     convergence(f, U0, Uc);
     for (int k = 0; k < 4; ++k) memcpy(U[k], Uc[k], nfield(d) * sizeof(double));
   }
+  f->dt = dt;
   f->time = f->time + dt;
   derive_all(f, U, f->u, f->v, f->p, f->cs);
   /* the reference's order of checks: check_for_nans on rho, u, v, p at the stage assignment

@@ -46,6 +46,10 @@ int oracle_solve_rect(const cato_config* cfg, const double* x_nodes, const doubl
 /* Whole fluid_t. */
 oracle_fluid* oracle_create(const cato_config* cfg);
 void oracle_destroy(oracle_fluid* f);
+/* allow_subcycle and subcycle_tolerance of the deck's [time] section */
+int oracle_set_subcycle(oracle_fluid* f, int allow, double tolerance);
+/* dt of the last step (after any subcycling) */
+double oracle_dt(const oracle_fluid* f);
 int oracle_set_primitive(oracle_fluid* f, const double* rho, const double* u, const double* v,
                          const double* p);
 double oracle_get_timestep(oracle_fluid* f);

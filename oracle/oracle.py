@@ -52,6 +52,9 @@ def lib():
         L.oracle_solve_rect.argtypes = [cfgp] + [_dp] * 10
         L.oracle_set_rectilinear.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.oracle_set_time.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int64]
+        L.oracle_set_subcycle.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
+        L.oracle_dt.restype = ctypes.c_double
+        L.oracle_dt.argtypes = [ctypes.c_void_p]
         L.oracle_set_pow_mode.argtypes = [ctypes.c_int]
         L.oracle_set_energy_source.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                                _dp, _dp, _dp]
@@ -207,6 +210,16 @@ class OracleFluid:
 
     def set_time(self, time: float, iteration: int) -> None:
         lib().oracle_set_time(self._h, float(time), int(iteration))
+
+    def set_subcycle(self, allow: bool, tolerance: float = 1e-3) -> None:
+        """[time] allow_subcycle / subcycle_error_tolerance: SSP steps repeat with dt / 10
+        while a convergence norm exceeds the tolerance."""
+        lib().oracle_set_subcycle(self._h, int(bool(allow)), float(tolerance))
+
+    @property
+    def dt(self) -> float:
+        """dt of the last step (after any subcycling)."""
+        return lib().oracle_dt(self._h)
 
     def set_energy_source(self, source=None) -> None:
         """An EnergySource (fvleg_2d_gb300.config) or None."""

@@ -164,3 +164,40 @@ def test_pressure_input_keys_and_table(tmp_path):
     assert const.scheme().constant_bc_pressure == 3.0 * f["press_to_nondim"]
     with pytest.raises(DeckError):
         parse_deck(PBC_DECK.replace("bc_pressure_input_file = 'drive.dat'", ""))
+
+
+def test_fortran_es_editing():
+    from fvleg_2d_gb300.deck import fortran_es
+
+    assert fortran_es(1.23456e-3, 16, 6) == "    1.234560E-03"
+    assert fortran_es(-0.5, 16, 6) == "   -5.000000E-01"
+    assert fortran_es(0.0, 14, 4) == "    0.0000E+00"
+    assert fortran_es(1e-120, 16, 6) == "    1.000000-120"  # three-digit exponent: no E
+    assert fortran_es(2.5, 10, 3) == " 2.500E+00"
+
+
+def test_run_history_files(tmp_path):
+    """residual_hist.csv (mod_fluid.f90:244-246, 1207-1223), timing.csv and timing_summary.yaml
+    (mod_timing.f90) in the reference's formats."""
+    from fvleg_2d_gb300.deck import RunHistory
+
+    h = RunHistory(str(tmp_path), t_to_dim=2.0)
+    h.residual(1, 0.5, 0.25, [1e-3, 2e-4, 0.0, 3e-5])
+    h.timing(1, 0.25)
+    h.close()
+    res = (tmp_path / "residual_hist.csv").read_text().splitlines()
+    assert res[0] == "iteration,time,dt,rho,rho_u,rho_v,rho_E"
+    assert res[1] == ("1,    1.000000E+00,    5.000000E-01,    1.000000E-03,    2.000000E-04,"
+                      "    0.000000E+00,    3.000000E-05,")
+    tim = (tmp_path / "timing.csv").read_text().splitlines()
+    assert tim[0] == "iteration, elapsed_wall_time[sec], elapsed_cpu_time[sec], timestep[sec]"
+    f = tim[1].split(", ")
+    assert f[0] == "1" and len(f) == 4 and f[3].strip() == "2.5000E-01"
+    summ = (tmp_path / "timing_summary.yaml").read_text().splitlines()
+    assert len(summ) == 6 and summ[0].startswith("Total elapsed wall time [s]:")
+
+
+def test_deck_reads_the_subcycle_keys():
+    text = DECK.replace("[time]", "[time]\nallow_subcycle = .true.\nsubcycle_error_tolerance = 2e-4")
+    d = parse_deck(text)
+    assert d.allow_subcycle and d.subcycle_error_tolerance == 2e-4
