@@ -288,16 +288,15 @@ __device__ __forceinline__ void prim_from_cons(double g, double g1, double r, do
   u = abs_lt(ru, TINY) ? 0.0 : div_rn(ru, r);
   v = abs_lt(rv, TINY) ? 0.0 : div_rn(rv, r);
   double e = abs_lt(rE, TINY) ? 0.0 : div_rn(rE, r);
-  // explicitly rounded (identical in translation units built with FMA contraction); the
-  // products on the integer pipe
-  double s = __dadd_rn(mul_rn(u, u), mul_rn(v, v));
+  // explicitly rounded: identical in translation units built with FMA contraction
+  double s = __dadd_rn(__dmul_rn(u, u), __dmul_rn(v, v));
   if (abs_lt(s, EPS)) s = 0.0;
   double h = half(s);
   double dd = e - h;
   if (abs_lt(dd, EPS)) dd = 0.0;
-  p = mul_rn(mul_rn(r, g1), dd);
+  p = (r * g1) * dd;
   double pr = abs_lt(p, TINY) ? 0.0 : div_rn(p, r);
-  cs = Num<double>::sqrt(mul_rn(pr, g));
+  cs = Num<double>::sqrt(pr * g);
   // mach_u = u / cs, mach_v = v / cs, then |mach| < 1e-13 zeroes the velocity
   if (mach_below_1e13(u, cs)) u = 0.0;  // each test reads only its own component and cs
   if (mach_below_1e13(v, cs)) v = 0.0;
@@ -396,7 +395,7 @@ __device__ __forceinline__ double slope_step<double>(double q, double phi, doubl
     const bool zneg = ((bd >> 63) != 0ULL) != minus;  // the sign of the zero added to q
     return ((bq >> 63) && zneg) ? -0.0 : 0.0;
   }
-  const double t = mul_rn(half(phi), d);
+  const double t = half(phi) * d;
   return minus ? q - t : q + t;
 }
 

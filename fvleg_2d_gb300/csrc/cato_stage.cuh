@@ -421,12 +421,14 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
           if (A.kind == 2) {
             r = L;
           } else if (A.kind == 0) {
-            r = ua[k] + Num<double>::mul(L, cc);
+            r = ua[k] + __dmul_rn(L, cc);
             if (abs_lt(r, Num<double>::eps)) r = 0.0;
           } else {
-            double s = Num<double>::mul(ua[k], A.a) + Num<double>::mul(uk[k], A.b);
+            // explicitly rounded products: the reference's order also where the translation
+            // unit contracts (the double-float kernels)
+            double s = __dmul_rn(ua[k], A.a) + __dmul_rn(uk[k], A.b);
             if (abs_lt(s, Num<double>::eps)) s = 0.0;
-            r = s + Num<double>::mul(L, cc);
+            r = s + __dmul_rn(L, cc);
             if (abs_lt(r, Num<double>::eps)) r = 0.0;
           }
           un[k] = r;
