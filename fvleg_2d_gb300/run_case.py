@@ -5,7 +5,9 @@ for the synthetic workloads), e.g. to profile one kernel on a small case:
 
 Workloads: ``sod`` (400x40 Sod tube), ``quadrant`` (four-quadrant Riemann problem, HLLC / van
 Leer / SSP-RK3), ``kh`` (Kelvin-Helmholtz, Roe / superbee / SSP-RK3), ``circles`` (random circles,
-SLAU / MLP5 / SSP-RK2, seeded).
+SLAU / MLP5 / SSP-RK2, seeded), ``batch`` (the batched configuration's generator: ``--n``
+instances of uneven sides in [64, 1024], random circles, SLAU / MLP5 / SSP-RK2, advanced together
+in one batch).
 """
 from __future__ import annotations
 
@@ -32,9 +34,28 @@ def make(name: str, n: int, precision: str, seed: int = 0):
     raise ValueError(f"unknown workload {name!r}")
 
 
+def run_batch(n: int, precision: str, steps: int, seed: int, plan: str) -> dict:
+    """``n`` instances of the batched configuration (seeded sides and states) in one batch."""
+    from .batch import Batch
+
+    rng = np.random.default_rng(seed)
+    insts = [ic.random_circles(nx, ny, rng, precision=precision)
+             for nx, ny in ic.batch_sides(n, rng)]
+    b = Batch(n, precision=precision)
+    if plan:
+        b.set_plan(*(int(x) for x in plan.split(",")))
+    for cfg, prims in insts:
+        b.add(cfg, prims)
+    ms = b.step(steps)
+    cells = sum(c.ni * c.nj for c, _ in insts)
+    b.close()
+    return {"workload": "batch", "instances": n, "cells": cells, "precision": precision,
+            "steps": steps, "ms": ms, "cell_updates_per_s": cells * steps / (ms / 1e3)}
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("workload", choices=["sod", "quadrant", "kh", "circles"])
+    ap.add_argument("workload", choices=["sod", "quadrant", "kh", "circles", "batch"])
     ap.add_argument("--n", type=int, default=1024)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed_df"])
     ap.add_argument("--steps", type=int, default=2)
@@ -49,6 +70,9 @@ def main(argv=None) -> int:
     ap.add_argument("--t-start", type=float, default=0.0,
                     help="first advance the flow to this time with the mixed path")
     a = ap.parse_args(argv)
+    if a.workload == "batch":
+        print(json.dumps(run_batch(a.n, a.precision, a.steps, a.seed, a.plan)))
+        return 0
     cfg, prims = make(a.workload, a.n, a.precision, a.seed)
     if a.flux or a.limiter:
         old_g = cfg.ghost_layers()
