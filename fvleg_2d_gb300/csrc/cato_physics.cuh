@@ -1295,7 +1295,8 @@ inline Geom uniform_geom(double dx, double dy) {
 }
 
 // x * p for p = 2^k (k != kNotPow2): the exponent step when x and the product are normal, a
-// signed zero for a zero x (p > 0), otherwise the IEEE product; bit-identical to x * p
+// signed zero for a zero x (p > 0); otherwise (and for any p that is not a power of two) the
+// FP64 instruction; bit-identical to x * p
 __device__ __forceinline__ double mul_pow2(double x, double p, int k) {
   const uint64_t u = intdiv::bits_of(x);
   const int e = (int)((u >> 52) & 0x7ffu);
@@ -1304,7 +1305,7 @@ __device__ __forceinline__ double mul_pow2(double x, double p, int k) {
     if (e >= 1 && e <= 2046 && e + k >= 1 && e + k <= 2046)
       return intdiv::double_of(u + ((uint64_t)(int64_t)k << 52));
   }
-  return Num<double>::mul(x, p);
+  return x * p;
 }
 
 __device__ __forceinline__ double divergence_fp64(double Fi, double Fim, double Fj, double Fjm,
@@ -1318,23 +1319,21 @@ __device__ __forceinline__ double divergence_fp64(double Fi, double Fim, double 
   // (the scale is 1 or above; compares on the integer pipe, mi * REL_TOL = REL_TOL for mi = 1)
   using N = Num<double>;
   const long long ONE = 0x3ff0000000000000LL;
-  // products with the edge lengths: exponent steps when those are powers of two, else on the
-  // integer pipe; x * 1.0 (the scale is 1) is x itself
+  // products with the edge lengths: exponent steps when those are powers of two; x * 1.0 (the
+  // scale is 1) is x itself
   if (__double_as_longlong(mi) == ONE) {
     a = mul_pow2(Fi, G.l2, G.k2) + (-mul_pow2(Fim, G.l4, G.k4));
     if (abs_lt(a, REL_TOL)) a = 0.0;
   } else {
-    a = N::mul(mul_pow2(N::div(Fi, mi), G.l2, G.k2) + (-mul_pow2(N::div(Fim, mi), G.l4, G.k4)),
-               mi);
-    if (abs_lt(a, N::mul(mi, REL_TOL))) a = 0.0;
+    a = (mul_pow2(N::div(Fi, mi), G.l2, G.k2) + (-mul_pow2(N::div(Fim, mi), G.l4, G.k4))) * mi;
+    if (abs_lt(a, mi * REL_TOL)) a = 0.0;
   }
   if (__double_as_longlong(mj) == ONE) {
     b = mul_pow2(Fj, G.l3, G.k3) + (-mul_pow2(Fjm, G.l1, G.k1));
     if (abs_lt(b, REL_TOL)) b = 0.0;
   } else {
-    b = N::mul(mul_pow2(N::div(Fj, mj), G.l3, G.k3) + (-mul_pow2(N::div(Fjm, mj), G.l1, G.k1)),
-               mj);
-    if (abs_lt(b, N::mul(mj, REL_TOL))) b = 0.0;
+    b = (mul_pow2(N::div(Fj, mj), G.l3, G.k3) + (-mul_pow2(N::div(Fjm, mj), G.l1, G.k1))) * mj;
+    if (abs_lt(b, mj * REL_TOL)) b = 0.0;
   }
   double s = a + b;
   if (abs_lt(s, NEAR0)) s = 0.0;
