@@ -1034,59 +1034,62 @@ __device__ __forceinline__ void flux_slau(const FluxConsts<R>& K, const Prim<R>&
 template <typename R, int DIR>
 __device__ __forceinline__ void flux_roe(const FluxConsts<R>& K, const Prim<R>& A, const Prim<R>& B,
                                          const R fa[5], const R fb[5], R F[4]) {
+  // products through Num<R>::mul (the integer pipe on the FP64 path), in the same left-to-right
+  // order as the expressions they spell out
+  auto m = [](R x, R y) { return Num<R>::mul(x, y); };
   const R g = R(K.gamma);
   R rl = rabs(A.r), ul = A.u, vl = A.v, pl = rabs(A.p);
   R rr = rabs(B.r), ur = B.u, vr = B.v, pr = rabs(B.p);
   const R gq = R(K.g_over_gm1);
-  R rav = Num<R>::sqrt(rl * rr);
-  R q_pl = Num<R>::div(pl, rl), q_rav = Num<R>::div(rav, rl), q_gpl = Num<R>::div(g * pl, rl);
-  R hl = gq * q_pl + half(ul * ul + vl * vl);
-  R hr = gq * Num<R>::div(pr, rr) + half(ur * ur + vr * vr);
+  R rav = Num<R>::sqrt(m(rl, rr));
+  R q_pl = Num<R>::div(pl, rl), q_rav = Num<R>::div(rav, rl), q_gpl = Num<R>::div(m(g, pl), rl);
+  R hl = m(gq, q_pl) + half(m(ul, ul) + m(vl, vl));
+  R hr = m(gq, Num<R>::div(pr, rr)) + half(m(ur, ur) + m(vr, vr));
   R gam1 = R(K.gm1);
   R dd = q_rav;
   R dd1 = Num<R>::div(R(1), R(1) + dd);
-  R uav = (ul + dd * ur) * dd1;
-  R vav = (vl + dd * vr) * dd1;
-  R hav = (hl + dd * hr) * dd1;
-  R q2a = half(uav * uav + vav * vav);
-  R c2a = gam1 * (hav - q2a);
+  R uav = m(ul + m(dd, ur), dd1);
+  R vav = m(vl + m(dd, vr), dd1);
+  R hav = m(hl + m(dd, hr), dd1);
+  R q2a = half(m(uav, uav) + m(vav, vav));
+  R c2a = m(gam1, hav - q2a);
   R cav = Num<R>::sqrt(c2a);
   // x n_x + y n_y with the unit normal's exact 1 and 0 (a product with 1 is the operand)
   auto dotn = [](R x, R y) { return DIR == 0 ? add_mul0(x, y) : add_mul0(y, x); };
   R uv = dotn(uav, vav);
   R du = dotn(ur - ul, vr - vl);
   R du_trans = DIR == 0 ? add_mul0(vr - vl, -(ur - ul)) : add_mul0(-(ur - ul), vr - vl);
-  R cs_R = Num<R>::sqrt(Num<R>::div(g * pr, rr));
+  R cs_R = Num<R>::sqrt(Num<R>::div(m(g, pr), rr));
   R cs_L = Num<R>::sqrt(q_gpl);
   R h1 = rabs(rmin(uv - cav, dotn(ul, vl) - cs_L));
   R h2 = rabs(uv);
   R h4 = rabs(rmax(uv + cav, dotn(ur, vr) + cs_R));
   R e1 = h1, e2 = h2, e4 = h4;
   if (K.harten) {
-    R delta = R(K.harten_delta) * cav;
-    e1 = (h1 > delta) ? h1 : Num<R>::div(half(h1 * h1 + delta * delta), delta);
-    e2 = (h2 > delta) ? h2 : Num<R>::div(half(h2 * h2 + delta * delta), delta);
-    e4 = (h4 > delta) ? h4 : Num<R>::div(half(h4 * h4 + delta * delta), delta);
+    R delta = m(R(K.harten_delta), cav);
+    e1 = (h1 > delta) ? h1 : Num<R>::div(half(m(h1, h1) + m(delta, delta)), delta);
+    e2 = (h2 > delta) ? h2 : Num<R>::div(half(m(h2, h2) + m(delta, delta)), delta);
+    e4 = (h4 > delta) ? h4 : Num<R>::div(half(m(h4, h4) + m(delta, delta)), delta);
   }
-  h1 = rav * cav * du;
-  h2 = Num<R>::div(e1 * (pr - pl - h1), twice(c2a));
-  R h3 = e2 * (rr - rl - Num<R>::div(pr - pl, c2a));
-  h4 = e2 * rav;
-  R h5 = Num<R>::div(e4 * (pr - pl + h1), twice(c2a));
+  h1 = m(m(rav, cav), du);
+  h2 = Num<R>::div(m(e1, pr - pl - h1), twice(c2a));
+  R h3 = m(e2, rr - rl - Num<R>::div(pr - pl, c2a));
+  h4 = m(e2, rav);
+  R h5 = Num<R>::div(m(e4, pr - pl + h1), twice(c2a));
   R psi = Num<R>::div(rabs(cs_R - cs_L), rmax(cs_R, cs_L));
   // the normal-direction terms carry the exact 1, the tangential ones the exact 0
   auto on = [](bool axis, R a, R b) { return axis ? a + b : add_mul0(a, b); };
-  R FR0 = rr * uv, FR1 = on(DIR == 0, rr * ur * uv, pr), FR2 = on(DIR == 1, rr * vr * uv, pr);
-  R FR3 = rr * hr * uv;
-  R FL0 = rl * uv, FL1 = on(DIR == 0, rl * ul * uv, pl), FL2 = on(DIR == 1, rl * vl * uv, pl);
-  R FL3 = rl * hl * uv;
+  R FR0 = m(rr, uv), FR1 = on(DIR == 0, m(m(rr, ur), uv), pr), FR2 = on(DIR == 1, m(m(rr, vr), uv), pr);
+  R FR3 = m(m(rr, hr), uv);
+  R FL0 = m(rl, uv), FL1 = on(DIR == 0, m(m(rl, ul), uv), pl), FL2 = on(DIR == 1, m(m(rl, vl), uv), pl);
+  R FL3 = m(m(rl, hl), uv);
   R m0 = (h2 + h3 + h5);
-  R m1 = (h2 * on(DIR == 0, uav, -cav) + h3 * uav + h4 * on(DIR == 0, ur - ul, -du) +
-          h5 * on(DIR == 0, uav, cav));
-  R m2 = (h2 * on(DIR == 1, vav, -cav) + h3 * vav + h4 * on(DIR == 1, vr - vl, -du) +
-          h5 * on(DIR == 1, vav, cav));
-  R m3 = (h2 * (hav - cav * uv) + h3 * q2a + h4 * (uav * (ur - ul) + vav * (vr - vl) - uv * du) +
-          h5 * (hav + cav * uv));
+  R m1 = (m(h2, on(DIR == 0, uav, -cav)) + m(h3, uav) + m(h4, on(DIR == 0, ur - ul, -du)) +
+          m(h5, on(DIR == 0, uav, cav)));
+  R m2 = (m(h2, on(DIR == 1, vav, -cav)) + m(h3, vav) + m(h4, on(DIR == 1, vr - vl, -du)) +
+          m(h5, on(DIR == 1, vav, cav)));
+  R m3 = (m(h2, hav - m(cav, uv)) + m(h3, q2a) +
+          m(h4, m(uav, ur - ul) + m(vav, vr - vl) - m(uv, du)) + m(h5, hav + m(cav, uv)));
   F[0] = half(FR0 + FL0 - m0);
   F[1] = half(FR1 + FL1 - m1);
   F[2] = half(FR2 + FL2 - m2);
@@ -1098,10 +1101,10 @@ __device__ __forceinline__ void flux_roe(const FluxConsts<R>& K, const Prim<R>& 
     fmax = rmax(fmax, (ratio < R(1)) ? R(0) : R(1));
   }
   // -(du_trans n_y) + psi du n_x and du_trans n_x + psi du n_y
-  const R c1 = DIR == 0 ? add_mul0(psi * du, -du_trans) : add_mul0(-du_trans, psi * du);
-  const R c2 = DIR == 0 ? add_mul0(du_trans, psi * du) : add_mul0(psi * du, du_trans);
-  F[1] = F[1] - half(fmax) * rav * cav * c1;
-  F[2] = F[2] - half(fmax) * rav * cav * c2;
+  const R c1 = DIR == 0 ? add_mul0(m(psi, du), -du_trans) : add_mul0(-du_trans, m(psi, du));
+  const R c2 = DIR == 0 ? add_mul0(du_trans, m(psi, du)) : add_mul0(m(psi, du), du_trans);
+  F[1] = F[1] - m(m(m(half(fmax), rav), cav), c1);
+  F[2] = F[2] - m(m(m(half(fmax), rav), cav), c2);
 }
 
 // AUSM+-up (basic), ausm_plus_solver.f90:499-643 + upwinding of the commented driver :313-325.
