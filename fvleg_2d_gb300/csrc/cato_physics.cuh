@@ -593,12 +593,25 @@ __device__ __forceinline__ df flushed(df d) {
   return fabsf(d.hi) < 2.220446049250313080847263336181640625e-16f ? df(0.0f) : d;
 }
 
+// Double-float edge values out of line (one copy per kernel instead of one per variable and
+// direction: the double-float stage kernels otherwise outgrow the instruction cache)
+struct DfPair {
+  df L, R;
+};
+static __device__ __noinline__ DfPair recon_tvd2_df(int lim, df qm1, df q0, df qp1, df qp2) {
+  const df Dm = flushed(q0 - qm1), D0 = flushed(qp1 - q0), Dp = flushed(qp2 - qp1);
+  DfPair e;
+  e.L = q0 + df_half(tvd_slope_df(lim, D0, Dm));
+  e.R = qp1 - df_half(tvd_slope_df(lim, D0, Dp));
+  return e;
+}
+
 template <>
 __device__ __forceinline__ void recon_tvd2<df>(int lim, df qm1, df q0, df qp1, df qp2, df& L,
                                                df& Rr) {
-  const df Dm = flushed(q0 - qm1), D0 = flushed(qp1 - q0), Dp = flushed(qp2 - qp1);
-  L = q0 + df_half(tvd_slope_df(lim, D0, Dm));
-  Rr = qp1 - df_half(tvd_slope_df(lim, D0, Dp));
+  const DfPair e = recon_tvd2_df(lim, qm1, q0, qp1, qp2);
+  L = e.L;
+  Rr = e.R;
 }
 
 // One side of the MLP limiter: the slope phi * dq, phi = max(0, min(alpha r, alpha, beta)),
@@ -700,15 +713,26 @@ __device__ __forceinline__ void recon_mlp_df(df qm2, df qm1, df q0, df qp1, df q
            : qp1 - df_half(mlp_side_df(D0, Dp, Dm, n1, e1, n0, e0, bdR, rR_p1, aRt, bR, mR));
 }
 
+template <int ORDER>
+static __device__ __noinline__ DfPair recon_mlp_df_ool(df qm2, df qm1, df q0, df qp1, df qp2,
+                                                       df qp3, df t0p, df t0m, df t1p, df t1m) {
+  DfPair e;
+  recon_mlp_df<ORDER>(qm2, qm1, q0, qp1, qp2, qp3, t0p, t0m, t1p, t1m, e.L, e.R);
+  return e;
+}
 template <>
 __device__ __forceinline__ void recon_mlp<df, 3>(df qm2, df qm1, df q0, df qp1, df qp2, df qp3,
                                                  df t0p, df t0m, df t1p, df t1m, df& L, df& Rr) {
-  recon_mlp_df<3>(qm2, qm1, q0, qp1, qp2, qp3, t0p, t0m, t1p, t1m, L, Rr);
+  const DfPair e = recon_mlp_df_ool<3>(qm2, qm1, q0, qp1, qp2, qp3, t0p, t0m, t1p, t1m);
+  L = e.L;
+  Rr = e.R;
 }
 template <>
 __device__ __forceinline__ void recon_mlp<df, 5>(df qm2, df qm1, df q0, df qp1, df qp2, df qp3,
                                                  df t0p, df t0m, df t1p, df t1m, df& L, df& Rr) {
-  recon_mlp_df<5>(qm2, qm1, q0, qp1, qp2, qp3, t0p, t0m, t1p, t1m, L, Rr);
+  const DfPair e = recon_mlp_df_ool<5>(qm2, qm1, q0, qp1, qp2, qp3, t0p, t0m, t1p, t1m);
+  L = e.L;
+  Rr = e.R;
 }
 
 // ---------------------------------------------------------------------------------------------
