@@ -543,12 +543,19 @@ template <typename R> constexpr int min_blocks() {
   return Prec<R>::kind == 2 ? CATO_DF_MIN_BLOCKS
                             : (Prec<R>::kind == 1 ? CATO_F32_MIN_BLOCKS : CATO_F64_MIN_BLOCKS);
 }
-// the persistent FP64 batch kernels (256-thread CTAs)
+// the persistent batch kernels (256-thread CTAs) run best with more resident warps than the
+// single-grid kernels: FP64 and double-float at most 85 registers (3 CTAs per SM), measured on
+// the batched random-circle workload (SLAU + MLP5) at +28 % (FP64, over the compiler's 229
+// registers) and +21 % (double-float, over 122); both spill a little to the stack.  FP64 at 128
+// registers gave +20 %, double-float at 64 less than at 85.
 #ifndef CATO_F64_BATCH_MIN_BLOCKS
-#define CATO_F64_BATCH_MIN_BLOCKS CATO_F64_MIN_BLOCKS
+#define CATO_F64_BATCH_MIN_BLOCKS 3
+#endif
+#ifndef CATO_DF_BATCH_MIN_BLOCKS
+#define CATO_DF_BATCH_MIN_BLOCKS 3
 #endif
 template <typename R> constexpr int batch_min_blocks() {
-  return Prec<R>::kind == 2 ? CATO_DF_MIN_BLOCKS
+  return Prec<R>::kind == 2 ? CATO_DF_BATCH_MIN_BLOCKS
                             : (Prec<R>::kind == 1 ? CATO_F32_BATCH_MIN_BLOCKS
                                                   : CATO_F64_BATCH_MIN_BLOCKS);
 }
