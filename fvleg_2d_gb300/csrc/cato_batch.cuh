@@ -79,7 +79,7 @@ __device__ __forceinline__ void batch_stage_args(InstDesc* d, const BatchStageAr
 }
 
 template <typename R, int NG, int FLUX, int RECON>
-__global__ void __launch_bounds__(256, batch_min_blocks<R>())
+__global__ void __launch_bounds__(256, batch_min_blocks<R, FLUX>())
     batch_stage_kernel(const BatchStageArgs B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;

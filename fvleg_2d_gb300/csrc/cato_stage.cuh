@@ -554,10 +554,17 @@ template <typename R> constexpr int min_blocks() {
 #ifndef CATO_DF_BATCH_MIN_BLOCKS
 #define CATO_DF_BATCH_MIN_BLOCKS 3
 #endif
-template <typename R> constexpr int batch_min_blocks() {
-  return Prec<R>::kind == 2 ? CATO_DF_BATCH_MIN_BLOCKS
-                            : (Prec<R>::kind == 1 ? CATO_F32_BATCH_MIN_BLOCKS
-                                                  : CATO_F64_BATCH_MIN_BLOCKS);
+// FP64 M-AUSMPW+ (two interpolators' edge states live at once) spills too much at 85: at most
+// 128 registers (205 against 168 M cell-updates/s); Roe and the other fluxes measured best at 85
+#ifndef CATO_F64_BATCH_MIN_BLOCKS_MAUSMPW
+#define CATO_F64_BATCH_MIN_BLOCKS_MAUSMPW 2
+#endif
+template <typename R, int FLUX> constexpr int batch_min_blocks() {
+  return Prec<R>::kind == 2
+             ? CATO_DF_BATCH_MIN_BLOCKS
+             : (Prec<R>::kind == 1 ? CATO_F32_BATCH_MIN_BLOCKS
+                                   : (FLUX == FLUX_M_AUSMPW ? CATO_F64_BATCH_MIN_BLOCKS_MAUSMPW
+                                                            : CATO_F64_BATCH_MIN_BLOCKS));
 }
 
 template <typename R, int NG, int FLUX, int RECON, bool EXT, int MB>

@@ -34,12 +34,15 @@ def make(name: str, n: int, precision: str, seed: int = 0):
     raise ValueError(f"unknown workload {name!r}")
 
 
-def run_batch(n: int, precision: str, steps: int, seed: int, plan: str) -> dict:
-    """``n`` instances of the batched configuration (seeded sides and states) in one batch."""
+def run_batch(n: int, precision: str, steps: int, seed: int, plan: str, flux: str = "",
+              limiter: str = "") -> dict:
+    """``n`` instances of the batched configuration (seeded sides and states) in one batch;
+    ``flux`` / ``limiter`` replace SLAU / MLP5 when given."""
     from .batch import Batch
 
     rng = np.random.default_rng(seed)
-    insts = [ic.random_circles(nx, ny, rng, precision=precision)
+    over = {k: v for k, v in (("flux_solver", flux), ("limiter", limiter)) if v}
+    insts = [ic.random_circles(nx, ny, rng, precision=precision, **over)
              for nx, ny in ic.batch_sides(n, rng)]
     b = Batch(n, precision=precision)
     if plan:
@@ -71,7 +74,7 @@ def main(argv=None) -> int:
                     help="first advance the flow to this time with the mixed path")
     a = ap.parse_args(argv)
     if a.workload == "batch":
-        print(json.dumps(run_batch(a.n, a.precision, a.steps, a.seed, a.plan)))
+        print(json.dumps(run_batch(a.n, a.precision, a.steps, a.seed, a.plan, a.flux, a.limiter)))
         return 0
     cfg, prims = make(a.workload, a.n, a.precision, a.seed)
     if a.flux or a.limiter:
