@@ -68,6 +68,11 @@ def load(build_if_missing: bool = False):
         "cato_gpu_convergence": (ctypes.c_int, [H, _dp]),
         "cato_gpu_set_step_options": (ctypes.c_int, [H, ctypes.c_int32, ctypes.c_int32,
                                                      ctypes.c_double]),
+        "cato_gpu_step_begin": (ctypes.c_int, [H, ctypes.c_double]),
+        "cato_gpu_step_stage": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int32)]),
+        "cato_gpu_step_end": (ctypes.c_int, [H, _dp, ctypes.POINTER(ctypes.c_int32)]),
+        "cato_gpu_halo_export": (ctypes.c_int, [H, ctypes.c_int32, _dp]),
+        "cato_gpu_halo_import": (ctypes.c_int, [H, ctypes.c_int32, _dp]),
         "cato_gpu_solve": (ctypes.c_int, [H] + [_dp] * 8 + [i64]),
         "cato_gpu_interpolate_edges": (ctypes.c_int, [H, _dp, i64, _dp, _dp]),
         "cato_gpu_status": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int32)]),

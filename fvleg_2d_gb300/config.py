@@ -38,7 +38,7 @@ RK_IDS = {
 }
 # bc_factory.f90:46-59 names
 BC_IDS = {"zero_gradient": 0, "symmetry": 1, "mirror": 1, "reflection": 1, "periodic": 2,
-          "outlet": 3, "outflow": 3, "pressure_input": 4}
+          "outlet": 3, "outflow": 3, "pressure_input": 4, "exchange": 5}
 PRECISION_IDS = {"fp64": 0, "mixed": 1, "mixed_df": 2}
 # side order of cato_config.bc: the reference's application order (flux_solver.f90:165-183)
 SIDES = ("+x", "+y", "-x", "-y")

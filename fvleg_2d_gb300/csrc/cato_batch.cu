@@ -352,6 +352,9 @@ int cato_batch_add(cato_batch* b, const cato_config* cfg, const double* rho, con
   if (cfg->precision != b->prec || cfg->rk != b->rk) return CATO_ERR_CONFIG;
   // the pressure-input boundary runs per-stage kernels of its own: single handles only
   if (cfg->bc[CATO_PLUS_X] == CATO_BC_PRESSURE_INPUT) return CATO_ERR_CONFIG;
+  // slabs of a split grid step through single handles (their ghost rows are exchanged)
+  if (cfg->bc[CATO_PLUS_Y] == CATO_BC_EXCHANGE || cfg->bc[CATO_MINUS_Y] == CATO_BC_EXCHANGE)
+    return CATO_ERR_CONFIG;
   if (ld < cfg->ni + 2 * cfg->n_ghost) return CATO_ERR_ARG;
   int s = -1;
   for (int i = 0; i < b->capacity; ++i)

@@ -45,6 +45,11 @@ struct cato_handle {
   cato_config cfg{};
   int ni = 0, nj = 0, ng = 2, pitch = 0;
   size_t field_elems = 0;
+  // a slab with CATO_BC_EXCHANGE sides: U, S and the uploaded primitives hold ng ghost rows
+  // below row 0 and above row nj - 1 (the buffers start row_off elements before U[v] etc.)
+  bool exchange = false;
+  size_t row_off = 0;
+  int next_stage = -1;  // stage-by-stage step in progress: the next stage; -1 = none
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // device buffers
@@ -294,7 +299,8 @@ static int enqueue_source(cato_handle* h) {
 }
 
 // Enqueue one full time step (step control + every stage) on the handle's stream.
-static int enqueue_step(cato_handle* h) {
+// The step-control kernel and the step's energy source field.
+static int enqueue_step_begin(cato_handle* h) {
   step_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctl);
   CK(cudaGetLastError());
   {
@@ -302,34 +308,62 @@ static int enqueue_step(cato_handle* h) {
     if (rcs) return rcs;
   }
   if (h->event_hook) CK(cudaEventRecord(h->event_hook[1], h->stream));
+  return CATO_OK;
+}
+
+// The stencil operand of stage k: the uploaded primitives or U^n for the first stage, else the
+// previous stage's output.
+static double* const* stage_input(cato_handle* h, int k) {
+  if (k == 0) return h->raw_pending ? h->prim_raw : h->U;
+  return h->S[(k - 1) & 1];
+}
+
+// RK stage k of the step.
+static int enqueue_stage(cato_handle* h, int k) {
+  const int ns = (int)h->stages.size();
+  const Stage& st = h->stages[k];
+  StageArgs A = base_args(h);
+  A.kind = st.kind;
+  A.a = st.a;
+  A.b = st.b;
+  A.coef = st.coef;
+  A.last = (k == ns - 1);
+  const bool raw = (k == 0) && h->raw_pending;
+  double** Un = h->U;
+  double** prev = (k == 0) ? Un : h->S[(k - 1) & 1];
+  double** out = A.last ? Un : h->S[k & 1];
+  for (int v = 0; v < 4; ++v) {
+    A.Uk[v] = prev[v];
+    A.Ua[v] = Un[v];
+    A.Uo[v] = out[v];
+    A.Pin[v] = raw ? h->prim_raw[v] : nullptr;
+  }
+  A.src_q = h->src_on ? h->src_field : nullptr;
+  const int rcb = enqueue_pbc(h, A, k == 0 && h->cfg.rk >= CATO_RK_1_3);
+  if (rcb) return rcb;
+  CK(launch(h, A));
+  if (h->event_hook) CK(cudaEventRecord(h->event_hook[k + 2], h->stream));
+  return CATO_OK;
+}
+
+static int enqueue_step(cato_handle* h) {
+  int rc = enqueue_step_begin(h);
+  if (rc) return rc;
   const int ns = (int)h->stages.size();
   for (int k = 0; k < ns; ++k) {
-    const Stage& st = h->stages[k];
-    StageArgs A = base_args(h);
-    A.kind = st.kind;
-    A.a = st.a;
-    A.b = st.b;
-    A.coef = st.coef;
-    A.last = (k == ns - 1);
-    const bool raw = (k == 0) && h->raw_pending;
-    double** Un = h->U;
-    // stencil operand: U^n for the first stage, else the previous stage's output
-    double** prev = (k == 0) ? Un : h->S[(k - 1) & 1];
-    double** out = A.last ? Un : h->S[k & 1];
-    for (int v = 0; v < 4; ++v) {
-      A.Uk[v] = prev[v];
-      A.Ua[v] = Un[v];
-      A.Uo[v] = out[v];
-      A.Pin[v] = raw ? h->prim_raw[v] : nullptr;
-    }
-    A.src_q = h->src_on ? h->src_field : nullptr;
-    const int rcb = enqueue_pbc(h, A, k == 0 && h->cfg.rk >= CATO_RK_1_3);
-    if (rcb) return rcb;
-    CK(launch(h, A));
-    if (h->event_hook) CK(cudaEventRecord(h->event_hook[k + 2], h->stream));
+    rc = enqueue_stage(h, k);
+    if (rc) return rc;
   }
   h->raw_pending = false;
   return CATO_OK;
+}
+
+// Entry points that step a handle on their own cannot refresh a slab's ghost rows between
+// stages.
+static int refuse_exchange(cato_handle* h, const char* what) {
+  return fail(h, CATO_ERR_CONFIG,
+              std::string(what) +
+                  ": a slab with exchange sides steps through cato_gpu_step_begin/stage/end");
 }
 
 static int pull_ctl(cato_handle* h) {
@@ -526,14 +560,21 @@ int cato_config_check(const cato_config* c) {
   const int need = (c->limiter == CATO_LIM_MLP5) ? 3 : 2;  // mod_input.f90:320-338
   if (c->n_ghost != need) return CATO_ERR_CONFIG;
   if (c->ni < c->n_ghost || c->nj < c->n_ghost) return CATO_ERR_CONFIG;
-  bool outlet = false;
+  bool outlet = false, exchange = false, pinput = false;
   for (int s = 0; s < 4; ++s) {
-    if (c->bc[s] < CATO_BC_ZERO_GRADIENT || c->bc[s] > CATO_BC_PRESSURE_INPUT)
-      return CATO_ERR_CONFIG;
+    if (c->bc[s] < CATO_BC_ZERO_GRADIENT || c->bc[s] > CATO_BC_EXCHANGE) return CATO_ERR_CONFIG;
     outlet |= c->bc[s] == CATO_BC_OUTLET;
     // apply_pressure_input_primitive_var_bc only implements +x (pressure_input_bc.f90:404-409)
     if (c->bc[s] == CATO_BC_PRESSURE_INPUT && s != CATO_PLUS_X) return CATO_ERR_CONFIG;
+    pinput |= c->bc[s] == CATO_BC_PRESSURE_INPUT;
+    // slabs are cut along j only
+    if (c->bc[s] == CATO_BC_EXCHANGE && s != CATO_PLUS_Y && s != CATO_MINUS_Y)
+      return CATO_ERR_CONFIG;
+    exchange |= c->bc[s] == CATO_BC_EXCHANGE;
   }
+  // the pressure-input state uses the maximum pressure of the whole boundary column
+  // (pressure_input_bc.f90:300-312), which a slab does not hold
+  if (exchange && pinput) return CATO_ERR_CONFIG;
   // outlet_bc_constructor stops on an ambient pressure <= 0 (outlet_bc.f90:54-59)
   if (outlet && !(c->bc_pressure > 0.0)) return CATO_ERR_CONFIG;
   // periodic must be paired on an axis: an unpaired periodic side leaves ghost corners unset
@@ -563,6 +604,8 @@ int cato_gpu_create(const cato_config* cfg, cato_handle** out) {
   h->ng = cfg->n_ghost;
   h->pitch = (cfg->ni + 31) / 32 * 32;
   h->field_elems = (size_t)h->pitch * h->nj;
+  h->exchange = cfg->bc[CATO_PLUS_Y] == CATO_BC_EXCHANGE || cfg->bc[CATO_MINUS_Y] == CATO_BC_EXCHANGE;
+  h->row_off = h->exchange ? (size_t)h->ng * h->pitch : 0;
   h->stages = build_stages(cfg->rk);
   fill_consts(h);
   default_plan(h);
@@ -573,19 +616,25 @@ int cato_gpu_create(const cato_config* cfg, cato_handle** out) {
   cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete h; return CATO_ERR_CUDA; }
   h->own_stream = true;
-  const size_t fb = h->field_elems * sizeof(double);
-  auto dalloc = [&](void** p, size_t bytes) -> bool {
-    cudaError_t ee = cudaMalloc(p, bytes);
+  // the state buffers, with the ghost rows of the exchange sides around them
+  const size_t fb = (h->field_elems + 2 * h->row_off) * sizeof(double);
+  auto dalloc = [&](double** p, size_t bytes) -> bool {
+    void* q = nullptr;
+    cudaError_t ee = cudaMalloc(&q, bytes);
     if (ee != cudaSuccess) { (void)cudaGetLastError(); return false; }
+    *p = static_cast<double*>(q) + h->row_off;
     return true;
   };
   for (int v = 0; v < 4; ++v) {
-    if (!dalloc((void**)&h->U[v], fb)) return cleanup(CATO_ERR_OOM);
-    if (!dalloc((void**)&h->S[0][v], fb)) return cleanup(CATO_ERR_OOM);
-    if (!dalloc((void**)&h->S[1][v], fb)) return cleanup(CATO_ERR_OOM);
+    if (!dalloc(&h->U[v], fb)) return cleanup(CATO_ERR_OOM);
+    if (!dalloc(&h->S[0][v], fb)) return cleanup(CATO_ERR_OOM);
+    if (!dalloc(&h->S[1][v], fb)) return cleanup(CATO_ERR_OOM);
     h->prim_raw[v] = h->S[1][v];  // S1 is first written by stage 2, after stage 1 read these
   }
-  if (!dalloc((void**)&h->ctl, sizeof(StepCtl))) return cleanup(CATO_ERR_OOM);
+  if (cudaMalloc((void**)&h->ctl, sizeof(StepCtl)) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return cleanup(CATO_ERR_OOM);
+  }
   if (cudaMallocHost((void**)&h->ctl_host, sizeof(StepCtl)) != cudaSuccess) return cleanup(CATO_ERR_OOM);
   std::memset(h->ctl_host, 0, sizeof(StepCtl));
   h->ctl_host->dt_min = ~0ULL;
@@ -610,9 +659,10 @@ int cato_gpu_create(const cato_config* cfg, cato_handle** out) {
 int cato_gpu_destroy(cato_handle* h) {
   if (!h) return CATO_ERR_ARG;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  auto base = [&](double* p) { return p ? p - h->row_off : nullptr; };
   for (int v = 0; v < 4; ++v) {
-    cudaFree(h->U[v]);
-    for (int s = 0; s < 2; ++s) cudaFree(h->S[s][v]);
+    cudaFree(base(h->U[v]));
+    for (int s = 0; s < 2; ++s) cudaFree(base(h->S[s][v]));
     cudaFree(h->bak[v]);
     cudaFree(h->bak_raw[v]);
   }
@@ -649,6 +699,19 @@ int cato_gpu_upload_primitive(cato_handle* h, const double* rho, const double* u
     int rc = h2d_interior(h, h->prim_raw[k], src[k], ld);
     if (rc) return rc;
   }
+  // a slab's ghost rows beyond its exchange sides: the neighbouring slabs' rows of the same state
+  for (int side : {CATO_MINUS_Y, CATO_PLUS_Y}) {
+    if (h->cfg.bc[side] != CATO_BC_EXCHANGE) continue;
+    const int j0 = side == CATO_MINUS_Y ? -h->ng : h->nj;  // first ghost row, 0-based
+    for (int k = 0; k < 4; ++k) {
+      const double* first = src[k] + (size_t)(j0 + h->ng) * ld + h->ng;
+      CK(cudaMemcpy2DAsync(h->prim_raw[k] + (ptrdiff_t)j0 * h->pitch,
+                           (size_t)h->pitch * sizeof(double), first, (size_t)ld * sizeof(double),
+                           (size_t)h->ni * sizeof(double), (size_t)h->ng, cudaMemcpyHostToDevice,
+                           h->stream));
+    }
+  }
+  h->next_stage = -1;
   StepCtl c{};
   c.dt_min = ~0ULL;
   c.t_end = INFINITY;
@@ -735,6 +798,9 @@ int cato_gpu_set_step_options(cato_handle* h, int32_t keep_step_start, int32_t a
   if (!h) return CATO_ERR_ARG;
   if (allow_subcycle && !(subcycle_tolerance > 0.0))
     return fail(h, CATO_ERR_ARG, "subcycle tolerance must be positive");
+  // a subcycle decision needs the norms of the whole grid
+  if (h->exchange && (keep_step_start || allow_subcycle))
+    return fail(h, CATO_ERR_CONFIG, "step options on a slab");
   // the pressure-input boundary's clock advances with every residual evaluation in the
   // reference, so a retried step would see other boundary times: not combined here
   if (allow_subcycle && h->cfg.bc[CATO_PLUS_X] == CATO_BC_PRESSURE_INPUT)
@@ -748,6 +814,8 @@ int cato_gpu_set_step_options(cato_handle* h, int32_t keep_step_start, int32_t a
 int cato_gpu_integrate(cato_handle* h, double dt, double* dt_used, int32_t* error_code) {
   if (!h) return CATO_ERR_ARG;
   if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  if (h->exchange) return refuse_exchange(h, "cato_gpu_integrate");
+  if (h->next_stage >= 0) return fail(h, CATO_ERR_STATE, "a stage-by-stage step is open");
   // one step regardless of t_end; fixed dt when dt > 0
   int rc = pbc_prepare(h);
   if (rc) return rc;
@@ -777,10 +845,106 @@ int cato_gpu_integrate(cato_handle* h, double dt, double* dt_used, int32_t* erro
   return CATO_OK;
 }
 
+// Stage-by-stage step (slab exchange): the kernels of enqueue_step, with the host between stages.
+int cato_gpu_step_begin(cato_handle* h, double dt) {
+  if (!h) return CATO_ERR_ARG;
+  if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  if (h->next_stage >= 0) return fail(h, CATO_ERR_STATE, "a stage-by-stage step is open");
+  if (h->keep_start) return fail(h, CATO_ERR_CONFIG, "step options with stage-by-stage steps");
+  int rc = pbc_prepare(h);
+  if (rc) return rc;
+  rc = pull_ctl(h);
+  if (rc) return rc;
+  StepCtl c = *h->ctl_host;
+  c.t_end = INFINITY;
+  c.max_iter = c.iter + 1;
+  c.fixed_dt = dt > 0.0 ? dt : 0.0;
+  *h->ctl_host = c;
+  CK(cudaMemcpyAsync(h->ctl, h->ctl_host, sizeof(StepCtl), cudaMemcpyHostToDevice, h->stream));
+  // a state with an error status takes no step (the kernels see active = 0)
+  rc = enqueue_step_begin(h);
+  if (rc) return rc;
+  h->next_stage = 0;
+  return CATO_OK;
+}
+
+int cato_gpu_step_stage(cato_handle* h, int32_t* stages_left) {
+  if (!h) return CATO_ERR_ARG;
+  const int ns = (int)h->stages.size();
+  if (h->next_stage < 0 || h->next_stage >= ns)
+    return fail(h, CATO_ERR_STATE, "no stage left in this step (cato_gpu_step_begin first)");
+  const int rc = enqueue_stage(h, h->next_stage);
+  if (rc) return rc;
+  h->next_stage += 1;
+  if (stages_left) *stages_left = ns - h->next_stage;
+  return CATO_OK;
+}
+
+int cato_gpu_step_end(cato_handle* h, double* dt_used, int32_t* error_code) {
+  if (!h) return CATO_ERR_ARG;
+  if (h->next_stage != (int)h->stages.size())
+    return fail(h, CATO_ERR_STATE, "the step's stages have not all run");
+  h->next_stage = -1;
+  h->raw_pending = false;
+  const long long it0 = h->ctl_host->iter;
+  const int rc = pull_ctl(h);
+  if (rc) return rc;
+  if (h->ctl_host->iter > it0) h->stepped = true;
+  if (dt_used) *dt_used = h->ctl_host->dt;
+  if (error_code) *error_code = status_code(h->ctl_host->status);
+  return CATO_OK;
+}
+
+// The next stage's input rows next to (export) or beyond (import) an exchange side.
+static int halo_rows(cato_handle* h, int32_t side, double** base) {
+  if (side != CATO_PLUS_Y && side != CATO_MINUS_Y) return fail(h, CATO_ERR_ARG, "side must be +-y");
+  if (h->cfg.bc[side] != CATO_BC_EXCHANGE) return fail(h, CATO_ERR_ARG, "not an exchange side");
+  if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  const int ns = (int)h->stages.size();
+  const int k = h->next_stage < 0 ? 0 : h->next_stage;
+  if (k >= ns) return fail(h, CATO_ERR_STATE, "every stage of this step has run");
+  double* const* in = stage_input(h, k);
+  for (int v = 0; v < 4; ++v) base[v] = in[v];
+  return CATO_OK;
+}
+
+int cato_gpu_halo_export(cato_handle* h, int32_t side, double* rows) {
+  if (!h || !rows) return CATO_ERR_ARG;
+  double* in[4];
+  int rc = halo_rows(h, side, in);
+  if (rc) return rc;
+  const int j0 = side == CATO_MINUS_Y ? 0 : h->nj - h->ng;  // first interior row sent
+  const size_t plane = (size_t)h->ng * h->ni;
+  for (int v = 0; v < 4; ++v)
+    CK(cudaMemcpy2DAsync(rows + v * plane, (size_t)h->ni * sizeof(double),
+                         in[v] + (ptrdiff_t)j0 * h->pitch, (size_t)h->pitch * sizeof(double),
+                         (size_t)h->ni * sizeof(double), (size_t)h->ng, cudaMemcpyDeviceToHost,
+                         h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return CATO_OK;
+}
+
+int cato_gpu_halo_import(cato_handle* h, int32_t side, const double* rows) {
+  if (!h || !rows) return CATO_ERR_ARG;
+  double* in[4];
+  int rc = halo_rows(h, side, in);
+  if (rc) return rc;
+  const int j0 = side == CATO_MINUS_Y ? -h->ng : h->nj;  // first ghost row written
+  const size_t plane = (size_t)h->ng * h->ni;
+  for (int v = 0; v < 4; ++v)
+    CK(cudaMemcpy2DAsync(in[v] + (ptrdiff_t)j0 * h->pitch, (size_t)h->pitch * sizeof(double),
+                         rows + v * plane, (size_t)h->ni * sizeof(double),
+                         (size_t)h->ni * sizeof(double), (size_t)h->ng, cudaMemcpyHostToDevice,
+                         h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return CATO_OK;
+}
+
 int cato_gpu_run(cato_handle* h, int64_t max_steps, double t_end, int64_t* steps_done,
                  double* time, int32_t* error_code) {
   if (!h) return CATO_ERR_ARG;
   if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  if (h->exchange) return refuse_exchange(h, "cato_gpu_run");
   int rc = pbc_prepare(h);
   if (rc) return rc;
   rc = pull_ctl(h);
@@ -885,6 +1049,7 @@ int cato_gpu_solve(cato_handle* h, double* rho, double* u, double* v, double* p,
   if (!rho || !u || !v || !p || !d_rho_dt || !d_rho_u_dt || !d_rho_v_dt || !d_rho_E_dt)
     return fail(h, CATO_ERR_ARG, "null field pointer");
   if (ld < h->ni + 2 * h->ng) return fail(h, CATO_ERR_ARG, "leading dimension too small");
+  if (h->exchange) return fail(h, CATO_ERR_CONFIG, "solve on a slab");
   int rc;
   if ((rc = pbc_prepare(h))) return rc;
   if ((rc = ensure_scratch(h))) return rc;
@@ -940,6 +1105,9 @@ int cato_gpu_interpolate_edges(cato_handle* h, const double* q, int64_t ld, doub
   if (!h) return CATO_ERR_ARG;
   if (!q || !i_edges || !j_edges) return fail(h, CATO_ERR_ARG, "null pointer");
   if (ld < h->ni + 2 * h->ng) return fail(h, CATO_ERR_ARG, "leading dimension too small");
+  // the ghosts of a single solve come from the boundary conditions, which a slab's exchange
+  // sides do not have
+  if (h->exchange) return fail(h, CATO_ERR_CONFIG, "interpolate_edges on a slab");
   int rc;
   if ((rc = ensure_halo(h))) return rc;
   const long long hld = h->ni + 2 * h->ng;
@@ -1002,6 +1170,7 @@ int cato_gpu_run_timed(cato_handle* h, int64_t n_steps, float* total_ms, float* 
                        int32_t capacity) {
   if (!h || !total_ms || n_steps < 0) return CATO_ERR_ARG;
   if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  if (h->exchange) return refuse_exchange(h, "cato_gpu_run_timed");
   const int nk = 1 + (int)h->stages.size();
   if (kernel_ms && capacity < nk) return fail(h, CATO_ERR_ARG, "capacity too small");
   int rc = pbc_prepare(h);
@@ -1071,6 +1240,7 @@ int cato_gpu_tune(cato_handle* h, int32_t steps, int32_t* steps_taken, float* be
   if (!h || steps < 1) return CATO_ERR_ARG;
   if (steps_taken) *steps_taken = 0;
   if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  if (h->exchange) return refuse_exchange(h, "cato_gpu_tune");
   // candidates: the default plan, 256-wide strips, half and a quarter of the rows per CTA; each
   // with both FP64 register budgets
   const Plan p0 = h->plan;
@@ -1180,6 +1350,7 @@ int cato_gpu_launches_per_step(const cato_handle* h, int32_t* n) {
 int cato_gpu_profile_step(cato_handle* h, float* kernel_ms, int32_t capacity, int32_t* n_kernels) {
   if (!h || !kernel_ms) return CATO_ERR_ARG;
   if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
+  if (h->exchange) return refuse_exchange(h, "cato_gpu_profile_step");
   const int nk = 1 + (int)h->stages.size();
   if (capacity < nk) return fail(h, CATO_ERR_ARG, "capacity too small");
   int rc = pbc_prepare(h);
@@ -1213,6 +1384,9 @@ int cato_gpu_set_energy_source(cato_handle* h, const cato_energy_source* src, in
                                const double* time, const double* value,
                                const double* critical_density) {
   if (!h) return CATO_ERR_ARG;
+  // the source is placed by cell centroids measured from the grid's origin, which a slab's
+  // uniform geometry does not know
+  if (src && h->exchange) return fail(h, CATO_ERR_CONFIG, "energy source on a slab");
   CK(cudaStreamSynchronize(h->stream));
   if (!src) {
     h->src_on = false;

@@ -61,6 +61,9 @@ extern "C" int cato_gpu_solve_noalloc(const cato_config* cfg, double* rho, doubl
   if (cfg->precision != CATO_FP64) return CATO_ERR_CONFIG;
   // the pressure-input boundary needs per-row device state: handle entry points only
   if (cfg->bc[CATO_PLUS_X] == CATO_BC_PRESSURE_INPUT) return CATO_ERR_CONFIG;
+  // slab exchange sides have no boundary condition to fill their ghosts from
+  if (cfg->bc[CATO_PLUS_Y] == CATO_BC_EXCHANGE || cfg->bc[CATO_MINUS_Y] == CATO_BC_EXCHANGE)
+    return CATO_ERR_CONFIG;
   const int ni = cfg->ni, nj = cfg->nj, ng = cfg->n_ghost;
   if (ld < ni + 2 * ng) return CATO_ERR_ARG;
   const int pitch = (ni + 31) / 32 * 32;

@@ -60,7 +60,7 @@ enum { FLUX_AUSMPW = 0, FLUX_SLAU = 1, FLUX_SLAU2 = 2, FLUX_SD_SLAU = 3, FLUX_SD
        FLUX_ROE = 5, FLUX_AUSM_UP = 6, FLUX_HLLC = 7, FLUX_M_AUSMPW = 8 };
 enum { LIM_MINMOD = 0, LIM_SUPERBEE = 1, LIM_VANLEER = 2, LIM_MLP3 = 3, LIM_MLP5 = 4 };
 enum { BC_ZERO_GRADIENT = 0, BC_SYMMETRY = 1, BC_PERIODIC = 2, BC_OUTLET = 3,
-       BC_PRESSURE_INPUT = 4 };
+       BC_PRESSURE_INPUT = 4, BC_EXCHANGE = 5 };
 enum { SIDE_PX = 0, SIDE_PY = 1, SIDE_MX = 2, SIDE_MY = 3 };
 
 // Status word bits written by the kernels (mapped to the reference's error codes on the host).

@@ -64,17 +64,21 @@ struct StageArgs {
 };
 
 // Source interior index of (possibly ghost) index g in [-ng, n+ng) along an axis with
-// boundary types lo/hi; flip = the normal velocity component is negated (symmetry).
+// boundary types lo/hi; flip = the normal velocity component is negated (symmetry).  An
+// exchange side (the rows axis of a slab only) keeps g: its ghost rows are stored below row 0
+// and above row n - 1 of the slab's buffers, copied from the neighbouring slab.
 __device__ __forceinline__ int map_index(int g, int n, int bc_lo, int bc_hi, bool& flip) {
   flip = false;
   if (g < 0) {
     if (bc_lo == BC_PERIODIC) return max(n + g, 0);
     if (bc_lo == BC_SYMMETRY) { flip = true; return min(-g - 1, n - 1); }
+    if (bc_lo == BC_EXCHANGE) return g;
     return 0;
   }
   if (g >= n) {
     if (bc_hi == BC_PERIODIC) return min(g - n, n - 1);
     if (bc_hi == BC_SYMMETRY) { flip = true; return max(2 * n - 1 - g, 0); }
+    if (bc_hi == BC_EXCHANGE) return g;
     return n - 1;
   }
   return g;

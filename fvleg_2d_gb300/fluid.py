@@ -17,7 +17,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from .config import STATUS_NAMES, SchemeConfig
+from .config import SIDES, STATUS_NAMES, SchemeConfig
 
 
 class CatoError(RuntimeError):
@@ -33,6 +33,12 @@ def _check(rc: int, h=None, what: str = ""):
             m = _lib.load().cato_gpu_last_error(h)
             msg = m.decode() if m else ""
         raise CatoError(rc, f"{what} {msg}".strip())
+
+
+def _c_ptr(a: np.ndarray):
+    """Pointer to a C-contiguous float64 array (the slab edge rows)."""
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
 def _field(cfg: SchemeConfig) -> np.ndarray:
@@ -177,6 +183,48 @@ class Fluid(_Handle):
         _check(self.L.cato_gpu_integrate(self.h, float(dt) if dt else 0.0, ctypes.byref(used),
                                          ctypes.byref(ec)), self.h, "integrate")
         return used.value, ec.value
+
+    # stage-by-stage stepping of a slab (``exchange`` sides): see fvleg_2d_gb300.slabs
+    def step_begin(self, dt: float | None = None) -> None:
+        """Open a step with this dt (the slabs' minimum CFL dt); None: the own CFL dt."""
+        _check(self.L.cato_gpu_step_begin(self.h, float(dt) if dt else 0.0), self.h, "step_begin")
+
+    def step_stage(self) -> int:
+        """Run the next RK stage of the open step; returns the stages still to run."""
+        left = ctypes.c_int32()
+        _check(self.L.cato_gpu_step_stage(self.h, ctypes.byref(left)), self.h, "step_stage")
+        return left.value
+
+    def step_end(self) -> tuple[float, int]:
+        """Close the step: (dt taken, error code)."""
+        used = ctypes.c_double()
+        ec = ctypes.c_int32()
+        _check(self.L.cato_gpu_step_end(self.h, ctypes.byref(used), ctypes.byref(ec)), self.h,
+               "step_end")
+        return used.value, ec.value
+
+    def stage_count(self) -> int:
+        n = ctypes.c_int32()
+        _check(self.L.cato_gpu_launches_per_step(self.h, ctypes.byref(n)), self.h)
+        return n.value - 1
+
+    def halo_export(self, side: str) -> np.ndarray:
+        """The n_ghost interior rows of the next stage's input next to exchange side "+y"/"-y":
+        shape (4, n_ghost, ni), rows in increasing j."""
+        g = self.cfg.ghost_layers()
+        rows = np.empty((4, g, self.cfg.ni))  # C order: [field][row][column]
+        _check(self.L.cato_gpu_halo_export(self.h, SIDES.index(side), _c_ptr(rows)), self.h,
+               "halo_export")
+        return rows
+
+    def halo_import(self, side: str, rows: np.ndarray) -> None:
+        """Write the ghost rows beyond exchange side "+y"/"-y" of the next stage's input."""
+        g = self.cfg.ghost_layers()
+        rows = np.ascontiguousarray(rows, dtype=np.float64)
+        if rows.shape != (4, g, self.cfg.ni):
+            raise ValueError(f"halo rows {rows.shape} != {(4, g, self.cfg.ni)}")
+        _check(self.L.cato_gpu_halo_import(self.h, SIDES.index(side), _c_ptr(rows)), self.h,
+               "halo_import")
 
     def run(self, t_end: float, max_iterations: int = -1) -> int:
         """The main.f90:138-198 time loop (CFL dt each step, no last-step trim) on the device.

@@ -82,10 +82,16 @@ enum cato_bc {
   CATO_BC_PERIODIC = 2,      /* priority 2, periodic_bc.fypp:78-283 */
   CATO_BC_OUTLET = 3,        /* priority 0, outlet_bc.f90:63-176: characteristic subsonic outflow
                                 to bc_pressure on +x, line copies on the other sides */
-  CATO_BC_PRESSURE_INPUT = 4 /* priority 0, +x only, pressure_input_bc.f90:256-414: the
+  CATO_BC_PRESSURE_INPUT = 4, /* priority 0, +x only, pressure_input_bc.f90:256-414: the
                                 characteristic inlet/outlet state toward a target pressure and
                                 density, constant (bc_pressure, bc_density) or tabulated in time
                                 (cato_gpu_set_bc_table) */
+  CATO_BC_EXCHANGE = 5       /* +-y only: not a boundary but the cut between two slabs of one
+                                grid split by rows (one handle per GPU); the n_ghost rows beyond
+                                it are the neighbouring slab's interior rows, copied in before
+                                every stage (cato_gpu_halo_import), as the reference's coarray
+                                images exchange their edges (field_2d.f90:551-654).  The x
+                                boundaries treat these rows as interior rows. */
 };
 
 /* Sides in the reference's application order within one priority (flux_solver.f90:165-183). */
@@ -312,6 +318,30 @@ int cato_gpu_tune(cato_handle* h, int32_t steps, int32_t* steps_taken, float* be
  * Off by default; with either on, cato_gpu_run takes its steps from the host. */
 int cato_gpu_set_step_options(cato_handle* h, int32_t keep_step_start, int32_t allow_subcycle,
                               double subcycle_tolerance);
+
+/* One time step taken stage by stage, for grids split into slabs by rows (CATO_BC_EXCHANGE
+ * sides), whose ghost rows must be refreshed from the neighbouring slabs before every stage:
+ *   cato_gpu_step_begin(h, dt);               dt > 0: this step's dt, e.g. the minimum of the
+ *                                             slabs' cato_gpu_get_timestep (min_to_all,
+ *                                             mod_collectives.f90:159-163); dt <= 0: own CFL dt
+ *   repeat: halo export / exchange / import;  (the rows of the next stage's input)
+ *           cato_gpu_step_stage(h, &left);    runs the next RK stage; left = stages still to run
+ *   cato_gpu_step_end(h, &dt_used, &error_code);
+ * The sequence of kernels is the one cato_gpu_integrate enqueues; any handle may use it.  Step
+ * options (subcycling, the kept step start) are not combined with it. */
+int cato_gpu_step_begin(cato_handle* h, double dt);
+int cato_gpu_step_stage(cato_handle* h, int32_t* stages_left);
+int cato_gpu_step_end(cato_handle* h, double* dt_used, int32_t* error_code);
+
+/* Edge rows of the next stage's input for the slab exchange.  side: CATO_PLUS_Y or
+ * CATO_MINUS_Y, which must be a CATO_BC_EXCHANGE side.  rows: 4 fields (rho, rho u, rho v, rho E;
+ * or the primitives rho, u, v, p before the first stage after an upload) x n_ghost rows (in
+ * increasing j) x ni columns, contiguous doubles.  export copies out the n_ghost interior rows
+ * next to `side`; import writes the n_ghost ghost rows beyond `side` (the neighbour's export of
+ * its opposite side).  Between cato_gpu_step_begin and the last cato_gpu_step_stage, or before
+ * a step (then the rows of the first stage's input). */
+int cato_gpu_halo_export(cato_handle* h, int32_t side, double* rows);
+int cato_gpu_halo_import(cato_handle* h, int32_t side, const double* rows);
 
 /* Select the CUDA device used by handles created afterwards on this host thread. */
 int cato_gpu_select_device(int32_t device);

@@ -418,9 +418,13 @@ static void apply_pressure_input_px(dims_t d, double gamma, double p_const, doub
   free(edge);
 }
 
+/* jlo..jhi: the rows the x-periodic copy covers: the interior rows (periodic_bc.fypp:176-192),
+ * and the ghost rows beyond a slab's exchange side, which are interior rows of the whole grid */
 static void apply_one_bc(dims_t d, int type, int side, int do_corners, double gamma,
-                         double p_b, double rho_b, const pbc_ctx_t* pc, double* f[4]) {
+                         double p_b, double rho_b, const pbc_ctx_t* pc, double* f[4], int jlo,
+                         int jhi) {
   const int ng = d.ng, ni = d.ni, nj = d.nj;
+  if (type == CATO_BC_EXCHANGE) return; /* filled from the neighbouring slab */
   if (type == CATO_BC_PRESSURE_INPUT) {
     if (side == CATO_PLUS_X) apply_pressure_input_px(d, gamma, p_b, rho_b, pc, f);
     return;
@@ -470,7 +474,7 @@ static void apply_one_bc(dims_t d, int type, int side, int do_corners, double ga
       double* a = f[k];
       if (side == CATO_PLUS_X || side == CATO_MINUS_X) {
         /* ihi+1:ihi_halo <- ilo:ilo+ng-1 ; ilo_halo:ilo-1 <- ihi-ng+1:ihi */
-        for (int j = 1; j <= nj; ++j)
+        for (int j = jlo; j <= jhi; ++j)
           for (int g = 1; g <= ng; ++g) {
             AT(a, ni + g, j) = AT(a, g, j);
             AT(a, 1 - g, j) = AT(a, ni + 1 - g, j);
@@ -495,8 +499,10 @@ static void apply_one_bc(dims_t d, int type, int side, int do_corners, double ga
   }
 }
 
-/* periodic 2, zero-gradient / symmetry 1, outlet and pressure input 0 (the constructors) */
+/* periodic 2, zero-gradient / symmetry 1, outlet and pressure input 0 (the constructors); a
+ * slab's exchange side is no boundary condition (-1: never applied) */
 static int bc_priority(int type) {
+  if (type == CATO_BC_EXCHANGE) return -1;
   return type == CATO_BC_PERIODIC ? 2
          : (type == CATO_BC_OUTLET || type == CATO_BC_PRESSURE_INPUT ? 0 : 1);
 }
@@ -511,11 +517,13 @@ static int apply_bc_at(const cato_config* c, const pbc_ctx_t* pc, double* rho, d
   for (int s = 0; s < 4; ++s) all_periodic &= (c->bc[s] == CATO_BC_PERIODIC);
   int maxp = 0;
   for (int s = 0; s < 4; ++s) maxp = bc_priority(c->bc[s]) > maxp ? bc_priority(c->bc[s]) : maxp;
+  const int jlo = c->bc[CATO_MINUS_Y] == CATO_BC_EXCHANGE ? 1 - d.ng : 1;
+  const int jhi = c->bc[CATO_PLUS_Y] == CATO_BC_EXCHANGE ? d.nj + d.ng : d.nj;
   for (int prio = maxp; prio >= 0; --prio)
     for (int s = 0; s < 4; ++s)
       if (bc_priority(c->bc[s]) == prio)
         apply_one_bc(d, c->bc[s], s, all_periodic, c->gamma, c->bc_pressure, c->bc_density,
-                     pc, f);
+                     pc, f, jlo, jhi);
   return 0;
 }
 
@@ -529,7 +537,8 @@ int oracle_apply_bc_side(const cato_config* c, int side, int type, int do_corner
                          double* u, double* v, double* p) {
   dims_t d = mkdims(c);
   double* f[4] = {rho, u, v, p};
-  apply_one_bc(d, type, side, do_corners, c->gamma, c->bc_pressure, c->bc_density, NULL, f);
+  apply_one_bc(d, type, side, do_corners, c->gamma, c->bc_pressure, c->bc_density, NULL, f, 1,
+               d.nj);
   return 0;
 }
 
@@ -1280,6 +1289,11 @@ struct oracle_fluid {
   /* allow_subcycle / subcycle_tolerance (mod_fluid.f90:98-99, 856-887) */
   int subcycle;
   double subcycle_tol;
+  /* a slab of a row-split grid: fills the ghost rows beyond its exchange sides with the
+   * neighbouring slabs' rows of the same stage before the boundary conditions (time_derivative
+   * calls sync_fields on rho, u, v, p: mod_fluid.f90:452-458, 485; field_2d.f90:551-654) */
+  oracle_exchange_fn xchg;
+  void* xchg_user;
 };
 
 static void source_field(oracle_fluid* f);
@@ -1462,6 +1476,7 @@ static int residual(oracle_fluid* f, const double* pr, const double* pu, const d
   memcpy(f->sp[1], pu, n);
   memcpy(f->sp[2], pv, n);
   memcpy(f->sp[3], pp, n);
+  if (f->xchg) f->xchg(f->xchg_user, f->sp[0], f->sp[1], f->sp[2], f->sp[3]);
   pbc_ctx_t pc = {f->pbc_n, f->pbc_tab, f->pbc_tab ? f->pbc_tab + f->pbc_n : NULL,
                   f->pbc_tab ? f->pbc_tab + 2 * f->pbc_n : NULL, f->bc_time};
   int rc = solve_geo(&f->c, f->cells, &pc, f->sp[0], f->sp[1], f->sp[2], f->sp[3], f->L[0],
@@ -1683,6 +1698,13 @@ static int subcycle_check(const oracle_fluid* f) {
 
 double oracle_dt(const oracle_fluid* f) { return f->dt; }
 
+int oracle_set_exchange(oracle_fluid* f, oracle_exchange_fn fn, void* user) {
+  if (!f) return CATO_ERR_ARG;
+  f->xchg = fn;
+  f->xchg_user = user;
+  return 0;
+}
+
 int oracle_set_subcycle(oracle_fluid* f, int allow, double tolerance) {
   f->subcycle = allow ? 1 : 0;
   f->subcycle_tol = tolerance;
@@ -1855,14 +1877,19 @@ int oracle_config_check(const cato_config* c) {
   int need = (c->limiter == CATO_LIM_MLP5) ? 3 : 2; /* mod_input.f90:320-338 */
   if (c->n_ghost != need) return CATO_ERR_CONFIG;
   if (c->ni < c->n_ghost || c->nj < c->n_ghost) return CATO_ERR_CONFIG;
-  int outlet = 0;
+  int outlet = 0, exchange = 0, pinput = 0;
   for (int s = 0; s < 4; ++s) {
-    if (c->bc[s] < CATO_BC_ZERO_GRADIENT || c->bc[s] > CATO_BC_PRESSURE_INPUT)
-      return CATO_ERR_CONFIG;
+    if (c->bc[s] < CATO_BC_ZERO_GRADIENT || c->bc[s] > CATO_BC_EXCHANGE) return CATO_ERR_CONFIG;
     /* the pressure input only implements +x (pressure_input_bc.f90:404-409) */
     if (c->bc[s] == CATO_BC_PRESSURE_INPUT && s != CATO_PLUS_X) return CATO_ERR_CONFIG;
     outlet |= c->bc[s] == CATO_BC_OUTLET;
+    pinput |= c->bc[s] == CATO_BC_PRESSURE_INPUT;
+    /* slab cuts are rows: +-y only */
+    if (c->bc[s] == CATO_BC_EXCHANGE && s != CATO_PLUS_Y && s != CATO_MINUS_Y)
+      return CATO_ERR_CONFIG;
+    exchange |= c->bc[s] == CATO_BC_EXCHANGE;
   }
+  if (exchange && pinput) return CATO_ERR_CONFIG;
   if (outlet && !(c->bc_pressure > 0.0)) return CATO_ERR_CONFIG; /* outlet_bc.f90:54-59 */
   /* periodic must be paired on an axis (an unpaired side leaves ghost cells unset) */
   if ((c->bc[CATO_PLUS_X] == CATO_BC_PERIODIC) != (c->bc[CATO_MINUS_X] == CATO_BC_PERIODIC))

@@ -48,6 +48,11 @@ oracle_fluid* oracle_create(const cato_config* cfg);
 void oracle_destroy(oracle_fluid* f);
 /* allow_subcycle and subcycle_tolerance of the deck's [time] section */
 int oracle_set_subcycle(oracle_fluid* f, int allow, double tolerance);
+/* Slab of a row-split grid (CATO_BC_EXCHANGE sides): fn(user, rho, u, v, p) receives the
+ * halo-padded primitives of every residual evaluation before its boundary conditions and fills
+ * the ghost rows beyond the exchange sides (interior columns) with the neighbours' rows. */
+typedef void (*oracle_exchange_fn)(void* user, double* rho, double* u, double* v, double* p);
+int oracle_set_exchange(oracle_fluid* f, oracle_exchange_fn fn, void* user);
 /* dt of the last step (after any subcycling) */
 double oracle_dt(const oracle_fluid* f);
 int oracle_set_primitive(oracle_fluid* f, const double* rho, const double* u, const double* v,

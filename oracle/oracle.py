@@ -22,6 +22,8 @@ _LIB_PATH = os.path.join(_HERE, "_build", "libcato_oracle.so")
 _lib = None
 
 _dp = ctypes.POINTER(ctypes.c_double)
+# oracle_exchange_fn(user, rho, u, v, p)
+_XCHG = ctypes.CFUNCTYPE(None, ctypes.c_void_p, _dp, _dp, _dp, _dp)
 
 
 def build() -> str:
@@ -53,6 +55,7 @@ def lib():
         L.oracle_set_rectilinear.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.oracle_set_time.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int64]
         L.oracle_set_subcycle.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
+        L.oracle_set_exchange.argtypes = [ctypes.c_void_p, _XCHG, ctypes.c_void_p]
         L.oracle_dt.restype = ctypes.c_double
         L.oracle_dt.argtypes = [ctypes.c_void_p]
         L.oracle_set_pow_mode.argtypes = [ctypes.c_int]
@@ -220,6 +223,24 @@ class OracleFluid:
     def dt(self) -> float:
         """dt of the last step (after any subcycling)."""
         return lib().oracle_dt(self._h)
+
+    def set_exchange(self, fn) -> None:
+        """Slab of a row-split grid: ``fn(q)`` gets the four halo-padded primitive fields
+        (rho, u, v, p; views, Fortran order) of every residual evaluation before the boundary
+        conditions and writes the ghost rows beyond the exchange sides.  None removes it."""
+        if fn is None:
+            self._xchg = None
+            lib().oracle_set_exchange(self._h, _XCHG(), None)
+            return
+        shape = self.cfg.halo_shape
+        n = shape[0] * shape[1]
+
+        def cb(_user, r, u, v, p):
+            fn([np.ctypeslib.as_array(a, shape=(n,)).reshape(shape, order="F")
+                for a in (r, u, v, p)])
+
+        self._xchg = _XCHG(cb)  # kept alive while the oracle may call it
+        lib().oracle_set_exchange(self._h, self._xchg, None)
 
     def set_energy_source(self, source=None) -> None:
         """An EnergySource (fvleg_2d_gb300.config) or None."""
