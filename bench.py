@@ -446,6 +446,49 @@ def bench_rectilinear(args, uniform_values):
     return out
 
 
+def bench_slabs(args, one_grid):
+    """The developed quadrant grid split into 2 row slabs on this one GPU (fvleg_2d_gb300.slabs):
+    each stage waits for the edge rows of both slabs to pass through the host, as a
+    multi-GPU run would exchange them between processes.  Timed on the host clock (every stage
+    synchronises), against the one-grid value of the same precision and plan."""
+    import time
+
+    from fvleg_2d_gb300 import slabs
+    from fvleg_2d_gb300.fluid import Fluid
+
+    cfg0, prims = quadrant_state(args)
+    world = 2
+    out = {"workload": f"developed quadrant state, {args.n}x{args.n}, 2 row slabs on one GPU "
+                       "(host-staged edge-row exchange before every stage)"}
+    for precision in ("fp64", "mixed"):
+        cfg = dataclasses.replace(cfg0, precision=precision)
+        parts = [slabs.slab_config(cfg, r, world) for r in range(world)]
+        fluids = [Fluid(c).initialize(*slabs.slab_fields(cfg, prims, j0, j1))
+                  for c, j0, j1 in parts]
+        plan = one_grid[precision]["plan"]
+        for f in fluids:
+            f.set_plan(plan["threads"], plan["rows_per_cta"])
+            f.set_kernel_variant(plan["kernel_variant"])
+        run = slabs.SlabRun(fluids, slabs.SlabComm(world, False))
+        for _ in range(args.warmup):
+            run.step()
+        with ClockSampler(env_int("LOCAL_RANK", 0)) as clk:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                run.step()
+            secs = time.perf_counter() - t0
+        value = cfg.ni * cfg.nj * args.steps / secs
+        g = cfg.ghost_layers()
+        out[precision] = {"value": value, "unit": "cell-updates/s",
+                          "ms_per_step": secs * 1e3 / args.steps,
+                          "vs_one_grid": value / one_grid[precision]["value"],
+                          "exchange_bytes_per_stage": 2 * 2 * 4 * g * cfg.ni * 8,
+                          "clocks": clk.summary()}
+        for f in fluids:
+            f.close()
+    return out
+
+
 def error_stats(x):
     """Median, p90, p99, max and the count above 1e-6 of a list of per-instance errors."""
     import numpy as np
@@ -673,6 +716,7 @@ def main() -> int:
     ap.add_argument("--batch-precisions", default="fp64,mixed_df,mixed")
     ap.add_argument("--no-rectilinear", action="store_true")
     ap.add_argument("--no-kh", action="store_true")
+    ap.add_argument("--no-slabs", action="store_true")
     ap.add_argument("--kh-n", type=int, default=8192)
     ap.add_argument("--kh-steps", type=int, default=200)
     ap.add_argument("--kh-fp64-steps", type=int, default=20)
@@ -715,6 +759,7 @@ def main() -> int:
     rect = None if args.no_rectilinear else bench_rectilinear(
         args, {"fp64": fp64["value"], "mixed": mixed["value"], "mixed_df": mixed_df["value"]})
     kh = None if args.no_kh else bench_kh(args, peak)
+    slab = None if args.no_slabs else bench_slabs(args, {"fp64": fp64, "mixed": mixed})
     if args.no_batched:
         batched = None
     elif world > 1:
@@ -764,6 +809,7 @@ def main() -> int:
             "clocks": mixed_df["clocks"], "plan": mixed_df["plan"], "e2e": e2e_df,
         },
         "rectilinear": rect,
+        "slabs": slab,
         "kelvin_helmholtz": kh,
         "batched": batched,
         "serving": serving,
