@@ -316,9 +316,11 @@ def _sm_count() -> int:
         return 152
 
 
-def bench_e2e(args, cfg, prims):
+def bench_e2e(args, cfg, prims, plan):
     """Through the C-ABI with pinned host buffers: upload, per-step integrate (dt and error code
-    back to the host each step), download of the final conserved state."""
+    back to the host each step), download of the final conserved state.  The handle runs the
+    plan the device-timed leg of the same precision tuned (a second tuning on two steps per
+    candidate picks a slower plan now and then)."""
     import ctypes
 
     from fvleg_2d_gb300 import _lib
@@ -330,7 +332,8 @@ def bench_e2e(args, cfg, prims):
     f = Fluid(cfg)
     # warm-up on the same handle (allocations, module load)
     f.initialize(*(p.array for p in pinned[:4]))
-    f.tune(2)  # the same autotuning as the device-timed leg, outside the timed region
+    f.set_plan(plan["threads"], plan["rows_per_cta"])
+    f.set_kernel_variant(plan["kernel_variant"])
     for _ in range(min(args.warmup, 2)):
         f.integrate()
     L, h, ld = f.L, f.h, f.ld
@@ -740,9 +743,11 @@ def main() -> int:
     fp64, cfg, prims = bench_precision(args, "fp64", dist, world, peak)
     mixed, _, _ = bench_precision(args, "mixed", dist, world, peak)
     mixed_df, _, _ = bench_precision(args, "mixed_df", dist, world, peak)
+    plans = {"fp64": fp64["plan"], "mixed": mixed["plan"], "mixed_df": mixed_df["plan"]}
+
     def e2e_of(precision):
         c = dataclasses.replace(cfg, precision=precision)
-        r = bench_e2e(args, c, prims)
+        r = bench_e2e(args, c, prims, plans[precision])
         r["value"] = -allreduce_max(dist, -r["value"]) * world  # slowest replica
         return r
 
