@@ -9,10 +9,11 @@ with its ``units`` and ``description`` attributes, dimensional and in the deck's
 system (``units.f90:94-143``); and for the ``xdmf`` format the XDMF description of
 ``write_xdmf`` (``:386-529``) that points at ``<name>.h5:/<dataset>``.
 
-The datasets are written to ``<name>.h5`` with h5py when it is installed.  Without an HDF5
-library they go to ``<name>.npz`` with the same names, shapes and attributes
-(``<dataset>.units``, ``<dataset>.description``), arrays stored transposed as an HDF5 file written
-from Fortran reads in C order.  Scaling follows the reference: a field is written as
+The datasets are written to ``<name>.h5``: with h5py when it is installed, else with
+:mod:`fvleg_2d_gb300.h5lite` (superblock version 0, contiguous datasets, fixed-length string
+attributes), arrays stored transposed as an HDF5 file written from Fortran reads in C order.
+``fmt="npz"`` writes ``<name>.npz`` with the same names, shapes and attributes
+(``<dataset>.units``, ``<dataset>.description``) instead.  Scaling follows the reference: a field is written as
 ``data * to_dim * unit_factor`` with ``to_dim = 1 / to_nondim`` of that field
 (``field_2d.f90:490-521, 804-823``); the sound speed is never made non-dimensional there, so it
 is written with ``to_dim = 1``; 32-bit output clamps to +-huge(real32) and flushes below
@@ -160,7 +161,7 @@ def write_contour(fluid, results_dir: str, deck=None, *, iteration: int | None =
     title = title if title is not None else (deck.title if deck is not None else "")
     unit_system = unit_system or (deck.units if deck is not None else "cgs")
     fmt = fmt or (deck.contour_format if deck is not None else "xdmf")
-    if fmt not in ("xdmf", "hdf5", "h5"):
+    if fmt not in ("xdmf", "hdf5", "h5", "npz"):
         raise ValueError(f"Unsupported I/O contour format '{fmt}' (must be .xdmf .h5 or .hdf5)")
     ds = contour_datasets(st, cfg, nodes, t, dt, it, deck, title, unit_system, plot_64bit,
                           plot_volume, plot_grid_indices)
@@ -171,7 +172,7 @@ def write_contour(fluid, results_dir: str, deck=None, *, iteration: int | None =
         import h5py
     except ImportError:
         h5py = None
-    if h5py is not None:
+    if fmt != "npz" and h5py is not None:
         path = os.path.join(results_dir, stem + ".h5")
         with h5py.File(path, "w") as h5:
             for name, (val, units, desc) in ds.items():
@@ -180,6 +181,15 @@ def write_contour(fluid, results_dir: str, deck=None, *, iteration: int | None =
                     d.attrs["units"] = units
                 if desc is not None:
                     d.attrs["description"] = desc
+    elif fmt != "npz":
+        from . import h5lite
+
+        path = os.path.join(results_dir, stem + ".h5")
+        out = {}
+        for name, (val, units, desc) in ds.items():
+            attrs = {k: v for k, v in (("units", units), ("description", desc)) if v is not None}
+            out[name] = (val.T if np.ndim(val) == 2 else val, attrs)
+        h5lite.write_file(path, out)
     else:
         path = os.path.join(results_dir, stem + ".npz")
         out = {}

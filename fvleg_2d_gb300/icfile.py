@@ -17,10 +17,12 @@ primitives by ``density_to_nondim``, ``vel_to_nondim`` and ``press_to_nondim``
 (``mod_fluid.f90:347-350``; the factors of ``set_refrence_quantities``,
 ``src/lib/non_dimensional.f90:95-135``).
 
-Without an HDF5 library (h5py), ``.npz`` files with the same dataset names, shapes and
-transposition (and the units as ``<name>.units`` strings) stand in for the HDF5 file;
-:func:`write_ic` writes one, :func:`read_ic` reads either (``.h5`` through ``h5py`` when that is
-installed).
+``.h5`` / ``.hdf5`` files are read through h5py when it is installed, else through
+:mod:`fvleg_2d_gb300.h5lite` (the format subset pycato's h5py files use: gzip-compressed chunks,
+variable-length string attributes; checked on the reference's own ``tests/unit/simple.h5``).
+:func:`write_ic` writes HDF5 the same way (contiguous datasets) for a ``.h5`` / ``.hdf5`` path,
+and otherwise an ``.npz`` file with the same dataset names, shapes and transposition (the units
+as ``<name>.units`` strings).
 """
 from __future__ import annotations
 
@@ -62,10 +64,19 @@ class InitialCondition:
 
 
 def write_ic(path: str, x, y, rho, u, v, p, n_ghost: int) -> None:
-    """Write the pycato layout to ``path`` (``.npz``).  ``x``, ``y``: node coordinates including
-    ghost nodes, shape (ni+1+2g, nj+1+2g); fields: (ni+2g, nj+2g); all in (i, j) order and in
-    cgs units."""
+    """Write the pycato layout to ``path`` (HDF5 for ``.h5`` / ``.hdf5``, else ``.npz``).
+    ``x``, ``y``: node coordinates including ghost nodes, shape (ni+1+2g, nj+1+2g); fields:
+    (ni+2g, nj+2g); all in (i, j) order and in cgs units."""
     x, y = np.asarray(x, np.float64), np.asarray(y, np.float64)
+    if path.endswith((".h5", ".hdf5")):
+        from . import h5lite
+
+        ds = {"n_ghost_layers": (np.int64(n_ghost), {}),
+              "x": (x.T, {"units": "cm"}), "y": (y.T, {"units": "cm"})}
+        for (name, unit), a in zip(_FIELDS, (rho, u, v, p)):
+            ds[name] = (np.asarray(a, np.float64).T, {"units": unit})
+        h5lite.write_file(path, ds)
+        return
     out = {"n_ghost_layers": np.int32(n_ghost), "x": x.T.copy(), "y": y.T.copy(),
            "x.units": "cm", "y.units": "cm"}
     for (name, unit), a in zip(_FIELDS, (rho, u, v, p)):
@@ -79,17 +90,31 @@ def _load(path: str) -> dict:
     if not os.path.exists(path):
         raise ICFileError(f'File not found: "{path}"')
     if path.endswith((".h5", ".hdf5")):
+        names = ("x", "y") + tuple(n for n, _ in _FIELDS)
         try:
             import h5py
-        except ImportError as exc:
-            raise ICFileError(f"{path}: reading HDF5 needs h5py, which is not installed; "
-                              "convert the file to the .npz layout (write_ic)") from exc
-        with h5py.File(path, "r") as h5:
-            d = {"n_ghost_layers": np.asarray(h5["/n_ghost_layers"])}
-            for name in ("x", "y") + tuple(n for n, _ in _FIELDS):
-                d[name] = np.asarray(h5["/" + name], dtype=np.float64)
-                u = h5["/" + name].attrs.get("units", "")
-                d[name + ".units"] = u.decode() if isinstance(u, bytes) else str(u)
+        except ImportError:
+            h5py = None
+        if h5py is not None:
+            with h5py.File(path, "r") as h5:
+                d = {"n_ghost_layers": np.asarray(h5["/n_ghost_layers"])}
+                for name in names:
+                    d[name] = np.asarray(h5["/" + name], dtype=np.float64)
+                    u = h5["/" + name].attrs.get("units", "")
+                    d[name + ".units"] = u.decode() if isinstance(u, bytes) else str(u)
+            return d
+        from . import h5lite
+
+        try:
+            with h5lite.H5File(path) as h5:
+                d = {"n_ghost_layers": np.asarray(h5.read("n_ghost_layers"))}
+                for name in names:
+                    d[name] = np.asarray(h5.read(name), dtype=np.float64)
+                    d[name + ".units"] = str(h5.attrs(name).get("units", ""))
+        except KeyError as exc:
+            raise ICFileError(f"{path}: dataset {exc} missing") from exc
+        except h5lite.H5Error as exc:
+            raise ICFileError(f"{path}: {exc}") from exc
         return d
     with np.load(path, allow_pickle=False) as z:
         return {k: z[k] for k in z.files}

@@ -12,6 +12,11 @@ tests are read as text:
 * ``tests/unit/test_geometry/test_quad_cell.pf`` and ``mod_test_grid.f90`` -- cell metrics and
   the simple grid's node coordinates.
 
+It also copies the reference's one HDF5 file, ``tests/unit/simple.h5`` (written by
+``make_simple_grid.py`` through h5py: gzip-compressed chunks, variable-length string
+attributes), byte for byte to ``tests/golden/reference_simple.h5``: the known-answer input of the
+HDF5 reader (``fvleg_2d_gb300/h5lite.py``).
+
 Run from the repository root with the environment variable REFERENCE naming the reference
 checkout:  ``REFERENCE=<checkout> python tests/golden/make_golden.py``.
 """
@@ -20,6 +25,7 @@ from __future__ import annotations
 import json
 import os
 import re
+import shutil
 import sys
 
 REF = os.environ.get("REFERENCE", "")
@@ -191,7 +197,9 @@ def main() -> int:
         return 1
     with open(OUT, "w") as f:
         json.dump(data, f, indent=1)
-    print(f"wrote {OUT}: {len(data['bc']['cases'])} BC tests, {n_checks} asserts")
+    h5 = os.path.join(os.path.dirname(OUT), "reference_simple.h5")
+    shutil.copyfile(os.path.join(REF, "tests", "unit", "simple.h5"), h5)
+    print(f"wrote {OUT}: {len(data['bc']['cases'])} BC tests, {n_checks} asserts; {h5}")
     return 0
 
 

@@ -108,6 +108,14 @@ def test_unsupported_format(tmp_path):
     with pytest.raises(ValueError, match="Unsupported"):
         write_contour(F(), str(tmp_path), fmt="vtk")
     paths = write_contour(F(), str(tmp_path), fmt="xdmf")
-    z = np.load(paths["data"])
-    assert z["density"].shape == (2, 3)  # stored transposed, as HDF5 written from Fortran
+    assert paths["data"].endswith("step_0000000.h5")
+    from fvleg_2d_gb300 import h5lite
+
+    with h5lite.H5File(paths["data"]) as h5:
+        assert h5.read("density").shape == (2, 3)  # stored transposed, as HDF5 from Fortran
+        assert h5.attrs("density")["units"] == "g/cc"
+        assert h5.read("iteration") == 0 and isinstance(h5.read("title"), str)
+        assert "step_0000000.h5:/density" in open(paths["xdmf"]).read()
+    z = np.load(write_contour(F(), str(tmp_path), fmt="npz")["data"])
+    assert z["density"].shape == (2, 3)
     assert str(z["density.units"]) == "g/cc"

@@ -111,6 +111,6 @@ def test_errors(tmp_path):
     with pytest.raises(ICFileError, match="not rectilinear"):
         read_ic(str(tmp_path / "shear.npz"), ng)
     if importlib.util.find_spec("h5py") is None:
-        (tmp_path / "ic.h5").write_bytes(b"")
-        with pytest.raises(ICFileError, match="h5py"):
+        (tmp_path / "ic.h5").write_bytes(b"not an HDF5 file")
+        with pytest.raises(ICFileError, match="not an HDF5 file"):
             read_ic(str(tmp_path / "ic.h5"), ng)
