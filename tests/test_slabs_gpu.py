@@ -61,6 +61,28 @@ def test_slabs_match_the_one_grid_run(cato_lib, name, world, precision):
                                           err_msg=f"{k} rows {j0}:{j1}")
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed_df"])
+def test_slabs_of_a_rectilinear_grid(cato_lib, precision):
+    """Non-uniform rows: each slab gets its own y nodes; the rows beyond a cut take only their
+    states from the neighbour (the metrics of interior cells are the slab's)."""
+    cfg, prims = ic.riemann_quadrant(48, precision=precision, limiter="MLP3")
+    xs = np.concatenate([np.linspace(0.0, 0.3, 21), np.linspace(0.3, 1.0, 29)[1:]])
+    ys = np.concatenate([np.linspace(0.0, 0.6, 31), np.linspace(0.6, 1.0, 19)[1:]])
+    one = Fluid(cfg).set_rectilinear(xs, ys).initialize(*prims)
+    dts = [one.integrate()[0] for _ in range(STEPS)]
+    parts = [slabs.slab_config(cfg, r, 3) for r in range(3)]
+    fluids = [Fluid(c).set_rectilinear(xs, ys[j0:j1 + 1])
+              .initialize(*slabs.slab_fields(cfg, prims, j0, j1)) for c, j0, j1 in parts]
+    run = slabs.SlabRun(fluids, slabs.SlabComm(3, False))
+    assert [run.step()[0] for _ in range(STEPS)] == dts
+    g = cfg.ghost_layers()
+    ref = one.state(("rho", "rho_E"))
+    for f, (c, j0, j1) in zip(fluids, parts):
+        st = f.state(("rho", "rho_E"))
+        for k in st:
+            np.testing.assert_array_equal(st[k][g:-g, g:-g], ref[k][g:-g, g:-g][:, j0:j1])
+
+
 def test_slab_handles_refuse_the_whole_grid_entry_points(cato_lib):
     cfg, prims = ic.riemann_quadrant(32)
     c0, j0, j1 = slabs.slab_config(cfg, 0, 2)
