@@ -33,9 +33,20 @@ static __global__ void upload_init_kernel(int ni, int nj, int pitch, double gamm
   const double g1 = gamma - 1.0, one_over_g1 = 1.0 / g1;
   double dmin = INFINITY;
   int st = 0;
-  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < (long long)ni * nj;
+  // rows of the grid-stride loop: a 32-bit index split while the grid has fewer than 2^32 cells
+  // (a 64-bit integer division per cell costs more than the rest of the cell's work)
+  const long long total = (long long)ni * nj;
+  const bool narrow = total <= 0xffffffffLL;
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < total;
        n += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(n % ni), j = (int)(n / ni);
+    int i, j;
+    if (narrow) {
+      j = (int)((unsigned)n / (unsigned)ni);
+      i = (int)((unsigned)n - (unsigned)j * (unsigned)ni);
+    } else {
+      j = (int)(n / ni);
+      i = (int)(n - (long long)j * ni);
+    }
     const size_t idx = (size_t)j * pitch + i;
     const double r = r_[idx], u = u_[idx], v = v_[idx], p = p_[idx];
     rho[idx] = r;
@@ -46,11 +57,13 @@ static __global__ void upload_init_kernel(int ni, int nj, int pitch, double gamm
     double E = p * one_over_g1 + (r * 0.5) * s;
     if (abs_lt(E, EPS)) E = 0.0;
     rhoE[idx] = E;
-    const double pr = abs_lt(p, TINY) ? 0.0 : p / r;
-    const double cs = sqrt(gamma * pr);
+    // the divisions and the square root on the integer pipe (correctly rounded, so the values
+    // equal the FP64 instructions')
+    const double pr = abs_lt(p, TINY) ? 0.0 : div_rn(p, r);
+    const double cs = sqrt_rn(gamma * pr);
     // min_dx / min_dy of the cell: per column / row on a rectilinear grid
     const double cdx = dxc ? dxc[i] : dx, cdy = dyc ? dyc[j] : dy;
-    const double d = cfl / (((fabs(u) + cs) / cdx) + ((fabs(v) + cs) / cdy));
+    const double d = div_rn(cfl, div_rn(fabs(u) + cs, cdx) + div_rn(fabs(v) + cs, cdy));
     if (d < dmin) dmin = d;
     if (isnan(r) || isnan(u) || isnan(v) || isnan(p)) st |= ST_NAN;
     // initialize_from_hdf5 refuses ~0 density or pressure (mod_fluid.f90:352-360)
