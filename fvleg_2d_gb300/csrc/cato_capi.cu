@@ -1225,7 +1225,7 @@ int cato_gpu_set_plan(cato_handle* h, int32_t threads, int32_t rows_per_cta) {
 
 int cato_gpu_set_kernel_variant(cato_handle* h, int32_t variant) {
   if (!h) return CATO_ERR_ARG;
-  if (variant < 0 || variant > 1) return fail(h, CATO_ERR_ARG, "invalid kernel variant");
+  if (variant < 0 || variant > 2) return fail(h, CATO_ERR_ARG, "invalid kernel variant");
   h->plan.variant = variant;
   return CATO_OK;
 }
@@ -1241,20 +1241,20 @@ int cato_gpu_tune(cato_handle* h, int32_t steps, int32_t* steps_taken, float* be
   if (steps_taken) *steps_taken = 0;
   if (!h->uploaded) return fail(h, CATO_ERR_STATE, "no state uploaded");
   if (h->exchange) return refuse_exchange(h, "cato_gpu_tune");
-  // candidates: the default plan, 256-wide strips, half and a quarter of the rows per CTA; each
-  // with both FP64 register budgets
+  // candidates: the default plan and 256-wide strips, each with the default, half and a quarter
+  // of the rows per CTA, and with every FP64 register budget
   const Plan p0 = h->plan;
   std::vector<Plan> cands;
   const int wide = 256, half_rows = std::max(8, p0.rows_per_cta / 2);
   const int quarter_rows = std::max(8, p0.rows_per_cta / 4);
-  const int nvar = h->cfg.precision == CATO_FP64 ? 2 : 1;
+  const int nvar = h->cfg.precision == CATO_FP64 ? 3 : 1;
   for (int v = 0; v < nvar; ++v) {
-    Plan a = p0, b = p0, c = p0, d = p0;
-    a.variant = b.variant = c.variant = d.variant = v;
-    b.threads = wide;
-    c.rows_per_cta = half_rows;
-    d.rows_per_cta = quarter_rows;
-    for (const Plan& q : {a, b, c, d}) {
+    Plan a = p0, b = p0, c = p0, d = p0, e = p0, f = p0;
+    a.variant = b.variant = c.variant = d.variant = e.variant = f.variant = v;
+    b.threads = e.threads = f.threads = wide;
+    c.rows_per_cta = e.rows_per_cta = half_rows;
+    d.rows_per_cta = f.rows_per_cta = quarter_rows;
+    for (const Plan& q : {a, b, c, d, e, f}) {
       bool dup = false;
       for (const Plan& x : cands)
         dup |= x.threads == q.threads && x.rows_per_cta == q.rows_per_cta && x.variant == q.variant;

@@ -45,7 +45,8 @@ cudaError_t launch_stage_ext(dim3 grid, int threads, cudaStream_t stream, const 
 
 // The FP32 path has a lean variant without the rectilinear, source and pressure-input code
 // (it is issue-bound: those checks cost ~3 %); double-float keeps one kernel.  The FP64 path
-// has one kernel per register budget (variant 0: the compiler's choice, 1: at most 128).
+// has one kernel per register budget (variant 0: the compiler's choice, 1: at most 128, 2: at
+// most 85).
 template <typename R, int NG, int FLUX, int RECON>
 cudaError_t launch_stage_one(dim3 grid, int threads, cudaStream_t stream, const StageArgs& A,
                              const FluxConsts<R>& K, int variant) {
@@ -64,9 +65,15 @@ cudaError_t launch_stage_one(dim3 grid, int threads, cudaStream_t stream, const 
       cudaError_t e = launch_stage_ext<R, NG, FLUX, RECON, true, CATO_F64_MIN_BLOCKS_ALT>(
           grid, threads, stream, A, K);
       if (e != cudaSuccess) return e;
+      e = launch_stage_ext<R, NG, FLUX, RECON, true, CATO_F64_MIN_BLOCKS_ALT2>(grid, threads,
+                                                                              stream, A, K);
+      if (e != cudaSuccess) return e;
     } else if (variant == 1) {
       return launch_stage_ext<R, NG, FLUX, RECON, true, CATO_F64_MIN_BLOCKS_ALT>(grid, threads,
                                                                                 stream, A, K);
+    } else if (variant == 2) {
+      return launch_stage_ext<R, NG, FLUX, RECON, true, CATO_F64_MIN_BLOCKS_ALT2>(grid, threads,
+                                                                                 stream, A, K);
     }
   }
   return launch_stage_ext<R, NG, FLUX, RECON, true>(grid, threads, stream, A, K);
@@ -145,7 +152,7 @@ CATO_DECLARE_PREC(df)
 #undef CATO_DECLARE_STAGE
 #undef CATO_DECLARE_ONE
 
-// variant: the FP64 kernel's register budget (0 or 1, see launch_stage_one); ignored otherwise
+// variant: the FP64 kernel's register budget (0, 1 or 2, see launch_stage_one); ignored otherwise
 template <typename R>
 inline cudaError_t launch_stage(int flux, int recon, dim3 grid, int threads, cudaStream_t s,
                                 const StageArgs& A, const FluxConsts<R>& K, int variant = 0) {

@@ -551,15 +551,20 @@ __device__ __forceinline__ void stage_tile(const StageArgs& A, const FluxConsts<
 #ifndef CATO_F32_BATCH_MIN_BLOCKS
 #define CATO_F32_BATCH_MIN_BLOCKS 4
 #endif
-// and for the FP64 kernels, which come in two register budgets (kernel variants 0 and 1): the
-// compiler's choice, and at most 128 registers (two 256-thread CTAs per SM).  Which is faster
-// depends on the flux, the reconstruction and the flow (cato_gpu_tune measures it); both give
-// bit-identical results.
+// and for the FP64 kernels, which come in three register budgets (kernel variants 0, 1, 2): the
+// compiler's choice, at most 128 registers (two 256-thread CTAs per SM) and at most 85 (three).
+// Which is faster depends on the flux, the reconstruction, the plan and the flow
+// (cato_gpu_tune measures it; the 4096^2 quadrant and Kelvin-Helmholtz grids run best with 85
+// registers in 256-thread strips of 16 rows: +3 % and +4 % over the best 128-register plan);
+// all give bit-identical results.
 #ifndef CATO_F64_MIN_BLOCKS
 #define CATO_F64_MIN_BLOCKS 1
 #endif
 #ifndef CATO_F64_MIN_BLOCKS_ALT
 #define CATO_F64_MIN_BLOCKS_ALT 2
+#endif
+#ifndef CATO_F64_MIN_BLOCKS_ALT2
+#define CATO_F64_MIN_BLOCKS_ALT2 3
 #endif
 template <typename R> constexpr int min_blocks() {
   return Prec<R>::kind == 2 ? CATO_DF_MIN_BLOCKS

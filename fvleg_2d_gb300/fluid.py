@@ -259,7 +259,8 @@ class Fluid(_Handle):
         return t.value, r.value
 
     def set_kernel_variant(self, variant: int) -> None:
-        """FP64 stage kernel register budget: 0 (compiler's choice) or 1 (<= 128 registers)."""
+        """FP64 stage kernel register budget: 0 (compiler's choice), 1 (<= 128 registers) or
+        2 (<= 85)."""
         _check(self.L.cato_gpu_set_kernel_variant(self.h, int(variant)), self.h, "variant")
 
     def get_kernel_variant(self) -> int:

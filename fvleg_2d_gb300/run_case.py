@@ -65,7 +65,7 @@ def main(argv=None) -> int:
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--plan", default="", help="threads,rows_per_cta (default: the handle's)")
     ap.add_argument("--variant", type=int, default=-1,
-                    help="FP64 stage kernel register budget 0 or 1 (default: the handle's)")
+                    help="FP64 stage kernel register budget 0, 1 or 2 (default: the handle's)")
     ap.add_argument("--tune", action="store_true",
                     help="autotune plan and variant on real steps before the timed ones")
     ap.add_argument("--flux", default="", help="edge flux instead of the workload's (e.g. Roe)")

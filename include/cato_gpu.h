@@ -293,15 +293,16 @@ int cato_gpu_set_plan(cato_handle* h, int32_t threads, int32_t rows_per_cta);
 int cato_gpu_get_plan(const cato_handle* h, int32_t* threads, int32_t* rows_per_cta);
 
 /* Register budget of the FP64 stage kernel (the third knob): 0 = the compiler's choice (fewer
- * resident warps, more registers each), 1 = at most 128 registers per thread.  Which is faster
- * depends on the flux, the reconstruction and the flow; the results are bit-identical.  Accepted
- * and ignored by the mixed precisions. */
+ * resident warps, more registers each), 1 = at most 128 registers per thread, 2 = at most 85.
+ * Which is faster depends on the flux, the reconstruction, the plan and the flow; the results
+ * are bit-identical.  Accepted and ignored by the mixed precisions. */
 int cato_gpu_set_kernel_variant(cato_handle* h, int32_t variant);
 int cato_gpu_get_kernel_variant(const cato_handle* h, int32_t* variant);
 
-/* Autotune the stage kernel on the live state: a few candidate plans (the current one, 256-wide
- * strips, half and a quarter of the rows per CTA), each with both FP64 register budgets, run `steps` CFL steps
- * each (timed with CUDA events), and the fastest stays set.  These are real steps of the run
+/* Autotune the stage kernel on the live state: a few candidate plans (the current strip width
+ * and 256-wide strips, each with the current, half and a quarter of the rows per CTA), each
+ * with every FP64 register budget, run `steps` CFL steps each (timed with CUDA events), and the
+ * fastest stays set.  These are real steps of the run
  * (the solution advances by *steps_taken steps, bit-identical whichever candidate runs them);
  * *best_ms = the fastest candidate's time per step.  Returns the first fluid error, if any. */
 int cato_gpu_tune(cato_handle* h, int32_t steps, int32_t* steps_taken, float* best_ms);

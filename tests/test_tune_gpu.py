@@ -23,7 +23,7 @@ def test_variants_bit_identical(flux, limiter):
     cfg = _cfg(flux, limiter)
     prims = random_prims(cfg, np.random.default_rng(3))
     out = []
-    for variant in (0, 1):
+    for variant in (0, 1, 2):
         f = Fluid(cfg).initialize(*prims)
         f.set_kernel_variant(variant)
         assert f.get_kernel_variant() == variant
@@ -32,6 +32,7 @@ def test_variants_bit_identical(flux, limiter):
         f.close()
     for k in out[0]:
         assert np.array_equal(out[0][k], out[1][k]), k
+        assert np.array_equal(out[0][k], out[2][k]), k
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -40,10 +41,10 @@ def test_tune_matches_untuned_run(precision):
     prims = random_prims(cfg, np.random.default_rng(5))
     f = Fluid(cfg).initialize(*prims)
     taken, ms = f.tune(1)
-    # small grid: one plan fits (256-wide strips exceed it, half of 8 rows is 8), with both
+    # small grid: one plan fits (256-wide strips exceed it, half of 8 rows is 8), with the three
     # FP64 register budgets
-    assert taken == (2 if precision == "fp64" else 1) and ms > 0.0
-    assert f.get_kernel_variant() in (0, 1)
+    assert taken == (3 if precision == "fp64" else 1) and ms > 0.0
+    assert f.get_kernel_variant() in (0, 1, 2)
     threads, rows = f.get_plan()
     assert 64 <= threads <= 256 and rows >= 1
     f.run_timed(2)
@@ -61,5 +62,5 @@ def test_variant_rejects_bad_values():
     cfg = _cfg("HLLC", "van_leer")
     f = Fluid(cfg)
     with pytest.raises(Exception):
-        f.set_kernel_variant(2)
+        f.set_kernel_variant(3)
     f.close()
