@@ -2,8 +2,8 @@
 SSP-RK2, CFL 0.5, 500 steps): every instance's final density against its FP64 run.
 
 The bound is the accuracy target of the mixed-precision batched form, relative L1 density error
-<= 1e-6, for the double-float
-path on every instance that finishes in both precisions.  Some random-circle flows are
+<= 1e-6, for the double-float path on every instance that finishes in both precisions.  Some
+random-circle flows are
 dynamically unstable: the FP64 run itself, started from the same state perturbed by 1e-13
 (relative, per cell), drifts from the unperturbed FP64 run by up to ~1e-5 after 500 steps, so
 no arithmetic that is not bit-identical to FP64 can stay within 1e-6 of it there.  For such an
