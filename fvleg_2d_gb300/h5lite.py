@@ -461,11 +461,10 @@ def write_file(path: str, datasets: dict, root_attrs: dict | None = None) -> Non
     out in their C order (callers that follow h5py's convention pass the transpose of a Fortran
     (i, j) array); a str value is a scalar fixed-length ASCII string dataset, and str attribute
     values are fixed-length ASCII strings."""
-    names = sorted(datasets)
-    if any("/" in n.strip("/") for n in names):
-        raise H5Error("root-level datasets only")
-    names = [n.strip("/") for n in names]
     items = {n.strip("/"): v for n, v in datasets.items()}
+    if any("/" in n for n in items):
+        raise H5Error("root-level datasets only")
+    names = sorted(items)  # a symbol-table node lists its entries in name order
     leaf_k = max(4, (len(names) + 1) // 2)
     int_k = 16
     # local heap: the empty name at 0, then the names

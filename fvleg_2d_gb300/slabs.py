@@ -117,6 +117,8 @@ class SlabComm:
         to its opposite side)."""
         imports = {r: {} for r in self.local}
         pending = []
+        if self.dist is not None:
+            import torch
         for r in self.local:
             for side in self.sides(r):
                 nb = neighbour(r, side, self.world, self.periodic_y)
@@ -124,8 +126,6 @@ class SlabComm:
                 if nb in imports:
                     imports[nb][_OPPOSITE[side]] = rows
                     continue
-                import torch
-
                 pending.append(self.dist.isend(torch.from_numpy(np.ascontiguousarray(rows)),
                                                dst=nb, tag=_TAG[side]))
                 buf = torch.empty(rows.shape, dtype=torch.float64)
