@@ -825,8 +825,55 @@ def main() -> int:
         "batched": batched,
         "serving": serving,
     }
+    try:  # last, so that a tail of the line shows every leg
+        line["summary"] = summary_of(line)
+    except (KeyError, TypeError) as exc:
+        line["summary"] = {"unavailable": repr(exc)}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def summary_of(line: dict) -> dict:
+    """The figures of every leg in one short object (cell-updates/s in G, errors, latencies)."""
+    def g(v):
+        return None if v is None else round(v / 1e9, 4)
+
+    out = {"unit": "G cell-updates/s",
+           "quadrant": {"fp64": g(line["value"]), "mixed": g(line["mixed"]["value"]),
+                        "mixed_df": g(line["mixed_df"]["value"])},
+           "quadrant_e2e": {"fp64": g(line["e2e"]["value"]),
+                            "mixed": g(line["mixed"]["e2e"]["value"]),
+                            "mixed_df": g(line["mixed_df"]["e2e"]["value"])},
+           "fp64_hbm_frac": round(line["roofline"]["frac"], 4),
+           "fp64_pipe_frac": round((line["roofline"].get("fp64_pipe") or {}).get("frac", 0.0), 4)}
+    if line.get("cpu_baseline"):
+        out["cpu_oracle"] = g(line["cpu_baseline"]["value"])
+    kh = line.get("kelvin_helmholtz")
+    if kh:
+        out["kh"] = {p: g(kh[p]["value"]) for p in ("fp64", "mixed", "mixed_df") if p in kh}
+    sl = line.get("slabs")
+    if sl:
+        out["slabs_2_on_1_gpu"] = {p: g(sl[p]["value"]) for p in ("fp64", "mixed") if p in sl}
+    b = line.get("batched")
+    if b:
+        bt = {}
+        for p in ("fp64", "mixed_df", "mixed"):
+            if isinstance(b.get(p), dict) and "value" in b[p]:
+                e = b[p].get("density_error_vs_fp64")
+                bt[p] = {"value": g(b[p]["value"])}
+                if e:
+                    bt[p].update({"l1_median": e["rel_l1"]["median"], "l1_max": e["rel_l1"]["max"],
+                                  "l1_above_1e-6": e["rel_l1"]["above_1e-6"],
+                                  "instances": e["instances_compared"]})
+        out["batched"] = bt
+    sv = line.get("serving")
+    if sv:
+        out["serving_100_per_s"] = {
+            p: {"completed": r["completed"], "p50_s": round(r["p50_latency_s"], 2),
+                "p99_s": round(r["p99_latency_s"], 2), "value": g(r["cell_updates_per_s"])}
+            for p, rows in sv.items() if isinstance(rows, list)
+            for r in rows if r.get("rate_per_s") == 100.0}
+    return out
 
 
 if __name__ == "__main__":
