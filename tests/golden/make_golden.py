@@ -10,7 +10,9 @@ tests are read as text:
 * ``tests/unit/test_limiters/test_limiters.f90`` -- flux-limiter values;
 * ``tests/unit/test_reconstruction/test_reconstruction.pf`` -- TVD2 edge values;
 * ``tests/unit/test_geometry/test_quad_cell.pf`` and ``mod_test_grid.f90`` -- cell metrics and
-  the simple grid's node coordinates.
+  the simple grid's node coordinates;
+* ``tests/unit/test_field/test_field.f90`` -- the halo exchange of an 8x8 field over 2x2 images
+  (``sync_edges``): each image's interior values and the halo rows it receives across j.
 
 It also copies the reference's one HDF5 file, ``tests/unit/simple.h5`` (written by
 ``make_simple_grid.py`` through h5py: gzip-compressed chunks, variable-length string
@@ -177,6 +179,36 @@ def grid_nodes() -> dict:
             "source": "tests/unit/test_geometry/mod_test_grid.f90"}
 
 
+def field_halo() -> dict:
+    """test_halo_exchange: per image (1..4) its interior rows ``field%data(a:b, j) = [..]`` and
+    the asserted halo rows ``field%data(ilo_halo:ihi_halo, jhi_halo[ - 1])`` /
+    ``(.., jlo_halo[ + 1])`` (a scalar 0.0 assert is a row of zeros)."""
+    src = read("tests/unit/test_field/test_field.f90")
+    body = src[src.index("subroutine test_halo_exchange"):src.index("end subroutine test_halo_exchange")]
+    setup, checks = body.split("call field%sync_edges()")
+    images = {}
+    parts = re.split(r"case\((\d)\)", setup)
+    for k in range(1, len(parts), 2):
+        img = int(parts[k])
+        rows = {}
+        for a, b, j, vals in re.findall(r"field%data\((\d+):(\d+),\s*(\d+)\)\s*=\s*\[([^\]]*)\]",
+                                        parts[k + 1]):
+            rows[j] = {"i0": int(a), "i1": int(b), "values": nums(vals)}
+        images[str(img)] = {"rows": rows}
+    parts = re.split(r"case\((\d)\)", checks)
+    for k in range(1, len(parts), 2):
+        img = str(int(parts[k]))
+        halo = {}
+        pat = (r"call assert_equal\((\[[^\]]*\]|0\.0_rk),\s*&?\s*"
+               r"field%data\(ilo_halo:ihi_halo,\s*(j(?:hi|lo)_halo(?:\s*[-+]\s*1)?)\)")
+        for vals, where in re.findall(pat, parts[k + 1]):
+            key = where.replace(" ", "")
+            halo[key] = nums(vals) if vals.startswith("[") else [0.0] * 8
+        images[img]["halo_rows"] = halo
+    return {"ni": 8, "nj": 8, "n_halo": 2, "images": images,
+            "source": "tests/unit/test_field/test_field.f90 (test_halo_exchange)"}
+
+
 def main() -> int:
     if not REF or not os.path.isdir(REF):
         print("set REFERENCE to the reference checkout", file=sys.stderr)
@@ -190,6 +222,7 @@ def main() -> int:
         "tvd2_none": tvd2_none(),
         "quad_cell": quad_cell(),
         "grid_nodes": grid_nodes(),
+        "field_halo": field_halo(),
     }
     n_checks = sum(len(c["checks"]) for c in data["bc"]["cases"])
     if n_checks < 40:

@@ -17,6 +17,8 @@ from fvleg_2d_gb300 import ic, slabs
 from fvleg_2d_gb300.config import SchemeConfig
 
 STEPS = 6
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden",
+                                     "reference_unit_vectors.json")))
 
 
 def _cases():
@@ -134,6 +136,49 @@ def test_local_swap_routes_rows_to_the_neighbours():
                 nb = slabs.neighbour(r, s, world, periodic)
                 # beyond my -y side: the neighbour's rows next to its +y side, and vice versa
                 assert rows[0, 0, 0] == 10 * nb + (1 if s == "-y" else 0)
+
+
+def test_exchange_reproduces_the_reference_halo_rows():
+    """The reference's own halo-exchange test (tests/unit/test_field/test_field.f90,
+    test_halo_exchange: an 8x8 field over 2x2 images, 2 halo cells) asserts the rows each image
+    receives across j.  Cut the same field into 2 row slabs (all columns each): the rows the slab
+    exchange puts beyond each cut equal the asserted rows on every column they share (the
+    columns beyond the x boundary are boundary-condition ghosts there, not exchanged rows)."""
+    gold = GOLDEN["field_halo"]
+    ni, nj, g = gold["ni"], gold["nj"], gold["n_halo"]
+    field = np.zeros((ni + 2 * g, nj + 2 * g), order="F")  # (1-g:ni+g, 1-g:nj+g)
+    for img in gold["images"].values():
+        for j, row in img["rows"].items():
+            field[row["i0"] - 1 + g:row["i1"] + g, int(j) - 1 + g] = row["values"]
+    comm = slabs.SlabComm(2, False)
+    parts = slabs.split_rows(nj, 2, g)  # rows 1-4 and 5-8: the images' j split
+    # four copies of the field stand in for rho, u, v, p
+    q = {r: [field[:, j0:j1 + 2 * g].copy(order="F") for _ in range(4)]
+         for r, (j0, j1) in enumerate(parts)}
+    ex = {r: {s: _rows_of(q[r], g, ni, parts[r][1] - parts[r][0], s) for s in comm.sides(r)}
+          for r in q}
+    im = comm.swap(ex)
+    for r, (j0, j1) in enumerate(parts):
+        for s, rows in im[r].items():
+            _put_ghosts(q[r], g, ni, j1 - j0, s, rows)
+    checked = 0
+    for name, img in gold["images"].items():
+        k = int(name)
+        i_lo = 1 if k in (1, 3) else 5                  # first interior column of the image
+        r = 0 if k in (1, 2) else 1                     # the slab holding its rows
+        j0, j1 = parts[r]
+        for key, want in img["halo_rows"].items():
+            jj = {"jhi_halo": j1 + g, "jhi_halo-1": j1 + g - 1,
+                  "jlo_halo": j0 + 1 - g, "jlo_halo+1": j0 + 2 - g}[key]  # global 1-based j
+            if not (1 <= jj <= nj) or (j0 < jj <= j1):
+                continue  # a physical boundary row, or not beyond a cut
+            local = jj - (j0 + 1 - g)  # row index in the slab's halo-padded array
+            for pos, val in enumerate(want):
+                i = i_lo - g + pos  # global 1-based column of the asserted entry
+                if 1 <= i <= ni:
+                    assert q[r][0][i - 1 + g, local] == val, (name, key, i)
+                    checked += 1
+    assert checked >= 40
 
 
 def test_oracle_config_accepts_exchange_on_y_only(oracle):
