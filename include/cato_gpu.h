@@ -329,7 +329,9 @@ int cato_gpu_set_step_options(cato_handle* h, int32_t keep_step_start, int32_t a
  *           cato_gpu_step_stage(h, &left);    runs the next RK stage; left = stages still to run
  *   cato_gpu_step_end(h, &dt_used, &error_code);
  * The sequence of kernels is the one cato_gpu_integrate enqueues; any handle may use it.  Step
- * options (subcycling, the kept step start) are not combined with it. */
+ * options (subcycling, the kept step start) are not combined with it.  On a slab,
+ * cato_gpu_conservation_sums covers the slab's rows (the grid's totals are the sums over the
+ * slabs) and cato_gpu_convergence gives the slab's own relative norms. */
 int cato_gpu_step_begin(cato_handle* h, double dt);
 int cato_gpu_step_stage(cato_handle* h, int32_t* stages_left);
 int cato_gpu_step_end(cato_handle* h, double* dt_used, int32_t* error_code);
