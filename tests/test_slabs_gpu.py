@@ -59,6 +59,9 @@ def test_slabs_match_the_one_grid_run(cato_lib, name, world, precision):
         for k in st:
             np.testing.assert_array_equal(st[k][g:-g, g:-g], ref[k][g:-g, g:-g][:, j0:j1],
                                           err_msg=f"{k} rows {j0}:{j1}")
+    # the grid's totals are the sums over the slabs (other summation order: to rounding)
+    np.testing.assert_allclose(sum(f.conservation_sums() for f in fluids),
+                               one.conservation_sums(), rtol=1e-12, atol=1e-12)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed_df"])
